@@ -1,0 +1,556 @@
+"""Benchmark: RAJA data-parallel primitives on GB300 (bandwidth-sweep config).
+
+One step = one pass of every primitive of the bandwidth-sweep configuration
+at N = 2^28 elements each (inputs resident in HBM, every input larger than
+the 129 MB L2, so no flush is needed between steps):
+
+  ReduceSum f32, ReduceSum f64       uniform[-1,1)
+  ReduceMinLoc / ReduceMaxLoc        f32 and f64 uniform[-1,1)
+  exclusive_scan int64               uniform{0..1023}
+  radix sort u32, u64                uniform over the full range
+  sort_pairs                         f32 normal(0,1) keys, int32 index values
+  MultiReduceSum histogram           int32 Zipf(1.1) into 256 and 65536 bins
+
+value = algorithmic bytes of all primitives / device time of the step
+(GB/s); the per-primitive bytes follow the fixed convention: sum/min/max
+sizeof(T) per element, scan 2 sizeof(T), LSD radix sort
+N sizeof(K) (2P+1) with P = bits/8 digit passes (+ N sizeof(V) 2P for
+values), histogram 4 bytes per element.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the oracle's OpenMP restatement of RAJA's
+omp_parallel_for_exec path on the host cores (RAJA itself cannot be built
+here: its camp submodule is absent), on a bounded sample of the same
+workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "primitive GB/s (aggregate over the bandwidth-sweep primitives)"
+UNIT = "GB/s"
+
+
+# ----------------------------------------------------------------- workload
+def primitive_table(n: int):
+    """(name, algorithmic bytes) for one step at n elements per primitive."""
+    return [
+        ("reduce_sum_f32", 4 * n), ("reduce_sum_f64", 8 * n),
+        ("minloc_f32", 4 * n), ("maxloc_f32", 4 * n),
+        ("minloc_f64", 8 * n), ("maxloc_f64", 8 * n),
+        ("exclusive_scan_i64", 16 * n),
+        ("sort_u32", 4 * n * (2 * 4 + 1)), ("sort_u64", 8 * n * (2 * 8 + 1)),
+        ("sort_pairs_f32_i32", 4 * n * (2 * 4 + 1) + 4 * n * 2 * 4),
+        ("histogram_256", 4 * n), ("histogram_65536", 4 * n),
+    ]
+
+
+def zipf_cdf(nbins: int, s: float = 1.1):
+    import numpy as np
+    w = 1.0 / np.arange(1, nbins + 1, dtype=np.float64) ** s
+    c = np.cumsum(w)
+    return c / c[-1]
+
+
+def make_inputs(n: int, seed: int, device: str):
+    """Seeded synthetic inputs of the bandwidth-sweep configuration."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    t = {}
+    t["f32"] = torch.rand(n, generator=g, device=device, dtype=torch.float32) * 2 - 1
+    t["f64"] = torch.rand(n, generator=g, device=device, dtype=torch.float64) * 2 - 1
+    t["scan_in"] = torch.randint(0, 1024, (n,), generator=g, device=device, dtype=torch.int64)
+    t["u32"] = torch.randint(-2 ** 31, 2 ** 31, (n,), generator=g, device=device,
+                             dtype=torch.int32).view(torch.uint32)
+    t["u64"] = torch.randint(-2 ** 63, 2 ** 63 - 1, (n,), generator=g, device=device,
+                             dtype=torch.int64).view(torch.uint64)
+    t["pk"] = torch.randn(n, generator=g, device=device, dtype=torch.float32)
+    t["pv"] = torch.arange(n, device=device, dtype=torch.int32)
+    for nb in (256, 65536):
+        cdf = torch.from_numpy(zipf_cdf(nb)).to(device)
+        u = torch.rand(n, generator=g, device=device, dtype=torch.float64)
+        t[f"z{nb}"] = torch.searchsorted(cdf, u, right=True).clamp_(0, nb - 1).to(torch.int32)
+        del u
+    return t
+
+
+def make_outputs(n: int, device: str):
+    import torch
+    return {
+        "scan_out": torch.empty(n, dtype=torch.int64, device=device),
+        "u32_out": torch.empty(n, dtype=torch.int32, device=device).view(torch.uint32),
+        "u64_out": torch.empty(n, dtype=torch.int64, device=device).view(torch.uint64),
+        "pk_out": torch.empty(n, dtype=torch.float32, device=device),
+        "pv_out": torch.empty(n, dtype=torch.int32, device=device),
+        "sum": torch.empty(2, dtype=torch.float64, device=device),
+        "loc_f32": torch.empty(4, dtype=torch.float32, device=device),
+        "loc_f64": torch.empty(4, dtype=torch.float64, device=device),
+        "idx": torch.empty(4, dtype=torch.int64, device=device),
+        "h256": torch.zeros(256, dtype=torch.int64, device=device),
+        "h65536": torch.zeros(65536, dtype=torch.int64, device=device),
+    }
+
+
+def step_calls(lib, t, o, n: int, stream: int):
+    """The step as a list of (name, zero-arg callable) over the C ABI."""
+    P = lambda x: x.data_ptr()  # noqa: E731
+    s = stream
+    o_sum, o_lf, o_ld, o_ix = P(o["sum"]), P(o["loc_f32"]), P(o["loc_f64"]), P(o["idx"])
+    return [
+        ("reduce_sum_f32", lambda: lib.b200_reduce_sum_f32(P(t["f32"]), n, 0, o_sum, s)),
+        ("reduce_sum_f64", lambda: lib.b200_reduce_sum_f64(P(t["f64"]), n, 0, o_sum + 8, s)),
+        ("minloc_f32", lambda: lib.b200_reduce_minloc_f32(P(t["f32"]), n, o_lf, o_ix, s)),
+        ("maxloc_f32", lambda: lib.b200_reduce_maxloc_f32(P(t["f32"]), n, o_lf + 4, o_ix + 8, s)),
+        ("minloc_f64", lambda: lib.b200_reduce_minloc_f64(P(t["f64"]), n, o_ld, o_ix + 16, s)),
+        ("maxloc_f64", lambda: lib.b200_reduce_maxloc_f64(P(t["f64"]), n, o_ld + 8, o_ix + 24, s)),
+        ("exclusive_scan_i64", lambda: lib.b200_scan_exclusive_i64(
+            P(t["scan_in"]), P(o["scan_out"]), n, 0, 0, s)),
+        ("sort_u32", lambda: lib.b200_sort_keys_copy_u32(P(t["u32"]), P(o["u32_out"]), n, 0, s)),
+        ("sort_u64", lambda: lib.b200_sort_keys_copy_u64(P(t["u64"]), P(o["u64_out"]), n, 0, s)),
+        ("sort_pairs_f32_i32", lambda: lib.b200_sort_pairs_copy_f32_i32(
+            P(t["pk"]), P(t["pv"]), P(o["pk_out"]), P(o["pv_out"]), n, 0, s)),
+        ("histogram_256", lambda: lib.b200_histogram_i32(P(t["z256"]), n, 256, P(o["h256"]), s)),
+        ("histogram_65536", lambda: lib.b200_histogram_i32(P(t["z65536"]), n, 65536,
+                                                           P(o["h65536"]), s)),
+    ]
+
+
+def run_step(calls):
+    for name, fn in calls:
+        rc = fn()
+        if rc != 0:
+            from raja_gb300 import _lib
+            _lib.check(name, rc)
+
+
+# ------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+# -------------------------------------------------------------- cpu legs
+def cpu_suite(n: int, seed: int = 0):
+    """Time the oracle's OpenMP restatement over the suite at n elements.
+
+    Returns (total algorithmic bytes, seconds, cores, per-primitive times)."""
+    import numpy as np
+
+    import oracle
+    rng = np.random.default_rng(seed)
+    f32 = rng.uniform(-1, 1, n).astype(np.float32)
+    f64 = rng.uniform(-1, 1, n)
+    si = rng.integers(0, 1024, n).astype(np.int64)
+    u32 = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    u64 = rng.integers(0, 2 ** 64, n, dtype=np.uint64)
+    pk = rng.normal(0, 1, n).astype(np.float32)
+    pv = np.arange(n, dtype=np.int32)
+    zs = {nb: np.searchsorted(zipf_cdf(nb), rng.random(n), side="right").clip(0, nb - 1)
+          .astype(np.int32) for nb in (256, 65536)}
+    out = np.empty_like(si)
+    calls = [
+        ("reduce_sum_f32", lambda: oracle.reduce_sum(f32, parallel=True)),
+        ("reduce_sum_f64", lambda: oracle.reduce_sum(f64, parallel=True)),
+        ("minloc_f32", lambda: oracle.reduce_minloc(f32, parallel=True)),
+        ("maxloc_f32", lambda: oracle.reduce_maxloc(f32, parallel=True)),
+        ("minloc_f64", lambda: oracle.reduce_minloc(f64, parallel=True)),
+        ("maxloc_f64", lambda: oracle.reduce_maxloc(f64, parallel=True)),
+        ("exclusive_scan_i64", lambda: oracle.scan(si, "plus", exclusive=True, init=0,
+                                                   parallel=True, out=out)),
+        ("sort_u32", lambda: oracle.sort(u32, parallel=True, stable=False)),
+        ("sort_u64", lambda: oracle.sort(u64, parallel=True, stable=False)),
+        ("sort_pairs_f32_i32", lambda: oracle.sort_pairs(pk, pv, parallel=True, stable=False)),
+        ("histogram_256", lambda: oracle.histogram(zs[256], 256, parallel=True)),
+        ("histogram_65536", lambda: oracle.histogram(zs[65536], 65536, parallel=True)),
+    ]
+    table = dict(primitive_table(n))
+    per = {}
+    total = 0.0
+    for name, fn in calls:
+        t0 = time.perf_counter()
+        fn()
+        dt = time.perf_counter() - t0
+        per[name] = dt
+        total += dt
+    return sum(table.values()), total, oracle.max_threads(), per
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+# ------------------------------------------------------------- reference
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    n = 1 << args.cpu_log2n
+    for _ in range(args.warmup):
+        cpu_suite(n)
+    tot_bytes, tot_s = 0, 0.0
+    per_acc: dict[str, float] = {}
+    cores = 1
+    for k in range(args.steps):
+        b, s, cores, per = cpu_suite(n, seed=k)
+        tot_bytes += b
+        tot_s += s
+        for nm, v in per.items():
+            per_acc[nm] = per_acc.get(nm, 0.0) + v
+    value = tot_bytes / tot_s / 1e9
+    table = dict(primitive_table(n))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * tot_s / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "mixed (f32,f64,i32,i64,u32,u64)",
+        "data": "synthetic (seeded, bandwidth-sweep shapes)",
+        "config": config_block(args, n_override=n),
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"every primitive at N=2^{args.cpu_log2n} per step "
+                                   f"(oracle OpenMP restatement of omp_parallel_for_exec; "
+                                   f"RAJA cannot be compiled here), CPU {cpu_model()}"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "primitives": {nm: round(table[nm] * args.steps / per_acc[nm] / 1e9, 3) for nm in per_acc},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_block(args, n_override=None):
+    n = n_override or (1 << args.log2n)
+    return {"workload": "bandwidth sweep (BASELINE configs[1]) at N=2^%d per primitive"
+                        % (n.bit_length() - 1),
+            "n": n, "primitives": [p for p, _ in primitive_table(n)],
+            "l2_flush": "none: every input is larger than the 129 MB L2",
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+# ------------------------------------------------------------------ main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--log2n", type=int, default=28)
+    ap.add_argument("--cpu-log2n", type=int, default=22)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import raja_gb300
+    from raja_gb300 import _lib
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = _lib.load()
+    n = 1 << args.log2n
+    dev = "cuda"
+    inputs = make_inputs(n, seed=rank, device=dev)
+    outs = make_outputs(n, dev)
+    stream = torch.cuda.current_stream()
+    calls = step_calls(lib, inputs, outs, n, stream.cuda_stream)
+    table = dict(primitive_table(n))
+    step_bytes = sum(table.values())
+
+    for _ in range(args.warmup):
+        run_step(calls)
+    raja_gb300.synchronize()
+
+    # ---- timed region: K steps, barrier + sync on both sides
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        run_step(calls)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    raja_gb300.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * step_bytes * args.steps / (ms / 1e3) / 1e9
+    launches_per_step = None
+
+    # ---- per-primitive breakdown and per-kernel times (CUDA events on the
+    # launching stream, inside the library)
+    per_prim = {}
+    reps = max(3, min(10, args.steps))
+    for name, fn in calls:
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            rc = fn()
+            _lib.check(name, rc)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t_ms = a.elapsed_time(b) / reps
+        per_prim[name] = {"ms": round(t_ms, 4), "gbs": round(table[name] / t_ms / 1e6, 1)}
+    raja_gb300.prof_reset()
+    raja_gb300.prof_enable(True)
+    for _ in range(reps):
+        run_step(calls)
+    torch.cuda.synchronize()
+    kern = raja_gb300.prof_read()
+    raja_gb300.prof_enable(False)
+    launches_per_step = sum(v[0] for v in kern.values()) // reps
+    kernels = {k: {"launches_per_step": v[0] // reps, "ms_per_step": round(v[1] / reps, 4)}
+               for k, v in kern.items()}
+
+    peaks = load_peaks()
+    hbm_peak = peaks.get("hbm_gbs") or 6800.0
+    peak_src = "measured" if peaks.get("hbm_gbs") else "fallback"
+    for v in per_prim.values():
+        v["frac_of_" + peak_src + "_hbm"] = round(v["gbs"] / hbm_peak, 3)
+    roof = roofline(kernels, n, hbm_peak, peak_src)
+
+    # ---- e2e through the public API with host buffers
+    e2e = run_e2e(args, lib, inputs, outs, n, stream, table, dist)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = run_cpu_baseline(args)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "mixed (f32,f64,i32,i64,u32,u64)",
+            "data": "synthetic (seeded on device, bandwidth-sweep shapes)",
+            "config": config_block(args),
+            "frac_of_hbm_peak": round(value / world / hbm_peak, 3),
+            "hbm_peak_gbs": hbm_peak, "hbm_peak_source": peak_src,
+            "primitives": per_prim, "kernels": kernels,
+            "roofline": roof, "e2e": e2e, "cpu_baseline": cpu,
+            "gpu_launches": launches_per_step * args.steps if launches_per_step else None,
+            "gpu_launches_per_step": launches_per_step,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def load_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# bytes each launch of a named kernel moves, by the fixed convention
+def kernel_bytes(name: str, n: int):
+    per = {
+        "b200_onesweep_k32": 2 * 4 * n,            # read + write every key once
+        "b200_onesweep_k64": 2 * 8 * n,
+        "b200_onesweep_k32_v32": 2 * 4 * n + 2 * 4 * n,
+        "b200_sort_hist": None,                   # key read (bytes differ per key width)
+        "b200_scan_exclusive_i64": 16 * n,
+        "b200_reduce_sum_f32": 4 * n, "b200_reduce_sum_f64": 8 * n,
+        "b200_reduce_minloc_f32": 4 * n, "b200_reduce_maxloc_f32": 4 * n,
+        "b200_reduce_minloc_f64": 8 * n, "b200_reduce_maxloc_f64": 8 * n,
+        "b200_histogram_rep": 4 * n, "b200_histogram_agg": 4 * n,
+    }
+    return per.get(name)
+
+
+def roofline(kernels: dict, n: int, peak: float, src: str) -> dict:
+    if not kernels:
+        return None
+    top = max(kernels.items(), key=lambda kv: kv[1]["ms_per_step"])
+    name, v = top
+    per_launch_bytes = kernel_bytes(name, n)
+    avg_ms = v["ms_per_step"] / max(v["launches_per_step"], 1)
+    achieved = per_launch_bytes / avg_ms / 1e6 if per_launch_bytes else None
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(tp) as f:
+            tr = json.load(f)
+        if name in tr:
+            # captured on a smaller case; traffic scales with the units processed
+            traffic = int(tr[name]["bytes_per_launch"] * n / tr[name]["n"])
+    except (OSError, ValueError, KeyError):
+        pass
+    return {"kernel": name, "bound": "hbm",
+            "achieved": round(achieved, 1) if achieved else None, "peak": peak,
+            "peak_source": src, "unit": "GB/s",
+            "frac": round(achieved / peak, 3) if achieved else None,
+            "traffic": traffic, "algorithmic_bytes_per_launch": per_launch_bytes,
+            "avg_launch_ms": round(avg_ms, 4),
+            "share_of_step": None}
+
+
+def run_e2e(args, lib, inputs, outs, n, stream, table, dist):
+    """Same step through the C ABI with host buffers: every step copies its
+    inputs host->device from pinned memory and reads results back."""
+    import torch
+    keys_in = ["f32", "f64", "scan_in", "u32", "u64", "pk", "pv", "z256", "z65536"]
+    host = {k: torch.empty(inputs[k].shape, dtype=inputs[k].dtype, pin_memory=True)
+            for k in keys_in}
+    for k in keys_in:
+        host[k].copy_(inputs[k])
+    out_keys = ["scan_out", "u32_out", "u64_out", "pk_out", "pv_out", "sum", "loc_f32",
+                "loc_f64", "idx", "h256", "h65536"]
+    host_out = {k: torch.empty(outs[k].shape, dtype=outs[k].dtype, pin_memory=True)
+                for k in out_keys}
+    h2d = sum(host[k].numel() * host[k].element_size() for k in keys_in)
+    d2h = sum(host_out[k].numel() * host_out[k].element_size() for k in out_keys)
+    calls = step_calls(lib, inputs, outs, n, stream.cuda_stream)
+
+    def one():
+        for k in keys_in:
+            inputs[k].copy_(host[k], non_blocking=True)
+        outs["h256"].zero_()
+        outs["h65536"].zero_()
+        run_step(calls)
+        for k in out_keys:
+            host_out[k].copy_(outs[k], non_blocking=True)
+
+    one()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(args.e2e_steps):
+        one()
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    world = dist.get_world_size() if dist else 1
+    value = world * sum(table.values()) * args.e2e_steps / (ms / 1e3) / 1e9
+    return {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
+            "ms_per_step": round(ms / args.e2e_steps, 3),
+            "path": "pinned host -> device copies, C-ABI calls, device -> pinned host copies"}
+
+
+def run_cpu_baseline(args):
+    import oracle
+    oracle.build()
+    n = 1 << args.cpu_log2n
+    cpu_suite(n)                      # warm-up (page faults, thread pool)
+    b, s, cores, _ = cpu_suite(n, seed=1)
+    reps = max(1, int(10.0 / max(s, 1e-3)))
+    reps = min(reps, 8)
+    tb, ts = 0, 0.0
+    for r in range(reps):
+        b, s, cores, _ = cpu_suite(n, seed=2 + r)
+        tb += b
+        ts += s
+    return {"value": round(tb / ts / 1e9, 3), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{reps} passes of every primitive at N=2^{args.cpu_log2n} "
+                      f"(oracle OpenMP restatement of omp_parallel_for_exec), CPU {cpu_model()}",
+            "seconds": round(ts, 2)}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,309 @@
+/*
+ * b200prims.h -- C ABI of the GB300 (sm_103a) data-parallel primitive library
+ * (libb200prims.so).
+ *
+ * This is the drop-in boundary that replaces RAJA's CUDA back-end for the
+ * fixed-type primitives of its data-parallel path.  Every entry point below
+ * names the reference interface it stands in for (paths are relative to the
+ * RAJA v2025.09.1 source tree).  The templated C++ layer in
+ * include/raja_b200/ (the b200_exec / b200_reduce / b200_work policies) and
+ * the Python host mirror (raja_gb300) both call these functions.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  All data pointers are device-accessible
+ *     (cudaMalloc'd, managed, or mapped pinned memory).  Results of reductions
+ *     are written by the device into `out*` pointers, which must also be
+ *     device-accessible.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *     Every call is stream-ordered and returns once the work is enqueued; call
+ *     b200_stream_synchronize() to wait and to collect device-side errors.
+ *   - Every function returns an int status (B200_OK == 0).  Nothing aborts or
+ *     throws across this boundary; b200_last_error_string() explains the last
+ *     failure on the calling host thread.
+ *   - Element counts are size_t.  The reference scans and sorts use an `int`
+ *     length (policy/cuda/scan.hpp:163, policy/cuda/sort.hpp:115); this
+ *     library accepts any n < 2^40 for scans and reductions and n < 2^32 for
+ *     sorts.
+ */
+#ifndef B200PRIMS_H
+#define B200PRIMS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define B200_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------
+ * Replace the reference's error paths: CUDA API failures raised as
+ * std::runtime_error by CAMP_CUDA_API_INVOKE_AND_CHECK
+ * (policy/cuda/raja_cudaerrchk.hpp:116-137) and RAJA_ABORT_OR_THROW for bad
+ * launch geometry (util/macros.hpp:143-152).                              */
+#define B200_OK 0
+#define B200_ERR_ARG 1         /* invalid argument (size, op, alignment)   */
+#define B200_ERR_CUDA 2        /* a CUDA runtime call failed                */
+#define B200_ERR_TIMEOUT 3     /* a bounded device wait gave up             */
+#define B200_ERR_NOMEM 4       /* scratch allocation failed                 */
+#define B200_ERR_UNSUPPORTED 5 /* type/op combination not provided          */
+
+/* ---- reduction modes (bit flags) ---------------------------------------
+ * NAIVE: accumulate in the element type, like cuda_reduce
+ *        (policy/cuda/reduce.hpp:133-214).
+ * COMPENSATED: per-thread two-sum (Neumaier) accumulation in the element
+ *        type, cross-block combine in FP64 (FP32 inputs) or double-double
+ *        (FP64 inputs).  Affects floating-point sums, dots and scans only.
+ * DETERMINISTIC: fixed-size chunks and a fixed combine tree, so the result
+ *        depends only on (n, data) and not on the grid or the GPU.        */
+#define B200_MODE_NAIVE 0
+#define B200_MODE_COMPENSATED 1
+#define B200_MODE_DETERMINISTIC 2
+
+/* ---- scan operators (RAJA::operators::plus/minimum/maximum,
+ *      util/Operators.hpp:363-372, 555-591)                              */
+#define B200_OP_SUM 0
+#define B200_OP_MIN 1
+#define B200_OP_MAX 2
+
+typedef void* b200_stream_t;
+
+/* ======================================================================
+ * Runtime (replaces MemUtils_CUDA.hpp:69-284 pools/launch/sync glue and
+ * src/MemUtils_CUDA.cpp:44-53 globals)
+ * ====================================================================== */
+
+/* ABI version of the loaded library (== B200_ABI_VERSION). */
+int b200_abi_version(void);
+
+/* Message for the last failing call on this host thread ("" if none). */
+const char* b200_last_error_string(void);
+
+/* Wait for `stream`, then read and clear the device status word of the
+ * current device.  Returns B200_ERR_TIMEOUT if a bounded device wait (scan
+ * or sort look-back) gave up since the last check.  Replaces
+ * cuda::synchronize / res.wait() (MemUtils_CUDA.hpp:205-247). */
+int b200_stream_synchronize(b200_stream_t stream);
+
+/* Test hook: upper bound on polling iterations of every device-side wait
+ * (0 restores the default).  Used to exercise the timeout path without a
+ * GPU fault (the reference spins without a bound, reduce.hpp:425-426). */
+int b200_set_spin_limit(uint64_t limit);
+
+/* Test hook: launch one scan tile whose predecessor never publishes, so its
+ * bounded look-back must give up; the next b200_stream_synchronize() on
+ * `stream` returns B200_ERR_TIMEOUT.  Exercises the failure path without a
+ * GPU fault, trap or hang. */
+int b200_selftest_scan_timeout(b200_stream_t stream);
+
+/* Device properties the launch heuristics use (current device). */
+int b200_device_info(int* sm_count, int* cc_major, int* cc_minor);
+
+/* Release the scratch arenas held for every stream of the current device. */
+int b200_release_scratch(void);
+
+/* Kernel timing instrumentation: when enabled, every library kernel launch
+ * is bracketed by CUDA events on its stream; b200_prof_read() accumulates
+ * per-kernel launch counts and total milliseconds (read after a sync).
+ * Returns the number of kernel names written (at most `cap`). */
+int b200_prof_enable(int enable);
+int b200_prof_reset(void);
+int b200_prof_read(char* names, size_t name_stride, uint64_t* launches,
+                   double* total_ms, int cap);
+
+/* ======================================================================
+ * forall -- fixed-type bodies of the RAJA::forall hot loop
+ * (policy/cuda/forall.hpp:371-655, kernel forallp_cuda_kernel).  Arbitrary
+ * lambda bodies go through the templated b200_exec policy in
+ * include/raja_b200/forall.hpp; these entry points cover the loop bodies
+ * the benchmark configurations name.
+ * ====================================================================== */
+
+/* y[i] += a * x[i]  for i in [0, n) */
+int b200_forall_axpy_f64(double a, const double* x, double* y, size_t n,
+                         b200_stream_t stream);
+int b200_forall_axpy_f32(float a, const float* x, float* y, size_t n,
+                         b200_stream_t stream);
+
+/* ======================================================================
+ * Reducers -- ReduceSum / ReduceMin / ReduceMax / ReduceMinLoc /
+ * ReduceMaxLoc / ReduceBitOr / ReduceBitAnd over a contiguous array
+ * (policy/cuda/reduce.hpp:968-1378; last-block combine :133-214;
+ * expt::Reduce params policy/cuda/params/reduce.hpp:21-62).
+ *
+ * Results are the reduction of x[0..n) alone (the identity when n == 0):
+ * the reducer's init value is folded in by the caller, as RAJA's host-side
+ * final combine does (reduce.hpp:1128-1149).
+ * Sum output type is the accumulator type: double for f32/f64 inputs,
+ * the element type (two's-complement wrap-around) for integers.
+ * MinLoc/MaxLoc break ties by the lowest index, which reproduces seq_exec's
+ * first-wins rule (util/Operators.hpp:555-591); plain Min/Max do the same
+ * internally so that +0.0/-0.0 ties are bit-identical to seq_exec.
+ * ====================================================================== */
+
+int b200_reduce_sum_f32(const float* x, size_t n, int mode, double* out,
+                        b200_stream_t stream);
+int b200_reduce_sum_f64(const double* x, size_t n, int mode, double* out,
+                        b200_stream_t stream);
+int b200_reduce_sum_i32(const int32_t* x, size_t n, int mode, int32_t* out,
+                        b200_stream_t stream);
+int b200_reduce_sum_i64(const int64_t* x, size_t n, int mode, int64_t* out,
+                        b200_stream_t stream);
+int b200_reduce_sum_u32(const uint32_t* x, size_t n, int mode, uint32_t* out,
+                        b200_stream_t stream);
+int b200_reduce_sum_u64(const uint64_t* x, size_t n, int mode, uint64_t* out,
+                        b200_stream_t stream);
+
+/* dot = sum_i x[i]*y[i]  (ReduceSum of products, BASELINE configs 1 and 3) */
+int b200_dot_f32(const float* x, const float* y, size_t n, int mode,
+                 double* out, b200_stream_t stream);
+int b200_dot_f64(const double* x, const double* y, size_t n, int mode,
+                 double* out, b200_stream_t stream);
+
+int b200_reduce_min_f32(const float* x, size_t n, float* out, b200_stream_t stream);
+int b200_reduce_min_f64(const double* x, size_t n, double* out, b200_stream_t stream);
+int b200_reduce_min_i32(const int32_t* x, size_t n, int32_t* out, b200_stream_t stream);
+int b200_reduce_min_i64(const int64_t* x, size_t n, int64_t* out, b200_stream_t stream);
+int b200_reduce_min_u32(const uint32_t* x, size_t n, uint32_t* out, b200_stream_t stream);
+int b200_reduce_min_u64(const uint64_t* x, size_t n, uint64_t* out, b200_stream_t stream);
+int b200_reduce_max_f32(const float* x, size_t n, float* out, b200_stream_t stream);
+int b200_reduce_max_f64(const double* x, size_t n, double* out, b200_stream_t stream);
+int b200_reduce_max_i32(const int32_t* x, size_t n, int32_t* out, b200_stream_t stream);
+int b200_reduce_max_i64(const int64_t* x, size_t n, int64_t* out, b200_stream_t stream);
+int b200_reduce_max_u32(const uint32_t* x, size_t n, uint32_t* out, b200_stream_t stream);
+int b200_reduce_max_u64(const uint64_t* x, size_t n, uint64_t* out, b200_stream_t stream);
+
+/* (value, index) of the minimum / maximum; identity (n == 0) is
+ * (+max / lowest, -1) like ValueLoc (pattern/detail/reduce.hpp:127-179). */
+int b200_reduce_minloc_f32(const float* x, size_t n, float* val, int64_t* idx,
+                           b200_stream_t stream);
+int b200_reduce_minloc_f64(const double* x, size_t n, double* val, int64_t* idx,
+                           b200_stream_t stream);
+int b200_reduce_minloc_i32(const int32_t* x, size_t n, int32_t* val, int64_t* idx,
+                           b200_stream_t stream);
+int b200_reduce_minloc_i64(const int64_t* x, size_t n, int64_t* val, int64_t* idx,
+                           b200_stream_t stream);
+int b200_reduce_maxloc_f32(const float* x, size_t n, float* val, int64_t* idx,
+                           b200_stream_t stream);
+int b200_reduce_maxloc_f64(const double* x, size_t n, double* val, int64_t* idx,
+                           b200_stream_t stream);
+int b200_reduce_maxloc_i32(const int32_t* x, size_t n, int32_t* val, int64_t* idx,
+                           b200_stream_t stream);
+int b200_reduce_maxloc_i64(const int64_t* x, size_t n, int64_t* val, int64_t* idx,
+                           b200_stream_t stream);
+
+/* ReduceBitOr / ReduceBitAnd (pattern/detail/reduce.hpp:505-560) */
+int b200_reduce_bitor_i32(const int32_t* x, size_t n, int32_t* out, b200_stream_t stream);
+int b200_reduce_bitor_i64(const int64_t* x, size_t n, int64_t* out, b200_stream_t stream);
+int b200_reduce_bitor_u32(const uint32_t* x, size_t n, uint32_t* out, b200_stream_t stream);
+int b200_reduce_bitor_u64(const uint64_t* x, size_t n, uint64_t* out, b200_stream_t stream);
+int b200_reduce_bitand_i32(const int32_t* x, size_t n, int32_t* out, b200_stream_t stream);
+int b200_reduce_bitand_i64(const int64_t* x, size_t n, int64_t* out, b200_stream_t stream);
+int b200_reduce_bitand_u32(const uint32_t* x, size_t n, uint32_t* out, b200_stream_t stream);
+int b200_reduce_bitand_u64(const uint64_t* x, size_t n, uint64_t* out, b200_stream_t stream);
+
+/* ======================================================================
+ * Scans -- impl::scan::{inclusive, exclusive, inclusive_inplace,
+ * exclusive_inplace} (policy/cuda/scan.hpp:45-235, which forwards to
+ * cub::DeviceScan).  Single-pass decoupled look-back; `in == out` gives the
+ * in-place forms.  `op` is B200_OP_*.  Exclusive scans write `init` first
+ * (policy/sequential/scan.hpp:127-153).  Integer sums wrap around; `mode`
+ * (B200_MODE_COMPENSATED) only affects f32/f64 sums.
+ * ====================================================================== */
+
+int b200_scan_inclusive_i32(const int32_t* in, int32_t* out, size_t n, int op,
+                            b200_stream_t stream);
+int b200_scan_inclusive_i64(const int64_t* in, int64_t* out, size_t n, int op,
+                            b200_stream_t stream);
+int b200_scan_inclusive_u32(const uint32_t* in, uint32_t* out, size_t n, int op,
+                            b200_stream_t stream);
+int b200_scan_inclusive_u64(const uint64_t* in, uint64_t* out, size_t n, int op,
+                            b200_stream_t stream);
+int b200_scan_inclusive_f32(const float* in, float* out, size_t n, int op,
+                            int mode, b200_stream_t stream);
+int b200_scan_inclusive_f64(const double* in, double* out, size_t n, int op,
+                            int mode, b200_stream_t stream);
+int b200_scan_exclusive_i32(const int32_t* in, int32_t* out, size_t n, int op,
+                            int32_t init, b200_stream_t stream);
+int b200_scan_exclusive_i64(const int64_t* in, int64_t* out, size_t n, int op,
+                            int64_t init, b200_stream_t stream);
+int b200_scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, int op,
+                            uint32_t init, b200_stream_t stream);
+int b200_scan_exclusive_u64(const uint64_t* in, uint64_t* out, size_t n, int op,
+                            uint64_t init, b200_stream_t stream);
+int b200_scan_exclusive_f32(const float* in, float* out, size_t n, int op,
+                            float init, int mode, b200_stream_t stream);
+int b200_scan_exclusive_f64(const double* in, double* out, size_t n, int op,
+                            double init, int mode, b200_stream_t stream);
+
+/* ======================================================================
+ * Sorts -- impl::sort::{stable, unstable, stable_pairs, unstable_pairs}
+ * (policy/cuda/sort.hpp:92-653, which forwards to cub::DeviceRadixSort).
+ * LSD radix sort, 8-bit digits, onesweep passes.  Always stable, so it
+ * serves both sort and stable_sort.  `descending` != 0 gives
+ * operators::greater order (stable: equal keys keep input order).
+ * Floating-point keys are ordered by their IEEE bit pattern (-0.0 before
+ * +0.0; NaNs at the ends), which matches operators::less on every non-NaN,
+ * non-signed-zero input.
+ * In-place forms sort `keys` (and permute `vals`) in place.  The _copy forms
+ * read keys_in/vals_in and write keys_out/vals_out, leaving the inputs
+ * untouched.  Scratch memory comes from the library's per-stream arena.
+ * ====================================================================== */
+
+int b200_sort_keys_u32(uint32_t* keys, size_t n, int descending, b200_stream_t stream);
+int b200_sort_keys_u64(uint64_t* keys, size_t n, int descending, b200_stream_t stream);
+int b200_sort_keys_i32(int32_t* keys, size_t n, int descending, b200_stream_t stream);
+int b200_sort_keys_i64(int64_t* keys, size_t n, int descending, b200_stream_t stream);
+int b200_sort_keys_f32(float* keys, size_t n, int descending, b200_stream_t stream);
+int b200_sort_keys_f64(double* keys, size_t n, int descending, b200_stream_t stream);
+
+int b200_sort_keys_copy_u32(const uint32_t* keys_in, uint32_t* keys_out, size_t n,
+                            int descending, b200_stream_t stream);
+int b200_sort_keys_copy_u64(const uint64_t* keys_in, uint64_t* keys_out, size_t n,
+                            int descending, b200_stream_t stream);
+int b200_sort_keys_copy_f32(const float* keys_in, float* keys_out, size_t n,
+                            int descending, b200_stream_t stream);
+
+/* sort_pairs / stable_sort_pairs (pattern/sort.hpp:196-230) */
+int b200_sort_pairs_u32_i32(uint32_t* keys, int32_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_u32_u32(uint32_t* keys, uint32_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_i32_i32(int32_t* keys, int32_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_f32_i32(float* keys, int32_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_u64_i32(uint64_t* keys, int32_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_u64_i64(uint64_t* keys, int64_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_i64_i64(int64_t* keys, int64_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_f64_i64(double* keys, int64_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_f64_i32(double* keys, int32_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_copy_f32_i32(const float* keys_in, const int32_t* vals_in,
+                                 float* keys_out, int32_t* vals_out, size_t n,
+                                 int descending, b200_stream_t stream);
+int b200_sort_pairs_copy_u32_i32(const uint32_t* keys_in, const int32_t* vals_in,
+                                 uint32_t* keys_out, int32_t* vals_out, size_t n,
+                                 int descending, b200_stream_t stream);
+
+/* ======================================================================
+ * Histogram -- MultiReduceSum<cuda_multi_reduce_atomic, T> with a +1 body,
+ * i.e. the binned atomic reduction of policy/cuda/multi_reduce.hpp:80-690.
+ * counts[b] += #{ i : x[i] == b } for b in [0, nbins); values outside
+ * [0, nbins) are not counted.  `counts` is accumulated into (zero it first
+ * for a fresh histogram, as MultiReduceSum(num_bins, 0) does).
+ * ====================================================================== */
+
+int b200_histogram_i32(const int32_t* x, size_t n, int32_t nbins, uint64_t* counts,
+                       b200_stream_t stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* B200PRIMS_H */

@@ -1,0 +1,234 @@
+// Internal definitions shared by the libb200prims translation units.
+//
+// Host side: error reporting, per-device properties, per-stream scratch
+// arenas, the device status word and the launch-timing instrumentation
+// (runtime.cu).  Device side: memory-ordering helpers, bounded waits, warp
+// utilities and 16-byte vector types.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+
+#include "../../include/b200prims.h"
+
+namespace b200 {
+
+// ------------------------------------------------------------------ host
+
+// Record a failure message for b200_last_error_string() and return `code`.
+int fail(int code, const char* fmt, ...);
+// Map a CUDA error to B200_ERR_CUDA (or B200_OK for cudaSuccess).
+int cuda_check(cudaError_t e, const char* what);
+// Clear the message of the calling thread (called on success paths).
+void clear_error();
+
+struct DeviceProps {
+  int device = -1;
+  int sms = 0;
+  int cc_major = 0;
+  int cc_minor = 0;
+  int max_threads_per_sm = 0;
+  size_t smem_per_block_optin = 0;
+  size_t smem_per_sm = 0;
+};
+// Properties of the current device (cached after the first query).
+int device_props(DeviceProps* out);
+
+// Device status word of the current device: kernels OR an error code into
+// it when a bounded wait gives up; b200_stream_synchronize() reads it.
+int status_word(uint32_t** out);
+
+// Polling bound for device waits (b200_set_spin_limit).
+uint32_t spin_limit();
+
+// Per-(device, stream) scratch arena.  The returned pointer stays valid for
+// work enqueued on `stream` until the next scratch() call on that stream.
+// `zeroed_counters` points at a small region (kCounterBytes) that was
+// zeroed when the arena was created; kernels that use it must leave it
+// zeroed when they finish (self-resetting tickets).
+constexpr size_t kCounterBytes = 4096;
+int scratch(cudaStream_t stream, size_t bytes, void** out,
+            uint32_t** zeroed_counters);
+
+// Launch-timing instrumentation (b200_prof_*).
+bool prof_on();
+void prof_begin(cudaStream_t s, const char* name, void** token);
+void prof_end(cudaStream_t s, void* token);
+
+// Round x up to a multiple of a.
+inline size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Carve successive aligned sub-buffers out of one scratch allocation.
+struct Carver {
+  char* base;
+  size_t off = 0;
+  explicit Carver(void* p) : base(static_cast<char*>(p)) {}
+  template <class T>
+  T* take(size_t count) {
+    off = round_up(off, 256);
+    T* p = reinterpret_cast<T*>(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+// Size that a Carver sequence needs (same rounding as Carver::take).
+struct Sizer {
+  size_t off = 0;
+  template <class T>
+  void take(size_t count) {
+    off = round_up(off, 256);
+    off += count * sizeof(T);
+  }
+  size_t bytes() const { return round_up(off, 256); }
+};
+
+// Launch `kern` with instrumentation and error checking.
+#define B200_LAUNCH(name, kern, grid, block, smem, stream, ...)              \
+  do {                                                                       \
+    void* _b200_tok = nullptr;                                               \
+    if (::b200::prof_on()) ::b200::prof_begin((stream), (name), &_b200_tok); \
+    kern<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);                \
+    cudaError_t _b200_e = cudaGetLastError();                                \
+    if (_b200_tok) ::b200::prof_end((stream), _b200_tok);                    \
+    if (_b200_e != cudaSuccess) return ::b200::cuda_check(_b200_e, (name));  \
+  } while (0)
+
+#define B200_CUDA(call)                                          \
+  do {                                                           \
+    cudaError_t _b200_e = (call);                                \
+    if (_b200_e != cudaSuccess) return ::b200::cuda_check(_b200_e, #call); \
+  } while (0)
+
+#define B200_TRY(call)                 \
+  do {                                 \
+    int _b200_rc = (call);             \
+    if (_b200_rc != B200_OK) return _b200_rc; \
+  } while (0)
+
+// ---------------------------------------------------------------- device
+
+// Error codes ORed into the status word (bit positions name the waiter).
+constexpr uint32_t kStatusScanTimeout = 1u << 0;
+constexpr uint32_t kStatusSortTimeout = 1u << 1;
+constexpr uint32_t kStatusSegTimeout = 1u << 2;
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_acquire64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release64(uint64_t* p, uint64_t v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed64(uint64_t* p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// Shuffle an arbitrary trivially-copyable value (size multiple of 4).
+template <class T>
+__device__ __forceinline__ T shfl_xor_any(const T& v, int mask) {
+  static_assert(sizeof(T) % 4 == 0, "shuffle type size");
+  constexpr int W = sizeof(T) / 4;
+  uint32_t w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int i = 0; i < W; ++i) w[i] = __shfl_xor_sync(0xffffffffu, w[i], mask);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+template <class T>
+__device__ __forceinline__ T shfl_up_any(const T& v, int delta) {
+  static_assert(sizeof(T) % 4 == 0, "shuffle type size");
+  constexpr int W = sizeof(T) / 4;
+  uint32_t w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int i = 0; i < W; ++i) w[i] = __shfl_up_sync(0xffffffffu, w[i], delta);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+template <class T>
+__device__ __forceinline__ T shfl_idx_any(const T& v, int src) {
+  static_assert(sizeof(T) % 4 == 0, "shuffle type size");
+  constexpr int W = sizeof(T) / 4;
+  uint32_t w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int i = 0; i < W; ++i) w[i] = __shfl_sync(0xffffffffu, w[i], src);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+// 16-byte vector of element type T.
+template <class T>
+struct alignas(16) Vec16 {
+  static constexpr int N = 16 / sizeof(T);
+  T v[N];
+};
+
+template <class T>
+__device__ __forceinline__ Vec16<T> ld_vec_stream(const T* p) {
+  // Streaming read-only load: data is touched once, keep it out of L1.
+  Vec16<T> r;
+  uint4 u = __ldcs(reinterpret_cast<const uint4*>(p));
+  memcpy(&r, &u, 16);
+  return r;
+}
+template <class T>
+__device__ __forceinline__ Vec16<T> ld_vec(const T* p) {
+  Vec16<T> r;
+  uint4 u = __ldg(reinterpret_cast<const uint4*>(p));
+  memcpy(&r, &u, 16);
+  return r;
+}
+template <class T>
+__device__ __forceinline__ void st_vec(T* p, const Vec16<T>& r) {
+  uint4 u;
+  memcpy(&u, &r, 16);
+  *reinterpret_cast<uint4*>(p) = u;
+}
+template <class T>
+__device__ __forceinline__ void st_vec_stream(T* p, const Vec16<T>& r) {
+  uint4 u;
+  memcpy(&u, &r, 16);
+  __stcs(reinterpret_cast<uint4*>(p), u);
+}
+
+// Error-free transformations (Knuth TwoSum, FMA-based TwoProd).
+template <class F>
+__device__ __forceinline__ void two_sum(F a, F b, F& s, F& e) {
+  s = a + b;
+  F bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+  p = a * b;
+  e = fmaf(a, b, -p);
+}
+__device__ __forceinline__ void two_prod(double a, double b, double& p, double& e) {
+  p = a * b;
+  e = fma(a, b, -p);
+}
+
+}  // namespace b200

@@ -1,0 +1,471 @@
+// Reducers: ReduceSum / dot / Min / Max / MinLoc / MaxLoc / BitOr / BitAnd.
+//
+// Reference: policy/cuda/reduce.hpp -- per-thread accumulation inside the
+// forall body, warp-shuffle block reduce (intrinsics.hpp:383-470) and a
+// last-block grid combine driven by an atomicInc ticket
+// (reduce.hpp:133-214), followed by a host-side combine of pinned tally
+// slots (reduce.hpp:1128-1149).
+//
+// GB300 design: one streaming kernel per reduction.  The index space is cut
+// into fixed chunks of 256 threads x 64 bytes; each thread issues four
+// independent 16-byte loads per chunk (8 for dot) so that ~128 KB per SM is
+// in flight, enough to cover HBM3e latency.  Blocks are sized to fill every
+// SM (occupancy x SM count).  Each block reduces with a fixed butterfly over
+// warp shuffles and shared memory, writes one partial, and the last block to
+// take a ticket combines the partials in index order and writes the result
+// to device memory -- no host round trip, no pinned tally.
+//
+// Floating-point sums support three modes (B200_MODE_*):
+//   naive         -- accumulate in the element type (the reference's rule);
+//   compensated   -- per-thread TwoSum (Neumaier) in the element type, FP64
+//                    across blocks for FP32 input, double-double for FP64;
+//   deterministic -- one partial per fixed chunk, combined in a fixed tree:
+//                    the result depends on (n, data) only, not on the grid.
+// Min/Max(/Loc) carry the element index and break ties by the lowest index,
+// which makes them bit-identical to seq_exec's first-wins rule
+// (util/Operators.hpp:555-591, pattern/detail/reduce.hpp:127-179).
+#include <cfloat>
+#include <climits>
+#include <type_traits>
+
+#include "b200_internal.cuh"
+
+namespace b200 {
+namespace {
+
+constexpr int RBLOCK = 256;
+
+template <class T>
+struct Chunk {
+  static constexpr int VN = 16 / sizeof(T);      // elements per 16-byte vector
+  static constexpr int NV = 4;                   // vectors per thread per chunk
+  static constexpr int ITEMS = VN * NV;          // elements per thread per chunk
+  static constexpr size_t SIZE = size_t(RBLOCK) * ITEMS;
+};
+
+// Read a value written by another block in this kernel (bypass L1).
+template <class P>
+__device__ __forceinline__ P ld_cg_any(const P* p) {
+  static_assert(sizeof(P) % 4 == 0, "partial size");
+  constexpr int W = sizeof(P) / 4;
+  uint32_t w[W];
+  const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
+#pragma unroll
+  for (int i = 0; i < W; ++i) w[i] = __ldcg(q + i);
+  P r;
+  memcpy(&r, w, sizeof(P));
+  return r;
+}
+
+template <class T>
+struct Lim;
+template <> struct Lim<float> { static __device__ float hi() { return FLT_MAX; } static __device__ float lo() { return -FLT_MAX; } };
+template <> struct Lim<double> { static __device__ double hi() { return DBL_MAX; } static __device__ double lo() { return -DBL_MAX; } };
+template <> struct Lim<int32_t> { static __device__ int32_t hi() { return INT_MAX; } static __device__ int32_t lo() { return INT_MIN; } };
+template <> struct Lim<int64_t> { static __device__ int64_t hi() { return LLONG_MAX; } static __device__ int64_t lo() { return LLONG_MIN; } };
+template <> struct Lim<uint32_t> { static __device__ uint32_t hi() { return UINT_MAX; } static __device__ uint32_t lo() { return 0u; } };
+template <> struct Lim<uint64_t> { static __device__ uint64_t hi() { return ULLONG_MAX; } static __device__ uint64_t lo() { return 0ull; } };
+
+struct OutPtrs {
+  void* val;
+  int64_t* idx;
+};
+
+// ----------------------------------------------------------------- ops
+// Each op defines: T, Acc, Part, identity(), add(acc, v, i) (or add2 for
+// dot), merge(earlier, later), to_part, part_identity, merge_part, store.
+
+// Naive floating-point sum / dot: accumulate in T.
+template <class TT>
+struct SumNaive {
+  using T = TT;
+  using Acc = T;
+  using Part = T;
+  static __device__ Acc identity() { return T(0); }
+  static __device__ void add(Acc& a, T v, int64_t) { a += v; }
+  static __device__ void add2(Acc& a, T x, T y) { a = fma(x, y, a); }
+  static __device__ Acc merge(Acc a, Acc b) { return a + b; }
+  static __device__ Part to_part(Acc a) { return a; }
+  static __device__ Part part_identity() { return T(0); }
+  static __device__ Part merge_part(Part a, Part b) { return a + b; }
+  static __device__ void store(OutPtrs o, Part p) { *static_cast<double*>(o.val) = double(p); }
+};
+
+template <class T>
+struct Pair { T s, c; };
+
+// Compensated FP32 sum / dot: TwoSum per thread, FP64 across blocks.
+struct SumCompF32 {
+  using T = float;
+  using Acc = Pair<float>;
+  using Part = double;
+  static __device__ Acc identity() { return {0.f, 0.f}; }
+  static __device__ void add(Acc& a, float v, int64_t) {
+    float s, e;
+    two_sum(a.s, v, s, e);
+    a.s = s;
+    a.c += e;
+  }
+  static __device__ void add2(Acc& a, float x, float y) {
+    float p, ep, s, es;
+    two_prod(x, y, p, ep);
+    two_sum(a.s, p, s, es);
+    a.s = s;
+    a.c += ep + es;
+  }
+  static __device__ Acc merge(Acc a, Acc b) {
+    float s, e;
+    two_sum(a.s, b.s, s, e);
+    return {s, a.c + b.c + e};
+  }
+  static __device__ Part to_part(Acc a) { return double(a.s) + double(a.c); }
+  static __device__ Part part_identity() { return 0.0; }
+  static __device__ Part merge_part(Part a, Part b) { return a + b; }
+  static __device__ void store(OutPtrs o, Part p) { *static_cast<double*>(o.val) = p; }
+};
+
+// Compensated FP64 sum / dot: double-double style accumulation throughout.
+struct SumCompF64 {
+  using T = double;
+  using Acc = Pair<double>;
+  using Part = Pair<double>;
+  static __device__ Acc identity() { return {0.0, 0.0}; }
+  static __device__ void add(Acc& a, double v, int64_t) {
+    double s, e;
+    two_sum(a.s, v, s, e);
+    a.s = s;
+    a.c += e;
+  }
+  static __device__ void add2(Acc& a, double x, double y) {
+    double p, ep, s, es;
+    two_prod(x, y, p, ep);
+    two_sum(a.s, p, s, es);
+    a.s = s;
+    a.c += ep + es;
+  }
+  static __device__ Acc merge(Acc a, Acc b) {
+    double s, e;
+    two_sum(a.s, b.s, s, e);
+    return {s, a.c + b.c + e};
+  }
+  static __device__ Part to_part(Acc a) { return a; }
+  static __device__ Part part_identity() { return {0.0, 0.0}; }
+  static __device__ Part merge_part(Part a, Part b) { return merge(a, b); }
+  static __device__ void store(OutPtrs o, Part p) { *static_cast<double*>(o.val) = p.s + p.c; }
+};
+
+// Integer sum with two's-complement wrap-around.
+template <class TT>
+struct SumInt {
+  using T = TT;
+  using U = typename std::make_unsigned<T>::type;
+  using Acc = U;
+  using Part = U;
+  static __device__ Acc identity() { return U(0); }
+  static __device__ void add(Acc& a, T v, int64_t) { a += U(v); }
+  static __device__ void add2(Acc& a, T x, T y) { a += U(x) * U(y); }
+  static __device__ Acc merge(Acc a, Acc b) { return a + b; }
+  static __device__ Part to_part(Acc a) { return a; }
+  static __device__ Part part_identity() { return U(0); }
+  static __device__ Part merge_part(Part a, Part b) { return a + b; }
+  static __device__ void store(OutPtrs o, Part p) { *static_cast<T*>(o.val) = T(p); }
+};
+
+template <class T>
+struct ValIdx {
+  T v;
+  int64_t i;
+};
+
+// Min / Max with location; ties resolve to the lowest index.
+template <class TT, bool MIN, bool WITH_LOC>
+struct Extremum {
+  using T = TT;
+  using Acc = ValIdx<T>;
+  using Part = Acc;
+  static __device__ bool better(T cand, T cur) { return MIN ? (cand < cur) : (cur < cand); }
+  static __device__ Acc identity() { return {MIN ? Lim<T>::hi() : Lim<T>::lo(), -1}; }
+  static __device__ void add(Acc& a, T v, int64_t i) {
+    // Indices reach a thread in ascending order: strict comparison keeps
+    // the first occurrence.
+    if (better(v, a.v)) { a.v = v; a.i = i; }
+  }
+  static __device__ void add2(Acc&, T, T) {}
+  static __device__ Acc merge(Acc a, Acc b) {
+    if (better(b.v, a.v) || (b.v == a.v && b.i < a.i)) return b;
+    return a;
+  }
+  static __device__ Part to_part(Acc a) { return a; }
+  static __device__ Part part_identity() { return identity(); }
+  static __device__ Part merge_part(Part a, Part b) { return merge(a, b); }
+  static __device__ void store(OutPtrs o, Part p) {
+    *static_cast<T*>(o.val) = p.v;
+    if (WITH_LOC) *o.idx = p.i;
+  }
+};
+
+template <class TT, bool OR>
+struct BitOp {
+  using T = TT;
+  using Acc = T;
+  using Part = T;
+  static __device__ Acc identity() { return OR ? T(0) : T(~T(0)); }
+  static __device__ void add(Acc& a, T v, int64_t) { a = OR ? (a | v) : (a & v); }
+  static __device__ void add2(Acc&, T, T) {}
+  static __device__ Acc merge(Acc a, Acc b) { return OR ? (a | b) : (a & b); }
+  static __device__ Part to_part(Acc a) { return a; }
+  static __device__ Part part_identity() { return identity(); }
+  static __device__ Part merge_part(Part a, Part b) { return merge(a, b); }
+  static __device__ void store(OutPtrs o, Part p) { *static_cast<T*>(o.val) = p; }
+};
+
+// Fixed-shape block reduction: butterfly inside each warp, then warp 0
+// combines the warp results in warp order.  Result valid in thread 0.
+template <class X, class F>
+__device__ __forceinline__ X block_reduce(X v, X ident, F merge, X* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = merge(v, shfl_xor_any(v, o));
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = (lane < RBLOCK / 32) ? sh[lane] : ident;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = merge(v, shfl_xor_any(v, o));
+  }
+  __syncthreads();
+  return v;
+}
+
+template <class Op, bool DOT>
+__global__ void __launch_bounds__(RBLOCK)
+reduce_kernel(const typename Op::T* __restrict__ x, const typename Op::T* __restrict__ y,
+              size_t n, int vec_ok, int det, typename Op::Part* __restrict__ parts,
+              unsigned int* ticket, OutPtrs out) {
+  using T = typename Op::T;
+  using Acc = typename Op::Acc;
+  using Part = typename Op::Part;
+  using C = Chunk<T>;
+  __shared__ Acc sh_acc[32];
+  __shared__ Part sh_part[32];
+  __shared__ bool am_last;
+
+  const int tid = threadIdx.x;
+  const size_t nchunks = (n + C::SIZE - 1) / C::SIZE;
+  Acc acc = Op::identity();
+
+  for (size_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const size_t base = c * C::SIZE;
+    if (det) acc = Op::identity();
+    if (vec_ok && base + C::SIZE <= n) {
+      Vec16<T> vx[C::NV], vy[C::NV];
+#pragma unroll
+      for (int j = 0; j < C::NV; ++j) {
+        const size_t e = base + (size_t(j) * RBLOCK + tid) * C::VN;
+        vx[j] = ld_vec(x + e);
+        if (DOT) vy[j] = ld_vec(y + e);
+      }
+#pragma unroll
+      for (int j = 0; j < C::NV; ++j) {
+        const size_t e = base + (size_t(j) * RBLOCK + tid) * C::VN;
+#pragma unroll
+        for (int k = 0; k < C::VN; ++k) {
+          if (DOT) Op::add2(acc, vx[j].v[k], vy[j].v[k]);
+          else Op::add(acc, vx[j].v[k], int64_t(e + k));
+        }
+      }
+    } else {
+      // Same element-to-thread mapping as the vector path, so the
+      // deterministic mode does not depend on pointer alignment.
+#pragma unroll
+      for (int j = 0; j < C::NV; ++j) {
+        const size_t e = base + (size_t(j) * RBLOCK + tid) * C::VN;
+#pragma unroll
+        for (int k = 0; k < C::VN; ++k) {
+          if (e + k < n) {
+            if (DOT) Op::add2(acc, x[e + k], y[e + k]);
+            else Op::add(acc, x[e + k], int64_t(e + k));
+          }
+        }
+      }
+    }
+    if (det) {
+      Acc r = block_reduce(acc, Op::identity(), [](Acc a, Acc b) { return Op::merge(a, b); }, sh_acc);
+      if (tid == 0) parts[c] = Op::to_part(r);
+    }
+  }
+  if (!det) {
+    Acc r = block_reduce(acc, Op::identity(), [](Acc a, Acc b) { return Op::merge(a, b); }, sh_acc);
+    if (tid == 0) parts[blockIdx.x] = Op::to_part(r);
+  }
+
+  // Last-block combine (reduce.hpp:133-214 restated): publish, take a
+  // ticket, and let the final block fold the partials in index order.
+  if (tid == 0) {
+    __threadfence();
+    unsigned int prev = atomicAdd(ticket, 1u);
+    am_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  const size_t nparts = det ? nchunks : size_t(gridDim.x);
+  Part p = Op::part_identity();
+  for (size_t i = tid; i < nparts; i += RBLOCK) p = Op::merge_part(p, ld_cg_any(parts + i));
+  p = block_reduce(p, Op::part_identity(), [](Part a, Part b) { return Op::merge_part(a, b); }, sh_part);
+  if (tid == 0) {
+    Op::store(out, p);
+    *ticket = 0u;  // leave the ticket zeroed for the next call on this stream
+  }
+}
+
+template <class Op, bool DOT>
+int grid_for(size_t n, int* grid) {
+  static int blocks_per_sm = 0;
+  DeviceProps props;
+  B200_TRY(device_props(&props));
+  if (blocks_per_sm == 0) {
+    int b = 0;
+    B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, reduce_kernel<Op, DOT>, RBLOCK, 0));
+    blocks_per_sm = b > 0 ? b : 1;
+  }
+  const size_t nchunks = (n + Chunk<typename Op::T>::SIZE - 1) / Chunk<typename Op::T>::SIZE;
+  size_t g = size_t(props.sms) * size_t(blocks_per_sm);
+  if (g > nchunks) g = nchunks;
+  if (g < 1) g = 1;
+  *grid = int(g);
+  return B200_OK;
+}
+
+template <class Op, bool DOT>
+int run_reduce(const char* name, const typename Op::T* x, const typename Op::T* y, size_t n,
+               bool det, OutPtrs out, b200_stream_t stream) {
+  using T = typename Op::T;
+  if (!out.val) return fail(B200_ERR_ARG, "%s: null output pointer", name);
+  if (n > 0 && (!x || (DOT && !y))) return fail(B200_ERR_ARG, "%s: null input pointer", name);
+  if (n >= (size_t(1) << 40)) return fail(B200_ERR_ARG, "%s: n=%zu too large", name, n);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int grid = 1;
+  B200_TRY((grid_for<Op, DOT>(n, &grid)));
+  const size_t nchunks = (n + Chunk<T>::SIZE - 1) / Chunk<T>::SIZE;
+  const size_t nparts = det ? (nchunks > 0 ? nchunks : 1) : size_t(grid);
+  void* scr = nullptr;
+  uint32_t* counters = nullptr;
+  B200_TRY(scratch(s, nparts * sizeof(typename Op::Part), &scr, &counters));
+  const bool vec_ok = (reinterpret_cast<uintptr_t>(x) % 16 == 0) &&
+                      (!DOT || reinterpret_cast<uintptr_t>(y) % 16 == 0);
+  B200_LAUNCH(name, (reduce_kernel<Op, DOT>), grid, RBLOCK, 0, s, x, y, n, int(vec_ok),
+              int(det), static_cast<typename Op::Part*>(scr), counters, out);
+  clear_error();
+  return B200_OK;
+}
+
+template <class T>
+int sum_fp(const char* name, const T* x, const T* y, size_t n, int mode, double* out,
+           b200_stream_t stream) {
+  if (mode & ~(B200_MODE_COMPENSATED | B200_MODE_DETERMINISTIC))
+    return fail(B200_ERR_ARG, "%s: unknown mode %d", name, mode);
+  const bool det = (mode & B200_MODE_DETERMINISTIC) != 0;
+  OutPtrs o{out, nullptr};
+  if (mode & B200_MODE_COMPENSATED) {
+    using Op = typename std::conditional<std::is_same<T, float>::value, SumCompF32, SumCompF64>::type;
+    return y ? run_reduce<Op, true>(name, x, y, n, det, o, stream)
+             : run_reduce<Op, false>(name, x, y, n, det, o, stream);
+  }
+  return y ? run_reduce<SumNaive<T>, true>(name, x, y, n, det, o, stream)
+           : run_reduce<SumNaive<T>, false>(name, x, y, n, det, o, stream);
+}
+
+template <class T>
+int sum_int(const char* name, const T* x, size_t n, int mode, T* out, b200_stream_t stream) {
+  if (mode & ~(B200_MODE_COMPENSATED | B200_MODE_DETERMINISTIC))
+    return fail(B200_ERR_ARG, "%s: unknown mode %d", name, mode);
+  // Integer sums are exact modulo 2^bits in every mode.
+  return run_reduce<SumInt<T>, false>(name, x, nullptr, n, false, OutPtrs{out, nullptr}, stream);
+}
+
+}  // namespace
+}  // namespace b200
+
+using namespace b200;
+
+extern "C" {
+
+int b200_reduce_sum_f32(const float* x, size_t n, int mode, double* out, b200_stream_t s) {
+  return sum_fp<float>("b200_reduce_sum_f32", x, nullptr, n, mode, out, s);
+}
+int b200_reduce_sum_f64(const double* x, size_t n, int mode, double* out, b200_stream_t s) {
+  return sum_fp<double>("b200_reduce_sum_f64", x, nullptr, n, mode, out, s);
+}
+int b200_dot_f32(const float* x, const float* y, size_t n, int mode, double* out, b200_stream_t s) {
+  if (n > 0 && !y) return fail(B200_ERR_ARG, "b200_dot_f32: null y");
+  return sum_fp<float>("b200_dot_f32", x, y ? y : x, n, mode, out, s);
+}
+int b200_dot_f64(const double* x, const double* y, size_t n, int mode, double* out, b200_stream_t s) {
+  if (n > 0 && !y) return fail(B200_ERR_ARG, "b200_dot_f64: null y");
+  return sum_fp<double>("b200_dot_f64", x, y ? y : x, n, mode, out, s);
+}
+int b200_reduce_sum_i32(const int32_t* x, size_t n, int mode, int32_t* out, b200_stream_t s) {
+  return sum_int<int32_t>("b200_reduce_sum_i32", x, n, mode, out, s);
+}
+int b200_reduce_sum_i64(const int64_t* x, size_t n, int mode, int64_t* out, b200_stream_t s) {
+  return sum_int<int64_t>("b200_reduce_sum_i64", x, n, mode, out, s);
+}
+int b200_reduce_sum_u32(const uint32_t* x, size_t n, int mode, uint32_t* out, b200_stream_t s) {
+  return sum_int<uint32_t>("b200_reduce_sum_u32", x, n, mode, out, s);
+}
+int b200_reduce_sum_u64(const uint64_t* x, size_t n, int mode, uint64_t* out, b200_stream_t s) {
+  return sum_int<uint64_t>("b200_reduce_sum_u64", x, n, mode, out, s);
+}
+
+#define B200_MINMAX(NAME, T, MIN)                                                        \
+  int b200_reduce_##NAME(const T* x, size_t n, T* out, b200_stream_t s) {                \
+    return run_reduce<Extremum<T, MIN, false>, false>("b200_reduce_" #NAME, x, nullptr, n, \
+                                                      false, OutPtrs{out, nullptr}, s);  \
+  }
+B200_MINMAX(min_f32, float, true)
+B200_MINMAX(min_f64, double, true)
+B200_MINMAX(min_i32, int32_t, true)
+B200_MINMAX(min_i64, int64_t, true)
+B200_MINMAX(min_u32, uint32_t, true)
+B200_MINMAX(min_u64, uint64_t, true)
+B200_MINMAX(max_f32, float, false)
+B200_MINMAX(max_f64, double, false)
+B200_MINMAX(max_i32, int32_t, false)
+B200_MINMAX(max_i64, int64_t, false)
+B200_MINMAX(max_u32, uint32_t, false)
+B200_MINMAX(max_u64, uint64_t, false)
+#undef B200_MINMAX
+
+#define B200_LOC(NAME, T, MIN)                                                            \
+  int b200_reduce_##NAME(const T* x, size_t n, T* val, int64_t* idx, b200_stream_t s) {   \
+    if (!idx) return fail(B200_ERR_ARG, "b200_reduce_" #NAME ": null index pointer");      \
+    return run_reduce<Extremum<T, MIN, true>, false>("b200_reduce_" #NAME, x, nullptr, n,  \
+                                                     false, OutPtrs{val, idx}, s);        \
+  }
+B200_LOC(minloc_f32, float, true)
+B200_LOC(minloc_f64, double, true)
+B200_LOC(minloc_i32, int32_t, true)
+B200_LOC(minloc_i64, int64_t, true)
+B200_LOC(maxloc_f32, float, false)
+B200_LOC(maxloc_f64, double, false)
+B200_LOC(maxloc_i32, int32_t, false)
+B200_LOC(maxloc_i64, int64_t, false)
+#undef B200_LOC
+
+#define B200_BIT(NAME, T, OR)                                                             \
+  int b200_reduce_##NAME(const T* x, size_t n, T* out, b200_stream_t s) {                 \
+    return run_reduce<BitOp<T, OR>, false>("b200_reduce_" #NAME, x, nullptr, n, false,     \
+                                           OutPtrs{out, nullptr}, s);                     \
+  }
+B200_BIT(bitor_i32, int32_t, true)
+B200_BIT(bitor_i64, int64_t, true)
+B200_BIT(bitor_u32, uint32_t, true)
+B200_BIT(bitor_u64, uint64_t, true)
+B200_BIT(bitand_i32, int32_t, false)
+B200_BIT(bitand_i64, int64_t, false)
+B200_BIT(bitand_u32, uint32_t, false)
+B200_BIT(bitand_u64, uint64_t, false)
+#undef B200_BIT
+
+}  // extern "C"

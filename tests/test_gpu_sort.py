@@ -1,0 +1,118 @@
+"""Radix sort through the C ABI vs the oracle's stable sorts: keys and
+values bit-exact (the radix sort is stable, so unstable sort is checked
+exactly too, which implies the reference's per-key multiset rule)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+SIZES = [0, 1, 2, 3, 100, 4095, 4096, 4097, 8193, 100003, (1 << 20) + 5]
+
+
+def test_golden_sort(prims):
+    g = np.load(os.path.join(G, "sort.npz"))
+    k, v = to_dev(g["ku"]), to_dev(np.arange(g["ku"].size, dtype=np.int32))
+    prims.sort_pairs(k, v)
+    np.testing.assert_array_equal(to_host(k), g["ku_sorted"])
+    np.testing.assert_array_equal(to_host(v), g["ku_perm"])
+    k, v = to_dev(g["kf"]), to_dev(np.arange(g["kf"].size, dtype=np.int32))
+    prims.sort_pairs(k, v)
+    np.testing.assert_array_equal(to_host(k), g["kf_sorted"])
+    np.testing.assert_array_equal(to_host(v), g["kf_perm"])
+    k = to_dev(g["k64"])
+    prims.sort(k)
+    np.testing.assert_array_equal(to_host(k), g["k64_sorted"])
+    k = to_dev(g["k64"])
+    prims.sort(k, descending=True)
+    np.testing.assert_array_equal(to_host(k), g["k64_desc"])
+    for desc, ks, ps in ((False, "kd_sorted", "kd_perm"), (True, "kd_desc", "kd_desc_perm")):
+        k, v = to_dev(g["kd"]), to_dev(np.arange(g["kd"].size, dtype=np.int32))
+        prims.sort_pairs(k, v, descending=desc)
+        np.testing.assert_array_equal(to_host(k), g[ks])
+        np.testing.assert_array_equal(to_host(v), g[ps])
+
+
+def _keys(kt, n, seed, dup=False):
+    rng = np.random.default_rng(seed)
+    if dup:
+        return rng.integers(-n, n + 1, n).astype(kt) if np.dtype(kt).kind != "u" else \
+            rng.integers(0, 2 * n + 1, n).astype(kt)
+    if np.dtype(kt).kind == "f":
+        return rng.normal(0, 1, n).astype(kt)
+    info = np.iinfo(kt)
+    if info.bits == 64:
+        return rng.integers(0, 2 ** 64, n, dtype=np.uint64).view(kt) if kt == np.int64 else \
+            rng.integers(0, 2 ** 64, n, dtype=np.uint64)
+    return rng.integers(info.min, info.max, n, dtype=np.int64).astype(kt)
+
+
+@pytest.mark.parametrize("kt", [np.uint32, np.int32, np.float32, np.uint64, np.int64, np.float64])
+def test_sort_keys_bit_exact(prims, orc, kt):
+    for i, n in enumerate(SIZES):
+        for dup in (False, True):
+            x = _keys(kt, n, 7 * i + dup, dup)
+            for desc in (False, True):
+                d = to_dev(x)
+                prims.sort(d, descending=desc)
+                np.testing.assert_array_equal(to_host(d), orc.sort(x, descending=desc),
+                                              err_msg=f"n={n} dup={dup} desc={desc}")
+
+
+PAIRS = [(np.uint32, np.int32), (np.uint32, np.uint32), (np.int32, np.int32),
+         (np.float32, np.int32), (np.uint64, np.int32), (np.uint64, np.int64),
+         (np.int64, np.int64), (np.float64, np.int64), (np.float64, np.int32)]
+
+
+@pytest.mark.parametrize("kt,vt", PAIRS)
+def test_sort_pairs_stable_bit_exact(prims, orc, kt, vt):
+    for i, n in enumerate(SIZES):
+        x = _keys(kt, n, 11 * i, dup=(i % 2 == 1))
+        v = np.arange(n).astype(vt)
+        for desc in (False, True):
+            dk, dv = to_dev(x), to_dev(v)
+            prims.sort_pairs(dk, dv, descending=desc)
+            ek, ev = orc.sort_pairs(x, v, descending=desc)
+            np.testing.assert_array_equal(to_host(dk), ek, err_msg=f"n={n} desc={desc}")
+            np.testing.assert_array_equal(to_host(dv), ev, err_msg=f"n={n} desc={desc}")
+
+
+def test_special_values_and_patterns(prims, orc):
+    # infinities, extremes, sorted / reverse-sorted / constant inputs
+    f = np.array([np.inf, -np.inf, 1.0, -1.0, 3.4e38, -3.4e38, 1e-45, -1e-45, 0.0] * 1000,
+                 dtype=np.float32)
+    for desc in (False, True):
+        d = to_dev(f)
+        prims.sort(d, descending=desc)
+        np.testing.assert_array_equal(to_host(d), orc.sort(f, descending=desc))
+    for x in (np.arange(100000, dtype=np.uint32), np.arange(100000, dtype=np.uint32)[::-1].copy(),
+              np.full(100000, 7, dtype=np.uint32)):
+        v = np.arange(x.size, dtype=np.int32)
+        dk, dv = to_dev(x), to_dev(v)
+        prims.sort_pairs(dk, dv)
+        ek, ev = orc.sort_pairs(x, v)
+        np.testing.assert_array_equal(to_host(dk), ek)
+        np.testing.assert_array_equal(to_host(dv), ev)
+
+
+def test_copy_forms_leave_input(prims, orc):
+    import torch
+    x = _keys(np.uint32, 300007, 5)
+    d = to_dev(x)
+    out = torch.empty_like(d)
+    prims.sort_copy(d, out)
+    np.testing.assert_array_equal(to_host(d), x)
+    np.testing.assert_array_equal(to_host(out), np.sort(x))
+    kf = _keys(np.float32, 300007, 6)
+    v = np.arange(kf.size, dtype=np.int32)
+    dk, dv = to_dev(kf), to_dev(v)
+    ok, ov = torch.empty_like(dk), torch.empty_like(dv)
+    prims.sort_pairs_copy(dk, dv, ok, ov, descending=True)
+    ek, ev = orc.sort_pairs(kf, v, descending=True)
+    np.testing.assert_array_equal(to_host(ok), ek)
+    np.testing.assert_array_equal(to_host(ov), ev)
+    np.testing.assert_array_equal(to_host(dk), kf)
