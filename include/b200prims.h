@@ -302,6 +302,65 @@ int b200_sort_pairs_copy_u32_i32(const uint32_t* keys_in, const int32_t* vals_in
 int b200_histogram_i32(const int32_t* x, size_t n, int32_t nbins, uint64_t* counts,
                        b200_stream_t stream);
 
+/* ======================================================================
+ * Batched loops -- WorkPool/WorkGroup with many uneven loops
+ * (pattern/WorkGroup.hpp:207-530; CUDA runners
+ * policy/cuda/WorkGroup/WorkRunner.hpp:38-407, which launch once per loop
+ * (ordered) or once with an average-length grid and no reducer support
+ * (unordered, :323-329)), IndexSet segments (policy/cuda/forall.hpp:675-706)
+ * and segmented scan / sort (no RAJA counterpart: the reference composition
+ * is one scan or sort call per segment).
+ *
+ * A plan is built once from the host array of loop lengths, like
+ * WorkPool::instantiate (pattern/WorkGroup.hpp:459-487).  Loop i covers
+ * indices [0, lens[i]); for the segmented primitives, segment i covers
+ * [offsets[i], offsets[i+1]) of one flattened array, offsets being the
+ * prefix sums of lens.  A plan belongs to the device current at creation.
+ * ====================================================================== */
+typedef struct b200_batch_plan_s* b200_batch_plan;
+
+int b200_batch_plan_create(const int64_t* lens_host, int nloops, b200_batch_plan* out);
+int b200_batch_plan_destroy(b200_batch_plan plan);
+int b200_batch_plan_info(b200_batch_plan plan, int64_t* total, int64_t* ntiles, int* tile,
+                         int* block);
+/* device array of the nloops+1 segment offsets */
+const int64_t* b200_batch_plan_offsets(b200_batch_plan plan);
+
+/* Every loop i: y_i[j] += a * x_i[j]; sums[i] = sum_j y_i[j] (after the
+ * update), for all loops in one persistent launch.  xs, ys: device arrays
+ * of nloops device pointers; sums: device array of nloops doubles.
+ * mode: B200_MODE_COMPENSATED for TwoSum partials (else naive FP32
+ * partials); the per-loop fold is always in tile order (deterministic). */
+int b200_batched_axpy_sum_f32(b200_batch_plan plan, float a, const float* const* xs,
+                              float* const* ys, double* sums, int mode, b200_stream_t stream);
+/* Time the kernel variants (block size x items per thread) on this plan and
+ * keep the fastest for later calls.  Runs the loops several times: y is
+ * updated by every run. */
+int b200_batch_autotune_axpy_sum_f32(b200_batch_plan plan, float a, const float* const* xs,
+                                     float* const* ys, double* sums, int mode,
+                                     b200_stream_t stream);
+/* One loop: the fused axpy + sum of a single loop (one launch per loop is
+ * what the ordered WorkGroup runner does). */
+int b200_loop_axpy_sum_f32(float a, const float* x, float* y, size_t n, double* sum, int mode,
+                           b200_stream_t stream);
+
+/* Segmented sum scans of int32 over the plan's segments (restart at each
+ * segment; exclusive writes 0 at each head). */
+int b200_segmented_scan_inclusive_i32(b200_batch_plan plan, const int32_t* in, int32_t* out,
+                                      b200_stream_t stream);
+int b200_segmented_scan_exclusive_i32(b200_batch_plan plan, const int32_t* in, int32_t* out,
+                                      b200_stream_t stream);
+/* Sort the keys of every segment independently, in place. */
+int b200_segmented_sort_keys_u32(b200_batch_plan plan, uint32_t* keys, int descending,
+                                 b200_stream_t stream);
+
+/* ---- CUDA graph capture of repeated sweeps (replaces per-call launches) */
+typedef struct b200_graph_s* b200_graph;
+int b200_graph_capture_begin(b200_stream_t stream);
+int b200_graph_capture_end(b200_stream_t stream, b200_graph* out);
+int b200_graph_launch(b200_graph graph, b200_stream_t stream);
+int b200_graph_destroy(b200_graph graph);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

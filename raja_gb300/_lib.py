@@ -77,6 +77,22 @@ def _signatures() -> dict[str, tuple]:
         sig[f"b200_sort_pairs_{kv}"] = (_I, [_P, _P, _SZ, _I, _P])
     for kv in ("f32_i32", "u32_i32"):
         sig[f"b200_sort_pairs_copy_{kv}"] = (_I, [_P, _P, _P, _P, _SZ, _I, _P])
+    sig.update({
+        "b200_batch_plan_create": (_I, [_P, _I, _P]),
+        "b200_batch_plan_destroy": (_I, [_P]),
+        "b200_batch_plan_info": (_I, [_P, _P, _P, _P, _P]),
+        "b200_batch_plan_offsets": (_P, [_P]),
+        "b200_batched_axpy_sum_f32": (_I, [_P, C.c_float, _P, _P, _P, _I, _P]),
+        "b200_batch_autotune_axpy_sum_f32": (_I, [_P, C.c_float, _P, _P, _P, _I, _P]),
+        "b200_loop_axpy_sum_f32": (_I, [C.c_float, _P, _P, _SZ, _P, _I, _P]),
+        "b200_segmented_scan_inclusive_i32": (_I, [_P, _P, _P, _P]),
+        "b200_segmented_scan_exclusive_i32": (_I, [_P, _P, _P, _P]),
+        "b200_segmented_sort_keys_u32": (_I, [_P, _P, _I, _P]),
+        "b200_graph_capture_begin": (_I, [_P]),
+        "b200_graph_capture_end": (_I, [_P, _P]),
+        "b200_graph_launch": (_I, [_P, _P]),
+        "b200_graph_destroy": (_I, [_P]),
+    })
     return sig
 
 

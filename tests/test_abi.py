@@ -13,7 +13,7 @@ HEADER = os.path.join(ROOT, "include", "b200prims.h")
 def declared_functions():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^\s*(?:int|const char\*)\s+(b200_\w+)\s*\(", src, flags=re.M)
+    names = re.findall(r"^\s*(?:int|const char\*|const int64_t\*)\s+(b200_\w+)\s*\(", src, flags=re.M)
     assert len(names) > 60
     return names
 
