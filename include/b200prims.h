@@ -174,6 +174,19 @@ int b200_reduce_max_i64(const int64_t* x, size_t n, int64_t* out, b200_stream_t 
 int b200_reduce_max_u32(const uint32_t* x, size_t n, uint32_t* out, b200_stream_t stream);
 int b200_reduce_max_u64(const uint64_t* x, size_t n, uint64_t* out, b200_stream_t stream);
 
+/* Allocation-free variant of b200_reduce_sum_f64 for callers that cannot
+ * let a library allocate device memory (a host whose own memory manager
+ * owns all of the GPU's memory; a latency-critical loop that cannot afford
+ * allocator calls).  It has no counterpart in the reference.  Its scratch
+ * is one static 128 KB device array per GPU, resident until the process
+ * exits: it calls no cudaMalloc or cudaFree.  The first call on a device
+ * looks up that array's device address (make that first call before any
+ * stream capture).  Deterministic mode accepts n <= 16,777,216 and returns
+ * B200_ERR_ARG beyond; the other modes take any n.  All calls on a device
+ * share the array, so calls that overlap on the GPU race. */
+int b200_reduce_sum_f64_noalloc(const double* x, size_t n, int mode, double* out,
+                                b200_stream_t stream);
+
 /* (value, index) of the minimum / maximum; identity (n == 0) is
  * (+max / lowest, -1) like ValueLoc (pattern/detail/reduce.hpp:127-179). */
 int b200_reduce_minloc_f32(const float* x, size_t n, float* val, int64_t* idx,

@@ -54,6 +54,7 @@ def _signatures() -> dict[str, tuple]:
         "b200_forall_axpy_f64": (_I, [C.c_double, _P, _P, _SZ, _P]),
         "b200_forall_axpy_f32": (_I, [C.c_float, _P, _P, _SZ, _P]),
         "b200_histogram_i32": (_I, [_P, _SZ, C.c_int32, _P, _P]),
+        "b200_reduce_sum_f64_noalloc": (_I, [_P, _SZ, _I, _P, _P]),
     }
     for t in ("f32", "f64", "i32", "i64", "u32", "u64"):
         sig[f"b200_reduce_sum_{t}"] = (_I, [_P, _SZ, _I, _P, _P])

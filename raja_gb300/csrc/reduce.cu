@@ -26,6 +26,7 @@
 // (util/Operators.hpp:555-591, pattern/detail/reduce.hpp:127-179).
 #include <cfloat>
 #include <climits>
+#include <mutex>
 #include <type_traits>
 
 #include "b200_internal.cuh"
@@ -469,3 +470,95 @@ B200_BIT(bitand_u64, uint64_t, false)
 #undef B200_BIT
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free FP64 sum.
+//
+// Some callers cannot let a library allocate device memory.  A host whose
+// memory manager owns the whole GPU -- it reserves all of HBM up front and
+// hands out slices itself -- has no room for a second allocator.  A
+// latency-critical loop cannot afford the allocator calls, which may
+// synchronise the device.  b200_reduce_sum_f64_noalloc serves both: it is
+// b200_reduce_sum_f64 with its scratch (the per-block partials and the
+// completion ticket) taken from the file-scope device array below instead
+// of the per-stream arena.  The caller still passes the input and the
+// output.  It calls no cudaMalloc, cudaFree or other allocating routine.
+//
+// Limits: the array holds kNoAllocParts partials of up to 16 bytes.  The
+// naive and compensated modes use one partial per block and fit on any
+// GPU; the deterministic mode uses one partial per 2048-element chunk, so
+// it accepts n <= kNoAllocParts * 2048 and rejects larger n.
+//
+// The array exists once per GPU that loads the library and stays resident
+// until the process exits.  Every call on that GPU shares it and it keeps
+// the last call's contents, so the ticket is cleared before each launch.
+// Calls that overlap on the GPU (issued on different streams without
+// ordering between them) race on the array and give wrong results.
+namespace {
+constexpr size_t kNoAllocParts = 8192;
+constexpr size_t kNoAllocPartBytes = kNoAllocParts * 16;
+constexpr size_t kNoAllocBytes = kNoAllocPartBytes + 256;  // partials, then the ticket
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {};
+
+// Device address of g_noalloc_scratch on the current device.  In host code
+// the symbol is only a stand-in, so its address is looked up once per
+// device (with that device current) on the first call there.
+int noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  B200_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(B200_ERR_ARG, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_check(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_addr[dev] = p;
+  }
+  *out = static_cast<unsigned char*>(g_noalloc_addr[dev]);
+  return B200_OK;
+}
+
+template <class Op>
+int run_reduce_noalloc(const char* name, const double* x, size_t n, bool det, double* out,
+                       b200_stream_t stream) {
+  if (!out) return fail(B200_ERR_ARG, "%s: null output pointer", name);
+  if (n > 0 && !x) return fail(B200_ERR_ARG, "%s: null input pointer", name);
+  const size_t chunk = Chunk<double>::SIZE;
+  const size_t nchunks = (n + chunk - 1) / chunk;
+  if (det && nchunks > kNoAllocParts)
+    return fail(B200_ERR_ARG,
+                "%s: n=%zu exceeds the deterministic-mode maximum of %zu elements "
+                "(%zu partials of static scratch)",
+                name, n, kNoAllocParts * chunk, kNoAllocParts);
+  int grid = 1;
+  B200_TRY((grid_for<Op, false>(n, &grid)));
+  if (size_t(grid) > kNoAllocParts) grid = int(kNoAllocParts);
+  unsigned char* base = nullptr;
+  B200_TRY(noalloc_scratch(&base));
+  auto* parts = reinterpret_cast<typename Op::Part*>(base);
+  auto* ticket = reinterpret_cast<unsigned int*>(base + kNoAllocPartBytes);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  B200_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));
+  const bool vec_ok = reinterpret_cast<uintptr_t>(x) % 16 == 0;
+  B200_LAUNCH(name, (reduce_kernel<Op, false>), grid, RBLOCK, 0, s, x, x, n, int(vec_ok), int(det),
+              parts, ticket, OutPtrs{out, nullptr});
+  clear_error();
+  return B200_OK;
+}
+}  // namespace
+
+extern "C" int b200_reduce_sum_f64_noalloc(const double* x, size_t n, int mode, double* out,
+                                           b200_stream_t stream) {
+  const char* name = "b200_reduce_sum_f64_noalloc";
+  if (mode & ~(B200_MODE_COMPENSATED | B200_MODE_DETERMINISTIC))
+    return fail(B200_ERR_ARG, "%s: unknown mode %d", name, mode);
+  const bool det = (mode & B200_MODE_DETERMINISTIC) != 0;
+  if (mode & B200_MODE_COMPENSATED) return run_reduce_noalloc<SumCompF64>(name, x, n, det, out, stream);
+  return run_reduce_noalloc<SumNaive<double>>(name, x, n, det, out, stream);
+}
