@@ -313,6 +313,7 @@ def main():
     ap.add_argument("--cpu-log2n", type=int, default=22)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -410,6 +411,17 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = run_cpu_baseline(args)
+    extras = {}
+    if not args.no_extras:
+        del inputs, outs
+        torch.cuda.empty_cache()
+        for nm, fn in (("batched_workgroup_cfg4", bench_batched), ("jacobi_cfg5", bench_jacobi),
+                       ("accuracy_cfg3", bench_accuracy)):
+            try:
+                extras[nm] = fn(lib)
+            except Exception as e:  # report, do not lose the headline line
+                extras[nm] = {"error": f"{type(e).__name__}: {e}"}
+            torch.cuda.empty_cache()
 
     if rank == 0:
         line = {
@@ -426,10 +438,293 @@ def main():
             "gpu_launches": launches_per_step * args.steps if launches_per_step else None,
             "gpu_launches_per_step": launches_per_step,
             "clocks": clk,
+            "extras": extras,
         }
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------ extra configs
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def bench_accuracy(lib, seed=3):
+    """Ill-conditioned FP32 sums / dots / scans at N=2^28: naive FP32,
+    compensated FP32 and FP64 against the exact long accumulator."""
+    import numpy as np
+    import torch
+
+    import oracle
+    n = 1 << 28
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+
+    def illcond():
+        sign = torch.randint(0, 2, (n,), generator=g, device="cuda", dtype=torch.int8).float() * 2 - 1
+        mag = torch.exp(torch.randn(n, generator=g, device="cuda") * 6.0).clamp_(1e-8, 1e8)
+        return (sign * mag).float()
+
+    x = illcond()
+    y = illcond()
+    s = torch.cuda.current_stream().cuda_stream
+    out = torch.zeros(4, dtype=torch.float64, device="cuda")
+    xh = x.cpu().numpy()
+    yh = y.cpu().numpy()
+    ex, exlo = oracle.exact_sum(xh)
+    cond = oracle.exact_abs_sum_f32(xh) / abs(ex) if ex else float("inf")
+    res = {"n": n, "cond_sum": cond}
+    x64 = x.double()
+    for nm, call in (("naive_f32", lambda: lib.b200_reduce_sum_f32(x.data_ptr(), n, 0, out.data_ptr(), s)),
+                     ("comp_f32", lambda: lib.b200_reduce_sum_f32(x.data_ptr(), n, 1, out.data_ptr(), s)),
+                     ("naive_f64", lambda: lib.b200_reduce_sum_f64(x64.data_ptr(), n, 0, out.data_ptr(), s))):
+        assert call() == 0
+        torch.cuda.synchronize()
+        v = out[0].item()
+        res[f"sum_rel_err_{nm}"] = abs((v - ex) - exlo) / abs(ex)
+    # dot with an independent copy
+    dx, dlo = oracle.exact_dot(xh, yh)
+    y64 = y.double()
+    for nm, call in (("naive_f32", lambda: lib.b200_dot_f32(x.data_ptr(), y.data_ptr(), n, 0, out.data_ptr(), s)),
+                     ("comp_f32", lambda: lib.b200_dot_f32(x.data_ptr(), y.data_ptr(), n, 1, out.data_ptr(), s)),
+                     ("naive_f64", lambda: lib.b200_dot_f64(x64.data_ptr(), y64.data_ptr(), n, 0, out.data_ptr(), s))):
+        assert call() == 0
+        torch.cuda.synchronize()
+        v = out[0].item()
+        res[f"dot_rel_err_{nm}"] = abs((v - dx) - dlo) / abs(dx)
+    # inclusive scan: max error over prefixes, relative to sum|x| so far
+    ref = oracle.dd_scan_f32(xh[: 1 << 26])
+    absp = np.cumsum(np.abs(xh[: 1 << 26].astype(np.float64)))
+    xs = x[: 1 << 26].contiguous()
+    o = torch.empty_like(xs)
+    for nm, mode in (("naive_f32", 0), ("comp_f32", 1)):
+        assert lib.b200_scan_inclusive_f32(xs.data_ptr(), o.data_ptr(), xs.numel(), 0, mode, s) == 0
+        torch.cuda.synchronize()
+        got = o.cpu().numpy().astype(np.float64)
+        res[f"scan_maxerr_over_abs_{nm}"] = float(np.max(np.abs(got - ref) / absp))
+    o64 = torch.empty(xs.numel(), dtype=torch.float64, device="cuda")
+    xs64 = xs.double()
+    assert lib.b200_scan_inclusive_f64(xs64.data_ptr(), o64.data_ptr(), xs.numel(), 0, 0, s) == 0
+    torch.cuda.synchronize()
+    res["scan_maxerr_over_abs_naive_f64"] = float(np.max(np.abs(o64.cpu().numpy() - ref) / absp))
+    res["scan_n"] = 1 << 26
+    res["comp_f32_no_worse_than_naive_f64"] = bool(
+        res["sum_rel_err_comp_f32"] <= res["sum_rel_err_naive_f64"] * 1.0000001 + 1e-300)
+    return res
+
+
+def bench_batched(lib, reps=5, seed=4):
+    """4096 uneven loops (lognormal median 2000, sigma 1.5, clipped to
+    [32, 2^20]): fp32 axpy + per-loop ReduceSum, one persistent autotuned
+    launch (and a CUDA graph of it) against one launch per loop."""
+    import numpy as np
+    import torch
+
+    import raja_gb300 as rg
+    rng = np.random.default_rng(seed)
+    lens = np.clip(np.round(np.exp(rng.normal(np.log(2000), 1.5, 4096))), 32, 1 << 20).astype(np.int64)
+    total = int(lens.sum())
+    x = torch.rand(total, device="cuda") * 2 - 1
+    y = torch.rand(total, device="cuda") * 2 - 1
+    offs = np.concatenate([[0], np.cumsum(lens)])
+    px = torch.tensor([x.data_ptr() + 4 * int(o) for o in offs[:-1]], dtype=torch.int64, device="cuda")
+    py = torch.tensor([y.data_ptr() + 4 * int(o) for o in offs[:-1]], dtype=torch.int64, device="cuda")
+    sums = torch.zeros(len(lens), dtype=torch.float64, device="cuda")
+    plan = rg.BatchPlan(lens)
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+    rg.batched_axpy_sum(plan, 1e-3, px, py, sums, autotune=True)
+    info = plan.info()
+
+    def plain():
+        for i, n in enumerate(lens):
+            o = int(offs[i])
+            lib.b200_loop_axpy_sum_f32(1e-3, x.data_ptr() + 4 * o, y.data_ptr() + 4 * o, int(n),
+                                       sums.data_ptr() + 8 * i, 1, s)
+
+    def batched():
+        lib.b200_batched_axpy_sum_f32(plan.handle, 1e-3, px.data_ptr(), py.data_ptr(),
+                                      sums.data_ptr(), 1, s)
+
+    out = {"loops": len(lens), "total_elems": total, "tile": info["tile"], "block": info["block"]}
+    for nm, fn in (("plain_per_loop", plain), ("batched_persistent", batched)):
+        fn()
+        torch.cuda.synchronize()
+        a, b = _events()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        out[nm + "_ms"] = round(a.elapsed_time(b) / reps, 4)
+    # graph of `reps` batched sweeps
+    cs = torch.cuda.Stream()
+    with torch.cuda.stream(cs):
+        gph = rg.Graph(cs)
+        with gph:
+            for _ in range(reps):
+                lib.b200_batched_axpy_sum_f32(plan.handle, 1e-3, px.data_ptr(), py.data_ptr(),
+                                              sums.data_ptr(), 1, cs.cuda_stream)
+        gph.launch()
+        cs.synchronize()
+        a, b = _events()
+        a.record(cs)
+        gph.launch()
+        b.record(cs)
+        cs.synchronize()
+        out["batched_graph_ms"] = round(a.elapsed_time(b) / reps, 4)
+        gph.close()
+    out["speedup_batched_vs_plain"] = round(out["plain_per_loop_ms"] / out["batched_persistent_ms"], 2)
+    out["speedup_graph_vs_plain"] = round(out["plain_per_loop_ms"] / out["batched_graph_ms"], 2)
+    out["batched_gbs"] = round(12 * total / out["batched_graph_ms"] / 1e6, 1)
+    # per-loop sum error (compensated FP32) vs naive FP64 over the same y
+    import oracle
+    yh = y.cpu().numpy()
+    sh = sums.cpu().numpy()
+    worst_c, worst_d = 0.0, 0.0
+    for i in range(0, len(lens), 64):
+        seg = yh[offs[i]:offs[i + 1]]
+        ex, lo = oracle.exact_sum(seg)
+        d = oracle.reduce_sum(seg.astype(np.float64))
+        den = float(np.abs(seg.astype(np.float64)).sum()) or 1.0
+        worst_c = max(worst_c, abs((sh[i] - ex) - lo) / den)
+        worst_d = max(worst_d, abs((d - ex) - lo) / den)
+    out["sum_err_over_abs_comp_f32"] = worst_c
+    out["sum_err_over_abs_naive_f64_seq"] = worst_d
+    # segmented scan (int32) and sort (u32) over 10,000 Pareto(1.5) segments
+    seg = np.minimum(np.floor(32 * (1 - rng.random(10000)) ** (-1 / 1.5)), 1 << 20).astype(np.int64)
+    splan = rg.BatchPlan(seg)
+    st = splan.total
+    v = torch.randint(0, 1 << 20, (st,), device="cuda", dtype=torch.int32)
+    o = torch.empty_like(v)
+    k = torch.randint(-2 ** 31, 2 ** 31, (st,), device="cuda", dtype=torch.int32)
+    kk = k.clone()
+    soffs = splan.offsets
+
+    def segscan():
+        lib.b200_segmented_scan_inclusive_i32(splan.handle, v.data_ptr(), o.data_ptr(), s)
+
+    def segscan_plain():
+        for i in range(len(seg)):
+            a0, n0 = int(soffs[i]), int(seg[i])
+            lib.b200_scan_inclusive_i32(v.data_ptr() + 4 * a0, o.data_ptr() + 4 * a0, n0, 0, s)
+
+    def segsort():
+        kk.copy_(k)
+        lib.b200_segmented_sort_keys_u32(splan.handle, kk.data_ptr(), 0, s)
+
+    def segsort_plain():
+        kk.copy_(k)
+        for i in range(len(seg)):
+            a0, n0 = int(soffs[i]), int(seg[i])
+            lib.b200_sort_keys_u32(kk.data_ptr() + 4 * a0, n0, 0, s)
+
+    out["segments"] = len(seg)
+    out["segment_elems"] = int(st)
+    for nm, fn in (("segscan_one_launch", segscan), ("segscan_per_segment", segscan_plain),
+                   ("segsort_batched", segsort), ("segsort_per_segment", segsort_plain)):
+        fn()
+        torch.cuda.synchronize()
+        a, b = _events()
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        out[nm + "_ms"] = round(a.elapsed_time(b), 4)
+    plan.close()
+    splan.close()
+    return out
+
+
+def bench_jacobi(lib, sweeps=20, seed=5):
+    """256 fp64 meshes with edges in {16..128}, 20 Jacobi 7-point sweeps
+    with a per-mesh max residual: per-mesh launches vs one fused launch per
+    sweep vs a CUDA graph of the 20 fused sweeps; plus one 512^3 mesh."""
+    import numpy as np
+    import torch
+
+    import raja_gb300 as rg
+    rng = np.random.default_rng(seed)
+    shapes = [tuple(int(v) for v in r) for r in rng.integers(16, 129, (256, 3))]
+    plan = rg.JacobiPlan(shapes)
+    u = torch.rand(plan.total, dtype=torch.float64, device="cuda")
+    un = u.clone()
+    res = torch.zeros(sweeps * len(shapes), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+    offs = plan.offsets
+
+    def plain():
+        for sw in range(sweeps):
+            src, dst = (u, un) if sw % 2 == 0 else (un, u)
+            for m, (a0, b0, c0) in enumerate(shapes):
+                o = int(offs[m])
+                lib.b200_jacobi_mesh_sweep_f64(a0, b0, c0, src.data_ptr() + 8 * o, dst.data_ptr() + 8 * o, None,
+                                               res.data_ptr() + 8 * (sw * len(shapes) + m), s)
+
+    def fused():
+        for sw in range(sweeps):
+            src, dst = (u, un) if sw % 2 == 0 else (un, u)
+            lib.b200_jacobi_sweep_f64(plan.handle, src.data_ptr(), dst.data_ptr(), None,
+                                      res.data_ptr() + 8 * sw * len(shapes), s)
+
+    out = {"meshes": len(shapes), "sweeps": sweeps, "interior_points": plan.interior_points()}
+    for nm, fn in (("plain_per_mesh", plain), ("fused", fused)):
+        fn()
+        torch.cuda.synchronize()
+        a, b = _events()
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        out[nm + "_ms"] = round(a.elapsed_time(b), 4)
+    cs = torch.cuda.Stream()
+    with torch.cuda.stream(cs):
+        gph = rg.Graph(cs)
+        with gph:
+            for sw in range(sweeps):
+                src, dst = (u, un) if sw % 2 == 0 else (un, u)
+                lib.b200_jacobi_sweep_f64(plan.handle, src.data_ptr(), dst.data_ptr(), None,
+                                          res.data_ptr() + 8 * sw * len(shapes), cs.cuda_stream)
+        gph.launch()
+        cs.synchronize()
+        a, b = _events()
+        a.record(cs)
+        gph.launch()
+        b.record(cs)
+        cs.synchronize()
+        out["fused_graph_ms"] = round(a.elapsed_time(b), 4)
+        gph.close()
+    out["speedup_graph_vs_plain"] = round(out["plain_per_mesh_ms"] / out["fused_graph_ms"], 2)
+    out["fused_gbs_16B_per_point"] = round(16 * out["interior_points"] * sweeps / out["fused_graph_ms"] / 1e6, 1)
+    plan.close()
+    del u, un
+    # one 512^3 mesh, 20 sweeps
+    big = rg.JacobiPlan([(512, 512, 512)])
+    u = torch.rand(big.total, dtype=torch.float64, device="cuda")
+    un = u.clone()
+    r = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+    def big_sweeps():
+        for sw in range(sweeps):
+            src, dst = (u, un) if sw % 2 == 0 else (un, u)
+            lib.b200_jacobi_sweep_f64(big.handle, src.data_ptr(), dst.data_ptr(), None, r.data_ptr(), s)
+
+    big_sweeps()
+    torch.cuda.synchronize()
+    a, b = _events()
+    a.record(stream)
+    big_sweeps()
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    out["mesh512_ms_per_sweep"] = round(ms / sweeps, 4)
+    out["mesh512_gbs_16B_per_point"] = round(16 * big.interior_points() * sweeps / ms / 1e6, 1)
+    out["mesh512_gpoints_per_s"] = round(big.interior_points() * sweeps / ms / 1e6, 2)
+    big.close()
+    return out
 
 
 def load_peaks() -> dict:
@@ -452,7 +747,7 @@ def kernel_bytes(name: str, n: int):
         "b200_reduce_sum_f32": 4 * n, "b200_reduce_sum_f64": 8 * n,
         "b200_reduce_minloc_f32": 4 * n, "b200_reduce_maxloc_f32": 4 * n,
         "b200_reduce_minloc_f64": 8 * n, "b200_reduce_maxloc_f64": 8 * n,
-        "b200_histogram_rep": 4 * n, "b200_histogram_agg": 4 * n,
+        "b200_histogram": 4 * n,
     }
     return per.get(name)
 

@@ -367,6 +367,34 @@ int b200_segmented_scan_exclusive_i32(b200_batch_plan plan, const int32_t* in, i
 int b200_segmented_sort_keys_u32(b200_batch_plan plan, uint32_t* keys, int descending,
                                  b200_stream_t stream);
 
+/* ======================================================================
+ * Batched 3-D Jacobi sweeps -- the config-5 mesh sweeps that the reference
+ * writes with RAJA::launch + View/OffsetLayout and a ReduceMax residual
+ * (pattern/launch/launch_core.hpp:150-460, util/OffsetLayout.hpp:166-244,
+ * examples/jacobi.cpp:223-489), one launch per mesh per sweep.
+ * Meshes are stored back to back, x fastest (mesh m starts at point
+ * offsets[m]).  One sweep updates the interior of every mesh:
+ *   unew = (f + sum of the six neighbours of u) / 6,
+ *   resid[m] = max |unew - u| over mesh m's interior;
+ * f may be NULL (f = 0).  Boundary points are never written, so u and
+ * unew must carry the same boundary values.
+ * ====================================================================== */
+typedef struct b200_jacobi_plan_s* b200_jacobi_plan;
+
+int b200_jacobi_plan_create(const int* nx, const int* ny, const int* nz, int nmeshes,
+                            b200_jacobi_plan* out);
+int b200_jacobi_plan_destroy(b200_jacobi_plan plan);
+int b200_jacobi_plan_info(b200_jacobi_plan plan, int64_t* total_points, int64_t* interior_points,
+                          int64_t* ntiles);
+/* host array of the nmeshes+1 point offsets */
+const int64_t* b200_jacobi_plan_offsets(b200_jacobi_plan plan);
+/* one sweep over every mesh of the plan in one launch */
+int b200_jacobi_sweep_f64(b200_jacobi_plan plan, const double* u, double* unew, const double* f,
+                          double* resid, b200_stream_t stream);
+/* one sweep of one mesh (the per-mesh launch of the reference formulation) */
+int b200_jacobi_mesh_sweep_f64(int nx, int ny, int nz, const double* u, double* unew,
+                               const double* f, double* resid, b200_stream_t stream);
+
 /* ---- CUDA graph capture of repeated sweeps (replaces per-call launches) */
 typedef struct b200_graph_s* b200_graph;
 int b200_graph_capture_begin(b200_stream_t stream);

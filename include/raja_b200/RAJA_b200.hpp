@@ -1,0 +1,1040 @@
+// RAJA_b200.hpp -- the b200 policy family for RAJA's data-parallel
+// primitive path on GB300 (sm_103a).
+//
+//   RAJA::b200_exec<BLOCK, Async>   forall over range / strided / list /
+//                                   IndexSet segments (replaces cuda_exec,
+//                                   policy/cuda/forall.hpp:554-706)
+//   RAJA::b200_reduce               ReduceSum/Min/Max/MinLoc/MaxLoc/BitOr/
+//                                   BitAnd captured in device lambdas
+//                                   (replaces cuda_reduce,
+//                                   policy/cuda/reduce.hpp:968-1378)
+//   expt::Reduce / ReduceLoc        forall params (policy/cuda/params/reduce.hpp)
+//   scans, sorts                    impl::scan / impl::sort overloads that
+//                                   forward to libb200prims (replace the CUB
+//                                   wrappers policy/cuda/scan.hpp, sort.hpp)
+//   RAJA::b200_work<BLOCK>          WorkGroup runner: unordered loops run in
+//                                   one persistent launch
+//                                   (policy/cuda/WorkGroup/WorkRunner.hpp)
+//   RAJA::b200_synchronize          RAJA::synchronize<> target
+//
+// Include after a RAJA front-end (the real RAJA or raja_compat).  Lambda
+// loop bodies stay templated and are compiled into the application with
+// nvcc --extended-lambda; fixed-type work goes through the C ABI in
+// b200prims.h.  Errors throw std::runtime_error, as RAJA's CUDA back-end
+// does (policy/cuda/raja_cudaerrchk.hpp:116-137).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <type_traits>
+#include <vector>
+
+#include "../b200prims.h"
+
+namespace RAJA {
+
+// ------------------------------------------------------------ policies
+template <int BLOCK = 256, bool Async = false>
+struct b200_exec {
+  static constexpr int block_size = BLOCK;
+  static constexpr bool async = Async;
+};
+template <int BLOCK = 256>
+using b200_exec_async = b200_exec<BLOCK, true>;
+struct b200_reduce {};
+template <int BLOCK = 256, bool Async = false>
+struct b200_work {};
+struct b200_synchronize {};
+
+namespace b200 {
+
+// Stream used by b200 policies (the legacy default stream unless set).
+inline cudaStream_t& stream() {
+  static thread_local cudaStream_t s = nullptr;
+  return s;
+}
+
+inline void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+inline void check(int rc, const char* what) {
+  if (rc != B200_OK)
+    throw std::runtime_error(std::string(what) + ": " + b200_last_error_string());
+}
+// Wait for the b200 stream and surface device-side errors (bounded waits
+// that gave up), like res.wait() + cudaErrchk.
+inline void wait() { check(b200_stream_synchronize(stream()), "b200 synchronize"); }
+
+inline int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    check_cuda(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev), "sm count");
+  }
+  return n;
+}
+
+namespace detail {
+
+// Launch context read by reducer copy constructors while forall_impl makes
+// the launch copy of the loop body (the role of RAJA's tl_status,
+// policy/cuda/MemUtils_CUDA.hpp:379-394).
+struct LaunchCtx {
+  bool active = false;
+  unsigned grid = 0;
+  cudaStream_t stream = nullptr;
+};
+inline LaunchCtx& ctx() {
+  static thread_local LaunchCtx c;
+  return c;
+}
+
+// Grid for a kernel: one block per BLOCK elements, capped at the resident
+// blocks of the whole GPU (the loop grid-strides beyond that).
+template <class Kernel>
+inline unsigned grid_for(Kernel k, int block, long long len) {
+  int bps = 0;
+  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, block, 0), "occupancy");
+  long long cap = (long long)sm_count() * (bps > 0 ? bps : 1);
+  long long g = (len + block - 1) / block;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return unsigned(g);
+}
+
+// ---- device combine helpers (block reduce + last-block ticket)
+template <class T, class Merge>
+__device__ inline T block_reduce(T v, Merge merge) {
+  __shared__ unsigned char sh_raw[32 * sizeof(T) + 16];
+  T* sh = reinterpret_cast<T*>(sh_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    T other;
+    unsigned w[sizeof(T) / 4];
+    memcpy(w, &v, sizeof(T));
+    for (int i = 0; i < int(sizeof(T) / 4); ++i) w[i] = __shfl_down_sync(0xffffffffu, w[i], o);
+    memcpy(&other, w, sizeof(T));
+    if (lane + o < 32) v = merge(v, other);
+  }
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = sh[lane < nw ? lane : 0];
+    for (int o = 16; o > 0; o >>= 1) {
+      T other;
+      unsigned w[sizeof(T) / 4];
+      memcpy(w, &v, sizeof(T));
+      for (int i = 0; i < int(sizeof(T) / 4); ++i) w[i] = __shfl_down_sync(0xffffffffu, w[i], o);
+      memcpy(&other, w, sizeof(T));
+      if (lane + o < nw) v = merge(v, other);
+    }
+  }
+  __syncthreads();
+  return v;  // valid in thread 0
+}
+
+template <class T>
+struct DevSlot {
+  T* partials;        // one per block
+  unsigned* ticket;   // zero before the launch; the last block re-zeroes it
+  T* result;          // written by the last block
+};
+
+// Read a value another block wrote in this kernel (bypass L1).
+template <class T>
+__device__ inline T ld_cg(const T* p) {
+  static_assert(sizeof(T) % 4 == 0, "reducer value size");
+  unsigned w[sizeof(T) / 4];
+  const unsigned* q = reinterpret_cast<const unsigned*>(p);
+  for (int i = 0; i < int(sizeof(T) / 4); ++i) w[i] = __ldcg(q + i);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+// Block reduce, publish one partial per block, and let the last block to
+// take the ticket fold all partials (reduce.hpp:133-214 restated).
+template <class T, class Merge>
+__device__ inline void grid_combine(const DevSlot<T>& s, T v, Merge merge) {
+  __shared__ bool last;
+  v = block_reduce(v, merge);
+  if (threadIdx.x == 0) {
+    s.partials[blockIdx.x] = v;
+    __threadfence();
+    last = atomicAdd(s.ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  bool have = false;
+  T r = v;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    const T p = ld_cg(s.partials + b);
+    r = have ? merge(r, p) : p;
+    have = true;
+  }
+  // threads without a partial hold v, the last block's own partial:
+  // re-merging it is harmless for idempotent merges but not for sums, so
+  // those threads contribute the identity by skipping the merge below
+  __shared__ unsigned char fin_raw[32 * sizeof(T) + 16];
+  T* fin = reinterpret_cast<T*>(fin_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const unsigned nb = gridDim.x;
+  // warp-level fold of the threads that hold partials (threads < nb)
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned w[sizeof(T) / 4];
+    memcpy(w, &r, sizeof(T));
+    for (int i = 0; i < int(sizeof(T) / 4); ++i) w[i] = __shfl_down_sync(0xffffffffu, w[i], o);
+    T other;
+    memcpy(&other, w, sizeof(T));
+    if (lane + o < 32 && threadIdx.x + o < nb) r = merge(r, other);
+  }
+  if (lane == 0) fin[warp] = r;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T acc = fin[0];
+    for (int w = 1; w < nw && unsigned(w * 32) < nb; ++w) acc = merge(acc, fin[w]);
+    *s.result = acc;
+    *s.ticket = 0u;
+  }
+}
+
+// Allocate one launch's slot on the stream: partials, ticket, result.
+template <class T>
+inline DevSlot<T> alloc_slot(unsigned grid, cudaStream_t s, void** block) {
+  const size_t pbytes = ((size_t(grid) * sizeof(T) + 255) / 256) * 256;
+  const size_t bytes = pbytes + 256 + sizeof(T);
+  check_cuda(cudaMallocAsync(block, bytes, s), "reducer slot");
+  char* b = static_cast<char*>(*block);
+  check_cuda(cudaMemsetAsync(b + pbytes, 0, sizeof(unsigned), s), "reducer ticket");
+  return DevSlot<T>{reinterpret_cast<T*>(b), reinterpret_cast<unsigned*>(b + pbytes),
+                    reinterpret_cast<T*>(b + pbytes + 256)};
+}
+
+// ---- ValLoc with lowest-index tie-break (device merges)
+template <class T, class I>
+struct VLoc {
+  T val;
+  I loc;
+};
+
+// Reducer kinds: how to combine values
+template <class T>
+struct SumK {
+  using V = T;
+  RAJA_HOST_DEVICE static V ident() { return T(0); }
+  RAJA_HOST_DEVICE static V merge(V a, V b) { return a + b; }
+  static V fold_init(V a, V b) { return a + b; }
+};
+template <class T>
+struct MinK {
+  using V = T;
+  RAJA_HOST_DEVICE static V ident() { return operators::limits<T>::max(); }
+  RAJA_HOST_DEVICE static V merge(V a, V b) { return (b < a) ? b : a; }
+  static V fold_init(V a, V b) { return (b < a) ? b : a; }
+};
+template <class T>
+struct MaxK {
+  using V = T;
+  RAJA_HOST_DEVICE static V ident() { return operators::limits<T>::min(); }
+  RAJA_HOST_DEVICE static V merge(V a, V b) { return (a < b) ? b : a; }
+  static V fold_init(V a, V b) { return (a < b) ? b : a; }
+};
+template <class T>
+struct OrK {
+  using V = T;
+  RAJA_HOST_DEVICE static V ident() { return T(0); }
+  RAJA_HOST_DEVICE static V merge(V a, V b) { return a | b; }
+  static V fold_init(V a, V b) { return a | b; }
+};
+template <class T>
+struct AndK {
+  using V = T;
+  RAJA_HOST_DEVICE static V ident() { return T(~T(0)); }
+  RAJA_HOST_DEVICE static V merge(V a, V b) { return a & b; }
+  static V fold_init(V a, V b) { return a & b; }
+};
+template <class T, class I, bool MIN>
+struct LocK {
+  using V = VLoc<T, I>;
+  RAJA_HOST_DEVICE static V ident() {
+    return V{MIN ? operators::limits<T>::max() : operators::limits<T>::min(), I(-1)};
+  }
+  // device merges: strictly better value wins, equal values keep the
+  // lowest location -- the order a sequential loop would have produced
+  RAJA_HOST_DEVICE static V merge(V a, V b) {
+    const bool better = MIN ? (b.val < a.val) : (a.val < b.val);
+    if (better || (b.val == a.val && b.loc < a.loc && !(a.loc == I(-1)))) return b;
+    return a;
+  }
+  // folding a launch result into the reducer's value: the earlier value
+  // wins ties (operators::minimum / maximum, util/Operators.hpp:555-591)
+  static V fold_init(V a, V b) { return (MIN ? (b.val < a.val) : (a.val < b.val)) ? b : a; }
+};
+
+// Device-capturable reducer.  The user's object (original) keeps the init
+// value and the list of launch results still to fold; the launch copy made
+// inside forall_impl gets a fresh device slot; the per-thread device copy
+// accumulates privately and its destructor runs the block + grid combine
+// (reduce.hpp:1047-1124 restated with a last-block ticket).
+template <class K>
+class DevReducer {
+ public:
+  using V = typename K::V;
+
+ protected:
+  struct Pending {
+    void* block;
+    V* result;
+    cudaStream_t stream;
+  };
+  struct Shared {
+    V init;
+    std::vector<Pending> pending;
+  };
+  Shared* shared_ = nullptr;
+  bool original_ = false;
+  bool launch_copy_ = false;
+  bool owner_ = false;
+  DevSlot<V> slot_{nullptr, nullptr, nullptr};
+  mutable V val_;
+
+ public:
+  explicit DevReducer(V init) : shared_(new Shared{init, {}}), original_(true), val_(K::ident()) {}
+
+  RAJA_HOST_DEVICE DevReducer(const DevReducer& o) : val_(K::ident()) {
+#if defined(__CUDA_ARCH__)
+    // per-thread copy of the launch copy: owns the combine
+    slot_ = o.slot_;
+    owner_ = o.launch_copy_;
+#else
+    shared_ = o.shared_;
+    LaunchCtx& c = ctx();
+    if (c.active && !o.launch_copy_) {
+      void* block = nullptr;
+      slot_ = alloc_slot<V>(c.grid, c.stream, &block);
+      shared_->pending.push_back(Pending{block, slot_.result, c.stream});
+      launch_copy_ = true;
+    } else {
+      slot_ = o.slot_;
+      launch_copy_ = o.launch_copy_;
+    }
+#endif
+  }
+  DevReducer& operator=(const DevReducer&) = delete;
+
+  RAJA_HOST_DEVICE ~DevReducer() {
+#if defined(__CUDA_ARCH__)
+    if (owner_) grid_combine(slot_, val_, [](V a, V b) { return K::merge(a, b); });
+#else
+    if (original_) {
+      try {
+        fold();
+      } catch (...) {
+      }
+      delete shared_;
+    }
+#endif
+  }
+
+  RAJA_HOST_DEVICE void combine(const V& v) const { val_ = K::merge(val_, v); }
+
+  // Fold the pending launch results into init, in launch order.
+  V fold() const {
+    if (!shared_) return V{};
+    for (const Pending& p : shared_->pending) {
+      check_cuda(cudaStreamSynchronize(p.stream), "reducer wait");
+      V r;
+      check_cuda(cudaMemcpy(&r, p.result, sizeof(V), cudaMemcpyDeviceToHost), "reducer result");
+      shared_->init = K::fold_init(shared_->init, r);
+      cudaFree(p.block);
+    }
+    shared_->pending.clear();
+    return shared_->init;
+  }
+  void reset_value(V v) {
+    fold();
+    shared_->init = v;
+  }
+};
+
+}  // namespace detail
+}  // namespace b200
+
+// ------------------------------------------------------------- reducers
+template <typename T>
+class ReduceSum<b200_reduce, T> : public b200::detail::DevReducer<b200::detail::SumK<T>> {
+  using B = b200::detail::DevReducer<b200::detail::SumK<T>>;
+
+ public:
+  explicit ReduceSum(T init = T(0)) : B(init) {}
+  RAJA_HOST_DEVICE ReduceSum(const ReduceSum& o) : B(o) {}
+  RAJA_HOST_DEVICE const ReduceSum& operator+=(T v) const { this->val_ += v; return *this; }
+  T get() const { return this->fold(); }
+  operator T() const { return get(); }
+  void reset(T v) { this->reset_value(v); }
+};
+template <typename T>
+class ReduceMin<b200_reduce, T> : public b200::detail::DevReducer<b200::detail::MinK<T>> {
+  using B = b200::detail::DevReducer<b200::detail::MinK<T>>;
+
+ public:
+  explicit ReduceMin(T init = operators::limits<T>::max()) : B(init) {}
+  RAJA_HOST_DEVICE ReduceMin(const ReduceMin& o) : B(o) {}
+  RAJA_HOST_DEVICE const ReduceMin& min(T v) const { this->combine(v); return *this; }
+  T get() const { return this->fold(); }
+  operator T() const { return get(); }
+  void reset(T v) { this->reset_value(v); }
+};
+template <typename T>
+class ReduceMax<b200_reduce, T> : public b200::detail::DevReducer<b200::detail::MaxK<T>> {
+  using B = b200::detail::DevReducer<b200::detail::MaxK<T>>;
+
+ public:
+  explicit ReduceMax(T init = operators::limits<T>::min()) : B(init) {}
+  RAJA_HOST_DEVICE ReduceMax(const ReduceMax& o) : B(o) {}
+  RAJA_HOST_DEVICE const ReduceMax& max(T v) const { this->combine(v); return *this; }
+  T get() const { return this->fold(); }
+  operator T() const { return get(); }
+  void reset(T v) { this->reset_value(v); }
+};
+template <typename T>
+class ReduceBitOr<b200_reduce, T> : public b200::detail::DevReducer<b200::detail::OrK<T>> {
+  using B = b200::detail::DevReducer<b200::detail::OrK<T>>;
+
+ public:
+  explicit ReduceBitOr(T init = T(0)) : B(init) {}
+  RAJA_HOST_DEVICE ReduceBitOr(const ReduceBitOr& o) : B(o) {}
+  RAJA_HOST_DEVICE const ReduceBitOr& operator|=(T v) const { this->val_ |= v; return *this; }
+  T get() const { return this->fold(); }
+  operator T() const { return get(); }
+};
+template <typename T>
+class ReduceBitAnd<b200_reduce, T> : public b200::detail::DevReducer<b200::detail::AndK<T>> {
+  using B = b200::detail::DevReducer<b200::detail::AndK<T>>;
+
+ public:
+  explicit ReduceBitAnd(T init = T(~T(0))) : B(init) {}
+  RAJA_HOST_DEVICE ReduceBitAnd(const ReduceBitAnd& o) : B(o) {}
+  RAJA_HOST_DEVICE const ReduceBitAnd& operator&=(T v) const { this->val_ &= v; return *this; }
+  T get() const { return this->fold(); }
+  operator T() const { return get(); }
+};
+// MinLoc / MaxLoc: the first extreme (lowest location among equal values),
+// and the init pair wins ties (pattern/detail/reduce.hpp:287-358).
+template <typename T, typename I>
+class ReduceMinLoc<b200_reduce, T, I>
+    : public b200::detail::DevReducer<b200::detail::LocK<T, I, true>> {
+  using K = b200::detail::LocK<T, I, true>;
+  using B = b200::detail::DevReducer<K>;
+
+ public:
+  ReduceMinLoc(T init, I idx) : B(typename K::V{init, idx}) {}
+  RAJA_HOST_DEVICE ReduceMinLoc(const ReduceMinLoc& o) : B(o) {}
+  RAJA_HOST_DEVICE const ReduceMinLoc& minloc(T v, I l) const {
+    if (v < this->val_.val || (v == this->val_.val && l < this->val_.loc)) this->val_ = {v, l};
+    return *this;
+  }
+  T get() const { return this->fold().val; }
+  I getLoc() const { return this->fold().loc; }
+  operator T() const { return get(); }
+  void reset(T v, I l) { this->reset_value(typename K::V{v, l}); }
+};
+template <typename T, typename I>
+class ReduceMaxLoc<b200_reduce, T, I>
+    : public b200::detail::DevReducer<b200::detail::LocK<T, I, false>> {
+  using K = b200::detail::LocK<T, I, false>;
+  using B = b200::detail::DevReducer<K>;
+
+ public:
+  ReduceMaxLoc(T init, I idx) : B(typename K::V{init, idx}) {}
+  RAJA_HOST_DEVICE ReduceMaxLoc(const ReduceMaxLoc& o) : B(o) {}
+  RAJA_HOST_DEVICE const ReduceMaxLoc& maxloc(T v, I l) const {
+    if (this->val_.val < v || (v == this->val_.val && l < this->val_.loc)) this->val_ = {v, l};
+    return *this;
+  }
+  T get() const { return this->fold().val; }
+  I getLoc() const { return this->fold().loc; }
+  operator T() const { return get(); }
+  void reset(T v, I l) { this->reset_value(typename K::V{v, l}); }
+};
+
+// ---------------------------------------------------------------- forall
+namespace b200 {
+namespace detail {
+
+template <int BLOCK, class Body, class T>
+__global__ void __launch_bounds__(BLOCK) forall_range_kernel(Body body_in, T begin, long long len) {
+  Body body(body_in);  // per-thread copy: reducers privatise here
+  const long long stride = (long long)gridDim.x * BLOCK;
+  for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < len; i += stride)
+    body(T(begin + T(i)));
+}
+template <int BLOCK, class Body, class T>
+__global__ void __launch_bounds__(BLOCK)
+forall_stride_kernel(Body body_in, T begin, T step, long long len) {
+  Body body(body_in);
+  const long long stride = (long long)gridDim.x * BLOCK;
+  for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < len; i += stride)
+    body(T(begin + T(i) * step));
+}
+template <int BLOCK, class Body, class T>
+__global__ void __launch_bounds__(BLOCK) forall_list_kernel(Body body_in, const T* idx, long long len) {
+  Body body(body_in);
+  const long long stride = (long long)gridDim.x * BLOCK;
+  for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < len; i += stride) body(idx[i]);
+}
+// All range segments of an IndexSet in one launch: a prefix of segment
+// lengths maps the flat iteration k to (segment, offset) by binary search.
+template <int BLOCK, class Body, class T>
+__global__ void __launch_bounds__(BLOCK)
+forall_indexset_kernel(Body body_in, const T* begins, const long long* prefix, int nseg,
+                       long long total) {
+  Body body(body_in);
+  const long long stride = (long long)gridDim.x * BLOCK;
+  for (long long k = (long long)blockIdx.x * BLOCK + threadIdx.x; k < total; k += stride) {
+    int lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (prefix[mid] <= k) lo = mid;
+      else hi = mid;
+    }
+    body(T(begins[lo] + T(k - prefix[lo])));
+  }
+}
+
+// Make the launch copy of the body with the context active, so captured
+// b200 reducers get their device slots for this grid.
+template <class Body>
+struct LaunchCopy {
+  Body body;
+  static Body make(const Body& b, unsigned grid, cudaStream_t s) {
+    LaunchCtx& c = ctx();
+    c.active = true;
+    c.grid = grid;
+    c.stream = s;
+    try {
+      Body copy(b);
+      c.active = false;
+      return copy;
+    } catch (...) {
+      c.active = false;
+      throw;
+    }
+  }
+};
+
+template <bool Async>
+inline void finish(const char* what) {
+  check_cuda(cudaGetLastError(), what);
+  if (!Async) wait();
+}
+
+}  // namespace detail
+}  // namespace b200
+
+template <int BLOCK, bool Async, class Body, class T>
+void forall_impl(b200_exec<BLOCK, Async>, const TypedRangeSegment<T>& r, Body&& body) {
+  using B = std::decay_t<Body>;
+  const long long len = (long long)r.size();
+  if (len <= 0) return;
+  auto k = b200::detail::forall_range_kernel<BLOCK, B, T>;
+  const unsigned g = b200::detail::grid_for(k, BLOCK, len);
+  cudaStream_t s = b200::stream();
+  B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
+  k<<<g, BLOCK, 0, s>>>(lb, r.b, len);
+  b200::detail::finish<Async>("b200 forall");
+}
+template <int BLOCK, bool Async, class Body, class T>
+void forall_impl(b200_exec<BLOCK, Async>, const TypedRangeStrideSegment<T>& r, Body&& body) {
+  using B = std::decay_t<Body>;
+  const long long len = (long long)r.size();
+  if (len <= 0) return;
+  auto k = b200::detail::forall_stride_kernel<BLOCK, B, T>;
+  const unsigned g = b200::detail::grid_for(k, BLOCK, len);
+  cudaStream_t s = b200::stream();
+  B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
+  k<<<g, BLOCK, 0, s>>>(lb, r.b, r.s, len);
+  b200::detail::finish<Async>("b200 forall");
+}
+template <int BLOCK, bool Async, class Body, class T>
+void forall_impl(b200_exec<BLOCK, Async>, const TypedListSegment<T>& l, Body&& body) {
+  using B = std::decay_t<Body>;
+  const long long len = (long long)l.size();
+  if (len <= 0) return;
+  auto k = b200::detail::forall_list_kernel<BLOCK, B, T>;
+  const unsigned g = b200::detail::grid_for(k, BLOCK, len);
+  cudaStream_t s = b200::stream();
+  B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
+  k<<<g, BLOCK, 0, s>>>(lb, l.data, len);
+  b200::detail::finish<Async>("b200 forall");
+}
+// IndexSet: one launch for all segments (the reference launches each
+// segment separately, policy/cuda/forall.hpp:675-706).
+template <int BLOCK, bool Async, class Body, class T>
+void forall_impl(b200_exec<BLOCK, Async>, const TypedIndexSet<T>& is, Body&& body) {
+  using B = std::decay_t<Body>;
+  const int nseg = int(is.segs.size());
+  if (nseg == 0) return;
+  std::vector<T> begins(nseg);
+  std::vector<long long> prefix(nseg + 1, 0);
+  for (int i = 0; i < nseg; ++i) {
+    begins[i] = is.segs[i].b;
+    prefix[i + 1] = prefix[i] + (long long)is.segs[i].size();
+  }
+  const long long total = prefix[nseg];
+  if (total == 0) return;
+  cudaStream_t s = b200::stream();
+  void* tbl = nullptr;
+  const size_t bb = ((nseg * sizeof(T) + 255) / 256) * 256;
+  b200::check_cuda(cudaMallocAsync(&tbl, bb + (nseg + 1) * sizeof(long long), s), "indexset table");
+  T* d_begins = static_cast<T*>(tbl);
+  long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + bb);
+  b200::check_cuda(cudaMemcpyAsync(d_begins, begins.data(), nseg * sizeof(T), cudaMemcpyHostToDevice, s),
+                   "indexset table");
+  b200::check_cuda(cudaMemcpyAsync(d_prefix, prefix.data(), (nseg + 1) * sizeof(long long),
+                                   cudaMemcpyHostToDevice, s),
+                   "indexset table");
+  auto k = b200::detail::forall_indexset_kernel<BLOCK, B, T>;
+  const unsigned g = b200::detail::grid_for(k, BLOCK, total);
+  B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
+  k<<<g, BLOCK, 0, s>>>(lb, d_begins, d_prefix, nseg, total);
+  b200::check_cuda(cudaGetLastError(), "b200 forall indexset");
+  b200::check_cuda(cudaFreeAsync(tbl, s), "indexset table");
+  if (!Async) b200::wait();
+}
+
+// ------------------------------------------------------ forall with params
+namespace b200 {
+namespace detail {
+
+// The K (kind) of an expt reducer param, from its operator.
+template <class R>
+struct ParamKind;
+template <template <class, class, class> class Op, class T, class VOp>
+struct ParamKind<expt::detail::Reducer<Op<T, T, T>, T, VOp>> {
+  using type = typename std::conditional<
+      std::is_same<Op<T, T, T>, operators::plus<T, T, T>>::value, SumK<T>,
+      typename std::conditional<
+          std::is_same<Op<T, T, T>, operators::minimum<T, T, T>>::value, MinK<T>,
+          typename std::conditional<
+              std::is_same<Op<T, T, T>, operators::maximum<T, T, T>>::value, MaxK<T>,
+              typename std::conditional<std::is_same<Op<T, T, T>, operators::bit_or<T, T, T>>::value,
+                                        OrK<T>, AndK<T>>::type>::type>::type>::type;
+  static T to_target(typename type::V v) { return v; }
+  static RAJA_HOST_DEVICE typename type::V from_valop(const VOp& v) { return v.val; }
+};
+template <class T, class I, class Op, class VOp>
+struct ParamKind<expt::detail::ReducerLoc<T, I, Op, VOp>> {
+  static constexpr bool is_min =
+      std::is_same<Op, operators::minimum<expt::ValLoc<T, I>, expt::ValLoc<T, I>, expt::ValLoc<T, I>>>::value;
+  using type = LocK<T, I, is_min>;
+  static expt::ValLoc<T, I> to_target(typename type::V v) { return expt::ValLoc<T, I>(v.val, v.loc); }
+  static RAJA_HOST_DEVICE typename type::V from_valop(const VOp& v) { return {v.val.val, v.val.loc}; }
+};
+
+// Minimal tuple usable in device code.
+template <class... Ts>
+struct DTuple;
+template <>
+struct DTuple<> {};
+template <class T, class... Ts>
+struct DTuple<T, Ts...> {
+  T head;
+  DTuple<Ts...> tail;
+};
+template <size_t I, class T, class... Ts>
+RAJA_HOST_DEVICE auto& dget(DTuple<T, Ts...>& t) {
+  if constexpr (I == 0) return t.head;
+  else return dget<I - 1>(t.tail);
+}
+template <size_t I, class T, class... Ts>
+RAJA_HOST_DEVICE const auto& dget(const DTuple<T, Ts...>& t) {
+  if constexpr (I == 0) return t.head;
+  else return dget<I - 1>(t.tail);
+}
+
+template <class R, class VOp>
+__device__ inline void combine_param(const DevSlot<typename ParamKind<R>::type::V>& slot, const VOp& v) {
+  using K = typename ParamKind<R>::type;
+  grid_combine(slot, ParamKind<R>::from_valop(v), [](typename K::V a, typename K::V b) { return K::merge(a, b); });
+}
+
+template <int BLOCK, class Body, class T, class... R, size_t... I>
+__device__ inline void params_body(Body& body, T begin, long long len,
+                                   const DTuple<DevSlot<typename ParamKind<R>::type::V>...>& slots,
+                                   std::index_sequence<I...>) {
+  DTuple<typename R::valop_type...> vals{};
+  const long long stride = (long long)gridDim.x * BLOCK;
+  for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < len; i += stride)
+    body(T(begin + T(i)), dget<I>(vals)...);
+  (combine_param<R>(dget<I>(slots), dget<I>(vals)), ...);
+}
+
+template <int BLOCK, class Body, class T, class... R>
+__global__ void __launch_bounds__(BLOCK)
+forall_params_kernel(Body body, T begin, long long len,
+                     DTuple<DevSlot<typename ParamKind<R>::type::V>...> slots) {
+  params_body<BLOCK, Body, T, R...>(body, begin, len, slots, std::index_sequence_for<R...>{});
+}
+
+}  // namespace detail
+}  // namespace b200
+
+template <class Slots, size_t... I, class... Red>
+void resolve_params(const Slots& slots, std::index_sequence<I...>, Red&... reds) {
+  auto one = [](auto& red, const auto& slot) {
+    using RK = b200::detail::ParamKind<std::decay_t<decltype(red)>>;
+    typename RK::type::V v;
+    b200::check_cuda(cudaMemcpy(&v, slot.result, sizeof(v), cudaMemcpyDeviceToHost), "param result");
+    red.combineTarget(RK::to_target(v));
+  };
+  (one(reds, b200::detail::dget<I>(slots)), ...);
+}
+
+template <int BLOCK, bool Async, class T, class Body, class... Red>
+void forall_params_impl(b200_exec<BLOCK, Async>, const TypedRangeSegment<T>& r, Body&& body,
+                        Red&... reds) {
+  using B = std::decay_t<Body>;
+  using Slots = b200::detail::DTuple<b200::detail::DevSlot<typename b200::detail::ParamKind<Red>::type::V>...>;
+  const long long len = (long long)r.size();
+  auto k = b200::detail::forall_params_kernel<BLOCK, B, T, Red...>;
+  const unsigned g = b200::detail::grid_for(k, BLOCK, len > 0 ? len : 1);
+  cudaStream_t s = b200::stream();
+  void* blocks[sizeof...(Red) + 1] = {};
+  size_t bi = 0;
+  Slots slots{b200::detail::alloc_slot<typename b200::detail::ParamKind<Red>::type::V>(g, s, &blocks[bi++])...};
+  k<<<g, BLOCK, 0, s>>>(body, r.b, len, slots);
+  b200::check_cuda(cudaGetLastError(), "b200 forall params");
+  b200::wait();  // param_resolve waits for the kernel, as the reference does
+  // resolve in parameter order: *target = op(*target, result)
+  resolve_params(slots, std::index_sequence_for<Red...>{}, reds...);
+  for (size_t i = 0; i < sizeof...(Red); ++i) cudaFree(blocks[i]);
+}
+
+// ----------------------------------------------------------------- scans
+namespace b200 {
+namespace detail {
+template <class F, class T>
+constexpr int scan_op() {
+  return std::is_same<F, operators::plus<T>>::value
+             ? B200_OP_SUM
+             : (std::is_same<F, operators::minimum<T>>::value
+                    ? B200_OP_MIN
+                    : (std::is_same<F, operators::maximum<T>>::value ? B200_OP_MAX : -1));
+}
+template <class T>
+inline int scan_incl(const T* in, T* out, size_t n, int op, cudaStream_t s);
+template <class T>
+inline int scan_excl(const T* in, T* out, size_t n, int op, T init, cudaStream_t s);
+#define B200_SCAN_BIND(SUF, T)                                                              \
+  template <>                                                                               \
+  inline int scan_incl<T>(const T* in, T* out, size_t n, int op, cudaStream_t s) {          \
+    return b200_scan_inclusive_##SUF(in, out, n, op, s);                                    \
+  }                                                                                         \
+  template <>                                                                               \
+  inline int scan_excl<T>(const T* in, T* out, size_t n, int op, T init, cudaStream_t s) {  \
+    return b200_scan_exclusive_##SUF(in, out, n, op, init, s);                              \
+  }
+B200_SCAN_BIND(i32, int32_t)
+B200_SCAN_BIND(i64, int64_t)
+B200_SCAN_BIND(u32, uint32_t)
+B200_SCAN_BIND(u64, uint64_t)
+#undef B200_SCAN_BIND
+template <>
+inline int scan_incl<float>(const float* in, float* out, size_t n, int op, cudaStream_t s) {
+  return b200_scan_inclusive_f32(in, out, n, op, B200_MODE_NAIVE, s);
+}
+template <>
+inline int scan_incl<double>(const double* in, double* out, size_t n, int op, cudaStream_t s) {
+  return b200_scan_inclusive_f64(in, out, n, op, B200_MODE_NAIVE, s);
+}
+template <>
+inline int scan_excl<float>(const float* in, float* out, size_t n, int op, float init, cudaStream_t s) {
+  return b200_scan_exclusive_f32(in, out, n, op, init, B200_MODE_NAIVE, s);
+}
+template <>
+inline int scan_excl<double>(const double* in, double* out, size_t n, int op, double init,
+                             cudaStream_t s) {
+  return b200_scan_exclusive_f64(in, out, n, op, init, B200_MODE_NAIVE, s);
+}
+}  // namespace detail
+}  // namespace b200
+
+// policy/cuda/scan.hpp:141-235 (CUB DeviceScan) replaced by libb200prims.
+template <int BLOCK, bool Async, typename T, typename F>
+void scan_inclusive(b200_exec<BLOCK, Async>, const T* b, const T* e, T* out, F) {
+  constexpr int op = b200::detail::scan_op<F, T>();
+  static_assert(op >= 0, "b200 scans take operators::plus / minimum / maximum");
+  b200::check(b200::detail::scan_incl<T>(b, out, size_t(e - b), op, b200::stream()), "b200 inclusive_scan");
+  if (!Async) b200::wait();
+}
+template <int BLOCK, bool Async, typename T, typename F>
+void scan_exclusive(b200_exec<BLOCK, Async>, const T* b, const T* e, T* out, F, T v) {
+  constexpr int op = b200::detail::scan_op<F, T>();
+  static_assert(op >= 0, "b200 scans take operators::plus / minimum / maximum");
+  b200::check(b200::detail::scan_excl<T>(b, out, size_t(e - b), op, v, b200::stream()),
+              "b200 exclusive_scan");
+  if (!Async) b200::wait();
+}
+
+// ----------------------------------------------------------------- sorts
+// policy/cuda/sort.hpp:92-653 (CUB DeviceRadixSort) replaced by the
+// stable radix sort of libb200prims; unstable forms forward to it.
+namespace b200d {
+template <class K>
+inline int keys(K* k, size_t n, int desc, cudaStream_t s);
+template <class K, class V>
+inline int pairs(K* k, V* v, size_t n, int desc, cudaStream_t s);
+#define B200_SORT_BIND(SUF, K)                                                       \
+  template <>                                                                        \
+  inline int keys<K>(K * k, size_t n, int desc, cudaStream_t s) {                    \
+    return b200_sort_keys_##SUF(k, n, desc, s);                                      \
+  }
+B200_SORT_BIND(u32, uint32_t)
+B200_SORT_BIND(u64, uint64_t)
+B200_SORT_BIND(i32, int32_t)
+B200_SORT_BIND(i64, int64_t)
+B200_SORT_BIND(f32, float)
+B200_SORT_BIND(f64, double)
+#undef B200_SORT_BIND
+#define B200_PAIRS_BIND(SUF, K, V)                                                   \
+  template <>                                                                        \
+  inline int pairs<K, V>(K * k, V * v, size_t n, int desc, cudaStream_t s) {         \
+    return b200_sort_pairs_##SUF(k, v, n, desc, s);                                  \
+  }
+B200_PAIRS_BIND(u32_i32, uint32_t, int32_t)
+B200_PAIRS_BIND(u32_u32, uint32_t, uint32_t)
+B200_PAIRS_BIND(i32_i32, int32_t, int32_t)
+B200_PAIRS_BIND(f32_i32, float, int32_t)
+B200_PAIRS_BIND(u64_i32, uint64_t, int32_t)
+B200_PAIRS_BIND(u64_i64, uint64_t, int64_t)
+B200_PAIRS_BIND(i64_i64, int64_t, int64_t)
+B200_PAIRS_BIND(f64_i64, double, int64_t)
+B200_PAIRS_BIND(f64_i32, double, int32_t)
+#undef B200_PAIRS_BIND
+template <class C, class T>
+constexpr int desc_of() {
+  static_assert(std::is_same<C, operators::less<T>>::value || std::is_same<C, operators::greater<T>>::value,
+                "b200 sorts take operators::less or operators::greater");
+  return std::is_same<C, operators::greater<T>>::value ? 1 : 0;
+}
+}  // namespace b200d
+
+template <int BLOCK, bool Async, typename T, typename C>
+void sort_stable(b200_exec<BLOCK, Async>, T* b, T* e, C) {
+  b200::check(b200d::keys<T>(b, size_t(e - b), b200d::desc_of<C, T>(), b200::stream()), "b200 sort");
+  if (!Async) b200::wait();
+}
+template <int BLOCK, bool Async, typename T, typename C>
+void sort_unstable(b200_exec<BLOCK, Async> p, T* b, T* e, C c) { sort_stable(p, b, e, c); }
+template <int BLOCK, bool Async, typename K, typename V, typename C>
+void sort_stable_pairs(b200_exec<BLOCK, Async>, K* kb, K* ke, V* vb, C) {
+  b200::check(b200d::pairs<K, V>(kb, vb, size_t(ke - kb), b200d::desc_of<C, K>(), b200::stream()),
+              "b200 sort_pairs");
+  if (!Async) b200::wait();
+}
+template <int BLOCK, bool Async, typename K, typename V, typename C>
+void sort_unstable_pairs(b200_exec<BLOCK, Async> p, K* kb, K* ke, V* vb, C c) {
+  sort_stable_pairs(p, kb, ke, vb, c);
+}
+
+// ------------------------------------------------------------- WorkGroup
+// b200_work: enqueued loops (range segment + trivially copyable device
+// lambda) are kept as (function pointer, body bytes, range).  The unordered
+// runner executes every loop in one persistent launch over fixed-size
+// tiles of all loops (load-balanced whatever the lengths); the ordered
+// runners launch the loops one after another, as the reference's ordered
+// CUDA runner does (policy/cuda/WorkGroup/WorkRunner.hpp:38-162).
+namespace b200 {
+namespace detail {
+using wg_fn = void (*)(const void* body, long long begin, long long lo, long long hi);
+
+template <class Body>
+__device__ void wg_run(const void* body, long long begin, long long lo, long long hi) {
+  const Body& b = *static_cast<const Body*>(body);
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) b(Index_type(begin + i));
+}
+// Device address of wg_run<Body>, read once per loop-body type by a
+// one-thread kernel (Dispatcher.hpp:43-48 does the same).
+template <class Body>
+__global__ void wg_get_fn(wg_fn* out) {
+  *out = wg_run<Body>;
+}
+template <class Body>
+inline wg_fn wg_fn_of() {
+  static wg_fn fp = nullptr;
+  if (!fp) {
+    wg_fn* d = nullptr;
+    check_cuda(cudaMalloc(&d, sizeof(wg_fn)), "WorkPool dispatcher");
+    wg_get_fn<Body><<<1, 1>>>(d);
+    check_cuda(cudaGetLastError(), "WorkPool dispatcher");
+    check_cuda(cudaMemcpy(&fp, d, sizeof(fp), cudaMemcpyDeviceToHost), "WorkPool dispatcher");
+    cudaFree(d);
+  }
+  return fp;
+}
+
+struct WgLoop {
+  wg_fn fn;
+  long long begin;
+  long long len;
+  size_t body_off;
+};
+struct WgTile {
+  int loop;
+  long long lo, hi;
+};
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+wg_kernel(const WgTile* tiles, long long ntiles, const WgLoop* loops, const unsigned char* bodies) {
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const WgTile tl = tiles[t];
+    const WgLoop lp = loops[tl.loop];
+    lp.fn(bodies + lp.body_off, lp.begin, tl.lo, tl.hi);
+  }
+}
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+wg_one_kernel(const WgLoop* loops, int which, const unsigned char* bodies) {
+  const WgLoop lp = loops[which];
+  const long long chunk = (lp.len + gridDim.x - 1) / gridDim.x;
+  const long long lo = (long long)blockIdx.x * chunk;
+  const long long hi = lo + chunk < lp.len ? lo + chunk : lp.len;
+  if (lo < hi) lp.fn(bodies + lp.body_off, lp.begin, lo, hi);
+}
+}  // namespace detail
+}  // namespace b200
+
+template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename Index, typename Alloc>
+class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, xargs<>, Alloc>;
+
+template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename Index, typename Alloc>
+class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, xargs<>, Alloc> {
+ public:
+  using policy = WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>;
+  using group_type = WorkGroup<policy, Index, xargs<>, Alloc>;
+  template <typename T, typename Body>
+  void enqueue(TypedRangeSegment<T> seg, Body body) {
+    static_assert(std::is_trivially_copyable<Body>::value,
+                  "b200_work loop bodies must be trivially copyable device lambdas");
+    const b200::detail::wg_fn fp = b200::detail::wg_fn_of<Body>();
+    const size_t off = (m_bytes.size() + 15) / 16 * 16;
+    m_bytes.resize(off + sizeof(Body));
+    std::memcpy(m_bytes.data() + off, &body, sizeof(Body));
+    m_loops.push_back(b200::detail::WgLoop{fp, (long long)seg.b, (long long)seg.size(), off});
+  }
+  void reserve(size_t n, size_t bytes) {
+    m_loops.reserve(n);
+    m_bytes.reserve(bytes);
+  }
+  size_t num_loops() const { return m_loops.size(); }
+  group_type instantiate();
+
+ private:
+  std::vector<b200::detail::WgLoop> m_loops;
+  std::vector<unsigned char> m_bytes;
+};
+
+template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename Index, typename Alloc>
+class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, xargs<>, Alloc> {
+ public:
+  using policy = WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>;
+  WorkGroup() = default;
+  WorkGroup(const WorkGroup&) = delete;
+  WorkGroup(WorkGroup&& o) noexcept { *this = std::move(o); }
+  WorkGroup& operator=(WorkGroup&& o) noexcept {
+    std::swap(m_dev, o.m_dev);
+    std::swap(m_nloops, o.m_nloops);
+    std::swap(m_ntiles, o.m_ntiles);
+    std::swap(m_loops_off, o.m_loops_off);
+    std::swap(m_tiles_off, o.m_tiles_off);
+    std::swap(m_bodies_off, o.m_bodies_off);
+    return *this;
+  }
+  ~WorkGroup() {
+    if (m_dev) cudaFree(m_dev);
+  }
+  // Upload loops, bodies and the tile table once (instantiate).
+  void setup(const std::vector<b200::detail::WgLoop>& loops, const std::vector<unsigned char>& bytes) {
+    constexpr long long TILE = (long long)BLOCK * 8;
+    std::vector<b200::detail::WgTile> tiles;
+    for (size_t i = 0; i < loops.size(); ++i)
+      for (long long lo = 0; lo < loops[i].len; lo += TILE)
+        tiles.push_back(b200::detail::WgTile{int(i), lo, lo + TILE < loops[i].len ? lo + TILE : loops[i].len});
+    m_nloops = int(loops.size());
+    m_ntiles = (long long)tiles.size();
+    m_loops_off = 0;
+    m_tiles_off = (loops.size() * sizeof(b200::detail::WgLoop) + 255) / 256 * 256;
+    m_bodies_off = m_tiles_off + (tiles.size() * sizeof(b200::detail::WgTile) + 255) / 256 * 256;
+    const size_t total = m_bodies_off + bytes.size() + 16;
+    b200::check_cuda(cudaMalloc(&m_dev, total), "WorkGroup storage");
+    char* d = static_cast<char*>(m_dev);
+    if (!loops.empty())
+      b200::check_cuda(cudaMemcpy(d + m_loops_off, loops.data(), loops.size() * sizeof(loops[0]),
+                                  cudaMemcpyHostToDevice), "WorkGroup loops");
+    if (!tiles.empty())
+      b200::check_cuda(cudaMemcpy(d + m_tiles_off, tiles.data(), tiles.size() * sizeof(tiles[0]),
+                                  cudaMemcpyHostToDevice), "WorkGroup tiles");
+    if (!bytes.empty())
+      b200::check_cuda(cudaMemcpy(d + m_bodies_off, bytes.data(), bytes.size(), cudaMemcpyHostToDevice),
+                       "WorkGroup bodies");
+  }
+  WorkSite<policy, Index, xargs<>, Alloc> run() {
+    if (m_nloops == 0) return {};
+    cudaStream_t s = b200::stream();
+    char* d = static_cast<char*>(m_dev);
+    auto* loops = reinterpret_cast<const b200::detail::WgLoop*>(d + m_loops_off);
+    auto* tiles = reinterpret_cast<const b200::detail::WgTile*>(d + m_tiles_off);
+    auto* bodies = reinterpret_cast<const unsigned char*>(d + m_bodies_off);
+    if (std::is_same<ORDER, unordered>::value) {
+      if (m_ntiles > 0) {
+        auto k = b200::detail::wg_kernel<BLOCK>;
+        const unsigned g = b200::detail::grid_for(k, BLOCK, m_ntiles * BLOCK);
+        k<<<g, BLOCK, 0, s>>>(tiles, m_ntiles, loops, bodies);
+      }
+    } else {
+      // one launch per loop, in (reverse) enqueue order
+      auto k = b200::detail::wg_one_kernel<BLOCK>;
+      for (int i = 0; i < m_nloops; ++i) {
+        const int which = std::is_same<ORDER, reverse_ordered>::value ? m_nloops - 1 - i : i;
+        const unsigned g = b200::detail::grid_for(k, BLOCK, 1ll << 22);
+        k<<<g, BLOCK, 0, s>>>(loops, which, bodies);
+      }
+    }
+    b200::check_cuda(cudaGetLastError(), "WorkGroup run");
+    if (!Async) b200::wait();
+    return {};
+  }
+  void clear() {}
+
+ private:
+  void* m_dev = nullptr;
+  int m_nloops = 0;
+  long long m_ntiles = 0;
+  size_t m_loops_off = 0, m_tiles_off = 0, m_bodies_off = 0;
+};
+
+template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename Index, typename Alloc>
+typename WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, xargs<>, Alloc>::group_type
+WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, xargs<>, Alloc>::instantiate() {
+  group_type g;
+  g.setup(m_loops, m_bytes);
+  m_loops.clear();
+  m_bytes.clear();
+  return g;
+}
+
+// ----------------------------------------------------------- synchronize
+template <>
+inline void synchronize<b200_synchronize>() {
+  b200::check_cuda(cudaDeviceSynchronize(), "synchronize");
+  b200::wait();
+}
+
+}  // namespace RAJA

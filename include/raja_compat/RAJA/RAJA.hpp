@@ -1,0 +1,659 @@
+// raja_compat -- a minimal RAJA-API front-end (namespace RAJA) for builds
+// where RAJA itself is not available.
+//
+// The reference's own headers cannot be compiled without its camp and BLT
+// submodules, so this header restates the small part of RAJA's front-end
+// that the data-parallel primitive path uses, with the reference's
+// semantics:
+//
+//   forall / forall with expt params       pattern/forall.hpp:323-652
+//   Reduce{Sum,Min,Max,MinLoc,MaxLoc,
+//          BitOr,BitAnd}<seq_reduce|omp_reduce>   pattern/reduce.hpp,
+//                                          pattern/detail/reduce.hpp:212-358
+//   expt::Reduce / ReduceLoc / ValOp /
+//          ValLoc / KernelName             pattern/params/*.hpp
+//   inclusive/exclusive_scan[_inplace]     pattern/scan.hpp:49-441
+//   sort / stable_sort / sort_pairs /
+//          stable_sort_pairs               pattern/sort.hpp:59-451
+//   WorkPool / WorkGroup / WorkSite        pattern/WorkGroup.hpp:117-530
+//   segments                               index/RangeSegment.hpp,
+//                                          index/ListSegment.hpp
+//
+// Back-ends plug in exactly as in RAJA: the front-end calls unqualified
+// implementation functions (forall_impl, impl::scan::*, impl::sort::*,
+// reducer specialisations) that are overloaded on the policy type.  This
+// header provides seq_exec / omp_parallel_for_exec and seq_reduce /
+// omp_reduce; include/raja_b200/RAJA_b200.hpp adds the b200 family.
+#pragma once
+
+#include <algorithm>
+#include <cstddef>
+#include <cstdint>
+#include <functional>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <tuple>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#if defined(_OPENMP)
+#include <omp.h>
+#endif
+
+#if defined(__CUDACC__)
+#define RAJA_HOST_DEVICE __host__ __device__
+#define RAJA_DEVICE __device__
+#define RAJA_HOST __host__
+#else
+#define RAJA_HOST_DEVICE
+#define RAJA_DEVICE
+#define RAJA_HOST
+#endif
+#define RAJA_INLINE inline
+
+namespace RAJA {
+
+using Index_type = std::ptrdiff_t;
+
+// ------------------------------------------------------------ operators
+// util/Operators.hpp: limits (:248-333), plus (:363-372), minimum /
+// maximum keep the first of equal values (:555-591).
+namespace operators {
+
+template <typename T, typename Enable = void>
+struct limits;
+template <typename T>
+struct limits<T, typename std::enable_if<std::is_integral<T>::value>::type> {
+  RAJA_HOST_DEVICE static constexpr T min() { return std::numeric_limits<T>::lowest(); }
+  RAJA_HOST_DEVICE static constexpr T max() { return std::numeric_limits<T>::max(); }
+};
+template <typename T>
+struct limits<T, typename std::enable_if<std::is_floating_point<T>::value>::type> {
+  RAJA_HOST_DEVICE static constexpr T min() { return -std::numeric_limits<T>::max(); }
+  RAJA_HOST_DEVICE static constexpr T max() { return std::numeric_limits<T>::max(); }
+};
+
+template <typename Ret, typename Arg1 = Ret, typename Arg2 = Arg1>
+struct plus {
+  using result_type = Ret;
+  RAJA_HOST_DEVICE constexpr Ret operator()(const Arg1& lhs, const Arg2& rhs) const { return lhs + rhs; }
+  RAJA_HOST_DEVICE static constexpr Ret identity() { return Ret(0); }
+};
+template <typename Ret, typename Arg1 = Ret, typename Arg2 = Arg1>
+struct minimum {
+  using result_type = Ret;
+  RAJA_HOST_DEVICE constexpr Ret operator()(const Arg1& lhs, const Arg2& rhs) const {
+    return (rhs < lhs) ? rhs : lhs;
+  }
+  RAJA_HOST_DEVICE static constexpr Ret identity() { return limits<Ret>::max(); }
+};
+template <typename Ret, typename Arg1 = Ret, typename Arg2 = Arg1>
+struct maximum {
+  using result_type = Ret;
+  RAJA_HOST_DEVICE constexpr Ret operator()(const Arg1& lhs, const Arg2& rhs) const {
+    return (lhs < rhs) ? rhs : lhs;
+  }
+  RAJA_HOST_DEVICE static constexpr Ret identity() { return limits<Ret>::min(); }
+};
+template <typename Ret, typename Arg1 = Ret, typename Arg2 = Arg1>
+struct bit_or {
+  using result_type = Ret;
+  RAJA_HOST_DEVICE constexpr Ret operator()(const Arg1& lhs, const Arg2& rhs) const { return lhs | rhs; }
+  RAJA_HOST_DEVICE static constexpr Ret identity() { return Ret(0); }
+};
+template <typename Ret, typename Arg1 = Ret, typename Arg2 = Arg1>
+struct bit_and {
+  using result_type = Ret;
+  RAJA_HOST_DEVICE constexpr Ret operator()(const Arg1& lhs, const Arg2& rhs) const { return lhs & rhs; }
+  RAJA_HOST_DEVICE static constexpr Ret identity() { return Ret(~Ret(0)); }
+};
+template <typename T>
+struct less {
+  RAJA_HOST_DEVICE constexpr bool operator()(const T& a, const T& b) const { return a < b; }
+};
+template <typename T>
+struct greater {
+  RAJA_HOST_DEVICE constexpr bool operator()(const T& a, const T& b) const { return b < a; }
+};
+
+}  // namespace operators
+
+// ------------------------------------------------------------- segments
+template <typename T>
+struct TypedRangeSegment {
+  using value_type = T;
+  T b, e;
+  RAJA_HOST_DEVICE TypedRangeSegment(T begin, T end) : b(begin), e(end < begin ? begin : end) {}
+  RAJA_HOST_DEVICE T size() const { return e - b; }
+};
+using RangeSegment = TypedRangeSegment<Index_type>;
+
+template <typename T>
+struct TypedRangeStrideSegment {
+  using value_type = T;
+  T b, e, s;
+  TypedRangeStrideSegment(T begin, T end, T stride) : b(begin), e(end), s(stride) {}
+  T size() const {
+    if (s > 0) return e > b ? (e - b + s - 1) / s : 0;
+    return b > e ? (b - e + (-s) - 1) / (-s) : 0;
+  }
+};
+using RangeStrideSegment = TypedRangeStrideSegment<Index_type>;
+
+// A list of indices.  `data` must be readable where the loop runs (host
+// memory for host policies, device or managed memory for b200 policies).
+template <typename T>
+struct TypedListSegment {
+  using value_type = T;
+  const T* data;
+  Index_type len;
+  TypedListSegment(const T* d, Index_type n) : data(d), len(n) {}
+  Index_type size() const { return len; }
+};
+using ListSegment = TypedListSegment<Index_type>;
+
+// IndexSet of range segments (index/IndexSet.hpp:87-364); forall over it
+// runs every segment, in order for the host policies.
+template <typename T>
+struct TypedIndexSet {
+  std::vector<TypedRangeSegment<T>> segs;
+  void push_back(TypedRangeSegment<T> s) { segs.push_back(s); }
+  size_t getNumSegments() const { return segs.size(); }
+};
+
+// ---------------------------------------------------------------- spans
+template <typename T>
+struct Span {
+  T* ptr;
+  Index_type n;
+  T* begin() const { return ptr; }
+  T* end() const { return ptr + n; }
+  Index_type size() const { return n; }
+};
+template <typename T>
+Span<T> make_span(T* p, Index_type n) { return Span<T>{p, n}; }
+
+// ------------------------------------------------------------ policies
+struct seq_exec {};
+struct omp_parallel_for_exec {};
+struct seq_reduce {};
+struct omp_reduce {};
+
+namespace expt {
+// ---- ValLoc / ValOp / KernelName (pattern/params/params_base.hpp:10-253)
+template <typename T, typename IndexType = Index_type>
+struct ValLoc {
+  using value_type = T;
+  using index_type = IndexType;
+  T val;
+  IndexType loc;
+  RAJA_HOST_DEVICE constexpr ValLoc() : val(T()), loc(IndexType(-1)) {}
+  RAJA_HOST_DEVICE constexpr ValLoc(T v) : val(v), loc(IndexType(-1)) {}
+  RAJA_HOST_DEVICE constexpr ValLoc(T v, IndexType l) : val(v), loc(l) {}
+  RAJA_HOST_DEVICE bool operator<(const ValLoc& o) const { return val < o.val; }
+  RAJA_HOST_DEVICE bool operator>(const ValLoc& o) const { return val > o.val; }
+  RAJA_HOST_DEVICE T getVal() const { return val; }
+  RAJA_HOST_DEVICE IndexType getLoc() const { return loc; }
+};
+
+template <typename T, template <typename, typename, typename> class Op>
+struct ValOp {
+  using value_type = T;
+  using op_type = Op<T, T, T>;
+  T val;
+  RAJA_HOST_DEVICE constexpr ValOp() : val(op_type::identity()) {}
+  RAJA_HOST_DEVICE constexpr explicit ValOp(T v) : val(v) {}
+  RAJA_HOST_DEVICE ValOp& operator+=(const T& r) { val += r; return *this; }
+  RAJA_HOST_DEVICE ValOp& operator|=(const T& r) { val |= r; return *this; }
+  RAJA_HOST_DEVICE ValOp& operator&=(const T& r) { val &= r; return *this; }
+  RAJA_HOST_DEVICE ValOp& min(const T& v) { if (v < val) val = v; return *this; }
+  RAJA_HOST_DEVICE ValOp& max(const T& v) { if (val < v) val = v; return *this; }
+  RAJA_HOST_DEVICE T get() const { return val; }
+};
+// ValOp over ValLoc: minloc / maxloc keep the first extreme
+template <typename T, typename I, template <typename, typename, typename> class Op>
+struct ValOp<ValLoc<T, I>, Op> {
+  using value_type = ValLoc<T, I>;
+  using op_type = Op<value_type, value_type, value_type>;
+  value_type val;
+  RAJA_HOST_DEVICE constexpr ValOp() : val(op_type::identity()) {}
+  RAJA_HOST_DEVICE ValOp& minloc(const T& v, I l) { if (v < val.val) val = value_type(v, l); return *this; }
+  RAJA_HOST_DEVICE ValOp& maxloc(const T& v, I l) { if (val.val < v) val = value_type(v, l); return *this; }
+  RAJA_HOST_DEVICE ValOp& min(value_type v) { if (v.val < val.val) val = v; return *this; }
+  RAJA_HOST_DEVICE ValOp& max(value_type v) { if (val.val < v.val) val = v; return *this; }
+  RAJA_HOST_DEVICE T getVal() const { return val.val; }
+  RAJA_HOST_DEVICE I getLoc() const { return val.loc; }
+};
+
+struct KernelName {
+  const char* name;
+};
+inline KernelName Name(const char* n) { return KernelName{n}; }
+
+namespace detail {
+template <typename Op, typename T, typename VOp>
+struct Reducer {
+  using op = Op;
+  using value_type = T;
+  using valop_type = VOp;
+  T* target;
+  Reducer(T* t) : target(t) {}
+  void combineTarget(T in) const { *target = Op{}(*target, in); }
+};
+template <typename T, typename I, typename Op, typename VOp>
+struct ReducerLoc {
+  using op = Op;
+  using value_type = ValLoc<T, I>;
+  using valop_type = VOp;
+  T* target;
+  I* index;
+  ReducerLoc(T* t, I* i) : target(t), index(i) {}
+  void combineTarget(value_type in) const {
+    value_type cur(*target, *index);
+    value_type r = Op{}(cur, in);
+    *target = r.val;
+    *index = r.loc;
+  }
+};
+template <typename X>
+struct is_reducer : std::false_type {};
+template <typename Op, typename T, typename VOp>
+struct is_reducer<Reducer<Op, T, VOp>> : std::true_type {};
+template <typename T, typename I, typename Op, typename VOp>
+struct is_reducer<ReducerLoc<T, I, Op, VOp>> : std::true_type {};
+}  // namespace detail
+
+// pattern/params/reducer.hpp:220-248
+template <template <typename, typename, typename> class Op, typename T>
+detail::Reducer<Op<T, T, T>, T, ValOp<T, Op>> Reduce(T* target) {
+  return detail::Reducer<Op<T, T, T>, T, ValOp<T, Op>>(target);
+}
+template <template <typename, typename, typename> class Op, typename T, typename I>
+detail::ReducerLoc<T, I, Op<ValLoc<T, I>, ValLoc<T, I>, ValLoc<T, I>>, ValOp<ValLoc<T, I>, Op>>
+ReduceLoc(T* target, I* index) {
+  return {target, index};
+}
+}  // namespace expt
+
+// operators::limits for ValLoc identities (pattern/detail/reduce.hpp:185-203)
+namespace operators {
+template <typename T, typename I>
+struct limits<expt::ValLoc<T, I>, void> {
+  RAJA_HOST_DEVICE static constexpr expt::ValLoc<T, I> min() { return expt::ValLoc<T, I>(limits<T>::min()); }
+  RAJA_HOST_DEVICE static constexpr expt::ValLoc<T, I> max() { return expt::ValLoc<T, I>(limits<T>::max()); }
+};
+}  // namespace operators
+
+// ------------------------------------------------------------- reducers
+// Reducer class templates; each policy specialises them.
+template <typename POL, typename T> class ReduceSum;
+template <typename POL, typename T> class ReduceMin;
+template <typename POL, typename T> class ReduceMax;
+template <typename POL, typename T, typename I = Index_type> class ReduceMinLoc;
+template <typename POL, typename T, typename I = Index_type> class ReduceMaxLoc;
+template <typename POL, typename T> class ReduceBitOr;
+template <typename POL, typename T> class ReduceBitAnd;
+
+namespace detail {
+// BaseCombinable semantics (pattern/detail/reduce.hpp:287-358): a copy
+// starts at the identity and folds into its parent when destroyed; the
+// parent holds init.  Host policies only.
+template <typename T, typename Op>
+class HostCombinable {
+ protected:
+  const HostCombinable* parent = nullptr;
+  T identity;
+  mutable T my;
+  mutable std::shared_ptr<std::vector<T>> omp_parts;  // omp: thread partials
+
+ public:
+  HostCombinable(T init, T ident) : identity(ident), my(init) {}
+  HostCombinable(const HostCombinable& o)
+      : parent(o.parent ? o.parent : &o), identity(o.identity), my(o.identity) {}
+  ~HostCombinable() {
+    if (parent) {
+#if defined(_OPENMP)
+#pragma omp critical(raja_compat_reduce)
+#endif
+      parent->my = Op{}(parent->my, my);
+    }
+  }
+  void combine(const T& v) const { my = Op{}(my, v); }
+  T get() const { return my; }
+  void reset(T init, T ident) {
+    my = init;
+    identity = ident;
+  }
+};
+}  // namespace detail
+
+#define RAJA_COMPAT_HOST_REDUCERS(POL)                                                           \
+  template <typename T>                                                                          \
+  class ReduceSum<POL, T> : public detail::HostCombinable<T, operators::plus<T>> {               \
+    using B = detail::HostCombinable<T, operators::plus<T>>;                                     \
+                                                                                                 \
+   public:                                                                                       \
+    explicit ReduceSum(T init = T(0)) : B(init, T(0)) {}                                         \
+    const ReduceSum& operator+=(T v) const { this->combine(v); return *this; }                   \
+    T get() const { return B::get(); }                                                           \
+    operator T() const { return get(); }                                                         \
+    void reset(T v) { B::reset(v, T(0)); }                                                       \
+  };                                                                                             \
+  template <typename T>                                                                          \
+  class ReduceMin<POL, T> : public detail::HostCombinable<T, operators::minimum<T>> {            \
+    using B = detail::HostCombinable<T, operators::minimum<T>>;                                  \
+                                                                                                 \
+   public:                                                                                       \
+    explicit ReduceMin(T init = operators::limits<T>::max()) : B(init, operators::limits<T>::max()) {} \
+    const ReduceMin& min(T v) const { this->combine(v); return *this; }                          \
+    T get() const { return B::get(); }                                                           \
+    operator T() const { return get(); }                                                         \
+  };                                                                                             \
+  template <typename T>                                                                          \
+  class ReduceMax<POL, T> : public detail::HostCombinable<T, operators::maximum<T>> {            \
+    using B = detail::HostCombinable<T, operators::maximum<T>>;                                  \
+                                                                                                 \
+   public:                                                                                       \
+    explicit ReduceMax(T init = operators::limits<T>::min()) : B(init, operators::limits<T>::min()) {} \
+    const ReduceMax& max(T v) const { this->combine(v); return *this; }                          \
+    T get() const { return B::get(); }                                                           \
+    operator T() const { return get(); }                                                         \
+  };                                                                                             \
+  template <typename T, typename I>                                                              \
+  class ReduceMinLoc<POL, T, I>                                                                  \
+      : public detail::HostCombinable<expt::ValLoc<T, I>, operators::minimum<expt::ValLoc<T, I>>> { \
+    using VL = expt::ValLoc<T, I>;                                                               \
+    using B = detail::HostCombinable<VL, operators::minimum<VL>>;                                \
+                                                                                                 \
+   public:                                                                                       \
+    ReduceMinLoc(T init, I idx) : B(VL(init, idx), VL(operators::limits<T>::max(), I(-1))) {}    \
+    const ReduceMinLoc& minloc(T v, I l) const { this->combine(VL(v, l)); return *this; }        \
+    T get() const { return B::get().val; }                                                       \
+    I getLoc() const { return B::get().loc; }                                                    \
+    operator T() const { return get(); }                                                         \
+    void reset(T v, I l) { B::reset(VL(v, l), VL(operators::limits<T>::max(), I(-1))); }         \
+  };                                                                                             \
+  template <typename T, typename I>                                                              \
+  class ReduceMaxLoc<POL, T, I>                                                                  \
+      : public detail::HostCombinable<expt::ValLoc<T, I>, operators::maximum<expt::ValLoc<T, I>>> { \
+    using VL = expt::ValLoc<T, I>;                                                               \
+    using B = detail::HostCombinable<VL, operators::maximum<VL>>;                                \
+                                                                                                 \
+   public:                                                                                       \
+    ReduceMaxLoc(T init, I idx) : B(VL(init, idx), VL(operators::limits<T>::min(), I(-1))) {}    \
+    const ReduceMaxLoc& maxloc(T v, I l) const { this->combine(VL(v, l)); return *this; }        \
+    T get() const { return B::get().val; }                                                       \
+    I getLoc() const { return B::get().loc; }                                                    \
+    operator T() const { return get(); }                                                         \
+    void reset(T v, I l) { B::reset(VL(v, l), VL(operators::limits<T>::min(), I(-1))); }         \
+  };                                                                                             \
+  template <typename T>                                                                          \
+  class ReduceBitOr<POL, T> : public detail::HostCombinable<T, operators::bit_or<T>> {           \
+    using B = detail::HostCombinable<T, operators::bit_or<T>>;                                   \
+                                                                                                 \
+   public:                                                                                       \
+    explicit ReduceBitOr(T init = T(0)) : B(init, T(0)) {}                                       \
+    const ReduceBitOr& operator|=(T v) const { this->combine(v); return *this; }                 \
+    T get() const { return B::get(); }                                                           \
+    operator T() const { return get(); }                                                         \
+  };                                                                                             \
+  template <typename T>                                                                          \
+  class ReduceBitAnd<POL, T> : public detail::HostCombinable<T, operators::bit_and<T>> {         \
+    using B = detail::HostCombinable<T, operators::bit_and<T>>;                                  \
+                                                                                                 \
+   public:                                                                                       \
+    explicit ReduceBitAnd(T init = T(~T(0))) : B(init, T(~T(0))) {}                              \
+    const ReduceBitAnd& operator&=(T v) const { this->combine(v); return *this; }                \
+    T get() const { return B::get(); }                                                           \
+    operator T() const { return get(); }                                                         \
+  };
+
+RAJA_COMPAT_HOST_REDUCERS(seq_reduce)
+RAJA_COMPAT_HOST_REDUCERS(omp_reduce)
+#undef RAJA_COMPAT_HOST_REDUCERS
+
+// ---------------------------------------------------------------- forall
+// Host implementations (policy/sequential/forall.hpp:58-102,
+// policy/openmp/forall.hpp:129-260).  The loop body is copied once per
+// thread, like thread_privatize, so captured reducers fold on destruction.
+template <typename Body, typename T>
+void forall_impl(seq_exec, const TypedRangeSegment<T>& r, Body&& body) {
+  auto b = body;
+  for (T i = r.b; i < r.e; ++i) b(i);
+}
+template <typename Body, typename T>
+void forall_impl(seq_exec, const TypedRangeStrideSegment<T>& r, Body&& body) {
+  auto b = body;
+  const Index_type n = r.size();
+  for (Index_type k = 0; k < n; ++k) b(T(r.b + k * r.s));
+}
+template <typename Body, typename T>
+void forall_impl(seq_exec, const TypedListSegment<T>& l, Body&& body) {
+  auto b = body;
+  for (Index_type k = 0; k < l.len; ++k) b(l.data[k]);
+}
+template <typename Body, typename T>
+void forall_impl(omp_parallel_for_exec, const TypedRangeSegment<T>& r, Body&& body) {
+#if defined(_OPENMP)
+#pragma omp parallel
+  {
+    auto b = body;
+#pragma omp for schedule(static)
+    for (T i = r.b; i < r.e; ++i) b(i);
+  }
+#else
+  forall_impl(seq_exec{}, r, body);
+#endif
+}
+template <typename Pol, typename Body, typename T>
+void forall_impl(Pol p, const TypedIndexSet<T>& is, Body&& body) {
+  for (const auto& s : is.segs) forall_impl(p, s, body);
+}
+
+// forall with expt params on host: each param gets a ValOp local starting
+// at its identity; after the loop the target is combined (param_resolve,
+// policy/sequential/params/reduce.hpp:42-46).
+template <typename T, typename Body, typename... Red>
+void forall_params_impl(seq_exec, const TypedRangeSegment<T>& r, Body&& body, Red&... reds) {
+  std::tuple<typename Red::valop_type...> vals;
+  std::apply([&](auto&... v) {
+    for (T i = r.b; i < r.e; ++i) body(i, v...);
+  }, vals);
+  std::apply([&](auto&... v) { (reds.combineTarget(v.val), ...); }, vals);
+}
+
+namespace detail {
+// Dispatch of forall(seg, params..., body): a KernelName is dropped for the
+// host policies; reducer params go to forall_params_impl.
+template <typename Pol, typename Seg, typename Body>
+void forall_with(Pol p, Seg&& seg, Body&& body) {
+  forall_impl(p, std::forward<Seg>(seg), std::forward<Body>(body));
+}
+template <typename Pol, typename Seg, typename Body, typename... Rest>
+void forall_with(Pol p, Seg&& seg, Body&& body, expt::KernelName, Rest&&... rest) {
+  forall_with(p, std::forward<Seg>(seg), std::forward<Body>(body), std::forward<Rest>(rest)...);
+}
+template <typename Pol, typename Seg, typename Body, typename R0, typename... Rest,
+          typename std::enable_if<expt::detail::is_reducer<std::decay_t<R0>>::value, int>::type = 0>
+void forall_with(Pol p, Seg&& seg, Body&& body, R0&& r0, Rest&&... rest) {
+  forall_params_impl(p, std::forward<Seg>(seg), std::forward<Body>(body), r0, rest...);
+}
+template <typename Pol, typename Seg, typename Tup, size_t... I>
+void forall_split(Seg&& seg, Tup&& tup, std::index_sequence<I...>) {
+  constexpr size_t N = std::tuple_size<std::decay_t<Tup>>::value;
+  forall_with(Pol{}, std::forward<Seg>(seg), std::get<N - 1>(tup), std::get<I>(tup)...);
+}
+}  // namespace detail
+
+// RAJA::forall<POLICY>(segment, [params...,] body)  (pattern/forall.hpp:545-627)
+template <typename Pol, typename Seg, typename... Args>
+void forall(Seg&& seg, Args&&... args) {
+  static_assert(sizeof...(Args) >= 1, "forall needs a loop body");
+  detail::forall_split<Pol>(std::forward<Seg>(seg), std::forward_as_tuple(std::forward<Args>(args)...),
+                            std::make_index_sequence<sizeof...(Args) - 1>{});
+}
+
+// ----------------------------------------------------------------- scans
+// pattern/scan.hpp front-ends.  Back-ends overload scan_inclusive /
+// scan_exclusive in namespace RAJA on their policy type; the front-end
+// calls them unqualified so argument-dependent lookup finds overloads
+// declared after this header (the role of impl::scan::* in
+// policy/*/scan.hpp).  Host implementations follow
+// policy/sequential/scan.hpp:43-153.
+template <typename T, typename F>
+void scan_inclusive(seq_exec, const T* b, const T* e, T* out, F f) {
+  if (b == e) return;
+  T agg = *b;
+  *out++ = agg;
+  for (const T* i = b + 1; i != e; ++i) {
+    agg = f(agg, *i);
+    *out++ = agg;
+  }
+}
+template <typename T, typename F>
+void scan_exclusive(seq_exec, const T* b, const T* e, T* out, F f, T v) {
+  const Index_type n = e - b;
+  T agg = v;
+  for (Index_type i = 0; i < n; ++i) {
+    const T t = b[i];
+    out[i] = agg;
+    agg = f(agg, t);
+  }
+}
+
+template <typename Pol, typename T, typename F = operators::plus<std::remove_const_t<T>>>
+void inclusive_scan(Span<T> in, Span<std::remove_const_t<T>> out, F f = F{}) {
+  if (in.size() == 0) return;
+  scan_inclusive(Pol{}, static_cast<const std::remove_const_t<T>*>(in.begin()),
+                 static_cast<const std::remove_const_t<T>*>(in.end()), out.begin(), f);
+}
+template <typename Pol, typename T, typename F = operators::plus<std::remove_const_t<T>>>
+void exclusive_scan(Span<T> in, Span<std::remove_const_t<T>> out, F f = F{},
+                    std::remove_const_t<T> v = F::identity()) {
+  if (in.size() == 0) return;
+  scan_exclusive(Pol{}, static_cast<const std::remove_const_t<T>*>(in.begin()),
+                 static_cast<const std::remove_const_t<T>*>(in.end()), out.begin(), f, v);
+}
+template <typename Pol, typename T, typename F = operators::plus<T>>
+void inclusive_scan_inplace(Span<T> io, F f = F{}) {
+  if (io.size() == 0) return;
+  scan_inclusive(Pol{}, static_cast<const T*>(io.begin()), static_cast<const T*>(io.end()), io.begin(), f);
+}
+template <typename Pol, typename T, typename F = operators::plus<T>>
+void exclusive_scan_inplace(Span<T> io, F f = F{}, T v = F::identity()) {
+  if (io.size() == 0) return;
+  scan_exclusive(Pol{}, static_cast<const T*>(io.begin()), static_cast<const T*>(io.end()), io.begin(), f, v);
+}
+
+// ----------------------------------------------------------------- sorts
+// pattern/sort.hpp; back-ends overload sort_stable / sort_unstable /
+// sort_stable_pairs / sort_unstable_pairs in namespace RAJA (found by ADL,
+// as above).  Host: stable merge sort (util/sort.hpp:577).
+template <typename T, typename C>
+void sort_stable(seq_exec, T* b, T* e, C c) { std::stable_sort(b, e, c); }
+template <typename T, typename C>
+void sort_unstable(seq_exec, T* b, T* e, C c) { std::stable_sort(b, e, c); }
+template <typename K, typename V, typename C>
+void sort_stable_pairs(seq_exec, K* kb, K* ke, V* vb, C c) {
+  const Index_type n = ke - kb;
+  std::vector<std::pair<K, V>> z(static_cast<size_t>(n));
+  for (Index_type i = 0; i < n; ++i) z[i] = {kb[i], vb[i]};
+  std::stable_sort(z.begin(), z.end(), [&](const std::pair<K, V>& a, const std::pair<K, V>& b) {
+    return c(a.first, b.first);
+  });
+  for (Index_type i = 0; i < n; ++i) {
+    kb[i] = z[i].first;
+    vb[i] = z[i].second;
+  }
+}
+template <typename K, typename V, typename C>
+void sort_unstable_pairs(seq_exec p, K* kb, K* ke, V* vb, C c) { sort_stable_pairs(p, kb, ke, vb, c); }
+
+template <typename Pol, typename T, typename C = operators::less<T>>
+void sort(Span<T> s, C c = C{}) { if (s.size() > 1) sort_unstable(Pol{}, s.begin(), s.end(), c); }
+template <typename Pol, typename T, typename C = operators::less<T>>
+void stable_sort(Span<T> s, C c = C{}) { if (s.size() > 1) sort_stable(Pol{}, s.begin(), s.end(), c); }
+template <typename Pol, typename K, typename V, typename C = operators::less<K>>
+void sort_pairs(Span<K> k, Span<V> v, C c = C{}) {
+  if (k.size() > 1) sort_unstable_pairs(Pol{}, k.begin(), k.end(), v.begin(), c);
+}
+template <typename Pol, typename K, typename V, typename C = operators::less<K>>
+void stable_sort_pairs(Span<K> k, Span<V> v, C c = C{}) {
+  if (k.size() > 1) sort_stable_pairs(Pol{}, k.begin(), k.end(), v.begin(), c);
+}
+
+// ------------------------------------------------------------- WorkGroup
+// pattern/WorkGroup.hpp:117-530.  Host runners execute the loops in
+// enqueue order (ordered) like the reference's WorkRunnerForallOrdered.
+struct ordered {};
+struct reverse_ordered {};
+struct unordered {};
+struct array_of_pointers {};
+struct ragged_array_of_objects {};
+struct constant_stride_array_of_objects {};
+template <typename EXEC, typename ORDER = ordered, typename STORAGE = ragged_array_of_objects>
+struct WorkGroupPolicy {
+  using exec_policy = EXEC;
+  using order_policy = ORDER;
+};
+template <typename... Args>
+struct xargs {};
+
+template <typename POL, typename Index, typename XArgs = xargs<>, typename Alloc = void>
+class WorkPool;
+template <typename POL, typename Index, typename XArgs = xargs<>, typename Alloc = void>
+class WorkGroup;
+template <typename POL, typename Index, typename XArgs = xargs<>, typename Alloc = void>
+class WorkSite {};
+
+namespace detail {
+// Host runner: type-erased loops kept in enqueue order.
+template <typename Index>
+struct HostLoops {
+  std::vector<std::function<void()>> loops;
+};
+}  // namespace detail
+
+template <typename EXEC, typename ORDER, typename STORAGE, typename Index, typename Alloc>
+class WorkPool<WorkGroupPolicy<EXEC, ORDER, STORAGE>, Index, xargs<>, Alloc> {
+ public:
+  using policy = WorkGroupPolicy<EXEC, ORDER, STORAGE>;
+  template <typename Seg, typename Body>
+  void enqueue(Seg seg, Body body) {
+    m_loops.push_back([seg, body]() { forall<EXEC>(seg, body); });
+  }
+  void reserve(size_t n, size_t) { m_loops.reserve(n); }
+  size_t num_loops() const { return m_loops.size(); }
+  WorkGroup<policy, Index, xargs<>, Alloc> instantiate() {
+    WorkGroup<policy, Index, xargs<>, Alloc> g;
+    g.m_loops = std::move(m_loops);
+    m_loops.clear();
+    return g;
+  }
+
+ private:
+  std::vector<std::function<void()>> m_loops;
+};
+
+template <typename EXEC, typename ORDER, typename STORAGE, typename Index, typename Alloc>
+class WorkGroup<WorkGroupPolicy<EXEC, ORDER, STORAGE>, Index, xargs<>, Alloc> {
+ public:
+  using policy = WorkGroupPolicy<EXEC, ORDER, STORAGE>;
+  WorkSite<policy, Index, xargs<>, Alloc> run() {
+    if (std::is_same<ORDER, reverse_ordered>::value) {
+      for (auto it = m_loops.rbegin(); it != m_loops.rend(); ++it) (*it)();
+    } else {
+      for (auto& f : m_loops) f();
+    }
+    return {};
+  }
+  void clear() { m_loops.clear(); }
+  std::vector<std::function<void()>> m_loops;
+};
+
+template <typename Pol>
+void synchronize() {}
+
+}  // namespace RAJA

@@ -229,3 +229,14 @@ def dd_scan_f32(x: np.ndarray) -> np.ndarray:
     out = np.empty(x.size, dtype=np.float64)
     _fn("orc_dd_scan_f32", None, [C.c_void_p, C.c_int64, C.c_void_p])(_p(x), x.size, _p(out))
     return out
+
+
+# ------------------------------------------------------------------ jacobi
+def jacobi_sweep(u: np.ndarray, unew: np.ndarray, f: np.ndarray | None, shape) -> float:
+    """One 7-point sweep of one mesh (shape = (nx, ny, nz), x fastest);
+    writes unew's interior and returns the max residual."""
+    nx, ny, nz = shape
+    fp = _p(f) if f is not None else None
+    fn = _fn("orc_jacobi_sweep_f64", C.c_double,
+             [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p])
+    return fn(nx, ny, nz, _p(u), _p(unew), fp)

@@ -634,4 +634,30 @@ void orc_dd_scan_f32(const float* x, int64_t n, double* out) {
   }
 }
 
+// ---- one 7-point Jacobi sweep of one 3-D mesh (x fastest) with the max
+// residual; the iteration / residual structure follows the reference's
+// examples/jacobi.cpp:223-489 (there 2-D), extended to 3-D as the batched
+// mesh configuration specifies.  Operation order matches the documented
+// definition: ((u[i-1]+u[i+1]) + (u[j-1]+u[j+1])) + (u[k-1]+u[k+1]) (+ f),
+// then * (1/6).
+double orc_jacobi_sweep_f64(int nx, int ny, int nz, const double* u, double* unew,
+                            const double* f) {
+  const int64_t sx = nx, sy = int64_t(nx) * ny;
+  double rmax = 0.0;
+  for (int k = 1; k < nz - 1; ++k)
+    for (int j = 1; j < ny - 1; ++j)
+      for (int i = 1; i < nx - 1; ++i) {
+        const int64_t c = k * sy + j * sx + i;
+        double acc = u[c - 1] + u[c + 1];
+        acc += u[c - sx] + u[c + sx];
+        acc += u[c - sy] + u[c + sy];
+        if (f) acc += f[c];
+        const double v = acc * (1.0 / 6.0);
+        unew[c] = v;
+        const double r = std::fabs(v - u[c]);
+        if (r > rmax) rmax = r;
+      }
+  return rmax;
+}
+
 }  // extern "C"

@@ -377,3 +377,180 @@ def prof_read(cap: int = 64) -> dict[str, tuple[int, float]]:
         nm = names.raw[i * stride:(i + 1) * stride].split(b"\0", 1)[0].decode()
         out[nm] = (int(launches[i]), float(ms[i]))
     return out
+
+
+# ------------------------------------------------------------- batched loops
+class BatchPlan:
+    """WorkPool-style plan over many loops (WorkPool::instantiate): loop i
+    covers [0, lens[i]); segment i of a flattened array covers
+    [offsets[i], offsets[i+1])."""
+
+    def __init__(self, lens):
+        import numpy as np
+        self._lens = np.ascontiguousarray(np.asarray(lens, dtype=np.int64))
+        h = C.c_void_p()
+        _lib.call("b200_batch_plan_create", self._lens.ctypes.data_as(C.c_void_p),
+                  int(self._lens.size), C.byref(h))
+        self.handle = h.value
+        self.offsets = np.concatenate([[0], np.cumsum(self._lens)]).astype(np.int64)
+
+    @property
+    def total(self) -> int:
+        return int(self.offsets[-1])
+
+    def info(self) -> dict:
+        total, ntiles, tile, block = C.c_int64(), C.c_int64(), C.c_int(), C.c_int()
+        _lib.call("b200_batch_plan_info", self.handle, C.byref(total), C.byref(ntiles),
+                  C.byref(tile), C.byref(block))
+        return {"total": total.value, "tiles": ntiles.value, "tile": tile.value,
+                "block": block.value}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().b200_batch_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batched_axpy_sum(plan: BatchPlan, a: float, xs, ys, sums, *, mode: int = MODE_COMPENSATED,
+                     autotune: bool = False, sync=True, stream=None):
+    """Every loop i: y_i += a*x_i and sums[i] = sum(y_i), in one persistent
+    launch.  xs / ys: int64 CUDA tensors of device pointers; sums: float64."""
+    name = "b200_batch_autotune_axpy_sum_f32" if autotune else "b200_batched_axpy_sum_f32"
+    _lib.call(name, plan.handle, float(a), xs.data_ptr(), ys.data_ptr(), sums.data_ptr(),
+              int(mode), _stream(stream))
+    _finish(sync, stream)
+    return sums
+
+
+def loop_axpy_sum(a: float, x, y, out, *, mode: int = MODE_COMPENSATED, stream=None):
+    """One loop's fused axpy + sum (one launch), result into out[0]."""
+    _lib.call("b200_loop_axpy_sum_f32", float(a), x.data_ptr(), y.data_ptr(), x.numel(),
+              out.data_ptr(), int(mode), _stream(stream))
+    return out
+
+
+def segmented_inclusive_scan(plan: BatchPlan, x, out=None, *, sync=True, stream=None):
+    """Inclusive int32 sum scan restarting at every segment of the plan."""
+    torch = _torch()
+    out = torch.empty_like(x) if out is None else out
+    _lib.call("b200_segmented_scan_inclusive_i32", plan.handle, x.data_ptr(), out.data_ptr(),
+              _stream(stream))
+    _finish(sync, stream)
+    return out
+
+
+def segmented_exclusive_scan(plan: BatchPlan, x, out=None, *, sync=True, stream=None):
+    """Exclusive int32 sum scan restarting at every segment (0 at heads)."""
+    torch = _torch()
+    out = torch.empty_like(x) if out is None else out
+    _lib.call("b200_segmented_scan_exclusive_i32", plan.handle, x.data_ptr(), out.data_ptr(),
+              _stream(stream))
+    _finish(sync, stream)
+    return out
+
+
+def segmented_sort(plan: BatchPlan, keys, descending: bool = False, *, sync=True, stream=None):
+    """Sort each segment of a uint32 key array independently, in place."""
+    _lib.call("b200_segmented_sort_keys_u32", plan.handle, keys.data_ptr(), int(bool(descending)),
+              _stream(stream))
+    _finish(sync, stream)
+    return keys
+
+
+# ------------------------------------------------------------------- jacobi
+class JacobiPlan:
+    """Batched 3-D meshes (x fastest, stored back to back) for Jacobi
+    sweeps; shapes is a list of (nx, ny, nz)."""
+
+    def __init__(self, shapes):
+        import numpy as np
+        sh = np.asarray(shapes, dtype=np.int32).reshape(-1, 3)
+        self.shapes = [tuple(int(v) for v in r) for r in sh]
+        nx, ny, nz = (np.ascontiguousarray(sh[:, i]) for i in range(3))
+        h = C.c_void_p()
+        _lib.call("b200_jacobi_plan_create", nx.ctypes.data_as(C.c_void_p),
+                  ny.ctypes.data_as(C.c_void_p), nz.ctypes.data_as(C.c_void_p), len(self.shapes),
+                  C.byref(h))
+        self.handle = h.value
+        sizes = sh[:, 0].astype(np.int64) * sh[:, 1] * sh[:, 2]
+        self.offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+
+    @property
+    def total(self) -> int:
+        return int(self.offsets[-1])
+
+    def interior_points(self) -> int:
+        return int(sum((a - 2) * (b - 2) * (c - 2) for a, b, c in self.shapes))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().b200_jacobi_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def jacobi_sweep(plan: JacobiPlan, u, unew, resid, f=None, *, sync=True, stream=None):
+    """One 7-point sweep of every mesh; resid[m] = max |unew - u| (float64)."""
+    _lib.call("b200_jacobi_sweep_f64", plan.handle, u.data_ptr(), unew.data_ptr(),
+              f.data_ptr() if f is not None else None, resid.data_ptr(), _stream(stream))
+    _finish(sync, stream)
+    return resid
+
+
+def jacobi_mesh_sweep(shape, u, unew, resid, f=None, *, sync=True, stream=None):
+    """One sweep of one mesh (one launch)."""
+    nx, ny, nz = shape
+    _lib.call("b200_jacobi_mesh_sweep_f64", int(nx), int(ny), int(nz), u.data_ptr(),
+              unew.data_ptr(), f.data_ptr() if f is not None else None, resid.data_ptr(),
+              _stream(stream))
+    _finish(sync, stream)
+    return resid
+
+
+# ------------------------------------------------------------------- graphs
+class Graph:
+    """Capture library calls issued on `stream` into a CUDA graph:
+
+        with rg.Graph(stream) as g:
+            rg.jacobi_sweep(..., sync=False, stream=stream)
+        g.launch()
+    """
+
+    def __init__(self, stream):
+        self.stream = _stream(stream)
+        self.handle = None
+
+    def __enter__(self):
+        _lib.call("b200_graph_capture_begin", self.stream)
+        return self
+
+    def __exit__(self, *exc):
+        h = C.c_void_p()
+        _lib.call("b200_graph_capture_end", self.stream, C.byref(h))
+        self.handle = h.value
+        return False
+
+    def launch(self):
+        _lib.call("b200_graph_launch", self.handle, self.stream)
+
+    def close(self):
+        if self.handle:
+            _lib.load().b200_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

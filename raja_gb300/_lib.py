@@ -89,6 +89,12 @@ def _signatures() -> dict[str, tuple]:
         "b200_segmented_scan_inclusive_i32": (_I, [_P, _P, _P, _P]),
         "b200_segmented_scan_exclusive_i32": (_I, [_P, _P, _P, _P]),
         "b200_segmented_sort_keys_u32": (_I, [_P, _P, _I, _P]),
+        "b200_jacobi_plan_create": (_I, [_P, _P, _P, _I, _P]),
+        "b200_jacobi_plan_destroy": (_I, [_P]),
+        "b200_jacobi_plan_info": (_I, [_P, _P, _P, _P]),
+        "b200_jacobi_plan_offsets": (_P, [_P]),
+        "b200_jacobi_sweep_f64": (_I, [_P, _P, _P, _P, _P, _P]),
+        "b200_jacobi_mesh_sweep_f64": (_I, [_I, _I, _I, _P, _P, _P, _P, _P]),
         "b200_graph_capture_begin": (_I, [_P]),
         "b200_graph_capture_end": (_I, [_P, _P]),
         "b200_graph_launch": (_I, [_P, _P]),

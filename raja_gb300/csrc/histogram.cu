@@ -10,40 +10,26 @@
 // opt-in); bins beyond that go straight to global 64-bit atomics.  Small
 // histograms are replicated R ways, interleaved so that lanes of one warp
 // that hit the same bin land on different banks and addresses.  Large
-// histograms aggregate within the warp first (__match_any_sync): one
-// shared atomic per distinct bin per warp instruction, so the heavy head of
-// a Zipf distribution does not serialise on one address.  At the end each
-// block adds its non-zero counters into the global 64-bit counts.
+// histograms use one copy and plain shared atomics: a warp-wide vote to
+// aggregate equal bins (__match_any_sync) costs ~80 cycles per warp on this
+// GPU, more than the few replays a Zipf head causes.  At the end each block
+// adds its non-zero counters into the global 64-bit counts.
 #include "b200_internal.cuh"
 
 namespace b200 {
 namespace {
 
-constexpr int HBLOCK = 512;
+constexpr int HBLOCK = 1024;
 
-template <bool AGG>
 __device__ __forceinline__ void count_one(uint32_t* sh, int R, int rsel, uint32_t v,
-                                          uint32_t nbins, uint32_t sbins,
-                                          unsigned long long* gcounts, bool valid) {
-  if (AGG) {
-    // warp aggregation; invalid lanes use unique keys that never match
-    const uint32_t key = valid ? v : (0x80000000u | threadIdx.x);
-    const uint32_t peers = __match_any_sync(0xffffffffu, key);
-    if (valid && (threadIdx.x & 31) == __ffs(peers) - 1) {
-      const uint32_t c = __popc(peers);
-      if (v < sbins) atomicAdd(sh + v, c);
-      else atomicAdd(gcounts + v, (unsigned long long)c);
-    }
-  } else {
-    if (valid) {
-      if (v < sbins) atomicAdd(sh + size_t(v) * R + rsel, 1u);
-      else atomicAdd(gcounts + v, 1ull);
-    }
+                                          uint32_t sbins, unsigned long long* gcounts,
+                                          bool valid) {
+  if (valid) {
+    if (v < sbins) atomicAdd(sh + size_t(v) * R + rsel, 1u);
+    else atomicAdd(gcounts + v, 1ull);
   }
-  (void)nbins;
 }
 
-template <bool AGG>
 __global__ void __launch_bounds__(HBLOCK)
 hist_kernel(const int32_t* __restrict__ x, size_t n, uint32_t nbins, uint32_t sbins, int R,
             int vec_ok, unsigned long long* __restrict__ gcounts) {
@@ -58,37 +44,30 @@ hist_kernel(const int32_t* __restrict__ x, size_t n, uint32_t nbins, uint32_t sb
   if (vec_ok) {
     const size_t nvec = n / 4;
     constexpr int U = 4;
-    // all lanes of a warp run the same number of iterations (for the match)
-    const size_t wstart = gt - (tid & 31);
-    for (size_t vb = wstart * 1; vb < nvec; vb += nt * U) {
+    size_t v = gt;
+    for (; v + (U - 1) * nt < nvec; v += U * nt) {
       int4 q[U];
-      bool ok[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const size_t vi = vb + size_t(u) * nt + (tid & 31);
-        ok[u] = vi < nvec;
-        q[u] = ok[u] ? __ldcs(reinterpret_cast<const int4*>(x) + vi) : make_int4(0, 0, 0, 0);
-      }
+      for (int u = 0; u < U; ++u) q[u] = __ldcs(reinterpret_cast<const int4*>(x) + v + u * nt);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const uint32_t e[4] = {uint32_t(q[u].x), uint32_t(q[u].y), uint32_t(q[u].z), uint32_t(q[u].w)};
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-          count_one<AGG>(sh, R, rsel, e[k], nbins, sbins, gcounts, ok[u] && e[k] < nbins);
+        for (int k = 0; k < 4; ++k) count_one(sh, R, rsel, e[k], sbins, gcounts, e[k] < nbins);
       }
+    }
+    for (; v < nvec; v += nt) {
+      const int4 q = __ldcs(reinterpret_cast<const int4*>(x) + v);
+      const uint32_t e[4] = {uint32_t(q.x), uint32_t(q.y), uint32_t(q.z), uint32_t(q.w)};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) count_one(sh, R, rsel, e[k], sbins, gcounts, e[k] < nbins);
     }
     done = nvec * 4;
   }
   // scalar remainder (or the whole input when unaligned)
-  {
-    const size_t rem = n - done;
-    const size_t wstart = gt - (tid & 31);
-    for (size_t b = wstart; b < rem; b += nt) {
-      const size_t i = b + (tid & 31);
-      const bool ok = i < rem;
-      const uint32_t v = ok ? uint32_t(x[done + i]) : 0u;
-      count_one<AGG>(sh, R, rsel, v, nbins, sbins, gcounts, ok && v < nbins);
-    }
+  for (size_t i = done + gt; i < n; i += nt) {
+    const uint32_t v = uint32_t(x[i]);
+    count_one(sh, R, rsel, v, sbins, gcounts, v < nbins);
   }
   __syncthreads();
   for (uint32_t b = tid; b < sbins; b += HBLOCK) {
@@ -114,39 +93,25 @@ extern "C" int b200_histogram_i32(const int32_t* x, size_t n, int32_t nbins, uin
   DeviceProps p;
   B200_TRY(device_props(&p));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // shared counters: up to 8 lane-interleaved replicas while they fit,
+  // otherwise one copy of as many bins as fit
   const size_t cap_words = (p.smem_per_block_optin > 4096 ? p.smem_per_block_optin - 4096 : 0) / 4;
-  const bool agg = nbins > 2048;
-  int R = 1;
-  uint32_t sbins;
-  if (!agg) {
-    R = 8;
-    while (R > 1 && size_t(nbins) * R > cap_words) R >>= 1;
-    sbins = uint32_t(nbins);
-    if (size_t(sbins) * R > cap_words) sbins = uint32_t(cap_words / R);
-  } else {
-    sbins = uint32_t(size_t(nbins) < cap_words ? size_t(nbins) : cap_words);
-  }
+  int R = 8;
+  while (R > 1 && size_t(nbins) * R > cap_words) R >>= 1;
+  uint32_t sbins = uint32_t(nbins);
+  if (size_t(sbins) * R > cap_words) sbins = uint32_t(cap_words / R);
   const size_t smem = size_t(sbins) * R * 4;
   int bps = 0;
-  if (agg) {
-    B200_CUDA(cudaFuncSetAttribute(hist_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, hist_kernel<true>, HBLOCK, smem));
-  } else {
-    B200_CUDA(cudaFuncSetAttribute(hist_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, hist_kernel<false>, HBLOCK, smem));
-  }
+  B200_CUDA(cudaFuncSetAttribute(hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, hist_kernel, HBLOCK, smem));
   if (bps < 1) bps = 1;
   size_t grid = size_t(p.sms) * bps;
   const size_t need = (n / 4 + HBLOCK - 1) / HBLOCK + 1;
   if (grid > need) grid = need;
   const bool vec_ok = reinterpret_cast<uintptr_t>(x) % 16 == 0;
   auto* gc = reinterpret_cast<unsigned long long*>(counts);
-  if (agg)
-    B200_LAUNCH("b200_histogram_agg", hist_kernel<true>, (unsigned)grid, HBLOCK, smem, s, x, n,
-                uint32_t(nbins), sbins, R, int(vec_ok), gc);
-  else
-    B200_LAUNCH("b200_histogram_rep", hist_kernel<false>, (unsigned)grid, HBLOCK, smem, s, x, n,
-                uint32_t(nbins), sbins, R, int(vec_ok), gc);
+  B200_LAUNCH("b200_histogram", hist_kernel, (unsigned)grid, HBLOCK, smem, s, x, n, uint32_t(nbins),
+              sbins, R, int(vec_ok), gc);
   clear_error();
   return B200_OK;
 }

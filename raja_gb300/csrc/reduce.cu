@@ -205,6 +205,53 @@ struct Extremum {
   }
 };
 
+// FP64 Min / Max with location, compared on the integer pipes.  GB300's
+// FP64 unit retires far fewer DSETP than the HBM stream delivers doubles,
+// so each double is mapped to an order-preserving int64 key instead:
+// -0.0 is folded onto +0.0 (they compare equal, as with operator<), the
+// bits of negative values except the sign are inverted, and NaNs are
+// skipped (operator< never selects them).  The original bits are kept for
+// the result; ties resolve to the lowest index as above.
+template <bool MIN, bool WITH_LOC>
+struct ExtremumF64 {
+  using T = double;
+  struct Acc {
+    long long key;
+    long long i;
+    long long bits;
+  };
+  using Part = Acc;
+  static __device__ __forceinline__ long long key_of(long long b) {
+    const long long c = ((b << 1) == 0) ? 0ll : b;
+    return c ^ ((c >> 63) & 0x7fffffffffffffffll);
+  }
+  static __device__ __forceinline__ bool is_nan(long long b) {
+    return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+  }
+  static __device__ Acc identity() {
+    const long long b = __double_as_longlong(MIN ? DBL_MAX : -DBL_MAX);
+    return {key_of(b), -1, b};
+  }
+  static __device__ void add(Acc& a, double v, int64_t i) {
+    const long long b = __double_as_longlong(v);
+    if (is_nan(b)) return;
+    const long long k = key_of(b);
+    if (MIN ? (k < a.key) : (a.key < k)) { a.key = k; a.i = i; a.bits = b; }
+  }
+  static __device__ void add2(Acc&, double, double) {}
+  static __device__ Acc merge(Acc a, Acc b) {
+    if ((MIN ? (b.key < a.key) : (a.key < b.key)) || (b.key == a.key && b.i < a.i)) return b;
+    return a;
+  }
+  static __device__ Part to_part(Acc a) { return a; }
+  static __device__ Part part_identity() { return identity(); }
+  static __device__ Part merge_part(Part a, Part b) { return merge(a, b); }
+  static __device__ void store(OutPtrs o, Part p) {
+    *static_cast<double*>(o.val) = __longlong_as_double(p.bits);
+    if (WITH_LOC) *o.idx = p.i;
+  }
+};
+
 template <class TT, bool OR>
 struct BitOp {
   using T = TT;
@@ -424,14 +471,19 @@ int b200_reduce_sum_u64(const uint64_t* x, size_t n, int mode, uint64_t* out, b2
     return run_reduce<Extremum<T, MIN, false>, false>("b200_reduce_" #NAME, x, nullptr, n, \
                                                       false, OutPtrs{out, nullptr}, s);  \
   }
+#define B200_MINMAX_F64(NAME, MIN)                                                        \
+  int b200_reduce_##NAME(const double* x, size_t n, double* out, b200_stream_t s) {        \
+    return run_reduce<ExtremumF64<MIN, false>, false>("b200_reduce_" #NAME, x, nullptr, n,  \
+                                                      false, OutPtrs{out, nullptr}, s);    \
+  }
 B200_MINMAX(min_f32, float, true)
-B200_MINMAX(min_f64, double, true)
+B200_MINMAX_F64(min_f64, true)
 B200_MINMAX(min_i32, int32_t, true)
 B200_MINMAX(min_i64, int64_t, true)
 B200_MINMAX(min_u32, uint32_t, true)
 B200_MINMAX(min_u64, uint64_t, true)
 B200_MINMAX(max_f32, float, false)
-B200_MINMAX(max_f64, double, false)
+B200_MINMAX_F64(max_f64, false)
 B200_MINMAX(max_i32, int32_t, false)
 B200_MINMAX(max_i64, int64_t, false)
 B200_MINMAX(max_u32, uint32_t, false)
@@ -445,11 +497,18 @@ B200_MINMAX(max_u64, uint64_t, false)
                                                      false, OutPtrs{val, idx}, s);        \
   }
 B200_LOC(minloc_f32, float, true)
-B200_LOC(minloc_f64, double, true)
+#define B200_LOC_F64(NAME, MIN)                                                           \
+  int b200_reduce_##NAME(const double* x, size_t n, double* val, int64_t* idx,              \
+                         b200_stream_t s) {                                                 \
+    if (!idx) return fail(B200_ERR_ARG, "b200_reduce_" #NAME ": null index pointer");       \
+    return run_reduce<ExtremumF64<MIN, true>, false>("b200_reduce_" #NAME, x, nullptr, n,   \
+                                                     false, OutPtrs{val, idx}, s);         \
+  }
+B200_LOC_F64(minloc_f64, true)
 B200_LOC(minloc_i32, int32_t, true)
 B200_LOC(minloc_i64, int64_t, true)
 B200_LOC(maxloc_f32, float, false)
-B200_LOC(maxloc_f64, double, false)
+B200_LOC_F64(maxloc_f64, false)
 B200_LOC(maxloc_i32, int32_t, false)
 B200_LOC(maxloc_i64, int64_t, false)
 #undef B200_LOC

@@ -8,16 +8,16 @@
 //
 // GB300 design: one single-pass kernel with decoupled look-back (Merrill &
 // Garland, "Single-pass Parallel Prefix Scan with Decoupled Look-back",
-// NVIDIA TR 2016).  A tile is 256 threads x 64 bytes.  Tiles take their id
+// NVIDIA TR 2016).  A tile is 256 threads x 128 bytes.  Tiles take their id
 // from an atomic counter in launch order, so every predecessor of a tile
 // has already started and will publish its aggregate without waiting on
 // anything: the look-back always terminates.  It is still bounded -- after
 // spin_limit polls the tile gives up, ORs a code into the device status
 // word and finishes, so a broken invariant can never hang the GPU.
-// Global traffic is one coalesced 16-byte read and one 16-byte write per
-// element group; tiles are transposed through an XOR-swizzled shared
-// buffer so every thread scans 64 contiguous bytes without bank conflicts.
-// The look-back is done by one warp that inspects 32 predecessors at once.
+// Global traffic is one TMA bulk read and one coalesced 16-byte write per
+// element group.  The look-back is done by one warp that inspects 256
+// predecessors per poll (eight per lane), so a distant inclusive prefix
+// costs one L2 round trip per 256 tiles.
 #include <cfloat>
 #include <climits>
 #include <type_traits>
@@ -31,12 +31,18 @@ constexpr int SBLOCK = 256;
 constexpr int SWARPS = SBLOCK / 32;
 constexpr uint32_t FLAG_AGG = 1, FLAG_INCL = 2;
 
+// A tile is 256 threads x G 16-byte granules.  Thread t owns granules
+// j*256 + t (j = 0..G-1): consecutive threads touch consecutive granules,
+// so both the TMA-filled shared buffer and the global stores are accessed
+// without bank conflicts and fully coalesced, with no transposition.
 template <class T>
 struct Tile {
-  static constexpr int VN = 16 / sizeof(T);
-  static constexpr int ITEMS = 64 / sizeof(T);
-  static constexpr int SIZE = SBLOCK * ITEMS;
+  static constexpr int VN = 16 / sizeof(T);   // elements per granule
+  static constexpr int G = 8;                 // granules per thread
+  static constexpr int ITEMS = G * VN;
+  static constexpr int SIZE = SBLOCK * ITEMS; // 32 KB
 };
+constexpr int LBJ = 8;  // predecessors each look-back lane inspects per poll
 
 template <class T>
 struct Inf;
@@ -176,15 +182,6 @@ __device__ __forceinline__ double fold_local<ScanSumCompF32>(double p, PairT<flo
   return p + (double(l.s) + double(l.c));
 }
 
-// XOR swizzle of 16-byte granules within groups of eight: conflict-free
-// for both the warp-striped (global side) and per-thread (scan side) views.
-template <class T>
-__device__ __forceinline__ int swz(int e) {
-  constexpr int VN = 16 / sizeof(T);
-  const int g = e / VN;
-  return ((g ^ ((g >> 3) & 7)) * VN) + (e % VN);
-}
-
 template <class P>
 __device__ __forceinline__ P ld_cg_val(const P* p) {
   static_assert(sizeof(P) % 4 == 0, "carry size");
@@ -198,185 +195,239 @@ __device__ __forceinline__ P ld_cg_val(const P* p) {
   return r;
 }
 
+template <class Op>
+struct ScanSmem {
+  using T = typename Op::T;
+  using Local = typename Op::Local;
+  alignas(128) T stage[Tile<T>::SIZE];       // the tile, filled by one TMA bulk copy
+  Local wtot[Tile<T>::G * SWARPS];           // warp totals, sub-tile major
+  Local pref[Tile<T>::G * SWARPS];           // their exclusive prefix in the tile
+  typename Op::Carry prefix;                 // the tile's carry-in
+  uint64_t bar;
+  uint32_t tile;
+};
+
+// One tile per block.  Tiles take their id from an atomic counter in
+// launch order, so every predecessor of a tile has already started and
+// publishes its aggregate without waiting on anything: the look-back
+// always terminates.  The tile arrives by one TMA bulk copy (cp.async.bulk
+// completed on an mbarrier) straight into shared memory, so no registers
+// stage it and five or more blocks fit per SM: while one block waits in its
+// look-back, the others keep HBM busy.
 template <class Op, bool EXCL>
 __global__ void __launch_bounds__(SBLOCK)
 scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op::T init,
-            int vec_ok, uint32_t* flags, typename Op::Carry* aggs, typename Op::Carry* incls,
-            uint32_t* tile_counter, uint32_t* status, uint32_t spin_limit) {
+            int tma_ok, int vec_out, uint32_t* flags, typename Op::Carry* aggs,
+            typename Op::Carry* incls, uint32_t* tile_counter, uint32_t* status,
+            uint32_t spin_limit) {
   using T = typename Op::T;
   using Local = typename Op::Local;
   using Carry = typename Op::Carry;
-  constexpr int VN = Tile<T>::VN, ITEMS = Tile<T>::ITEMS, TS = Tile<T>::SIZE;
-  __shared__ __align__(16) T sm[TS];
-  __shared__ Local sh_warp[SWARPS];
-  __shared__ Carry sh_prefix;
-  __shared__ uint32_t sh_tile;
-
+  constexpr int VN = Tile<T>::VN, G = Tile<T>::G, TS = Tile<T>::SIZE;
+  static_assert(G * SWARPS == 64, "prefix table: two entries per lane of warp 0");
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  ScanSmem<Op>& sm = *reinterpret_cast<ScanSmem<Op>*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) sh_tile = atomicAdd(tile_counter, 1u);
+  T* st = sm.stage;
+  if (tid == 0) {
+    sm.tile = atomicAdd(tile_counter, 1u);
+    mbar_init(&sm.bar, 1);
+    fence_mbar_init();
+    const size_t b0 = size_t(sm.tile) * TS;
+    if (tma_ok && b0 + TS <= n) {
+      mbar_arrive_expect_tx(&sm.bar, TS * sizeof(T));
+      tma_load_1d(st, in + b0, TS * sizeof(T), &sm.bar);
+    }
+  }
   __syncthreads();
-  const size_t tile = sh_tile;
+  const size_t tile = sm.tile;
   const size_t base = tile * TS;
   const bool full = base + TS <= n;
-
-  // ---- load the tile (coalesced) into swizzled shared memory
-  if (full && vec_ok) {
-#pragma unroll
-    for (int j = 0; j < ITEMS / VN; ++j) {
-      const int g = j * SBLOCK + tid;
-      Vec16<T> v = ld_vec_stream(in + base + size_t(g) * VN);
-      *reinterpret_cast<Vec16<T>*>(&sm[swz<T>(g * VN)]) = v;
+  if (tma_ok && full) {
+    if (!mbar_wait(&sm.bar, 0, spin_limit)) {
+      if (tid == 0) atomicOr(status, kStatusTmaTimeout);
+      mbar_wait(&sm.bar, 0, spin_limit);  // let the copy land before the block exits
     }
   } else {
-    for (int e = tid; e < TS; e += SBLOCK) {
-      const size_t i = base + e;
-      sm[swz<T>(e)] = (i < n) ? in[i] : T(0);
-    }
+    for (int e = tid; e < TS; e += SBLOCK) st[e] = (base + e < n) ? in[base + e] : T(0);
+    __syncthreads();
   }
-  __syncthreads();
-
-  // ---- per-thread sequential scan of 64 contiguous bytes
-  Local loc[ITEMS];
-  const int first = tid * ITEMS;
   {
-    T xs[ITEMS];
+    // ---- granule totals and per-sub-tile warp scans
+    Local lex[G];
 #pragma unroll
-    for (int q = 0; q < ITEMS / VN; ++q) {
-      // 16-byte shared reads: conflict-free under the swizzle
-      const Vec16<T> v = *reinterpret_cast<const Vec16<T>*>(&sm[swz<T>(first + q * VN)]);
-#pragma unroll
-      for (int k = 0; k < VN; ++k) xs[q * VN + k] = v.v[k];
-    }
-#pragma unroll
-    for (int k = 0; k < ITEMS; ++k) {
-      const size_t i = base + first + k;
-      const Local v = (i < n) ? Op::lift(xs[k]) : Op::ident();
-      loc[k] = (k == 0) ? v : Op::comb(loc[k - 1], v);
-    }
-  }
-
-  // ---- warp inclusive scan of thread totals
-  Local tot = loc[ITEMS - 1];
-  Local inc = tot;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    Local other = shfl_up_any(inc, o);
-    if (lane >= o) inc = Op::comb(other, inc);
-  }
-  Local lane_excl = shfl_up_any(inc, 1);
-  if (lane == 31) sh_warp[warp] = inc;
-  __syncthreads();
-
-  // ---- block: warp prefix and tile aggregate
-  Local tile_agg = sh_warp[0];
-  Local warp_excl = Op::ident();
-#pragma unroll
-  for (int w = 1; w < SWARPS; ++w) {
-    if (w == warp) warp_excl = tile_agg;
-    tile_agg = Op::comb(tile_agg, sh_warp[w]);
-  }
-  // thread prefix inside the tile (absent for thread 0)
-  const bool has_tp = tid != 0;
-  Local tp;
-  if (warp == 0) tp = lane_excl;
-  else tp = (lane == 0) ? warp_excl : Op::comb(warp_excl, lane_excl);
-
-  // ---- publish and look back (warp 0)
-  if (warp == 0) {
-    Carry prefix = Op::cident();
-    bool have = false;
-    if (tile == 0) {
-      if (EXCL) { prefix = Op::from_init(init); have = true; }
-      if (lane == 0) {
-        incls[0] = have ? Op::ccomb(prefix, Op::to_carry(tile_agg)) : Op::to_carry(tile_agg);
-        st_release(flags, FLAG_INCL);
-      }
-    } else {
-      if (lane == 0) {
-        aggs[tile] = Op::to_carry(tile_agg);
-        st_release(flags + tile, FLAG_AGG);
-      }
-      long long pred = (long long)tile - 1;
-      Carry acc = Op::cident();
-      bool timed_out = false;
-      while (true) {
-        const long long t = pred - lane;
-        uint32_t f = (t >= 0) ? ld_acquire(flags + t) : FLAG_INCL;
-        uint32_t spins = 0;
-        while (!__all_sync(0xffffffffu, f != 0)) {
-          if (f == 0) f = ld_acquire(flags + t);
-          if (++spins > spin_limit) { timed_out = true; break; }
-          if (spins > 8) __nanosleep(64);
-        }
-        timed_out = __any_sync(0xffffffffu, timed_out);
-        if (timed_out) break;
-        const uint32_t im = __ballot_sync(0xffffffffu, f == FLAG_INCL);
-        const int stop = im ? (__ffs(im) - 1) : 32;
-        Carry v = Op::cident();
-        if (lane < stop) v = ld_cg_val(aggs + t);
-        else if (lane == stop) v = ld_cg_val(incls + t);
-        // ordered combine: higher lane = earlier tile
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          Carry other = shfl_idx_any(v, (lane + o) & 31);
-          if (lane + o < 32) v = Op::ccomb(other, v);
-        }
-        const Carry window = shfl_idx_any(v, 0);
-        acc = Op::ccomb(window, acc);
-        if (im) break;
-        pred -= 32;
-      }
-      if (timed_out && lane == 0) atomicOr(status, kStatusScanTimeout);
-      prefix = acc;
-      have = true;
-      if (lane == 0) {
-        incls[tile] = Op::ccomb(prefix, Op::to_carry(tile_agg));
-        st_release(flags + tile, FLAG_INCL);
-      }
-    }
-    if (lane == 0) sh_prefix = prefix;
-    (void)have;
-  }
-  __syncthreads();
-
-  // ---- combine prefixes and write outputs into shared memory
-  const bool tile_has_prefix = EXCL || tile > 0;
-  Carry P = sh_prefix;
-  bool hasP = tile_has_prefix;
-  if (has_tp) {
-    if (hasP) P = fold_local<Op>(P, tp);
-    else P = Op::to_carry(tp);
-    hasP = true;
-  }
-#pragma unroll
-  for (int q = 0; q < ITEMS / VN; ++q) {
-    Vec16<T> v;
-#pragma unroll
-    for (int kk = 0; kk < VN; ++kk) {
-      const int k = q * VN + kk;
-      T r;
-      if (EXCL) r = (k == 0) ? Op::out_prefix(P) : Op::out(P, loc[k - 1]);
-      else r = hasP ? Op::out(P, loc[k]) : Op::out_local(loc[k]);
-      v.v[kk] = r;
-    }
-    *reinterpret_cast<Vec16<T>*>(&sm[swz<T>(first + q * VN)]) = v;
-  }
-  __syncthreads();
-
-  // ---- store the tile (coalesced)
-  if (full && vec_ok) {
-#pragma unroll
-    for (int j = 0; j < ITEMS / VN; ++j) {
+    for (int j = 0; j < G; ++j) {
       const int g = j * SBLOCK + tid;
-      Vec16<T> v = *reinterpret_cast<const Vec16<T>*>(&sm[swz<T>(g * VN)]);
-      st_vec_stream(out + base + size_t(g) * VN, v);
+      const Vec16<T> v = *reinterpret_cast<const Vec16<T>*>(&st[g * VN]);
+      Local tot = Op::ident();
+#pragma unroll
+      for (int k = 0; k < VN; ++k) {
+        const Local x = (full || base + size_t(g) * VN + k < n) ? Op::lift(v.v[k]) : Op::ident();
+        tot = (k == 0) ? x : Op::comb(tot, x);
+      }
+      Local inc = tot;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const Local other = shfl_up_any(inc, o);
+        if (lane >= o) inc = Op::comb(other, inc);
+      }
+      lex[j] = shfl_up_any(inc, 1);
+      if (lane == 31) sm.wtot[j * SWARPS + warp] = inc;
     }
-  } else {
-    for (int e = tid; e < TS; e += SBLOCK) {
-      const size_t i = base + e;
-      if (i < n) out[i] = sm[swz<T>(e)];
+    __syncthreads();
+
+    // ---- warp 0: prefix table, tile aggregate, publish, look-back
+    if (warp == 0) {
+      const Local a = sm.wtot[2 * lane], c = sm.wtot[2 * lane + 1];
+      Local pin = Op::comb(a, c);
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const Local other = shfl_up_any(pin, o);
+        if (lane >= o) pin = Op::comb(other, pin);
+      }
+      const Local pex = shfl_up_any(pin, 1);
+      if (lane == 0) {
+        sm.pref[0] = Op::ident();
+        sm.pref[1] = a;
+      } else {
+        sm.pref[2 * lane] = pex;
+        sm.pref[2 * lane + 1] = Op::comb(pex, a);
+      }
+      const Local tile_agg = shfl_idx_any(pin, 31);
+      Carry prefix = Op::cident();
+      if (tile == 0) {
+        if (EXCL) prefix = Op::from_init(init);
+        if (lane == 0) {
+          incls[0] = EXCL ? Op::ccomb(prefix, Op::to_carry(tile_agg)) : Op::to_carry(tile_agg);
+          st_release(flags, FLAG_INCL);
+        }
+      } else {
+        if (lane == 0) {
+          aggs[tile] = Op::to_carry(tile_agg);
+          st_release(flags + tile, FLAG_AGG);
+        }
+        // One warp inspects 32 x LBJ = 256 predecessors per poll: lane l
+        // covers tiles pred - l*LBJ - j, j = 0..LBJ-1 (nearest first).
+        long long pred = (long long)tile - 1;
+        Carry acc = Op::cident();
+        bool timed_out = false;
+        while (true) {
+          const long long t0 = pred - (long long)lane * LBJ;
+          uint32_t f[LBJ];
+#pragma unroll
+          for (int j = 0; j < LBJ; ++j) f[j] = (t0 - j >= 0) ? ld_acquire(flags + (t0 - j)) : FLAG_INCL;
+          uint32_t spins = 0;
+          while (true) {
+            bool ready = true;
+#pragma unroll
+            for (int j = 0; j < LBJ; ++j) ready = ready && (f[j] != 0);
+            if (__all_sync(0xffffffffu, ready)) break;
+            if (++spins > spin_limit) { timed_out = true; break; }
+            if (spins > 8) __nanosleep(64);
+#pragma unroll
+            for (int j = 0; j < LBJ; ++j)
+              if (f[j] == 0) f[j] = ld_acquire(flags + (t0 - j));
+          }
+          timed_out = __any_sync(0xffffffffu, timed_out);
+          if (timed_out) break;
+          int jstop = LBJ;
+#pragma unroll
+          for (int j = LBJ - 1; j >= 0; --j)
+            if (f[j] == FLAG_INCL) jstop = j;
+          const uint32_t im = __ballot_sync(0xffffffffu, jstop < LBJ);
+          const int stop = im ? (__ffs(im) - 1) : 32;
+          // fold this lane's window, earliest tile first
+          Carry v = Op::cident();
+          if (lane < stop) {
+            v = ld_cg_val(aggs + (t0 - (LBJ - 1)));
+#pragma unroll
+            for (int j = LBJ - 2; j >= 0; --j) v = Op::ccomb(v, ld_cg_val(aggs + (t0 - j)));
+          } else if (lane == stop) {
+            v = ld_cg_val(incls + (t0 - jstop));
+#pragma unroll
+            for (int j = LBJ - 2; j >= 0; --j)
+              if (j < jstop) v = Op::ccomb(v, ld_cg_val(aggs + (t0 - j)));
+          }
+          // ordered combine across lanes: higher lane = earlier tiles
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const Carry other = shfl_idx_any(v, (lane + o) & 31);
+            if (lane + o < 32) v = Op::ccomb(other, v);
+          }
+          acc = Op::ccomb(shfl_idx_any(v, 0), acc);
+          if (im) break;
+          pred -= 32 * LBJ;
+        }
+        if (timed_out && lane == 0) atomicOr(status, kStatusScanTimeout);
+        prefix = acc;
+        if (lane == 0) {
+          incls[tile] = Op::ccomb(prefix, Op::to_carry(tile_agg));
+          st_release(flags + tile, FLAG_INCL);
+        }
+      }
+      if (lane == 0) sm.prefix = prefix;
+    }
+    __syncthreads();
+
+    // ---- outputs: carry-in + prefix of earlier sub-tiles and warps + lane
+    // prefix + running scan of the granule, stored straight from registers
+    const Carry TP = sm.prefix;
+    const bool tile_has = EXCL || tile > 0;
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      const int g = j * SBLOCK + tid;
+      bool has_tp = true;
+      Local tp;
+      if (j == 0 && warp == 0) {
+        has_tp = lane > 0;
+        tp = lex[0];
+      } else {
+        const Local pw = sm.pref[j * SWARPS + warp];
+        tp = (lane > 0) ? Op::comb(pw, lex[j]) : pw;
+      }
+      Carry P = TP;
+      bool hasP = tile_has;
+      if (has_tp) {
+        P = hasP ? fold_local<Op>(TP, tp) : Op::to_carry(tp);
+        hasP = true;
+      }
+      const Vec16<T> v = *reinterpret_cast<const Vec16<T>*>(&st[g * VN]);
+      Vec16<T> o;
+      Local run = Op::ident();
+#pragma unroll
+      for (int k = 0; k < VN; ++k) {
+        const Local x = (full || base + size_t(g) * VN + k < n) ? Op::lift(v.v[k]) : Op::ident();
+        if (EXCL) o.v[k] = (k == 0) ? Op::out_prefix(P) : Op::out(P, run);
+        run = (k == 0) ? x : Op::comb(run, x);
+        if (!EXCL) o.v[k] = hasP ? Op::out(P, run) : Op::out_local(run);
+      }
+      T* dst = out + base + size_t(g) * VN;
+      if (full && vec_out) {
+        st_vec_stream(dst, o);
+      } else {
+#pragma unroll
+        for (int k = 0; k < VN; ++k)
+          if (base + size_t(g) * VN + k < n) dst[k] = o.v[k];
+      }
     }
   }
+}
+
+template <class Op, bool EXCL>
+int launch_scan(const char* name, unsigned grid, cudaStream_t s, const typename Op::T* in,
+                typename Op::T* out, size_t n, typename Op::T init, int tma_ok, int vec_out,
+                uint32_t* flags, typename Op::Carry* aggs, typename Op::Carry* incls,
+                uint32_t* counter, uint32_t* status, uint32_t lim) {
+  auto kern = scan_kernel<Op, EXCL>;
+  static bool attr = false;
+  if (!attr) {
+    B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(sizeof(ScanSmem<Op>))));
+    attr = true;
+  }
+  B200_LAUNCH(name, kern, grid, SBLOCK, sizeof(ScanSmem<Op>), s, in, out, n, init, tma_ok, vec_out,
+              flags, aggs, incls, counter, status, lim);
+  return B200_OK;
 }
 
 template <class Op, bool EXCL>
@@ -405,10 +456,10 @@ int run_scan(const char* name, const typename Op::T* in, typename Op::T* out, si
   uint32_t* status = nullptr;
   B200_TRY(status_word(&status));
   B200_CUDA(cudaMemsetAsync(flags, 0, (tiles + 64) * sizeof(uint32_t), s));
-  const bool vec_ok = reinterpret_cast<uintptr_t>(in) % 16 == 0 &&
-                      reinterpret_cast<uintptr_t>(out) % 16 == 0;
-  B200_LAUNCH(name, (scan_kernel<Op, EXCL>), (unsigned)tiles, SBLOCK, 0, s, in, out, n, init,
-              int(vec_ok), flags, aggs, incls, counter, status, spin_limit());
+  const int tma_ok = reinterpret_cast<uintptr_t>(in) % 16 == 0;
+  const int vec_out = reinterpret_cast<uintptr_t>(out) % 16 == 0;
+  B200_TRY((launch_scan<Op, EXCL>(name, unsigned(tiles), s, in, out, n, init, tma_ok, vec_out,
+                                   flags, aggs, incls, counter, status, spin_limit())));
   clear_error();
   return B200_OK;
 }
@@ -524,8 +575,8 @@ int b200_selftest_scan_timeout(b200_stream_t stream) {
   B200_CUDA(cudaStreamSynchronize(s));  // `one` lives on this stack frame
   uint32_t lim = spin_limit();
   if (lim > (1u << 16)) lim = 1u << 16;
-  B200_LAUNCH("b200_selftest_scan_timeout", (scan_kernel<Op, false>), 1, SBLOCK, 0, s, data, data,
-              n, 0, 1, flags, aggs, incls, flags + 32, status, lim);
+  B200_TRY((launch_scan<Op, false>("b200_selftest_scan_timeout", 1, s, data, data, n, 0, 1, 1,
+                                   flags, aggs, incls, flags + 32, status, lim)));
   clear_error();
   return B200_OK;
 }

@@ -10,16 +10,19 @@
 // GB300 design (onesweep, Adinets & Merrill, "Onesweep: A Faster Least
 // Significant Digit Radix Sort for GPUs", 2022):
 //   1. hist_kernel: one read of the keys builds the 256-bin histogram of
-//      every 8-bit digit position at once (warp-aggregated shared atomics,
-//      so skewed digits such as float exponents do not serialise);
+//      every 8-bit digit position at once (per-warp shared counters); it
+//      also zeroes the first pass's look-back status words;
 //   2. bins_kernel: exclusive scan of each histogram -> global digit bases;
 //   3. one onesweep_kernel per digit: a tile of 256 threads x 16 keys is
-//      loaded with coalesced warp-striped reads, ranked in registers with
-//      warp-level multisplit (__match_any_sync), its per-digit counts are
-//      published and a per-digit decoupled look-back over predecessor tiles
-//      yields the global offsets; keys (then values) are scattered through
-//      shared memory into digit order and written out in runs, so the
-//      global stores coalesce.
+//      loaded with coalesced warp-striped reads, ranked in registers with a
+//      warp-level multisplit built from eight ballots per key (on this GPU
+//      __match_any_sync costs ~80 cycles per warp, the ballots a few), its
+//      per-digit counts are published and a per-digit decoupled look-back
+//      (eight predecessors per poll) yields the global offsets; keys and
+//      values are scattered through shared memory into digit order and
+//      written out in runs, so the global stores coalesce.  Each pass
+//      zeroes its tiles' rows of the next pass's status words (two
+//      ping-pong buffers instead of one per pass).
 // Each pass reads and writes every key once; there is no separate upsweep.
 // Look-back waits are bounded (device status word, no trap).  Keys are
 // mapped to order-preserving unsigned bit patterns on the first pass and
@@ -95,33 +98,65 @@ __device__ __forceinline__ void st_relaxed(uint64_t* p, uint64_t v) {
 }
 
 // ------------------------------------------------------------ histogram
+// Every digit position's histogram from one read of the keys.  Each warp
+// counts into its own shared histograms with plain shared atomics (a warp's
+// lanes rarely collide on uniform digits, and a skewed digit costs a few
+// replays, not a serialised warp vote).  The kernel also zeroes the first
+// pass's look-back status words, so no separate memset pass is needed.
 template <class K, int P>
 __global__ void __launch_bounds__(RB)
-hist_kernel(const K* __restrict__ keys, size_t n, int desc, uint32_t* __restrict__ hist) {
+hist_kernel(const K* __restrict__ keys, size_t n, int desc, uint32_t* __restrict__ hist,
+            uint4* __restrict__ status0, size_t status_vec4) {
   using KB = KeyBits<K>;
   using U = typename KB::U;
-  __shared__ uint32_t sh[P][RADIX];
-  for (int i = threadIdx.x; i < P * RADIX; i += RB) (&sh[0][0])[i] = 0;
+  extern __shared__ uint32_t shh[];  // [WARPS][P][RADIX]
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < WARPS * P * RADIX; i += RB) shh[i] = 0;
+  const size_t gt = size_t(blockIdx.x) * RB + tid;
+  const size_t nt = size_t(gridDim.x) * RB;
+  for (size_t i = gt; i < status_vec4; i += nt) status0[i] = make_uint4(0, 0, 0, 0);
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const size_t warp_global = (size_t(blockIdx.x) * RB + threadIdx.x) >> 5;
-  const size_t nwarps = (size_t(gridDim.x) * RB) >> 5;
-  // Each warp takes 32 consecutive keys per step; all lanes iterate
-  // together so the warp-wide match below always sees the full warp.
-  for (size_t b = warp_global * 32; b < n; b += nwarps * 32) {
-    const size_t i = b + lane;
-    const bool valid = i < n;
-    const U u = valid ? KB::to_ord(keys[i], desc != 0) : U(0);
+  uint32_t* my = shh + warp * P * RADIX;
+  constexpr int VN = 16 / sizeof(K);
+  size_t done = 0;
+  if (reinterpret_cast<uintptr_t>(keys) % 16 == 0) {
+    const size_t nvec = n / VN;
+    constexpr int UN = 4;
+    size_t v = gt;
+    for (; v + (UN - 1) * nt < nvec; v += UN * nt) {
+      Vec16<K> q[UN];
 #pragma unroll
-    for (int p = 0; p < P; ++p) {
-      const uint32_t d = valid ? uint32_t((u >> (8 * p)) & 0xff) : uint32_t(RADIX + lane);
-      const uint32_t peers = __match_any_sync(0xffffffffu, d);
-      if (valid && lane == __ffs(peers) - 1) atomicAdd(&sh[p][d], uint32_t(__popc(peers)));
+      for (int u = 0; u < UN; ++u) q[u] = ld_vec_stream(keys + (v + u * nt) * VN);
+#pragma unroll
+      for (int u = 0; u < UN; ++u)
+#pragma unroll
+        for (int e = 0; e < VN; ++e) {
+          const U x = KB::to_ord(q[u].v[e], desc != 0);
+#pragma unroll
+          for (int p = 0; p < P; ++p) atomicAdd(my + p * RADIX + uint32_t((x >> (8 * p)) & 0xff), 1u);
+        }
     }
+    for (; v < nvec; v += nt) {
+      const Vec16<K> q = ld_vec_stream(keys + v * VN);
+#pragma unroll
+      for (int e = 0; e < VN; ++e) {
+        const U x = KB::to_ord(q.v[e], desc != 0);
+#pragma unroll
+        for (int p = 0; p < P; ++p) atomicAdd(my + p * RADIX + uint32_t((x >> (8 * p)) & 0xff), 1u);
+      }
+    }
+    done = nvec * VN;
+  }
+  for (size_t i = done + gt; i < n; i += nt) {
+    const U x = KB::to_ord(keys[i], desc != 0);
+#pragma unroll
+    for (int p = 0; p < P; ++p) atomicAdd(my + p * RADIX + uint32_t((x >> (8 * p)) & 0xff), 1u);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < P * RADIX; i += RB) {
-    const uint32_t c = (&sh[0][0])[i];
+  for (int i = tid; i < P * RADIX; i += RB) {
+    uint32_t c = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) c += shh[w * P * RADIX + i];
     if (c) atomicAdd(hist + i, c);
   }
 }
@@ -150,74 +185,91 @@ __global__ void __launch_bounds__(RADIX) bins_kernel(const uint32_t* __restrict_
 }
 
 // ------------------------------------------------------------- onesweep
-template <class K, class V, class ST>
+// One tile per block.  Tiles take their id from an atomic counter in launch
+// order, so every predecessor of a tile has started and publishes its
+// counts without waiting: the look-back terminates (and is bounded anyway).
+// The kernel is instruction-bound on this GPU (the HBM stream leaves ~50
+// warp instructions per 32 keys per pass), so the pass type (first / last)
+// is a template parameter, bounds are tile-local 32-bit compares, and keys
+// and values go through separate shared buffers so that both are written
+// out in one sweep.
+template <class K, class V, bool HAS_V, class ST>
 struct SweepSmem {
   using U = typename KeyBits<K>::U;
-  static constexpr size_t KV = sizeof(U) > sizeof(V) ? sizeof(U) : sizeof(V);
-  alignas(16) unsigned char kv[TILE * KV];   // keys, then values, in digit order
-  uint32_t whist[WARPS][RADIX];              // per-warp digit counters / offsets
-  ST gdst[RADIX];                            // global dst = gdst[d] + local position
+  alignas(16) U keys[TILE];                       // digit-ordered keys of the tile
+  alignas(16) V vals[HAS_V ? TILE : 1];           // digit-ordered values
+  uint32_t whist[WARPS][RADIX];                   // per-warp digit counters / offsets
+  ST gdst[RADIX];                                 // global dst = gdst[d] + local position
   uint32_t wtot[WARPS];
   uint32_t tile;
 };
 
-template <class K, class V, bool HAS_V, class ST>
+template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST>
 __global__ void __launch_bounds__(RB)
 onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __restrict__ vin,
-                V* __restrict__ vout, size_t n, int shift, int first, int last, int desc,
+                V* __restrict__ vout, size_t n, int shift, int desc,
                 const uint32_t* __restrict__ bins, ST* __restrict__ status,
-                uint32_t* __restrict__ tile_counter, uint32_t* __restrict__ err,
-                uint32_t spin_limit) {
+                ST* __restrict__ status_next, uint32_t* __restrict__ tile_counter,
+                uint32_t* __restrict__ err, uint32_t spin_limit) {
   using KB = KeyBits<K>;
   using U = typename KB::U;
   using S = Status<ST>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SweepSmem<K, V, ST>& sm = *reinterpret_cast<SweepSmem<K, V, ST>*>(smem_raw);
-  U* skeys = reinterpret_cast<U*>(sm.kv);
-  V* svals = reinterpret_cast<V*>(sm.kv);
-
+  SweepSmem<K, V, HAS_V, ST>& sm = *reinterpret_cast<SweepSmem<K, V, HAS_V, ST>*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < WARPS * RADIX; i += RB) (&sm.whist[0][0])[i] = 0;
+#pragma unroll
+  for (int w = 0; w < WARPS; ++w) sm.whist[w][tid] = 0;
   if (tid == 0) sm.tile = atomicAdd(tile_counter, 1u);
   __syncthreads();
   const size_t tile = sm.tile;
   const size_t tbase = tile * TILE;
-  const size_t wbase = tbase + size_t(warp) * (32 * KPT);
+  const int lim = (tbase + TILE <= n) ? TILE : int(n - tbase);  // valid keys in this tile
+  const K* kt = kin + tbase;
+  const int wofs = warp * (32 * KPT) + lane;
 
-  // ---- load keys (warp-striped, coalesced); padding keys sort last
+  // ---- keys (and values), warp-striped and coalesced; padding sorts last
   U u[KPT];
+  V v[HAS_V ? KPT : 1];
 #pragma unroll
   for (int k = 0; k < KPT; ++k) {
-    const size_t i = wbase + size_t(k) * 32 + lane;
-    if (i < n) {
-      const K key = kin[i];
-      u[k] = first ? KB::to_ord(key, desc != 0) : KB::raw(key);
+    const int e = wofs + k * 32;
+    if (e < lim) {
+      const K key = kt[e];
+      if (FIRST) {
+        U x = KB::to_ord(key, false);
+        u[k] = desc ? U(~x) : x;
+      } else {
+        u[k] = KB::raw(key);
+      }
+      if (HAS_V) v[k] = vin[tbase + e];
     } else {
       u[k] = ~U(0);
+      if (HAS_V) v[k] = V(0);
     }
   }
-  // values are loaded up front so their latency overlaps the ranking
-  V v[HAS_V ? KPT : 1];
-  if (HAS_V) {
-#pragma unroll
-    for (int k = 0; k < KPT; ++k) {
-      const size_t i = wbase + size_t(k) * 32 + lane;
-      v[k] = (i < n) ? vin[i] : V(0);
-    }
-  }
+  // this tile's row of the next pass's status words starts at zero
+  if (!LAST) status_next[tile * RADIX + tid] = ST(0);
 
-  // ---- warp-level multisplit ranking
+  // ---- warp-level multisplit ranking: the lanes holding the same digit
+  // are found with eight ballots (one per digit bit); the lowest such lane
+  // bumps the warp's counter for that digit and shares the old count.
   uint32_t pos[KPT];
   const uint32_t lt = lanemask_lt();
 #pragma unroll
   for (int k = 0; k < KPT; ++k) {
-    const uint32_t d = uint32_t((u[k] >> shift) & 0xff);
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t prior = sm.whist[warp][d];
-    __syncwarp();
-    if (lane == 31 - __clz(peers)) sm.whist[warp][d] = prior + __popc(peers);
-    __syncwarp();
-    pos[k] = prior + __popc(peers & lt);
+    const uint32_t d = uint32_t(u[k] >> shift) & 0xffu;
+    uint32_t peers = 0xffffffffu;
+#pragma unroll
+    for (int bit = 0; bit < 8; ++bit) {
+      const uint32_t bal = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+      // keep lanes whose bit equals mine: ~(bal ^ mine), mine = 0 or ~0
+      peers &= ~(bal ^ (0u - ((d >> bit) & 1u)));
+    }
+    const int leader = __ffs(peers) - 1;
+    uint32_t old = 0;
+    if (lane == leader) old = atomicAdd(&sm.whist[warp][d], uint32_t(__popc(peers)));
+    old = __shfl_sync(0xffffffffu, old, leader);
+    pos[k] = old + __popc(peers & lt);
   }
   __syncthreads();
 
@@ -230,8 +282,6 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
     sm.whist[w][d] = cnt;  // exclusive offset of warp w inside digit d
     cnt += c;
   }
-
-  // publish this tile's count for digit d
   ST* my_status = status + tile * RADIX + d;
   if (tile == 0) st_relaxed(my_status, ST(S::INCL | (ST(bins[d]) + cnt)));
   else st_relaxed(my_status, ST(S::AGG | ST(cnt)));
@@ -246,31 +296,46 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   if (lane == 31) sm.wtot[warp] = inc;
   __syncthreads();
   uint32_t lstart = inc - cnt;
-  for (int w = 0; w < warp; ++w) lstart += sm.wtot[w];
+#pragma unroll
+  for (int w = 0; w < WARPS - 1; ++w)
+    if (w < warp) lstart += sm.wtot[w];
 
-  // ---- decoupled look-back for digit d
+  // ---- decoupled look-back for digit d, LBW predecessors per poll: the
+  // loads of one window are independent, then consumed in order until an
+  // inclusive count is found.  A not-yet-published tile stops the
+  // consumption; the wait is bounded.
   ST gstart;
   if (tile == 0) {
     gstart = ST(bins[d]);
   } else {
+    constexpr int LBW = 8;
     ST acc = 0;
     long long t = (long long)tile - 1;
     uint32_t spins = 0;
-    while (true) {
-      const ST s = ld_relaxed(status + size_t(t) * RADIX + d);
-      const ST flag = s & ~S::MASK;
-      if (flag == 0) {
+    bool done = false;
+    while (!done) {
+      ST w[LBW];
+#pragma unroll
+      for (int j = 0; j < LBW; ++j)
+        w[j] = (t - j >= 0) ? ld_relaxed(status + size_t(t - j) * RADIX + d) : ST(S::INCL);
+      int used = LBW;
+#pragma unroll
+      for (int j = 0; j < LBW; ++j) {
+        if (j >= used) break;
+        const ST flag = w[j] & ~S::MASK;
+        if (flag == 0) { used = j; break; }
+        acc += w[j] & S::MASK;
+        if (flag == S::INCL) { done = true; break; }
+      }
+      if (done) break;
+      t -= used;
+      if (used < LBW) {
         if (++spins > spin_limit) {
           atomicOr(err, kStatusSortTimeout);
           break;
         }
-        if (spins > 8) __nanosleep(32);
-        continue;
+        if (spins > 4) __nanosleep(32);
       }
-      acc += s & S::MASK;
-      if (flag == S::INCL) break;
-      --t;
-      if (t < 0) break;  // unreachable: tile 0 publishes INCL
     }
     gstart = acc;
     st_relaxed(my_status, ST(S::INCL | (acc + cnt)));
@@ -280,37 +345,67 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   for (int w = 0; w < WARPS; ++w) sm.whist[w][d] += lstart;
   __syncthreads();
 
-  // ---- scatter keys into digit order in shared memory
+  // ---- scatter keys (and values) into digit order in shared memory
 #pragma unroll
   for (int k = 0; k < KPT; ++k) {
-    const uint32_t dk = uint32_t((u[k] >> shift) & 0xff);
-    pos[k] += sm.whist[warp][dk];
-    skeys[pos[k]] = u[k];
+    const uint32_t dk = uint32_t(u[k] >> shift) & 0xffu;
+    const uint32_t p = pos[k] + sm.whist[warp][dk];
+    sm.keys[p] = u[k];
+    if (HAS_V) sm.vals[p] = v[k];
   }
   __syncthreads();
 
-  // ---- write keys out in runs
-  ST dst[KPT];
+  // ---- write out in runs (one digit's run is contiguous in global)
 #pragma unroll
   for (int j = 0; j < KPT; ++j) {
     const int i = j * RB + tid;
-    const U uk = skeys[i];
-    const uint32_t dk = uint32_t((uk >> shift) & 0xff);
-    dst[j] = sm.gdst[dk] + ST(i);
-    if (dst[j] < n) kout[dst[j]] = last ? KB::from_ord(uk, desc != 0) : KB::cook(uk);
-  }
-
-  if (HAS_V) {
-    __syncthreads();  // keys fully read from shared memory
-#pragma unroll
-    for (int k = 0; k < KPT; ++k) svals[pos[k]] = v[k];
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < KPT; ++j) {
-      const int i = j * RB + tid;
-      if (dst[j] < n) vout[dst[j]] = svals[i];
+    const U uk = sm.keys[i];
+    const ST dst = sm.gdst[uint32_t(uk >> shift) & 0xffu] + ST(i);
+    if (dst < n) {
+      if (LAST) {
+        const U x = desc ? U(~uk) : uk;
+        kout[dst] = KB::from_ord(x, false);
+      } else {
+        kout[dst] = KB::cook(uk);
+      }
+      if (HAS_V) vout[dst] = sm.vals[i];
     }
   }
+}
+
+// Launch one pass (one block per tile).
+template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST>
+int launch_sweep_t(const char* name, size_t tiles, cudaStream_t s, const K* src, K* dst,
+                   const V* vsrc, V* vdst, size_t n, int shift, int desc, const uint32_t* bins,
+                   ST* status, ST* status_next, uint32_t* counter, uint32_t* err, uint32_t lim) {
+  using SM = SweepSmem<K, V, HAS_V, ST>;
+  auto kern = onesweep_kernel<K, V, HAS_V, ST, FIRST, LAST>;
+  static bool attr = false;
+  if (!attr) {
+    B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(SM))));
+    attr = true;
+  }
+  B200_LAUNCH(name, kern, (unsigned)tiles, RB, sizeof(SM), s, src, dst, vsrc, vdst, n, shift, desc,
+              bins, status, status_next, counter, err, lim);
+  return B200_OK;
+}
+
+template <class K, class V, bool HAS_V, class ST>
+int launch_sweep(const char* name, size_t tiles, cudaStream_t s, const K* src, K* dst,
+                 const V* vsrc, V* vdst, size_t n, int shift, int first, int last, int desc,
+                 const uint32_t* bins, ST* status, ST* status_next, uint32_t* counter,
+                 uint32_t* err, uint32_t lim) {
+  if (first)
+    return launch_sweep_t<K, V, HAS_V, ST, true, false>(name, tiles, s, src, dst, vsrc, vdst, n,
+                                                        shift, desc, bins, status, status_next,
+                                                        counter, err, lim);
+  if (last)
+    return launch_sweep_t<K, V, HAS_V, ST, false, true>(name, tiles, s, src, dst, vsrc, vdst, n,
+                                                        shift, desc, bins, status, status_next,
+                                                        counter, err, lim);
+  return launch_sweep_t<K, V, HAS_V, ST, false, false>(name, tiles, s, src, dst, vsrc, vdst, n,
+                                                       shift, desc, bins, status, status_next,
+                                                       counter, err, lim);
 }
 
 struct NoVal {};
@@ -334,34 +429,42 @@ int run_sort(const char* name, const K* kin, K* kout, const V* vin, V* vout, siz
   const size_t tiles = (n + TILE - 1) / TILE;
   const bool wide = n >= (size_t(1) << 30);
   const size_t st_bytes = wide ? sizeof(uint64_t) : sizeof(uint32_t);
+  const size_t st_buf = round_up(tiles * RADIX * st_bytes, 256);  // one pass's status words
   Sizer z;
   z.take<K>(n);                                    // alternate keys
   if (HAS_V) z.take<V>(n);                         // alternate values
   z.take<uint32_t>(P * RADIX);                     // bins
-  // zeroed region: hist, tile counters, status words
-  z.take<unsigned char>(P * RADIX * 4 + 64 * 4 + size_t(P) * tiles * RADIX * st_bytes);
+  z.take<uint32_t>(P * RADIX + 64);                // hist + tile counters (memset)
+  z.take<unsigned char>(2 * st_buf);               // ping-pong status words
   void* scr = nullptr;
   B200_TRY(scratch(s, z.bytes(), &scr, nullptr));
   Carver cv(scr);
   K* kalt = cv.take<K>(n);
   V* valt = HAS_V ? cv.take<V>(n) : nullptr;
   uint32_t* bins = cv.take<uint32_t>(P * RADIX);
-  const size_t zbytes = P * RADIX * 4 + 64 * 4 + size_t(P) * tiles * RADIX * st_bytes;
-  unsigned char* zr = cv.take<unsigned char>(zbytes);
-  uint32_t* hist = reinterpret_cast<uint32_t*>(zr);
+  uint32_t* hist = cv.take<uint32_t>(P * RADIX + 64);
   uint32_t* counters = hist + P * RADIX;
-  void* status = counters + 64;
-  B200_CUDA(cudaMemsetAsync(zr, 0, zbytes, s));
+  unsigned char* stat = cv.take<unsigned char>(2 * st_buf);
+  B200_CUDA(cudaMemsetAsync(hist, 0, (P * RADIX + 64) * sizeof(uint32_t), s));
   uint32_t* err = nullptr;
   B200_TRY(status_word(&err));
 
   DeviceProps props;
   B200_TRY(device_props(&props));
   {
-    size_t g = size_t(props.sms) * 4;
+    const size_t smem = size_t(WARPS) * P * RADIX * sizeof(uint32_t);
+    static int bps = 0;
+    if (bps == 0) {
+      B200_CUDA(cudaFuncSetAttribute(hist_kernel<K, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+      int b = 0;
+      B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, hist_kernel<K, P>, RB, smem));
+      bps = b > 0 ? b : 1;
+    }
+    size_t g = size_t(props.sms) * bps;
     const size_t need = (n + RB - 1) / RB;
     if (g > need) g = need;
-    B200_LAUNCH("b200_sort_hist", (hist_kernel<K, P>), (unsigned)g, RB, 0, s, kin, n, desc, hist);
+    B200_LAUNCH("b200_sort_hist", (hist_kernel<K, P>), (unsigned)g, RB, smem, s, kin, n, desc, hist,
+                reinterpret_cast<uint4*>(stat), st_buf / 16);
   }
   B200_LAUNCH("b200_sort_bins", bins_kernel<P>, 1, RADIX, 0, s, hist, bins);
 
@@ -382,28 +485,20 @@ int run_sort(const char* name, const K* kin, K* kout, const V* vin, V* vout, siz
       vdst = reinterpret_cast<VV*>((p & 1) ? vout : valt);
     }
     const int first = p == 0, last = p == P - 1;
+    void* cur = stat + size_t(p & 1) * st_buf;
+    void* nxt = last ? nullptr : stat + size_t((p + 1) & 1) * st_buf;
     if (wide) {
-      using SM = SweepSmem<K, VV, uint64_t>;
-      auto kern = onesweep_kernel<K, VV, HAS_V, uint64_t>;
-      static bool attr64 = false;
-      if (!attr64) {
-        B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(SM))));
-        attr64 = true;
-      }
-      uint64_t* st = static_cast<uint64_t*>(status) + size_t(p) * tiles * RADIX;
-      B200_LAUNCH(sweep_name, kern, (unsigned)tiles, RB, sizeof(SM), s, src, dstk, vsrc,
-                  vdst, n, 8 * p, first, last, desc, bins + p * RADIX, st, counters + p, err, lim);
+      B200_TRY((launch_sweep<K, VV, HAS_V, uint64_t>(sweep_name, tiles, s, src, dstk, vsrc, vdst, n,
+                                                     8 * p, first, last, desc, bins + p * RADIX,
+                                                     static_cast<uint64_t*>(cur),
+                                                     static_cast<uint64_t*>(nxt), counters + p,
+                                                     err, lim)));
     } else {
-      using SM = SweepSmem<K, VV, uint32_t>;
-      auto kern = onesweep_kernel<K, VV, HAS_V, uint32_t>;
-      static bool attr32 = false;
-      if (!attr32) {
-        B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(SM))));
-        attr32 = true;
-      }
-      uint32_t* st = static_cast<uint32_t*>(status) + size_t(p) * tiles * RADIX;
-      B200_LAUNCH(sweep_name, kern, (unsigned)tiles, RB, sizeof(SM), s, src, dstk, vsrc,
-                  vdst, n, 8 * p, first, last, desc, bins + p * RADIX, st, counters + p, err, lim);
+      B200_TRY((launch_sweep<K, VV, HAS_V, uint32_t>(sweep_name, tiles, s, src, dstk, vsrc, vdst, n,
+                                                     8 * p, first, last, desc, bins + p * RADIX,
+                                                     static_cast<uint32_t*>(cur),
+                                                     static_cast<uint32_t*>(nxt), counters + p,
+                                                     err, lim)));
     }
   }
   static_assert(P % 2 == 0, "even number of digit passes ends in the home buffer");

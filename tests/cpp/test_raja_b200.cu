@@ -1,0 +1,377 @@
+// RAJA-API programs on the b200 policies, checked against seq_exec on the
+// same inputs.  Mirrors the reference's functional tests:
+//   test/functional/forall/reduce-basic (segments, init values, planted
+//   MinLoc/MaxLoc extremes, reset, two-loop accumulation), the expt param
+//   reducers, forall over IndexSets, test/functional/scan (iota inputs,
+//   N in {357, 32000}, plus/min/max, non-identity offsets), sort /
+//   stable_sort / sort_pairs, and test/functional/workgroup (a[i] += i + 5).
+// Prints one PASS/FAIL line per case; the exit status is the failure count.
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+#include <vector>
+
+#include "RAJA/RAJA.hpp"
+#include "raja_b200/RAJA_b200.hpp"
+
+using RAJA::Index_type;
+using exec = RAJA::b200_exec<256>;
+using red = RAJA::b200_reduce;
+
+static int g_fail = 0;
+#define CHECK(name, cond)                              \
+  do {                                                 \
+    if (cond) {                                        \
+      printf("PASS %s\n", name);                       \
+    } else {                                           \
+      printf("FAIL %s (%s:%d)\n", name, __FILE__, __LINE__); \
+      ++g_fail;                                        \
+    }                                                  \
+  } while (0)
+
+template <class T>
+T* managed(size_t n) {
+  T* p = nullptr;
+  if (cudaMallocManaged(&p, (n ? n : 1) * sizeof(T)) != cudaSuccess) {
+    printf("FAIL cudaMallocManaged\n");
+    exit(1);
+  }
+  return p;
+}
+
+// ------------------------------------------------------------ reducers
+template <class Seg>
+void reduce_case(const char* tag, const Seg& seg, const std::vector<Index_type>& idx, std::mt19937& rng) {
+  const Index_type data_len = idx.back() + 1;
+  double* a = managed<double>(data_len);
+  int* b = managed<int>(data_len);
+  for (Index_type i = 0; i < data_len; ++i) {
+    a[i] = double(rng() % 100);
+    b[i] = int(rng() % 100);
+  }
+  const Index_type loc_idx = idx[idx.size() * 2 / 3];
+  a[loc_idx] = -100.0;  // planted unique minimum
+  char nm[128];
+
+  // device reducers (init 0 and 2, as the reference tests)
+  RAJA::ReduceSum<red, double> sum(0.0), sum2(2.0);
+  RAJA::ReduceMin<red, double> mn(1e9);
+  RAJA::ReduceMax<red, double> mx(-1e9);
+  RAJA::ReduceMinLoc<red, double, Index_type> mnl(101.0, -1), mninit(-100.0, -1);
+  RAJA::ReduceMaxLoc<red, double, Index_type> mxl(-100.0, -1);
+  RAJA::ReduceBitOr<red, int> bor(0);
+  RAJA::ReduceBitAnd<red, int> band(~0);
+  RAJA::forall<exec>(seg, [=] RAJA_DEVICE(Index_type i) {
+    sum += a[i];
+    sum2 += a[i];
+    mn.min(a[i]);
+    mx.max(a[i]);
+    mnl.minloc(a[i], i);
+    mninit.minloc(a[i], i);
+    mxl.maxloc(a[i], i);
+    bor |= b[i];
+    band &= b[i];
+  });
+  // host references (seq semantics)
+  RAJA::ReduceSum<RAJA::seq_reduce, double> hs(0.0);
+  RAJA::ReduceMinLoc<RAJA::seq_reduce, double, Index_type> hml(101.0, -1), hminit(-100.0, -1);
+  RAJA::ReduceMaxLoc<RAJA::seq_reduce, double, Index_type> hxl(-100.0, -1);
+  RAJA::ReduceMin<RAJA::seq_reduce, double> hmn(1e9);
+  RAJA::ReduceMax<RAJA::seq_reduce, double> hmx(-1e9);
+  RAJA::ReduceBitOr<RAJA::seq_reduce, int> hbor(0);
+  RAJA::ReduceBitAnd<RAJA::seq_reduce, int> hband(~0);
+  RAJA::forall<RAJA::seq_exec>(seg, [=](Index_type i) {
+    hs += a[i];
+    hml.minloc(a[i], i);
+    hminit.minloc(a[i], i);
+    hxl.maxloc(a[i], i);
+    hmn.min(a[i]);
+    hmx.max(a[i]);
+    hbor |= b[i];
+    hband &= b[i];
+  });
+  snprintf(nm, sizeof nm, "reduce_sum_%s", tag);
+  CHECK(nm, sum.get() == hs.get() && sum2.get() == hs.get() + 2.0);
+  snprintf(nm, sizeof nm, "reduce_minmax_%s", tag);
+  CHECK(nm, mn.get() == hmn.get() && mx.get() == hmx.get());
+  snprintf(nm, sizeof nm, "reduce_minloc_%s", tag);
+  CHECK(nm, mnl.get() == hml.get() && mnl.getLoc() == hml.getLoc() && mnl.get() == -100.0 &&
+                mnl.getLoc() == loc_idx);
+  snprintf(nm, sizeof nm, "reduce_minloc_init_wins_%s", tag);
+  CHECK(nm, mninit.get() == -100.0 && mninit.getLoc() == -1 && hminit.getLoc() == -1);
+  snprintf(nm, sizeof nm, "reduce_maxloc_%s", tag);
+  CHECK(nm, mxl.get() == hxl.get() && mxl.getLoc() == hxl.getLoc());
+  snprintf(nm, sizeof nm, "reduce_bit_%s", tag);
+  CHECK(nm, bor.get() == hbor.get() && band.get() == hband.get());
+
+  // reset, then two loops accumulate twice (test-forall-basic-ReduceSum.hpp)
+  sum.reset(0.0);
+  for (int k = 0; k < 2; ++k) RAJA::forall<exec>(seg, [=] RAJA_DEVICE(Index_type i) { sum += a[i]; });
+  snprintf(nm, sizeof nm, "reduce_sum_two_loops_%s", tag);
+  CHECK(nm, sum.get() == 2.0 * hs.get());
+  cudaFree(a);
+  cudaFree(b);
+}
+
+void test_reducers() {
+  std::mt19937 rng(12345);
+  std::vector<Index_type> idx;
+  auto range = [&](Index_type b, Index_type e) {
+    idx.clear();
+    for (Index_type i = b; i < e; ++i) idx.push_back(i);
+  };
+  range(0, 28);
+  reduce_case("r0_28", RAJA::RangeSegment(0, 28), idx, rng);
+  range(3, 642);
+  reduce_case("r3_642", RAJA::RangeSegment(3, 642), idx, rng);
+  range(0, 2057);
+  reduce_case("r0_2057", RAJA::RangeSegment(0, 2057), idx, rng);
+  idx.clear();
+  for (Index_type i = 0; i < 188; i += 2) idx.push_back(i);
+  reduce_case("s0_188_2", RAJA::RangeStrideSegment(0, 188, 2), idx, rng);
+  idx.clear();
+  for (Index_type i = 3; i < 1029; i += 3) idx.push_back(i);
+  reduce_case("s3_1029_3", RAJA::RangeStrideSegment(3, 1029, 3), idx, rng);
+  // random list segment (test-forall-basic-ReduceSum list case)
+  idx.clear();
+  for (Index_type i = 0; i < 10567; ++i)
+    if (Index_type(rng() % 10567) > i) idx.push_back(i);
+  Index_type* lst = managed<Index_type>(idx.size());
+  for (size_t i = 0; i < idx.size(); ++i) lst[i] = idx[i];
+  reduce_case("list", RAJA::ListSegment(lst, Index_type(idx.size())), idx, rng);
+  cudaFree(lst);
+
+  // large: fp64 ties everywhere, MinLoc picks the first index like seq
+  const Index_type n = (1 << 22) + 3;
+  double* x = managed<double>(n);
+  for (Index_type i = 0; i < n; ++i) x[i] = double(rng() % 5);
+  RAJA::ReduceMinLoc<red, double, Index_type> m(1e9, -1);
+  RAJA::ReduceMaxLoc<red, double, Index_type> M(-1e9, -1);
+  RAJA::forall<exec>(RAJA::RangeSegment(0, n), [=] RAJA_DEVICE(Index_type i) {
+    m.minloc(x[i], i);
+    M.maxloc(x[i], i);
+  });
+  Index_type first0 = -1, first4 = -1;
+  for (Index_type i = 0; i < n && (first0 < 0 || first4 < 0); ++i) {
+    if (x[i] == 0.0 && first0 < 0) first0 = i;
+    if (x[i] == 4.0 && first4 < 0) first4 = i;
+  }
+  CHECK("minloc_ties_lowest_index", m.get() == 0.0 && m.getLoc() == first0);
+  CHECK("maxloc_ties_lowest_index", M.get() == 4.0 && M.getLoc() == first4);
+  cudaFree(x);
+}
+
+// -------------------------------------------------------- forall + params
+void test_forall_and_params() {
+  const Index_type n = (1 << 20) + 7;
+  double* x = managed<double>(n);
+  double* y = managed<double>(n);
+  double* yh = managed<double>(n);
+  std::mt19937 rng(7);
+  for (Index_type i = 0; i < n; ++i) {
+    x[i] = double(rng() % 1000) / 8.0;
+    y[i] = yh[i] = double(rng() % 1000) / 16.0;
+  }
+  const double alpha = 2.5;
+  RAJA::forall<exec>(RAJA::RangeSegment(0, n), [=] RAJA_DEVICE(Index_type i) { y[i] += alpha * x[i]; });
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, n), [=](Index_type i) { yh[i] += alpha * x[i]; });
+  bool ok = true;
+  for (Index_type i = 0; i < n; ++i) ok = ok && (y[i] == yh[i]);  // exact: multiples of 1/16
+  CHECK("forall_daxpy", ok);
+
+  // expt::Reduce / ReduceLoc params: target = op(target, result)
+  double s = 10.0, lo = 1e300, hi = -1e300, vmin = 1e300;
+  Index_type imin = -1;
+  RAJA::forall<exec>(RAJA::RangeSegment(0, n), RAJA::expt::Reduce<RAJA::operators::plus>(&s),
+                     RAJA::expt::Reduce<RAJA::operators::minimum>(&lo),
+                     RAJA::expt::Reduce<RAJA::operators::maximum>(&hi),
+                     RAJA::expt::ReduceLoc<RAJA::operators::minimum>(&vmin, &imin),
+                     [=] RAJA_DEVICE(Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& vs,
+                                     RAJA::expt::ValOp<double, RAJA::operators::minimum>& vlo,
+                                     RAJA::expt::ValOp<double, RAJA::operators::maximum>& vhi,
+                                     RAJA::expt::ValOp<RAJA::expt::ValLoc<double, Index_type>,
+                                                       RAJA::operators::minimum>& vml) {
+                       vs += x[i];
+                       vlo.min(x[i]);
+                       vhi.max(x[i]);
+                       vml.minloc(x[i], i);
+                     });
+  double hs = 10.0, hlo = 1e300, hhi = -1e300;
+  Index_type himin = -1;
+  double hvmin = 1e300;
+  for (Index_type i = 0; i < n; ++i) {
+    hs += x[i];
+    hlo = x[i] < hlo ? x[i] : hlo;
+    hhi = hhi < x[i] ? x[i] : hhi;
+    if (x[i] < hvmin) {
+      hvmin = x[i];
+      himin = i;
+    }
+  }
+  CHECK("expt_reduce_sum", s == hs);
+  CHECK("expt_reduce_min_max", lo == hlo && hi == hhi);
+  CHECK("expt_reduceloc_min", vmin == hvmin && imin == himin);
+
+  // IndexSet: all segments in one launch
+  RAJA::TypedIndexSet<Index_type> is;
+  is.push_back(RAJA::RangeSegment(0, 100));
+  is.push_back(RAJA::RangeSegment(1000, 5000));
+  is.push_back(RAJA::RangeSegment(7, 7));
+  is.push_back(RAJA::RangeSegment(200000, 200333));
+  for (Index_type i = 0; i < n; ++i) y[i] = yh[i] = 0.0;
+  RAJA::ReduceSum<red, double> cnt(0.0);
+  RAJA::forall<exec>(is, [=] RAJA_DEVICE(Index_type i) {
+    y[i] += double(i);
+    cnt += 1.0;
+  });
+  RAJA::forall<RAJA::seq_exec>(is, [=](Index_type i) { yh[i] += double(i); });
+  ok = cnt.get() == 100 + 4000 + 333;
+  for (Index_type i = 0; i < n; ++i) ok = ok && (y[i] == yh[i]);
+  CHECK("forall_indexset_one_launch", ok);
+  cudaFree(x);
+  cudaFree(y);
+  cudaFree(yh);
+}
+
+// ------------------------------------------------------------------ scans
+template <class T, class Op>
+void scan_case(const char* tag, Index_type n, T offset) {
+  T* in = managed<T>(n);
+  T* out = managed<T>(n);
+  T* ref = managed<T>(n);
+  for (Index_type i = 0; i < n; ++i) in[i] = T(i + 1);  // std::iota(.., 1)
+  char nm[128];
+  RAJA::inclusive_scan<exec>(RAJA::make_span((const T*)in, n), RAJA::make_span(out, n), Op{});
+  RAJA::inclusive_scan<RAJA::seq_exec>(RAJA::make_span((const T*)in, n), RAJA::make_span(ref, n), Op{});
+  bool ok = true;
+  for (Index_type i = 0; i < n; ++i) ok = ok && out[i] == ref[i];
+  snprintf(nm, sizeof nm, "inclusive_scan_%s_%ld", tag, (long)n);
+  CHECK(nm, ok);
+  RAJA::exclusive_scan<exec>(RAJA::make_span((const T*)in, n), RAJA::make_span(out, n), Op{}, offset);
+  RAJA::exclusive_scan<RAJA::seq_exec>(RAJA::make_span((const T*)in, n), RAJA::make_span(ref, n), Op{}, offset);
+  ok = true;
+  for (Index_type i = 0; i < n; ++i) ok = ok && out[i] == ref[i];
+  snprintf(nm, sizeof nm, "exclusive_scan_%s_%ld", tag, (long)n);
+  CHECK(nm, ok);
+  for (Index_type i = 0; i < n; ++i) out[i] = in[i];
+  RAJA::inclusive_scan_inplace<exec>(RAJA::make_span(out, n), Op{});
+  RAJA::inclusive_scan<RAJA::seq_exec>(RAJA::make_span((const T*)in, n), RAJA::make_span(ref, n), Op{});
+  ok = true;
+  for (Index_type i = 0; i < n; ++i) ok = ok && out[i] == ref[i];
+  snprintf(nm, sizeof nm, "inclusive_scan_inplace_%s_%ld", tag, (long)n);
+  CHECK(nm, ok);
+  cudaFree(in);
+  cudaFree(out);
+  cudaFree(ref);
+}
+
+void test_scans() {
+  for (Index_type n : {Index_type(357), Index_type(32000), Index_type((1 << 20) + 1)}) {
+    const int off = n == 357 ? 15 : 2;
+    scan_case<int, RAJA::operators::plus<int>>("plus_int", n, off);
+    scan_case<int, RAJA::operators::minimum<int>>("min_int", n, off);
+    scan_case<int, RAJA::operators::maximum<int>>("max_int", n, off);
+    scan_case<double, RAJA::operators::plus<double>>("plus_double", n, double(off));
+    scan_case<double, RAJA::operators::minimum<double>>("min_double", n, double(off));
+    scan_case<long, RAJA::operators::plus<long>>("plus_long", n, long(off));
+  }
+}
+
+// ------------------------------------------------------------------ sorts
+void test_sorts() {
+  std::mt19937 rng(99);
+  for (Index_type n : {Index_type(0), Index_type(1), Index_type(10), Index_type(10000), Index_type(1 << 20)}) {
+    int* k = managed<int>(n);
+    int* kr = managed<int>(n);
+    int* v = managed<int>(n);
+    int* vr = managed<int>(n);
+    auto fill = [&] {
+      for (Index_type i = 0; i < n; ++i) {
+        k[i] = kr[i] = int(rng() % (2 * n + 1)) - int(n);  // U[-N, N]: duplicates
+        v[i] = vr[i] = int(i);
+      }
+    };
+    char nm[96];
+    fill();
+    RAJA::sort<exec>(RAJA::make_span(k, n));
+    RAJA::sort<RAJA::seq_exec>(RAJA::make_span(kr, n));
+    bool ok = true;
+    for (Index_type i = 0; i < n; ++i) ok = ok && k[i] == kr[i];
+    snprintf(nm, sizeof nm, "sort_%ld", (long)n);
+    CHECK(nm, ok);
+    fill();
+    RAJA::stable_sort<exec>(RAJA::make_span(k, n), RAJA::operators::greater<int>{});
+    RAJA::stable_sort<RAJA::seq_exec>(RAJA::make_span(kr, n), RAJA::operators::greater<int>{});
+    ok = true;
+    for (Index_type i = 0; i < n; ++i) ok = ok && k[i] == kr[i];
+    snprintf(nm, sizeof nm, "stable_sort_greater_%ld", (long)n);
+    CHECK(nm, ok);
+    fill();
+    RAJA::stable_sort_pairs<exec>(RAJA::make_span(k, n), RAJA::make_span(v, n));
+    RAJA::stable_sort_pairs<RAJA::seq_exec>(RAJA::make_span(kr, n), RAJA::make_span(vr, n));
+    ok = true;
+    for (Index_type i = 0; i < n; ++i) ok = ok && k[i] == kr[i] && v[i] == vr[i];
+    snprintf(nm, sizeof nm, "stable_sort_pairs_%ld", (long)n);
+    CHECK(nm, ok);
+    fill();
+    RAJA::sort_pairs<exec>(RAJA::make_span(k, n), RAJA::make_span(v, n), RAJA::operators::greater<int>{});
+    RAJA::stable_sort_pairs<RAJA::seq_exec>(RAJA::make_span(kr, n), RAJA::make_span(vr, n),
+                                            RAJA::operators::greater<int>{});
+    ok = true;
+    for (Index_type i = 0; i < n; ++i) ok = ok && k[i] == kr[i] && v[i] == vr[i];
+    snprintf(nm, sizeof nm, "sort_pairs_greater_%ld", (long)n);
+    CHECK(nm, ok);
+    cudaFree(k);
+    cudaFree(kr);
+    cudaFree(v);
+    cudaFree(vr);
+  }
+}
+
+// -------------------------------------------------------------- WorkGroup
+template <class ORDER>
+void workgroup_case(const char* tag) {
+  const Index_type n = 1 << 20;
+  int* a = managed<int>(n);
+  int* r = managed<int>(n);
+  for (Index_type i = 0; i < n; ++i) a[i] = r[i] = 0;
+  using pool_t = RAJA::WorkPool<RAJA::WorkGroupPolicy<RAJA::b200_work<256>, ORDER>, Index_type>;
+  using hpool_t = RAJA::WorkPool<RAJA::WorkGroupPolicy<RAJA::seq_exec, RAJA::ordered>, Index_type>;
+  pool_t pool;
+  hpool_t hpool;
+  std::mt19937 rng(5);
+  Index_type b = 0;
+  int loops = 0;
+  while (b < n) {
+    const Index_type len = Index_type(rng() % 5000);  // uneven lengths, some empty
+    const Index_type e = b + len < n ? b + len : n;
+    pool.enqueue(RAJA::RangeSegment(b, e), [=] RAJA_DEVICE(Index_type i) { a[i] += int(i) + 5; });
+    hpool.enqueue(RAJA::RangeSegment(b, e), [=](Index_type i) { r[i] += int(i) + 5; });
+    b = e + Index_type(rng() % 7);  // gaps stay untouched
+    ++loops;
+  }
+  auto g = pool.instantiate();
+  auto hg = hpool.instantiate();
+  g.run();
+  g.run();  // a group runs again with the same loops
+  hg.run();
+  hg.run();
+  bool ok = true;
+  for (Index_type i = 0; i < n; ++i) ok = ok && a[i] == r[i];
+  char nm[96];
+  snprintf(nm, sizeof nm, "workgroup_%s_%d_loops", tag, loops);
+  CHECK(nm, ok);
+  cudaFree(a);
+  cudaFree(r);
+}
+
+int main() {
+  test_reducers();
+  test_forall_and_params();
+  test_scans();
+  test_sorts();
+  workgroup_case<RAJA::unordered>("unordered");
+  workgroup_case<RAJA::ordered>("ordered");
+  printf("%d failures\n", g_fail);
+  return g_fail;
+}

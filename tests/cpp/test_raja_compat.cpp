@@ -1,0 +1,93 @@
+// Host-only checks of the raja_compat front-end (seq_exec / omp policies)
+// against the known answers of the reference's functional tests.
+#include <cstdio>
+#include <numeric>
+#include <vector>
+
+#include "RAJA/RAJA.hpp"
+
+using RAJA::Index_type;
+static int g_fail = 0;
+#define CHECK(name, cond)                                  \
+  do {                                                     \
+    if (cond) printf("PASS %s\n", name);                   \
+    else { printf("FAIL %s (line %d)\n", name, __LINE__); ++g_fail; } \
+  } while (0)
+
+int main() {
+  // ReduceSum with init 0 and 2; reset and two loops (test-forall-basic-ReduceSum.hpp)
+  std::vector<double> a(2057);
+  for (size_t i = 0; i < a.size(); ++i) a[i] = double((i * 7919) % 100);
+  double* p = a.data();
+  RAJA::ReduceSum<RAJA::seq_reduce, double> s0(0.0), s2(2.0);
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(3, 642), [=](Index_type i) { s0 += p[i]; s2 += p[i]; });
+  double ref = 0;
+  for (int i = 3; i < 642; ++i) ref += a[i];
+  CHECK("sum_init0_init2", s0.get() == ref && s2.get() == ref + 2);
+  s0.reset(0.0);
+  for (int k = 0; k < 2; ++k) RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(3, 642), [=](Index_type i) { s0 += p[i]; });
+  CHECK("sum_reset_two_loops", s0.get() == 2 * ref);
+  // MinLoc: init tie wins (mininit(-100, -1) with planted -100)
+  a[400] = -100.0;
+  RAJA::ReduceMinLoc<RAJA::seq_reduce, double, Index_type> mi(-100.0, -1), m(101.0, -1);
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 2057), [=](Index_type i) { mi.minloc(p[i], i); m.minloc(p[i], i); });
+  CHECK("minloc_init_wins", mi.get() == -100.0 && mi.getLoc() == -1);
+  CHECK("minloc_planted", m.get() == -100.0 && m.getLoc() == 400);
+  // omp reducer agrees with seq
+  RAJA::ReduceSum<RAJA::omp_reduce, double> so(0.0);
+  RAJA::forall<RAJA::omp_parallel_for_exec>(RAJA::RangeSegment(0, 2057), [=](Index_type i) { so += p[i]; });
+  double all = 0;
+  for (double v : a) all += v;
+  CHECK("omp_sum", so.get() == all);
+  // BitOr: 9 | 5 == 13
+  std::vector<int> nines(100, 9);
+  int* q = nines.data();
+  RAJA::ReduceBitOr<RAJA::seq_reduce, int> bo(5);
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 100), [=](Index_type i) { bo |= q[i]; });
+  CHECK("bitor_9_5", bo.get() == 13);
+  // scans: iota, plus / min / max, offsets 13, 15, 2
+  for (int n : {0, 357, 32000}) {
+    std::vector<int> in(n), out(n);
+    std::iota(in.begin(), in.end(), 1);
+    RAJA::inclusive_scan<RAJA::seq_exec>(RAJA::make_span((const int*)in.data(), n), RAJA::make_span(out.data(), n));
+    bool ok = true;
+    long acc = 0;
+    for (int i = 0; i < n; ++i) { acc += i + 1; ok = ok && out[i] == int(acc); }
+    CHECK("inclusive_plus_iota", ok);
+    const int off = n == 0 ? 13 : (n == 357 ? 15 : 2);
+    RAJA::exclusive_scan<RAJA::seq_exec>(RAJA::make_span((const int*)in.data(), n), RAJA::make_span(out.data(), n),
+                                         RAJA::operators::plus<int>{}, off);
+    ok = true;
+    acc = off;
+    for (int i = 0; i < n; ++i) { ok = ok && out[i] == int(acc); acc += i + 1; }
+    CHECK("exclusive_plus_offset", ok);
+    RAJA::inclusive_scan<RAJA::seq_exec>(RAJA::make_span((const int*)in.data(), n), RAJA::make_span(out.data(), n),
+                                         RAJA::operators::maximum<int>{});
+    ok = true;
+    for (int i = 0; i < n; ++i) ok = ok && out[i] == i + 1;
+    CHECK("inclusive_max_iota", ok);
+  }
+  // sorts: stable pairs keep input order among equal keys
+  std::vector<int> k{3, 1, 3, 2, 1}, v{0, 1, 2, 3, 4};
+  RAJA::stable_sort_pairs<RAJA::seq_exec>(RAJA::make_span(k.data(), 5), RAJA::make_span(v.data(), 5));
+  CHECK("stable_sort_pairs", k == std::vector<int>({1, 1, 2, 3, 3}) && v == std::vector<int>({1, 4, 3, 0, 2}));
+  RAJA::stable_sort<RAJA::seq_exec>(RAJA::make_span(k.data(), 5), RAJA::operators::greater<int>{});
+  CHECK("stable_sort_greater", k == std::vector<int>({3, 3, 2, 1, 1}));
+  // expt::Reduce on host: target = op(target, result)
+  double t = 1.0;
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 10), RAJA::expt::Reduce<RAJA::operators::plus>(&t),
+                               [=](Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& s) { s += double(i); });
+  CHECK("expt_reduce_host", t == 46.0);
+  // WorkGroup (ordered): a[i] += i + 5 (test-workgroup-Unordered-Single.hpp)
+  std::vector<int> w(100, 0);
+  int* wp = w.data();
+  RAJA::WorkPool<RAJA::WorkGroupPolicy<RAJA::seq_exec, RAJA::ordered>, Index_type> pool;
+  pool.enqueue(RAJA::RangeSegment(10, 60), [=](Index_type i) { wp[i] += int(i) + 5; });
+  auto g = pool.instantiate();
+  g.run();
+  bool ok = true;
+  for (int i = 0; i < 100; ++i) ok = ok && w[i] == ((i >= 10 && i < 60) ? i + 5 : 0);
+  CHECK("workgroup_seq", ok);
+  printf("%d failures\n", g_fail);
+  return g_fail;
+}
