@@ -45,6 +45,7 @@ struct b200_batch_plan_s {
   double* d_tile_part = nullptr;   // ntiles
   int variant = -1;                // autotuned kernel variant (-1: default)
   // segmented sort classification
+  bool has_empty = false;          // some loop has no iterations (no tile)
   std::vector<int> big_segments;   // segments longer than the block sort
   int32_t* d_small = nullptr;      // ids of the small segments
   int nsmall = 0;
@@ -552,6 +553,7 @@ int b200_batch_plan_create(const int64_t* lens, int nloops, b200_batch_plan* out
                 cudaMemcpyHostToDevice), "plan offsets copy");
   std::vector<int32_t> small;
   for (int i = 0; i < nloops; ++i) {
+    if (lens[i] == 0) p->has_empty = true;
     if (lens[i] <= 1) continue;
     if (lens[i] <= SEG_CAP) small.push_back(i);
     else p->big_segments.push_back(i);
@@ -607,9 +609,11 @@ int b200_batched_axpy_sum_f32(b200_batch_plan p, float a, const float* const* xs
   }
   const Variant v = kVariants[p->variant];
   B200_TRY(build_tiling(p, v.block * v.items));
+  // loops of length zero have no tile: their sums are zero
+  if (p->has_empty)
+    B200_CUDA(cudaMemsetAsync(sums, 0, p->nloops * sizeof(double), static_cast<cudaStream_t>(stream)));
   B200_TRY(dispatch_batched(p->variant, p, a, xs, ys, sums, (mode & B200_MODE_COMPENSATED) ? 1 : 0,
                             static_cast<cudaStream_t>(stream)));
-  // loops of length zero have no tile: their sums are zero
   clear_error();
   return B200_OK;
 }

@@ -15,9 +15,15 @@
 // spin_limit polls the tile gives up, ORs a code into the device status
 // word and finishes, so a broken invariant can never hang the GPU.
 // Global traffic is one TMA bulk read and one coalesced 16-byte write per
-// element group.  The look-back is done by one warp that inspects 256
-// predecessors per poll (eight per lane), so a distant inclusive prefix
-// costs one L2 round trip per 256 tiles.
+// element group.  A tile's status (flag + carry) is published with plain
+// relaxed stores and no fences: the carry is cut into 32-bit pieces, each
+// stored in a 64-bit word beside a copy of the flag, and a reader accepts a
+// status only when every word carries the same non-zero flag -- a torn read
+// (words from the aggregate and the inclusive publication, or not yet
+// written) shows up as a flag mismatch and is polled again.  Warp 0 does
+// the look-back, LBJ predecessors per lane per poll, with a short sleep
+// between polls so that the waiting tiles do not flood the L2 slices that
+// hold the status words.
 #include <cfloat>
 #include <climits>
 #include <type_traits>
@@ -35,14 +41,21 @@ constexpr uint32_t FLAG_AGG = 1, FLAG_INCL = 2;
 // j*256 + t (j = 0..G-1): consecutive threads touch consecutive granules,
 // so both the TMA-filled shared buffer and the global stores are accessed
 // without bank conflicts and fully coalesced, with no transposition.
-template <class T>
+// Tiles are 64 KB (G = 16); the compensated sums, whose in-tile values are
+// pairs, use 32 KB tiles to stay within the register budget.  Large tiles matter
+// here: each tile pays one look-back of a few L2 round trips, and the
+// bytes in flight per SM (three 64 KB tiles) set the bandwidth.
+template <class Op>
 struct Tile {
+  using T = typename Op::T;
   static constexpr int VN = 16 / sizeof(T);   // elements per granule
-  static constexpr int G = 8;                 // granules per thread
+  static constexpr int G = sizeof(typename Op::Local) > sizeof(T) ? 8 : 16;  // granules per thread
   static constexpr int ITEMS = G * VN;
-  static constexpr int SIZE = SBLOCK * ITEMS; // 32 KB
+  static constexpr int SIZE = SBLOCK * ITEMS;
+  static constexpr int PT = G * SWARPS / 32;  // prefix-table entries per lane
 };
-constexpr int LBJ = 8;  // predecessors each look-back lane inspects per poll
+constexpr int LBJ = 1;          // predecessors each look-back lane inspects per poll
+constexpr int LB_SLEEP_NS = 64; // pause between polls of a window that is not ready
 
 template <class T>
 struct Inf;
@@ -182,26 +195,57 @@ __device__ __forceinline__ double fold_local<ScanSumCompF32>(double p, PairT<flo
   return p + (double(l.s) + double(l.c));
 }
 
-template <class P>
-__device__ __forceinline__ P ld_cg_val(const P* p) {
-  static_assert(sizeof(P) % 4 == 0, "carry size");
-  constexpr int W = sizeof(P) / 4;
-  uint32_t w[W];
-  const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
+// ---------------------------------------------------- tile status words
+// Word = (flag << 32) | 32-bit piece of the carry; NW words per tile.
+template <class Carry>
+struct StatusWords {
+  static_assert(sizeof(Carry) % 4 == 0 && sizeof(Carry) <= 16, "carry size");
+  static constexpr int NW = sizeof(Carry) / 4;
+
+  static __device__ __forceinline__ void publish(uint64_t* w, uint32_t flag, const Carry& v) {
+    uint32_t piece[NW];
+    memcpy(piece, &v, sizeof(Carry));
+    const uint64_t f = uint64_t(flag) << 32;
+    if (NW == 1) {
+      asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(w), "l"(f | piece[0]) : "memory");
+    } else {
 #pragma unroll
-  for (int i = 0; i < W; ++i) w[i] = __ldcg(q + i);
-  P r;
-  memcpy(&r, w, sizeof(P));
-  return r;
-}
+      for (int i = 0; i < NW; i += 2)
+        asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(w + i),
+                     "l"(f | piece[i]), "l"(f | piece[(i + 1) % NW]) : "memory");
+    }
+  }
+  // The tile's flag if every word agrees on it, else 0 (not ready).
+  static __device__ __forceinline__ uint32_t poll(const uint64_t* w, Carry& v) {
+    uint64_t x[NW + (NW & 1)];
+    if (NW == 1) {
+      asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(x[0]) : "l"(w) : "memory");
+    } else {
+#pragma unroll
+      for (int i = 0; i < NW; i += 2)
+        asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];"
+                     : "=l"(x[i]), "=l"(x[i + 1]) : "l"(w + i) : "memory");
+    }
+    uint32_t flag = uint32_t(x[0] >> 32);
+    uint32_t piece[NW];
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+      if (uint32_t(x[i] >> 32) != flag) flag = 0;
+      piece[i] = uint32_t(x[i]);
+    }
+    memcpy(&v, piece, sizeof(Carry));
+    return flag;
+  }
+};
 
 template <class Op>
 struct ScanSmem {
   using T = typename Op::T;
   using Local = typename Op::Local;
-  alignas(128) T stage[Tile<T>::SIZE];       // the tile, filled by one TMA bulk copy
-  Local wtot[Tile<T>::G * SWARPS];           // warp totals, sub-tile major
-  Local pref[Tile<T>::G * SWARPS];           // their exclusive prefix in the tile
+  alignas(128) T stage[Tile<Op>::SIZE];      // the tile, filled by one TMA bulk copy
+  Local wsum[SWARPS];                        // warp totals over the whole tile
+  Local wtot[Tile<Op>::G * SWARPS];          // warp totals, sub-tile major
+  Local pref[Tile<Op>::G * SWARPS];          // their exclusive prefix in the tile
   typename Op::Carry prefix;                 // the tile's carry-in
   uint64_t bar;
   uint32_t tile;
@@ -214,17 +258,21 @@ struct ScanSmem {
 // completed on an mbarrier) straight into shared memory, so no registers
 // stage it and five or more blocks fit per SM: while one block waits in its
 // look-back, the others keep HBM busy.
+// Resident blocks per SM the register budget is cut for: three 64 KB
+// tiles fill the shared memory; four 32 KB ones for the compensated sums.
+template <class Op>
+constexpr int scan_min_blocks() { return Tile<Op>::G == 16 ? 3 : 4; }
+
 template <class Op, bool EXCL>
-__global__ void __launch_bounds__(SBLOCK)
+__global__ void __launch_bounds__(SBLOCK, scan_min_blocks<Op>())
 scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op::T init,
-            int tma_ok, int vec_out, uint32_t* flags, typename Op::Carry* aggs,
-            typename Op::Carry* incls, uint32_t* tile_counter, uint32_t* status,
-            uint32_t spin_limit) {
+            int tma_ok, int vec_out, uint64_t* words, uint32_t* tile_counter,
+            uint32_t* status, uint32_t spin_limit) {
   using T = typename Op::T;
   using Local = typename Op::Local;
   using Carry = typename Op::Carry;
-  constexpr int VN = Tile<T>::VN, G = Tile<T>::G, TS = Tile<T>::SIZE;
-  static_assert(G * SWARPS == 64, "prefix table: two entries per lane of warp 0");
+  constexpr int VN = Tile<Op>::VN, G = Tile<Op>::G, TS = Tile<Op>::SIZE, PT = Tile<Op>::PT;
+  static_assert(G * SWARPS == 32 * PT, "prefix table: PT entries per lane of warp 1");
   extern __shared__ __align__(128) unsigned char smem_raw[];
   ScanSmem<Op>& sm = *reinterpret_cast<ScanSmem<Op>*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -253,7 +301,9 @@ scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op
     __syncthreads();
   }
   {
-    // ---- granule totals and per-sub-tile warp scans
+    using SW = StatusWords<Carry>;
+    // ---- granule totals (registers) and the tile aggregate: thread
+    // totals, warp totals, then warp 0 folds the eight warps
     Local lex[G];
 #pragma unroll
     for (int j = 0; j < G; ++j) {
@@ -265,7 +315,63 @@ scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op
         const Local x = (full || base + size_t(g) * VN + k < n) ? Op::lift(v.v[k]) : Op::ident();
         tot = (k == 0) ? x : Op::comb(tot, x);
       }
-      Local inc = tot;
+      lex[j] = tot;
+    }
+    {
+      Local tt = lex[0];
+#pragma unroll
+      for (int j = 1; j < G; ++j) tt = Op::comb(tt, lex[j]);
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const Local other = shfl_up_any(tt, o);
+        if (lane >= o) tt = Op::comb(other, tt);
+      }
+      if (lane == 31) sm.wsum[warp] = tt;
+    }
+    __syncthreads();
+
+    // ---- warp 0 publishes the aggregate at once and issues the first
+    // look-back poll; its latency is hidden behind the sub-tile scans
+    Carry tile_agg = Op::cident();
+    long long pred = (long long)tile - 1;
+    Carry lbv[LBJ];
+    uint32_t lbf[LBJ];
+    auto load_window = [&](long long t0) {
+#pragma unroll
+      for (int j = 0; j < LBJ; ++j) {
+        if (t0 - j >= 0) {
+          lbf[j] = SW::poll(words + (t0 - j) * SW::NW, lbv[j]);
+        } else {  // before tile 0: never reached past tile 0's inclusive prefix
+          lbf[j] = FLAG_INCL;
+          lbv[j] = Op::cident();
+        }
+      }
+    };
+    if (warp == 0) {
+      Local wt = (lane < SWARPS) ? sm.wsum[lane] : Op::ident();
+#pragma unroll
+      for (int o = 1; o < SWARPS; o <<= 1) {
+        const Local other = shfl_up_any(wt, o);
+        if (lane >= o) wt = Op::comb(other, wt);
+      }
+      tile_agg = Op::to_carry(shfl_idx_any(wt, SWARPS - 1));
+      if (tile == 0) {
+        if (lane == 0) {
+          SW::publish(words, FLAG_INCL,
+                      EXCL ? Op::ccomb(Op::from_init(init), tile_agg) : tile_agg);
+          sm.prefix = EXCL ? Op::from_init(init) : Op::cident();
+        }
+      } else {
+        if (lane == 0) SW::publish(words + tile * SW::NW, FLAG_AGG, tile_agg);
+        load_window(pred - (long long)lane * LBJ);
+      }
+    }
+
+    // ---- per-sub-tile warp scans: lex[j] becomes the lane's exclusive
+    // prefix inside its warp's slice of sub-tile j
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      Local inc = lex[j];
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const Local other = shfl_up_any(inc, o);
@@ -276,96 +382,93 @@ scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op
     }
     __syncthreads();
 
-    // ---- warp 0: prefix table, tile aggregate, publish, look-back
-    if (warp == 0) {
-      const Local a = sm.wtot[2 * lane], c = sm.wtot[2 * lane + 1];
-      Local pin = Op::comb(a, c);
+    if (warp == 1) {
+      // ---- prefix table of the warp totals (sub-tile major): lane q
+      // holds entries q*PT .. q*PT+PT-1
+      Local e[PT];
+#pragma unroll
+      for (int i = 0; i < PT; ++i) e[i] = sm.wtot[PT * lane + i];
+      Local pin = e[0];
+#pragma unroll
+      for (int i = 1; i < PT; ++i) pin = Op::comb(pin, e[i]);
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const Local other = shfl_up_any(pin, o);
         if (lane >= o) pin = Op::comb(other, pin);
       }
-      const Local pex = shfl_up_any(pin, 1);
-      if (lane == 0) {
-        sm.pref[0] = Op::ident();
-        sm.pref[1] = a;
-      } else {
-        sm.pref[2 * lane] = pex;
-        sm.pref[2 * lane + 1] = Op::comb(pex, a);
+      Local run = shfl_up_any(pin, 1);
+#pragma unroll
+      for (int i = 0; i < PT; ++i) {
+        if (lane == 0 && i == 0) {
+          sm.pref[0] = Op::ident();
+          run = e[0];
+        } else {
+          sm.pref[PT * lane + i] = run;
+          run = Op::comb(run, e[i]);
+        }
       }
-      const Local tile_agg = shfl_idx_any(pin, 31);
-      Carry prefix = Op::cident();
-      if (tile == 0) {
-        if (EXCL) prefix = Op::from_init(init);
-        if (lane == 0) {
-          incls[0] = EXCL ? Op::ccomb(prefix, Op::to_carry(tile_agg)) : Op::to_carry(tile_agg);
-          st_release(flags, FLAG_INCL);
-        }
-      } else {
-        if (lane == 0) {
-          aggs[tile] = Op::to_carry(tile_agg);
-          st_release(flags + tile, FLAG_AGG);
-        }
-        // One warp inspects 32 x LBJ = 256 predecessors per poll: lane l
-        // covers tiles pred - l*LBJ - j, j = 0..LBJ-1 (nearest first).
-        long long pred = (long long)tile - 1;
-        Carry acc = Op::cident();
-        bool timed_out = false;
+    } else if (warp == 0 && tile > 0) {
+      // ---- decoupled look-back.  Lane q inspects tiles pred - q*LBJ - j
+      // (j = 0..LBJ-1), nearest first; the window is folded up to the
+      // nearest inclusive prefix, or wholly, and then the next window
+      // further back is inspected.
+      Carry acc = Op::cident();
+      bool timed_out = false;
+      while (true) {
+        const long long t0 = pred - (long long)lane * LBJ;
+        uint32_t spins = 0;
+        int stop, jstop;
         while (true) {
-          const long long t0 = pred - (long long)lane * LBJ;
-          uint32_t f[LBJ];
-#pragma unroll
-          for (int j = 0; j < LBJ; ++j) f[j] = (t0 - j >= 0) ? ld_acquire(flags + (t0 - j)) : FLAG_INCL;
-          uint32_t spins = 0;
-          while (true) {
-            bool ready = true;
-#pragma unroll
-            for (int j = 0; j < LBJ; ++j) ready = ready && (f[j] != 0);
-            if (__all_sync(0xffffffffu, ready)) break;
-            if (++spins > spin_limit) { timed_out = true; break; }
-            if (spins > 8) __nanosleep(64);
-#pragma unroll
-            for (int j = 0; j < LBJ; ++j)
-              if (f[j] == 0) f[j] = ld_acquire(flags + (t0 - j));
-          }
-          timed_out = __any_sync(0xffffffffu, timed_out);
-          if (timed_out) break;
-          int jstop = LBJ;
+          jstop = LBJ;
 #pragma unroll
           for (int j = LBJ - 1; j >= 0; --j)
-            if (f[j] == FLAG_INCL) jstop = j;
+            if (lbf[j] == FLAG_INCL) jstop = j;
           const uint32_t im = __ballot_sync(0xffffffffu, jstop < LBJ);
-          const int stop = im ? (__ffs(im) - 1) : 32;
-          // fold this lane's window, earliest tile first
-          Carry v = Op::cident();
-          if (lane < stop) {
-            v = ld_cg_val(aggs + (t0 - (LBJ - 1)));
+          stop = im ? (__ffs(im) - 1) : 32;
+          // every tile from the nearest one to the first inclusive prefix
+          // must have published
+          const int need = (lane < stop) ? LBJ - 1 : (lane == stop ? jstop : -1);
+          bool ok = true;
 #pragma unroll
-            for (int j = LBJ - 2; j >= 0; --j) v = Op::ccomb(v, ld_cg_val(aggs + (t0 - j)));
-          } else if (lane == stop) {
-            v = ld_cg_val(incls + (t0 - jstop));
-#pragma unroll
-            for (int j = LBJ - 2; j >= 0; --j)
-              if (j < jstop) v = Op::ccomb(v, ld_cg_val(aggs + (t0 - j)));
+          for (int j = 0; j < LBJ; ++j)
+            if (j <= need) ok = ok && (lbf[j] != 0);
+          if (__all_sync(0xffffffffu, ok)) break;
+          if (++spins > spin_limit) {
+            timed_out = true;
+            break;
           }
-          // ordered combine across lanes: higher lane = earlier tiles
+          __nanosleep(LB_SLEEP_NS);
 #pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const Carry other = shfl_idx_any(v, (lane + o) & 31);
-            if (lane + o < 32) v = Op::ccomb(other, v);
+          for (int j = 0; j < LBJ; ++j)
+            if (lbf[j] == 0) lbf[j] = SW::poll(words + (t0 - j) * SW::NW, lbv[j]);
+        }
+        if (timed_out) break;  // warp-uniform
+        // fold this lane's share of the window, earliest tile first
+        const int need = (lane < stop) ? LBJ - 1 : (lane == stop ? jstop : -1);
+        Carry x = Op::cident();
+        bool any = false;
+#pragma unroll
+        for (int j = LBJ - 1; j >= 0; --j)
+          if (j <= need) {
+            x = any ? Op::ccomb(x, lbv[j]) : lbv[j];
+            any = true;
           }
-          acc = Op::ccomb(shfl_idx_any(v, 0), acc);
-          if (im) break;
-          pred -= 32 * LBJ;
+        // ordered combine across lanes: a higher lane holds earlier tiles
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const Carry other = shfl_idx_any(x, (lane + o) & 31);
+          if (lane + o < 32) x = Op::ccomb(other, x);
         }
-        if (timed_out && lane == 0) atomicOr(status, kStatusScanTimeout);
-        prefix = acc;
-        if (lane == 0) {
-          incls[tile] = Op::ccomb(prefix, Op::to_carry(tile_agg));
-          st_release(flags + tile, FLAG_INCL);
-        }
+        acc = Op::ccomb(shfl_idx_any(x, 0), acc);
+        if (stop < 32) break;
+        pred -= 32 * LBJ;
+        load_window(pred - (long long)lane * LBJ);
       }
-      if (lane == 0) sm.prefix = prefix;
+      if (lane == 0) {
+        if (timed_out) atomicOr(status, kStatusScanTimeout);
+        SW::publish(words + tile * SW::NW, FLAG_INCL, Op::ccomb(acc, tile_agg));
+        sm.prefix = acc;
+      }
     }
     __syncthreads();
 
@@ -416,8 +519,7 @@ scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op
 template <class Op, bool EXCL>
 int launch_scan(const char* name, unsigned grid, cudaStream_t s, const typename Op::T* in,
                 typename Op::T* out, size_t n, typename Op::T init, int tma_ok, int vec_out,
-                uint32_t* flags, typename Op::Carry* aggs, typename Op::Carry* incls,
-                uint32_t* counter, uint32_t* status, uint32_t lim) {
+                uint64_t* words, uint32_t* counter, uint32_t* status, uint32_t lim) {
   auto kern = scan_kernel<Op, EXCL>;
   static bool attr = false;
   if (!attr) {
@@ -426,7 +528,7 @@ int launch_scan(const char* name, unsigned grid, cudaStream_t s, const typename 
     attr = true;
   }
   B200_LAUNCH(name, kern, grid, SBLOCK, sizeof(ScanSmem<Op>), s, in, out, n, init, tma_ok, vec_out,
-              flags, aggs, incls, counter, status, lim);
+              words, counter, status, lim);
   return B200_OK;
 }
 
@@ -441,25 +543,23 @@ int run_scan(const char* name, const typename Op::T* in, typename Op::T* out, si
   if (in != out && ((in < out && in + n > out) || (out < in && out + n > in)))
     return fail(B200_ERR_ARG, "%s: input and output overlap partially", name);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const size_t tiles = (n + Tile<T>::SIZE - 1) / Tile<T>::SIZE;
+  const size_t tiles = (n + Tile<Op>::SIZE - 1) / Tile<Op>::SIZE;
+  constexpr size_t NW = StatusWords<Carry>::NW;
+  const size_t nwords = tiles * NW + 16;  // status words + the tile counter
   Sizer z;
-  z.take<uint32_t>(tiles + 64);  // flags + tile counter
-  z.take<Carry>(tiles);
-  z.take<Carry>(tiles);
+  z.take<uint64_t>(nwords);
   void* scr = nullptr;
   B200_TRY(scratch(s, z.bytes(), &scr, nullptr));
   Carver cv(scr);
-  uint32_t* flags = cv.take<uint32_t>(tiles + 64);
-  Carry* aggs = cv.take<Carry>(tiles);
-  Carry* incls = cv.take<Carry>(tiles);
-  uint32_t* counter = flags + tiles;
+  uint64_t* words = cv.take<uint64_t>(nwords);
+  uint32_t* counter = reinterpret_cast<uint32_t*>(words + tiles * NW);
   uint32_t* status = nullptr;
   B200_TRY(status_word(&status));
-  B200_CUDA(cudaMemsetAsync(flags, 0, (tiles + 64) * sizeof(uint32_t), s));
+  B200_CUDA(cudaMemsetAsync(words, 0, nwords * sizeof(uint64_t), s));
   const int tma_ok = reinterpret_cast<uintptr_t>(in) % 16 == 0;
   const int vec_out = reinterpret_cast<uintptr_t>(out) % 16 == 0;
   B200_TRY((launch_scan<Op, EXCL>(name, unsigned(tiles), s, in, out, n, init, tma_ok, vec_out,
-                                   flags, aggs, incls, counter, status, spin_limit())));
+                                   words, counter, status, spin_limit())));
   clear_error();
   return B200_OK;
 }
@@ -553,30 +653,27 @@ int b200_scan_exclusive_f64(const double* in, double* out, size_t n, int op, dou
 int b200_selftest_scan_timeout(b200_stream_t stream) {
   using Op = ScanSumInt<int32_t>;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const size_t n = 2 * size_t(Tile<int32_t>::SIZE);
+  const size_t n = 2 * size_t(Tile<Op>::SIZE);
   Sizer z;
   z.take<int32_t>(n);
-  z.take<uint32_t>(64);
-  z.take<uint32_t>(64);
-  z.take<uint32_t>(64);
+  z.take<uint64_t>(64);
   void* scr = nullptr;
   B200_TRY(scratch(s, z.bytes(), &scr, nullptr));
   Carver cv(scr);
   int32_t* data = cv.take<int32_t>(n);
-  uint32_t* flags = cv.take<uint32_t>(64);
-  uint32_t* aggs = cv.take<uint32_t>(64);
-  uint32_t* incls = cv.take<uint32_t>(64);
+  uint64_t* words = cv.take<uint64_t>(64);
+  uint32_t* counter = reinterpret_cast<uint32_t*>(words + 32);
   uint32_t* status = nullptr;
   B200_TRY(status_word(&status));
   B200_CUDA(cudaMemsetAsync(data, 0, n * sizeof(int32_t), s));
-  B200_CUDA(cudaMemsetAsync(flags, 0, 64 * sizeof(uint32_t), s));
+  B200_CUDA(cudaMemsetAsync(words, 0, 64 * sizeof(uint64_t), s));
   const uint32_t one = 1;  // the tile counter: the block takes tile id 1
-  B200_CUDA(cudaMemcpyAsync(flags + 32, &one, sizeof(one), cudaMemcpyHostToDevice, s));
+  B200_CUDA(cudaMemcpyAsync(counter, &one, sizeof(one), cudaMemcpyHostToDevice, s));
   B200_CUDA(cudaStreamSynchronize(s));  // `one` lives on this stack frame
   uint32_t lim = spin_limit();
   if (lim > (1u << 16)) lim = 1u << 16;
   B200_TRY((launch_scan<Op, false>("b200_selftest_scan_timeout", 1, s, data, data, n, 0, 1, 1,
-                                   flags, aggs, incls, flags + 32, status, lim)));
+                                   words, counter, status, lim)));
   clear_error();
   return B200_OK;
 }

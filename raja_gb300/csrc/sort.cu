@@ -188,88 +188,94 @@ __global__ void __launch_bounds__(RADIX) bins_kernel(const uint32_t* __restrict_
 // One tile per block.  Tiles take their id from an atomic counter in launch
 // order, so every predecessor of a tile has started and publishes its
 // counts without waiting: the look-back terminates (and is bounded anyway).
-// The kernel is instruction-bound on this GPU (the HBM stream leaves ~50
-// warp instructions per 32 keys per pass), so the pass type (first / last)
-// is a template parameter, bounds are tile-local 32-bit compares, and keys
-// and values go through separate shared buffers so that both are written
-// out in one sweep.
+// The tile arrives by one TMA bulk copy into shared memory, the ranking
+// reads digits from there (no keys held in registers across it), and keys
+// and values are scattered into a second buffer: few registers, so five
+// blocks fit per SM and their loads, rankings and look-backs overlap.  The
+// pass type (first / last) is a template parameter and bounds are
+// tile-local 32-bit compares, to keep the instruction count down.
 template <class K, class V, bool HAS_V, class ST>
 struct SweepSmem {
   using U = typename KeyBits<K>::U;
+  alignas(128) K kin[TILE];                       // the tile as loaded (TMA)
+  alignas(128) V vin[HAS_V ? TILE : 1];
   alignas(16) U keys[TILE];                       // digit-ordered keys of the tile
   alignas(16) V vals[HAS_V ? TILE : 1];           // digit-ordered values
-  uint32_t whist[WARPS][RADIX];                   // per-warp digit counters / offsets
+  uint32_t wcnt[WARPS][RADIX];                    // per-warp digit counts, then running starts
   ST gdst[RADIX];                                 // global dst = gdst[d] + local position
   uint32_t wtot[WARPS];
+  uint64_t bar;
   uint32_t tile;
 };
 
 template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST>
-__global__ void __launch_bounds__(RB)
+__global__ void __launch_bounds__(RB, 4)
 onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __restrict__ vin,
                 V* __restrict__ vout, size_t n, int shift, int desc,
                 const uint32_t* __restrict__ bins, ST* __restrict__ status,
                 ST* __restrict__ status_next, uint32_t* __restrict__ tile_counter,
-                uint32_t* __restrict__ err, uint32_t spin_limit) {
+                uint32_t* __restrict__ err, uint32_t spin_limit, int tma_ok) {
   using KB = KeyBits<K>;
   using U = typename KB::U;
   using S = Status<ST>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   SweepSmem<K, V, HAS_V, ST>& sm = *reinterpret_cast<SweepSmem<K, V, HAS_V, ST>*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 #pragma unroll
-  for (int w = 0; w < WARPS; ++w) sm.whist[w][tid] = 0;
-  if (tid == 0) sm.tile = atomicAdd(tile_counter, 1u);
+  for (int w = 0; w < WARPS; ++w) sm.wcnt[w][tid] = 0;
+  if (tid == 0) {
+    sm.tile = atomicAdd(tile_counter, 1u);
+    mbar_init(&sm.bar, 1);
+    fence_mbar_init();
+    const size_t b0 = size_t(sm.tile) * TILE;
+    if (tma_ok && b0 + TILE <= n) {
+      constexpr uint32_t kb = TILE * sizeof(K), vb = HAS_V ? TILE * sizeof(V) : 0;
+      mbar_arrive_expect_tx(&sm.bar, kb + vb);
+      tma_load_1d(sm.kin, kin + b0, kb, &sm.bar);
+      if (HAS_V) tma_load_1d(sm.vin, vin + b0, vb, &sm.bar);
+    }
+  }
   __syncthreads();
   const size_t tile = sm.tile;
   const size_t tbase = tile * TILE;
   const int lim = (tbase + TILE <= n) ? TILE : int(n - tbase);  // valid keys in this tile
-  const K* kt = kin + tbase;
-  const int wofs = warp * (32 * KPT) + lane;
-
-  // ---- keys (and values), warp-striped and coalesced; padding sorts last
-  U u[KPT];
-  V v[HAS_V ? KPT : 1];
-#pragma unroll
-  for (int k = 0; k < KPT; ++k) {
-    const int e = wofs + k * 32;
-    if (e < lim) {
-      const K key = kt[e];
-      if (FIRST) {
-        U x = KB::to_ord(key, false);
-        u[k] = desc ? U(~x) : x;
-      } else {
-        u[k] = KB::raw(key);
-      }
-      if (HAS_V) v[k] = vin[tbase + e];
-    } else {
-      u[k] = ~U(0);
-      if (HAS_V) v[k] = V(0);
+  if (tma_ok && lim == TILE) {
+    if (!mbar_wait(&sm.bar, 0, spin_limit)) {
+      if (tid == 0) atomicOr(err, kStatusTmaTimeout);
+      mbar_wait(&sm.bar, 0, spin_limit);  // let the copy land before the block exits
     }
+  } else {
+    for (int e = tid; e < lim; e += RB) {
+      sm.kin[e] = kin[tbase + e];
+      if (HAS_V) sm.vin[e] = vin[tbase + e];
+    }
+    __syncthreads();
   }
   // this tile's row of the next pass's status words starts at zero
   if (!LAST) status_next[tile * RADIX + tid] = ST(0);
 
-  // ---- warp-level multisplit ranking: the lanes holding the same digit
-  // are found with eight ballots (one per digit bit); the lowest such lane
-  // bumps the warp's counter for that digit and shares the old count.
-  uint32_t pos[KPT];
-  const uint32_t lt = lanemask_lt();
+  // key e of the tile in order-preserving form; padding sorts last
+  auto ukey = [&](int e) -> U {
+    if (e >= lim) return ~U(0);
+    if (FIRST) {
+      const U x = KB::to_ord(sm.kin[e], false);
+      return desc ? U(~x) : x;
+    }
+    return KB::raw(sm.kin[e]);
+  };
+  const int wofs = warp * (32 * KPT) + lane;  // warp-striped positions
+
+  // ---- early counts: per-warp digit histograms with shared atomics, so
+  // the tile's counts are published before the expensive ranking and the
+  // look-backs of later tiles rarely wait for this one
+  uint32_t digs[KPT / 4];  // four 8-bit digits per register
+#pragma unroll
+  for (int q = 0; q < KPT / 4; ++q) digs[q] = 0;
 #pragma unroll
   for (int k = 0; k < KPT; ++k) {
-    const uint32_t d = uint32_t(u[k] >> shift) & 0xffu;
-    uint32_t peers = 0xffffffffu;
-#pragma unroll
-    for (int bit = 0; bit < 8; ++bit) {
-      const uint32_t bal = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
-      // keep lanes whose bit equals mine: ~(bal ^ mine), mine = 0 or ~0
-      peers &= ~(bal ^ (0u - ((d >> bit) & 1u)));
-    }
-    const int leader = __ffs(peers) - 1;
-    uint32_t old = 0;
-    if (lane == leader) old = atomicAdd(&sm.whist[warp][d], uint32_t(__popc(peers)));
-    old = __shfl_sync(0xffffffffu, old, leader);
-    pos[k] = old + __popc(peers & lt);
+    const uint32_t d = uint32_t(ukey(wofs + k * 32) >> shift) & 0xffu;
+    digs[k / 4] |= d << (8 * (k % 4));
+    atomicAdd(&sm.wcnt[warp][d], 1u);
   }
   __syncthreads();
 
@@ -278,8 +284,8 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   uint32_t cnt = 0;
 #pragma unroll
   for (int w = 0; w < WARPS; ++w) {
-    const uint32_t c = sm.whist[w][d];
-    sm.whist[w][d] = cnt;  // exclusive offset of warp w inside digit d
+    const uint32_t c = sm.wcnt[w][d];
+    sm.wcnt[w][d] = cnt;  // exclusive offset of warp w inside digit d
     cnt += c;
   }
   ST* my_status = status + tile * RADIX + d;
@@ -299,6 +305,35 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
 #pragma unroll
   for (int w = 0; w < WARPS - 1; ++w)
     if (w < warp) lstart += sm.wtot[w];
+#pragma unroll
+  for (int w = 0; w < WARPS; ++w) sm.wcnt[w][d] += lstart;  // tile-local start of (warp, digit)
+
+  __syncthreads();
+
+  // ---- warp-level multisplit ranking, scattered straight into digit order
+  // in shared memory: the lanes holding the same digit are found with eight
+  // ballots (one per digit bit); the lowest such lane bumps the warp's
+  // running start for that digit and shares the old one, which with the
+  // lane's rank among its peers is the key's tile-local position.
+  const uint32_t lt = lanemask_lt();
+#pragma unroll
+  for (int k = 0; k < KPT; ++k) {
+    const int e = wofs + k * 32;
+    const uint32_t dk = (digs[k / 4] >> (8 * (k % 4))) & 0xffu;
+    uint32_t peers = 0xffffffffu;
+#pragma unroll
+    for (int bit = 0; bit < 8; ++bit) {
+      const uint32_t bal = __ballot_sync(0xffffffffu, (dk >> bit) & 1u);
+      // keep lanes whose bit equals mine: ~(bal ^ mine), mine = 0 or ~0
+      peers &= ~(bal ^ (0u - ((dk >> bit) & 1u)));
+    }
+    const int leader = __ffs(peers) - 1;
+    uint32_t old = 0;
+    if (lane == leader) old = atomicAdd(&sm.wcnt[warp][dk], uint32_t(__popc(peers)));
+    const uint32_t p = __shfl_sync(0xffffffffu, old, leader) + __popc(peers & lt);
+    sm.keys[p] = ukey(e);
+    if (HAS_V) sm.vals[p] = (e < lim) ? sm.vin[e] : V(0);
+  }
 
   // ---- decoupled look-back for digit d, LBW predecessors per poll: the
   // loads of one window are independent, then consumed in order until an
@@ -334,25 +369,13 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
           atomicOr(err, kStatusSortTimeout);
           break;
         }
-        if (spins > 4) __nanosleep(32);
+        __nanosleep(100);
       }
     }
     gstart = acc;
     st_relaxed(my_status, ST(S::INCL | (acc + cnt)));
   }
   sm.gdst[d] = gstart - ST(lstart);
-#pragma unroll
-  for (int w = 0; w < WARPS; ++w) sm.whist[w][d] += lstart;
-  __syncthreads();
-
-  // ---- scatter keys (and values) into digit order in shared memory
-#pragma unroll
-  for (int k = 0; k < KPT; ++k) {
-    const uint32_t dk = uint32_t(u[k] >> shift) & 0xffu;
-    const uint32_t p = pos[k] + sm.whist[warp][dk];
-    sm.keys[p] = u[k];
-    if (HAS_V) sm.vals[p] = v[k];
-  }
   __syncthreads();
 
   // ---- write out in runs (one digit's run is contiguous in global)
@@ -378,6 +401,8 @@ template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST>
 int launch_sweep_t(const char* name, size_t tiles, cudaStream_t s, const K* src, K* dst,
                    const V* vsrc, V* vdst, size_t n, int shift, int desc, const uint32_t* bins,
                    ST* status, ST* status_next, uint32_t* counter, uint32_t* err, uint32_t lim) {
+  const int tma_ok = (reinterpret_cast<uintptr_t>(src) % 16 == 0) &&
+                     (!HAS_V || reinterpret_cast<uintptr_t>(vsrc) % 16 == 0);
   using SM = SweepSmem<K, V, HAS_V, ST>;
   auto kern = onesweep_kernel<K, V, HAS_V, ST, FIRST, LAST>;
   static bool attr = false;
@@ -386,7 +411,7 @@ int launch_sweep_t(const char* name, size_t tiles, cudaStream_t s, const K* src,
     attr = true;
   }
   B200_LAUNCH(name, kern, (unsigned)tiles, RB, sizeof(SM), s, src, dst, vsrc, vdst, n, shift, desc,
-              bins, status, status_next, counter, err, lim);
+              bins, status, status_next, counter, err, lim, tma_ok);
   return B200_OK;
 }
 
