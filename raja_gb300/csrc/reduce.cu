@@ -17,8 +17,10 @@
 //
 // Floating-point sums support three modes (B200_MODE_*):
 //   naive         -- accumulate in the element type (the reference's rule);
-//   compensated   -- per-thread TwoSum (Neumaier) in the element type, FP64
-//                    across blocks for FP32 input, double-double for FP64;
+//   compensated   -- FP32 input: per-thread cascaded TwoSum in FP32 (three
+//                    levels, so the per-element work stays on the FP32
+//                    pipes), double-double across threads and blocks; FP64
+//                    input: per-thread TwoSum and double-double throughout;
 //   deterministic -- one partial per fixed chunk, combined in a fixed tree:
 //                    the result depends on (n, data) only, not on the grid.
 // Min/Max(/Loc) carry the element index and break ties by the lowest index,
@@ -73,8 +75,10 @@ struct OutPtrs {
 };
 
 // ----------------------------------------------------------------- ops
-// Each op defines: T, Acc, Part, identity(), add(acc, v, i) (or add2 for
-// dot), merge(earlier, later), to_part, part_identity, merge_part, store.
+// Each op defines: T, Acc (per thread), Part (across threads and blocks),
+// identity(), add(acc, v, i) (or add2 for dot), merge(earlier, later),
+// to_part, part_identity, merge_part, store.  Each thread's Acc becomes a
+// Part before the block reduction.
 
 // Naive floating-point sum / dot: accumulate in T.
 template <class TT>
@@ -94,35 +98,63 @@ struct SumNaive {
 
 template <class T>
 struct Pair { T s, c; };
+struct Trip { float s, c, cc; };
+struct DD { double hi, lo; };
 
-// Compensated FP32 sum / dot: TwoSum per thread, FP64 across blocks.
+// Double-double sum (two_sum of the leading parts, trailing parts added,
+// then renormalised so that |lo| <= ulp(hi) / 2).
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+  double s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  const double hi = s + e;
+  return {hi, e - (hi - s)};
+}
+
+// Compensated FP32 sum / dot: cascaded TwoSum per thread in FP32,
+// double-double across threads and blocks.
 struct SumCompF32 {
   using T = float;
-  using Acc = Pair<float>;
-  using Part = double;
-  static __device__ Acc identity() { return {0.f, 0.f}; }
+  using Acc = Trip;
+  using Part = DD;
+  static __device__ Acc identity() { return {0.f, 0.f, 0.f}; }
+  // Cascaded compensation: the rounding error of the running sum goes into
+  // a compensated second level, whose own error is accumulated in a third.
   static __device__ void add(Acc& a, float v, int64_t) {
-    float s, e;
+    float s, e, c, e2;
     two_sum(a.s, v, s, e);
+    two_sum(a.c, e, c, e2);
     a.s = s;
-    a.c += e;
+    a.c = c;
+    a.cc += e2;
   }
   static __device__ void add2(Acc& a, float x, float y) {
-    float p, ep, s, es;
-    two_prod(x, y, p, ep);
+    float p, ep, s, es, c1, e1, c2, e2;
+    two_prod(x, y, p, ep);  // x*y = p + ep exactly
     two_sum(a.s, p, s, es);
+    two_sum(a.c, es, c1, e1);
+    two_sum(c1, ep, c2, e2);
     a.s = s;
-    a.c += ep + es;
+    a.c = c2;
+    a.cc += e1 + e2;
   }
   static __device__ Acc merge(Acc a, Acc b) {
-    float s, e;
+    float s, e, c, e2;
     two_sum(a.s, b.s, s, e);
-    return {s, a.c + b.c + e};
+    two_sum(a.c + b.c, e, c, e2);
+    return {s, c, a.cc + b.cc + e2};
   }
-  static __device__ Part to_part(Acc a) { return double(a.s) + double(a.c); }
-  static __device__ Part part_identity() { return 0.0; }
-  static __device__ Part merge_part(Part a, Part b) { return a + b; }
-  static __device__ void store(OutPtrs o, Part p) { *static_cast<double*>(o.val) = p; }
+  // The first two levels become one double-double exactly (two_sum in
+  // double), the third is added in double-double; from here on every
+  // combine is double-double.
+  static __device__ Part to_part(Acc a) {
+    double hi, lo;
+    two_sum(double(a.s), double(a.c), hi, lo);
+    return dd_add({hi, lo}, {double(a.cc), 0.0});
+  }
+  static __device__ Part part_identity() { return {0.0, 0.0}; }
+  static __device__ Part merge_part(Part a, Part b) { return dd_add(a, b); }
+  static __device__ void store(OutPtrs o, Part p) { *static_cast<double*>(o.val) = p.hi + p.lo; }
 };
 
 // Compensated FP64 sum / dot: double-double style accumulation throughout.
@@ -294,7 +326,6 @@ reduce_kernel(const typename Op::T* __restrict__ x, const typename Op::T* __rest
   using Acc = typename Op::Acc;
   using Part = typename Op::Part;
   using C = Chunk<T>;
-  __shared__ Acc sh_acc[32];
   __shared__ Part sh_part[32];
   __shared__ bool am_last;
 
@@ -338,13 +369,15 @@ reduce_kernel(const typename Op::T* __restrict__ x, const typename Op::T* __rest
       }
     }
     if (det) {
-      Acc r = block_reduce(acc, Op::identity(), [](Acc a, Acc b) { return Op::merge(a, b); }, sh_acc);
-      if (tid == 0) parts[c] = Op::to_part(r);
+      const Part r = block_reduce(Op::to_part(acc), Op::part_identity(),
+                                  [](Part a, Part b) { return Op::merge_part(a, b); }, sh_part);
+      if (tid == 0) parts[c] = r;
     }
   }
   if (!det) {
-    Acc r = block_reduce(acc, Op::identity(), [](Acc a, Acc b) { return Op::merge(a, b); }, sh_acc);
-    if (tid == 0) parts[blockIdx.x] = Op::to_part(r);
+    const Part r = block_reduce(Op::to_part(acc), Op::part_identity(),
+                                [](Part a, Part b) { return Op::merge_part(a, b); }, sh_part);
+    if (tid == 0) parts[blockIdx.x] = r;
   }
 
   // Last-block combine (reduce.hpp:133-214 restated): publish, take a

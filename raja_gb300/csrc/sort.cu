@@ -17,10 +17,11 @@
 //      loaded with coalesced warp-striped reads, ranked in registers with a
 //      warp-level multisplit built from eight ballots per key (on this GPU
 //      __match_any_sync costs ~80 cycles per warp, the ballots a few), its
-//      per-digit counts are published and a per-digit decoupled look-back
-//      (eight predecessors per poll) yields the global offsets; keys and
-//      values are scattered through shared memory into digit order and
-//      written out in runs, so the global stores coalesce.  Each pass
+//      per-digit counts are published before the ranking (early counts) and
+//      a per-digit decoupled look-back (eight predecessors per poll) yields
+//      the global offsets; the keys' tile positions are scattered into
+//      digit order in shared memory and keys and values are written out in
+//      runs, so the global stores coalesce.  Each pass
 //      zeroes its tiles' rows of the next pass's status words (two
 //      ping-pong buffers instead of one per pass).
 // Each pass reads and writes every key once; there is no separate upsweep.
@@ -188,19 +189,19 @@ __global__ void __launch_bounds__(RADIX) bins_kernel(const uint32_t* __restrict_
 // One tile per block.  Tiles take their id from an atomic counter in launch
 // order, so every predecessor of a tile has started and publishes its
 // counts without waiting: the look-back terminates (and is bounded anyway).
-// The tile arrives by one TMA bulk copy into shared memory, the ranking
-// reads digits from there (no keys held in registers across it), and keys
-// and values are scattered into a second buffer: few registers, so five
-// blocks fit per SM and their loads, rankings and look-backs overlap.  The
-// pass type (first / last) is a template parameter and bounds are
-// tile-local 32-bit compares, to keep the instruction count down.
+// The tile arrives by one TMA bulk copy into shared memory and stays there:
+// the ranking reads the digits from it (packed four per register) and
+// scatters only each key's 16-bit tile position into digit order; the
+// write-out fetches key and value through that index.  One copy of the tile
+// in shared memory and few registers, so four to six blocks fit per SM and
+// their loads, rankings and look-backs overlap.  The pass type (first /
+// last) is a template parameter and bounds are tile-local 32-bit compares,
+// to keep the instruction count down.
 template <class K, class V, bool HAS_V, class ST>
 struct SweepSmem {
-  using U = typename KeyBits<K>::U;
   alignas(128) K kin[TILE];                       // the tile as loaded (TMA)
   alignas(128) V vin[HAS_V ? TILE : 1];
-  alignas(16) U keys[TILE];                       // digit-ordered keys of the tile
-  alignas(16) V vals[HAS_V ? TILE : 1];           // digit-ordered values
+  uint16_t idx[TILE];                             // tile position of the i-th key in digit order
   uint32_t wcnt[WARPS][RADIX];                    // per-warp digit counts, then running starts
   ST gdst[RADIX];                                 // global dst = gdst[d] + local position
   uint32_t wtot[WARPS];
@@ -208,8 +209,16 @@ struct SweepSmem {
   uint32_t tile;
 };
 
+// Blocks per SM the shared memory allows (228 KB per SM, 1 KB reserved per
+// block), at most six; the register budget is cut to match.
+template <class K, class V, bool HAS_V, class ST>
+constexpr int sweep_min_blocks() {
+  constexpr int b = 233472 / int(sizeof(SweepSmem<K, V, HAS_V, ST>) + 1024);
+  return b < 1 ? 1 : (b > 6 ? 6 : b);
+}
+
 template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST>
-__global__ void __launch_bounds__(RB, 4)
+__global__ void __launch_bounds__(RB, (sweep_min_blocks<K, V, HAS_V, ST>()))
 onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __restrict__ vin,
                 V* __restrict__ vout, size_t n, int shift, int desc,
                 const uint32_t* __restrict__ bins, ST* __restrict__ status,
@@ -331,8 +340,7 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
     uint32_t old = 0;
     if (lane == leader) old = atomicAdd(&sm.wcnt[warp][dk], uint32_t(__popc(peers)));
     const uint32_t p = __shfl_sync(0xffffffffu, old, leader) + __popc(peers & lt);
-    sm.keys[p] = ukey(e);
-    if (HAS_V) sm.vals[p] = (e < lim) ? sm.vin[e] : V(0);
+    sm.idx[p] = uint16_t(e);
   }
 
   // ---- decoupled look-back for digit d, LBW predecessors per poll: the
@@ -378,11 +386,13 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   sm.gdst[d] = gstart - ST(lstart);
   __syncthreads();
 
-  // ---- write out in runs (one digit's run is contiguous in global)
+  // ---- write out in runs (one digit's run is contiguous in global): the
+  // i-th key in digit order is fetched from the loaded tile through idx
 #pragma unroll
   for (int j = 0; j < KPT; ++j) {
     const int i = j * RB + tid;
-    const U uk = sm.keys[i];
+    const int e = sm.idx[i];
+    const U uk = ukey(e);
     const ST dst = sm.gdst[uint32_t(uk >> shift) & 0xffu] + ST(i);
     if (dst < n) {
       if (LAST) {
@@ -391,7 +401,7 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
       } else {
         kout[dst] = KB::cook(uk);
       }
-      if (HAS_V) vout[dst] = sm.vals[i];
+      if (HAS_V) vout[dst] = sm.vin[e];
     }
   }
 }

@@ -152,3 +152,26 @@ def test_device_output_no_sync(prims):
     prims.reduce_sum(x, out=out)
     torch.cuda.synchronize()
     assert abs(out.item() - x.sum().item()) < 1e-9
+
+
+def test_compensated_f32_beats_naive_f64_ill_conditioned(prims, orc):
+    """FP32 sum with condition number ~1e10 (the last element cancels the
+    rest): the compensated FP32 sum (cascaded TwoSum per thread,
+    double-double across threads) is at least as accurate as the naive FP64
+    sum of the same values and within 1e-6 relative of the exact sum."""
+    rng = np.random.default_rng(21)
+    n = 1 << 22
+    sign = rng.choice([-1.0, 1.0], n)
+    x = (sign * np.clip(np.exp(rng.normal(0, 6, n)), 1e-8, 1e8)).astype(np.float32)
+    head, _ = orc.exact_sum(x[:-1])
+    x[-1] = np.float32(-head)
+    ex, exlo = orc.exact_sum(x)
+    assert ex != 0.0
+    cond = float(np.abs(x.astype(np.float64)).sum()) / abs(ex)
+    assert cond > 1e8
+    comp = prims.reduce_sum(to_dev(x), mode=1)
+    naive64 = prims.reduce_sum(to_dev(x.astype(np.float64)))
+    err_comp = abs((comp - ex) - exlo)
+    err_n64 = abs((naive64 - ex) - exlo)
+    assert err_comp <= max(err_n64, 0.5 * np.spacing(abs(ex))), (cond, err_comp, err_n64)
+    assert err_comp <= 1e-6 * abs(ex)
