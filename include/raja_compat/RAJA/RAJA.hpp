@@ -465,20 +465,46 @@ void forall_params_impl(seq_exec, const TypedRangeSegment<T>& r, Body&& body, Re
 }
 
 namespace detail {
-// Dispatch of forall(seg, params..., body): a KernelName is dropped for the
-// host policies; reducer params go to forall_params_impl.
-template <typename Pol, typename Seg, typename Body>
-void forall_with(Pol p, Seg&& seg, Body&& body) {
-  forall_impl(p, std::forward<Seg>(seg), std::forward<Body>(body));
-}
-template <typename Pol, typename Seg, typename Body, typename... Rest>
-void forall_with(Pol p, Seg&& seg, Body&& body, expt::KernelName, Rest&&... rest) {
-  forall_with(p, std::forward<Seg>(seg), std::forward<Body>(body), std::forward<Rest>(rest)...);
-}
-template <typename Pol, typename Seg, typename Body, typename R0, typename... Rest,
+// Dispatch of forall(seg, params..., body): kernel names (expt::Name) are
+// dropped wherever they appear (no plugin consumes them here); reducer
+// params are collected, in order, for forall_params_impl.
+template <typename Pol, typename Seg, typename Body, typename... Red>
+void forall_collect(Pol p, Seg&& seg, Body&& body, std::tuple<Red&...> reds);
+template <typename Pol, typename Seg, typename Body, typename... Red, typename... Rest>
+void forall_collect(Pol p, Seg&& seg, Body&& body, std::tuple<Red&...> reds, expt::KernelName,
+                    Rest&&... rest);
+template <typename Pol, typename Seg, typename Body, typename... Red, typename R0, typename... Rest,
           typename std::enable_if<expt::detail::is_reducer<std::decay_t<R0>>::value, int>::type = 0>
-void forall_with(Pol p, Seg&& seg, Body&& body, R0&& r0, Rest&&... rest) {
-  forall_params_impl(p, std::forward<Seg>(seg), std::forward<Body>(body), r0, rest...);
+void forall_collect(Pol p, Seg&& seg, Body&& body, std::tuple<Red&...> reds, R0& r0,
+                    Rest&&... rest);
+
+template <typename Pol, typename Seg, typename Body, typename... Red>
+void forall_collect(Pol p, Seg&& seg, Body&& body, std::tuple<Red&...> reds) {
+  std::apply([&](auto&... r) {
+    forall_params_impl(p, std::forward<Seg>(seg), std::forward<Body>(body), r...);
+  }, reds);
+}
+template <typename Pol, typename Seg, typename Body, typename... Red, typename... Rest>
+void forall_collect(Pol p, Seg&& seg, Body&& body, std::tuple<Red&...> reds, expt::KernelName,
+                    Rest&&... rest) {
+  forall_collect(p, std::forward<Seg>(seg), std::forward<Body>(body), reds,
+                 std::forward<Rest>(rest)...);
+}
+template <typename Pol, typename Seg, typename Body, typename... Red, typename R0, typename... Rest,
+          typename std::enable_if<expt::detail::is_reducer<std::decay_t<R0>>::value, int>::type>
+void forall_collect(Pol p, Seg&& seg, Body&& body, std::tuple<Red&...> reds, R0& r0,
+                    Rest&&... rest) {
+  forall_collect(p, std::forward<Seg>(seg), std::forward<Body>(body),
+                 std::tuple_cat(reds, std::tie(r0)), std::forward<Rest>(rest)...);
+}
+
+template <typename Pol, typename Seg, typename Body, typename... Params>
+void forall_with(Pol p, Seg&& seg, Body&& body, Params&&... params) {
+  if constexpr ((expt::detail::is_reducer<std::decay_t<Params>>::value || ... || false)) {
+    forall_collect(p, std::forward<Seg>(seg), std::forward<Body>(body), std::tuple<>(), params...);
+  } else {
+    forall_impl(p, std::forward<Seg>(seg), std::forward<Body>(body));
+  }
 }
 template <typename Pol, typename Seg, typename Tup, size_t... I>
 void forall_split(Seg&& seg, Tup&& tup, std::index_sequence<I...>) {

@@ -182,7 +182,8 @@ void test_forall_and_params() {
   // expt::Reduce / ReduceLoc params: target = op(target, result)
   double s = 10.0, lo = 1e300, hi = -1e300, vmin = 1e300;
   Index_type imin = -1;
-  RAJA::forall<exec>(RAJA::RangeSegment(0, n), RAJA::expt::Reduce<RAJA::operators::plus>(&s),
+  RAJA::forall<exec>(RAJA::RangeSegment(0, n), RAJA::expt::Name("expt_reduce"),
+                     RAJA::expt::Reduce<RAJA::operators::plus>(&s),
                      RAJA::expt::Reduce<RAJA::operators::minimum>(&lo),
                      RAJA::expt::Reduce<RAJA::operators::maximum>(&hi),
                      RAJA::expt::ReduceLoc<RAJA::operators::minimum>(&vmin, &imin),

@@ -78,6 +78,21 @@ int main() {
   RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 10), RAJA::expt::Reduce<RAJA::operators::plus>(&t),
                                [=](Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& s) { s += double(i); });
   CHECK("expt_reduce_host", t == 46.0);
+  // kernel names may sit before, between or after the reducer params
+  double t1 = 0.0, t2 = 100.0;
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 10), RAJA::expt::Name("a"),
+                               RAJA::expt::Reduce<RAJA::operators::plus>(&t1), RAJA::expt::Name("b"),
+                               RAJA::expt::Reduce<RAJA::operators::minimum>(&t2), RAJA::expt::Name("c"),
+                               [=](Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& s,
+                                   RAJA::expt::ValOp<double, RAJA::operators::minimum>& m) {
+                                 s += double(i);
+                                 m.min(double(i) + 3.0);
+                               });
+  CHECK("expt_reduce_names_anywhere", t1 == 45.0 && t2 == 3.0);
+  int named = 0;
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 4), RAJA::expt::Name("only"),
+                               [&](Index_type) { ++named; });
+  CHECK("forall_name_only", named == 4);
   // WorkGroup (ordered): a[i] += i + 5 (test-workgroup-Unordered-Single.hpp)
   std::vector<int> w(100, 0);
   int* wp = w.data();
