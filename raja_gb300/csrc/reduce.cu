@@ -63,7 +63,6 @@ __device__ __forceinline__ P ld_cg_any(const P* p) {
 template <class T>
 struct Lim;
 template <> struct Lim<float> { static __device__ float hi() { return FLT_MAX; } static __device__ float lo() { return -FLT_MAX; } };
-template <> struct Lim<double> { static __device__ double hi() { return DBL_MAX; } static __device__ double lo() { return -DBL_MAX; } };
 template <> struct Lim<int32_t> { static __device__ int32_t hi() { return INT_MAX; } static __device__ int32_t lo() { return INT_MIN; } };
 template <> struct Lim<int64_t> { static __device__ int64_t hi() { return LLONG_MAX; } static __device__ int64_t lo() { return LLONG_MIN; } };
 template <> struct Lim<uint32_t> { static __device__ uint32_t hi() { return UINT_MAX; } static __device__ uint32_t lo() { return 0u; } };
@@ -76,9 +75,9 @@ struct OutPtrs {
 
 // ----------------------------------------------------------------- ops
 // Each op defines: T, Acc (per thread), Part (across threads and blocks),
-// identity(), add(acc, v, i) (or add2 for dot), merge(earlier, later),
-// to_part, part_identity, merge_part, store.  Each thread's Acc becomes a
-// Part before the block reduction.
+// identity(), add(acc, v, i) (or add2 for dot), to_part, part_identity,
+// merge_part(earlier, later), store.  Each thread's Acc becomes a Part
+// before the block reduction.
 
 // Naive floating-point sum / dot: accumulate in T.
 template <class TT>
@@ -137,12 +136,6 @@ struct SumCompF32 {
     a.s = s;
     a.c = c2;
     a.cc += e1 + e2;
-  }
-  static __device__ Acc merge(Acc a, Acc b) {
-    float s, e, c, e2;
-    two_sum(a.s, b.s, s, e);
-    two_sum(a.c + b.c, e, c, e2);
-    return {s, c, a.cc + b.cc + e2};
   }
   // The first two levels become one double-double exactly (two_sum in
   // double), the third is added in double-double; from here on every

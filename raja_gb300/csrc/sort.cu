@@ -210,11 +210,12 @@ struct SweepSmem {
 };
 
 // Blocks per SM the shared memory allows (228 KB per SM, 1 KB reserved per
-// block), at most six; the register budget is cut to match.
+// block), at most five (48 registers, no spills); the register budget is
+// cut to match.
 template <class K, class V, bool HAS_V, class ST>
 constexpr int sweep_min_blocks() {
   constexpr int b = 233472 / int(sizeof(SweepSmem<K, V, HAS_V, ST>) + 1024);
-  return b < 1 ? 1 : (b > 6 ? 6 : b);
+  return b < 1 ? 1 : (b > 5 ? 5 : b);
 }
 
 template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST>

@@ -11,9 +11,10 @@ from conftest import to_dev, to_host
 pytestmark = pytest.mark.gpu
 
 G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-# tile boundaries: 4096 elements per tile for 4-byte types, 2048 for 8-byte
-SIZES = [0, 1, 2, 31, 32, 33, 2047, 2048, 2049, 4095, 4096, 4097, 12289, 65536 + 7,
-         (1 << 20) + 3]
+# tile boundaries: 64 KB tiles hold 16384 elements of a 4-byte type and 8192
+# of an 8-byte type; the compensated sums use 32 KB tiles (8192 / 4096)
+SIZES = [0, 1, 2, 31, 32, 33, 4095, 4096, 4097, 8191, 8192, 8193, 16383, 16384, 16385,
+         49153, 65536 + 7, (1 << 20) + 3]
 
 
 def test_golden_scan(prims):
