@@ -64,6 +64,11 @@ struct KeyBits {
     else if (std::is_signed<K>::value) u ^= SIGN;
     return desc ? U(~u) : u;
   }
+  // Raw key whose first-pass ordered form (desc applied) is all ones, so
+  // that padding sorts last.
+  static __device__ __forceinline__ K pad(bool desc) {
+    return from_ord(U(~U(0)), desc);
+  }
   static __device__ __forceinline__ K from_ord(U u, bool desc) {
     if (desc) u = ~u;
     if (std::is_floating_point<K>::value) u = (u & SIGN) ? U(u ^ SIGN) : U(~u);
@@ -80,6 +85,16 @@ struct Status {
   static constexpr ST INCL = ST(2) << SHIFT;
   static constexpr ST MASK = (ST(1) << SHIFT) - 1;
 };
+
+// Byte-aligned digit of an order-preserving key: one byte permute of the
+// key's 32-bit half that holds it (sel = 0x4440 | byte within the half; the
+// upper result bytes come from the zero operand).
+__device__ __forceinline__ uint32_t digit_of(uint32_t u, bool, uint32_t sel) {
+  return __byte_perm(u, 0u, sel);
+}
+__device__ __forceinline__ uint32_t digit_of(uint64_t u, bool hi, uint32_t sel) {
+  return __byte_perm(hi ? uint32_t(u >> 32) : uint32_t(u), 0u, sel);
+}
 
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
   uint32_t v;
@@ -255,18 +270,19 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
       mbar_wait(&sm.bar, 0, spin_limit);  // let the copy land before the block exits
     }
   } else {
-    for (int e = tid; e < lim; e += RB) {
-      sm.kin[e] = kin[tbase + e];
-      if (HAS_V) sm.vin[e] = vin[tbase + e];
+    // partial (last) tile: padding keys sort after every real key
+    const K padk = FIRST ? KB::pad(desc != 0) : KB::cook(~U(0));
+    for (int e = tid; e < TILE; e += RB) {
+      sm.kin[e] = (e < lim) ? kin[tbase + e] : padk;
+      if (HAS_V && e < lim) sm.vin[e] = vin[tbase + e];
     }
     __syncthreads();
   }
   // this tile's row of the next pass's status words starts at zero
   if (!LAST) status_next[tile * RADIX + tid] = ST(0);
 
-  // key e of the tile in order-preserving form; padding sorts last
+  // key e of the tile in order-preserving form (padding is all ones)
   auto ukey = [&](int e) -> U {
-    if (e >= lim) return ~U(0);
     if (FIRST) {
       const U x = KB::to_ord(sm.kin[e], false);
       return desc ? U(~x) : x;
@@ -274,6 +290,8 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
     return KB::raw(sm.kin[e]);
   };
   const int wofs = warp * (32 * KPT) + lane;  // warp-striped positions
+  const bool dhi = shift >= 32;
+  const uint32_t dsel = 0x4440u | uint32_t((shift >> 3) & 3);
 
   // ---- early counts: per-warp digit histograms with shared atomics, so
   // the tile's counts are published before the expensive ranking and the
@@ -283,8 +301,8 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   for (int q = 0; q < KPT / 4; ++q) digs[q] = 0;
 #pragma unroll
   for (int k = 0; k < KPT; ++k) {
-    const uint32_t d = uint32_t(ukey(wofs + k * 32) >> shift) & 0xffu;
-    digs[k / 4] |= d << (8 * (k % 4));
+    const uint32_t d = digit_of(ukey(wofs + k * 32), dhi, dsel);
+    digs[k / 4] += d << (8 * (k % 4));
     atomicAdd(&sm.wcnt[warp][d], 1u);
   }
   __syncthreads();
@@ -329,7 +347,7 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
 #pragma unroll
   for (int k = 0; k < KPT; ++k) {
     const int e = wofs + k * 32;
-    const uint32_t dk = (digs[k / 4] >> (8 * (k % 4))) & 0xffu;
+    const uint32_t dk = __byte_perm(digs[k / 4], 0u, 0x4440u + (k % 4));
     uint32_t peers = 0xffffffffu;
 #pragma unroll
     for (int bit = 0; bit < 8; ++bit) {
@@ -388,14 +406,16 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   __syncthreads();
 
   // ---- write out in runs (one digit's run is contiguous in global): the
-  // i-th key in digit order is fetched from the loaded tile through idx
+  // i-th key in digit order is fetched from the loaded tile through idx.
+  // Padding positions (e >= lim, last tile only) are skipped; every real
+  // key's destination lies in [0, n).
 #pragma unroll
   for (int j = 0; j < KPT; ++j) {
     const int i = j * RB + tid;
     const int e = sm.idx[i];
-    const U uk = ukey(e);
-    const ST dst = sm.gdst[uint32_t(uk >> shift) & 0xffu] + ST(i);
-    if (dst < n) {
+    if (e < lim) {
+      const U uk = ukey(e);
+      const ST dst = sm.gdst[digit_of(uk, dhi, dsel)] + ST(i);
       if (LAST) {
         const U x = desc ? U(~uk) : uk;
         kout[dst] = KB::from_ord(x, false);
