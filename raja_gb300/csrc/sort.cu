@@ -13,7 +13,7 @@
 //      every 8-bit digit position at once (per-warp shared counters); it
 //      also zeroes the first pass's look-back status words;
 //   2. bins_kernel: exclusive scan of each histogram -> global digit bases;
-//   3. one onesweep_kernel per digit: a tile of 256 threads x 24 keys is
+//   3. one onesweep_kernel per digit: a tile of 256 threads x 24-28 keys is
 //      loaded with coalesced warp-striped reads, ranked in registers with a
 //      warp-level multisplit built from eight ballots per key (on this GPU
 //      __match_any_sync costs ~80 cycles per warp, the ballots a few), its
@@ -38,8 +38,14 @@ namespace b200 {
 namespace {
 
 constexpr int RB = 256;       // threads per tile
-constexpr int KPT = 24;       // keys per thread (16, 20, 28, 32 measured slower overall)
-constexpr int TILE = RB * KPT;
+// Keys per thread of a onesweep tile, by shape (measured on GB300 at 2^28:
+// 28 is best for 32-bit keys alone, 24 for 64-bit keys and for pairs;
+// 16, 20 and 32 are slower).
+template <class K, bool HAS_V>
+struct SweepShape {
+  static constexpr int KPT = (sizeof(K) == 4 && !HAS_V) ? 28 : 24;
+  static constexpr int TILE = RB * KPT;
+};
 constexpr int RADIX = 256;
 constexpr int WARPS = RB / 32;
 
@@ -214,6 +220,7 @@ __global__ void __launch_bounds__(RADIX) bins_kernel(const uint32_t* __restrict_
 // to keep the instruction count down.
 template <class K, class V, bool HAS_V, class ST>
 struct SweepSmem {
+  static constexpr int TILE = SweepShape<K, HAS_V>::TILE;
   alignas(128) K kin[TILE];                       // the tile as loaded (TMA)
   alignas(128) V vin[HAS_V ? TILE : 1];
   uint16_t idx[TILE];                             // tile position of the i-th key in digit order
@@ -243,6 +250,7 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   using KB = KeyBits<K>;
   using U = typename KB::U;
   using S = Status<ST>;
+  constexpr int KPT = SweepShape<K, HAS_V>::KPT, TILE = SweepShape<K, HAS_V>::TILE;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SweepSmem<K, V, HAS_V, ST>& sm = *reinterpret_cast<SweepSmem<K, V, HAS_V, ST>*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -482,6 +490,7 @@ int run_sort(const char* name, const K* kin, K* kout, const V* vin, V* vout, siz
     clear_error();
     return B200_OK;
   }
+  constexpr int TILE = SweepShape<K, HAS_V>::TILE;
   const size_t tiles = (n + TILE - 1) / TILE;
   const bool wide = n >= (size_t(1) << 30);
   const size_t st_bytes = wide ? sizeof(uint64_t) : sizeof(uint32_t);

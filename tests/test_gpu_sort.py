@@ -11,8 +11,9 @@ from conftest import to_dev, to_host
 pytestmark = pytest.mark.gpu
 
 G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-# tiles hold 6144 keys (256 threads x 24)
-SIZES = [0, 1, 2, 3, 100, 4097, 6143, 6144, 6145, 12289, 100003, (1 << 20) + 5]
+# tiles hold 7168 keys for 32-bit keys alone (256 threads x 28), 6144 otherwise
+SIZES = [0, 1, 2, 3, 100, 4097, 6143, 6144, 6145, 7167, 7168, 7169, 14337, 100003,
+         (1 << 20) + 5]
 
 
 def test_golden_sort(prims):
