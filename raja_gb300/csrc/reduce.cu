@@ -37,6 +37,7 @@ namespace b200 {
 namespace {
 
 constexpr int RBLOCK = 256;
+constexpr int F64_DADD = 1;  // of 8 elements, added on the FP64 pipe by the FP64 sum (0-4 measured)
 
 template <class T>
 struct Chunk {
@@ -93,6 +94,57 @@ struct SumNaive {
   static __device__ Part part_identity() { return T(0); }
   static __device__ Part merge_part(Part a, Part b) { return a + b; }
   static __device__ void store(OutPtrs o, Part p) { *static_cast<double*>(o.val) = double(p); }
+};
+
+// FP64 sum that takes most per-element work off GB300's FP64 pipe (about
+// 1.6 DADD per clock per SM, below what HBM delivers).  Of each thread's
+// 8-element chunk, D elements are added in FP64 as usual; the mantissas of
+// the others are aligned to their largest exponent and summed exactly in
+// int64 on the integer pipes (53 bits placed at bits 59..7, so six terms
+// cannot overflow and only bits below 2^(emax-59) are dropped), then the
+// int64 sum is converted, scaled by a power of two and added once.  That
+// is at least as accurate as adding the elements one by one in FP64.
+// Chunks holding an infinity or NaN take the plain FP64 path, so IEEE
+// propagation is the reference's.
+template <int D>
+struct SumF64Aligned : SumNaive<double> {
+  static constexpr bool CHUNKED = true;
+  static __device__ __forceinline__ void add_chunk(double& a, const Vec16<double>* v) {
+    constexpr int M = 8 - D;  // elements taken by the integer path
+    double xs[8];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      xs[2 * j] = v[j].v[0];
+      xs[2 * j + 1] = v[j].v[1];
+    }
+    uint64_t b[M];
+    int e[M];
+    int emax = 1;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      b[i] = uint64_t(__double_as_longlong(xs[D + i]));
+      e[i] = int(uint32_t(b[i] >> 52) & 0x7ffu);
+      emax = max(emax, e[i]);
+    }
+    if (emax == 0x7ff) {  // infinity or NaN in the chunk
+#pragma unroll
+      for (int i = 0; i < 8; ++i) a += xs[i];
+      return;
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i) a += xs[i];
+    long long s = 0;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      const uint64_t mant = (b[i] & 0x000fffffffffffffull) | (e[i] ? (1ull << 52) : 0ull);
+      const int sh = min(emax - max(e[i], 1), 63);  // subnormals sit at exponent 1
+      const long long t = (long long)((mant << 7) >> sh);
+      s += ((long long)b[i] < 0) ? -t : t;
+    }
+    // value = s * 2^(emax - 1075 - 7); a power of two is exact to multiply
+    a += (emax >= 60) ? double(s) * __longlong_as_double((long long)(emax - 59) << 52)
+                      : scalbn(double(s), emax - 1082);
+  }
 };
 
 template <class T>
@@ -292,6 +344,12 @@ struct BitOp {
   static __device__ void store(OutPtrs o, Part p) { *static_cast<T*>(o.val) = p; }
 };
 
+// Ops that sum a whole chunk of a thread's full-vector loads at once.
+template <class Op, class = void>
+struct IsChunked : std::false_type {};
+template <class Op>
+struct IsChunked<Op, typename std::enable_if<Op::CHUNKED>::type> : std::true_type {};
+
 // Fixed-shape block reduction: butterfly inside each warp, then warp 0
 // combines the warp results in warp order.  Result valid in thread 0.
 template <class X, class F>
@@ -337,26 +395,47 @@ reduce_kernel(const typename Op::T* __restrict__ x, const typename Op::T* __rest
         vx[j] = ld_vec(x + e);
         if (DOT) vy[j] = ld_vec(y + e);
       }
+      if constexpr (!DOT && IsChunked<Op>::value) {
+        Op::add_chunk(acc, vx);
+      } else {
 #pragma unroll
-      for (int j = 0; j < C::NV; ++j) {
-        const size_t e = base + (size_t(j) * RBLOCK + tid) * C::VN;
+        for (int j = 0; j < C::NV; ++j) {
+          const size_t e = base + (size_t(j) * RBLOCK + tid) * C::VN;
 #pragma unroll
-        for (int k = 0; k < C::VN; ++k) {
-          if (DOT) Op::add2(acc, vx[j].v[k], vy[j].v[k]);
-          else Op::add(acc, vx[j].v[k], int64_t(e + k));
+          for (int k = 0; k < C::VN; ++k) {
+            if (DOT) Op::add2(acc, vx[j].v[k], vy[j].v[k]);
+            else Op::add(acc, vx[j].v[k], int64_t(e + k));
+          }
         }
       }
     } else {
-      // Same element-to-thread mapping as the vector path, so the
+      // Same element-to-thread mapping (and, for chunked ops, the same
+      // chunk arithmetic on full chunks) as the vector path, so the
       // deterministic mode does not depend on pointer alignment.
+      bool chunk_done = false;
+      if constexpr (!DOT && IsChunked<Op>::value) {
+        if (base + C::SIZE <= n) {
+          Vec16<T> vx[C::NV];
 #pragma unroll
-      for (int j = 0; j < C::NV; ++j) {
-        const size_t e = base + (size_t(j) * RBLOCK + tid) * C::VN;
+          for (int j = 0; j < C::NV; ++j) {
+            const size_t e = base + (size_t(j) * RBLOCK + tid) * C::VN;
 #pragma unroll
-        for (int k = 0; k < C::VN; ++k) {
-          if (e + k < n) {
-            if (DOT) Op::add2(acc, x[e + k], y[e + k]);
-            else Op::add(acc, x[e + k], int64_t(e + k));
+            for (int k = 0; k < C::VN; ++k) vx[j].v[k] = x[e + k];
+          }
+          Op::add_chunk(acc, vx);
+          chunk_done = true;
+        }
+      }
+      if (!chunk_done) {
+#pragma unroll
+        for (int j = 0; j < C::NV; ++j) {
+          const size_t e = base + (size_t(j) * RBLOCK + tid) * C::VN;
+#pragma unroll
+          for (int k = 0; k < C::VN; ++k) {
+            if (e + k < n) {
+              if (DOT) Op::add2(acc, x[e + k], y[e + k]);
+              else Op::add(acc, x[e + k], int64_t(e + k));
+            }
           }
         }
       }
@@ -446,8 +525,10 @@ int sum_fp(const char* name, const T* x, const T* y, size_t n, int mode, double*
     return y ? run_reduce<Op, true>(name, x, y, n, det, o, stream)
              : run_reduce<Op, false>(name, x, y, n, det, o, stream);
   }
+  using Naive = typename std::conditional<std::is_same<T, double>::value, SumF64Aligned<F64_DADD>,
+                                          SumNaive<T>>::type;
   return y ? run_reduce<SumNaive<T>, true>(name, x, y, n, det, o, stream)
-           : run_reduce<SumNaive<T>, false>(name, x, y, n, det, o, stream);
+           : run_reduce<Naive, false>(name, x, y, n, det, o, stream);
 }
 
 template <class T>

@@ -175,3 +175,36 @@ def test_compensated_f32_beats_naive_f64_ill_conditioned(prims, orc):
     err_n64 = abs((naive64 - ex) - exlo)
     assert err_comp <= max(err_n64, 0.5 * np.spacing(abs(ex))), (cond, err_comp, err_n64)
     assert err_comp <= 1e-6 * abs(ex)
+
+
+def test_f64_sum_special_values_and_exponent_spread(prims, orc):
+    """The FP64 sum adds most of each 8-element chunk as exponent-aligned
+    int64 mantissas: infinities and NaN must propagate as in FP64, and
+    subnormals, wide exponent spreads and huge values must stay within the
+    naive bound of the exact sum."""
+    rng = np.random.default_rng(31)
+    n = 8 * 256 * 64 + 13                      # whole chunks plus a ragged tail
+    for pos in (0, 7, 4103, n - 1):
+        x = rng.uniform(-1, 1, n)
+        x[pos] = np.inf
+        assert prims.reduce_sum(to_dev(x)) == np.inf
+        x[pos + 1 if pos + 1 < n else pos - 1] = -np.inf
+        assert math.isnan(prims.reduce_sum(to_dev(x)))
+        x = rng.uniform(-1, 1, n)
+        x[pos] = np.nan
+        assert math.isnan(prims.reduce_sum(to_dev(x)))
+    cases = {
+        "subnormal": rng.uniform(-1, 1, n) * 1e-310,
+        "spread": rng.uniform(-1, 1, n) * 10.0 ** rng.integers(-300, 300, n),
+        "huge": rng.uniform(0.5, 1, n) * 1e300,
+        "tiny_and_one": np.where(rng.random(n) < 0.5, 1.0, 1e-20) * rng.choice([-1, 1], n),
+        "zeros": np.where(rng.random(n) < 0.5, 0.0, -0.0),
+    }
+    for name, x in cases.items():
+        hi, _ = orc.exact_sum(x)
+        a = float(np.abs(x).sum()) if name != "huge" else float(np.abs(x / 1e300).sum()) * 1e300
+        got = prims.reduce_sum(to_dev(x))
+        assert abs(got - hi) <= naive_bound(n, U64, a) + 1e-300, name
+        got_det = prims.reduce_sum(to_dev(x), mode=2)
+        assert abs(got_det - hi) <= naive_bound(n, U64, a) + 1e-300, name
+    assert prims.reduce_sum(to_dev(np.full(n, 1e308))) == np.inf    # overflows as in FP64
