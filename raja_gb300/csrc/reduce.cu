@@ -30,6 +30,7 @@
 #include <climits>
 #include <mutex>
 #include <type_traits>
+#include <utility>
 
 #include "b200_internal.cuh"
 
@@ -109,7 +110,8 @@ struct SumNaive {
 template <int D>
 struct SumF64Aligned : SumNaive<double> {
   static constexpr bool CHUNKED = true;
-  static __device__ __forceinline__ void add_chunk(double& a, const Vec16<double>* v) {
+  static __device__ __forceinline__ void add_chunk(double& a, const Vec16<double>* v, size_t,
+                                                   size_t) {
     constexpr int M = 8 - D;  // elements taken by the integer path
     double xs[8];
 #pragma unroll
@@ -284,45 +286,84 @@ struct Extremum {
 
 // FP64 Min / Max with location, compared on the integer pipes.  GB300's
 // FP64 unit retires far fewer DSETP than the HBM stream delivers doubles,
-// so each double is mapped to an order-preserving int64 key instead:
-// -0.0 is folded onto +0.0 (they compare equal, as with operator<), the
-// bits of negative values except the sign are inverted, and NaNs are
-// skipped (operator< never selects them).  The original bits are kept for
-// the result; ties resolve to the lowest index as above.
+// so each double is mapped to an order-preserving int64 key instead: the
+// bits of negative values except the sign are inverted and one is added,
+// which also folds -0.0 onto +0.0 (they compare equal, as with
+// operator<).  NaNs are skipped (operator< never selects them): a chunk is
+// tested once for an all-ones exponent, and only chunks holding an
+// infinity or a NaN take the per-element test.  Per thread only the key
+// and the index are carried; the value's own bits are read back from the
+// input at the index once, when the thread's result becomes a partial, so
+// -0.0 keeps its sign.  Ties resolve to the lowest index as above.
 template <bool MIN, bool WITH_LOC>
 struct ExtremumF64 {
   using T = double;
+  static constexpr bool CHUNKED = true;
   struct Acc {
+    long long key;
+    long long i;
+  };
+  struct Part {
     long long key;
     long long i;
     long long bits;
   };
-  using Part = Acc;
   static __device__ __forceinline__ long long key_of(long long b) {
-    const long long c = ((b << 1) == 0) ? 0ll : b;
-    return c ^ ((c >> 63) & 0x7fffffffffffffffll);
+    const long long s = b >> 63;  // 0 or -1
+    return (b ^ (s & 0x7fffffffffffffffll)) - s;
   }
   static __device__ __forceinline__ bool is_nan(long long b) {
     return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
   }
-  static __device__ Acc identity() {
-    const long long b = __double_as_longlong(MIN ? DBL_MAX : -DBL_MAX);
-    return {key_of(b), -1, b};
+  static __device__ __forceinline__ long long ident_bits() {
+    return __double_as_longlong(MIN ? DBL_MAX : -DBL_MAX);
   }
+  static __device__ __forceinline__ bool better(long long k, long long than) {
+    return MIN ? (k < than) : (than < k);
+  }
+  static __device__ Acc identity() { return {key_of(ident_bits()), -1}; }
   static __device__ void add(Acc& a, double v, int64_t i) {
     const long long b = __double_as_longlong(v);
     if (is_nan(b)) return;
     const long long k = key_of(b);
-    if (MIN ? (k < a.key) : (a.key < k)) { a.key = k; a.i = i; a.bits = b; }
+    if (better(k, a.key)) { a.key = k; a.i = i; }
   }
   static __device__ void add2(Acc&, double, double) {}
-  static __device__ Acc merge(Acc a, Acc b) {
-    if ((MIN ? (b.key < a.key) : (a.key < b.key)) || (b.key == a.key && b.i < a.i)) return b;
+  // Elements (j, k) of the chunk sit at e0 + j * stride + k, in index order.
+  static __device__ __forceinline__ void add_chunk(Acc& a, const Vec16<double>* v, size_t e0,
+                                                   size_t stride) {
+    long long b[8];
+    bool special = false;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        b[2 * j + k] = __double_as_longlong(v[j].v[k]);
+        special |= (uint32_t(b[2 * j + k] >> 32) & 0x7ff00000u) == 0x7ff00000u;
+      }
+    if (special) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int k = 0; k < 2; ++k) add(a, v[j].v[k], int64_t(e0 + j * stride + k));
+      return;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const long long key = key_of(b[2 * j + k]);
+        if (better(key, a.key)) { a.key = key; a.i = (long long)(e0 + j * stride + k); }
+      }
+  }
+  static __device__ Part to_part_x(Acc a, const double* x) {
+    return {a.key, a.i, a.i >= 0 ? __double_as_longlong(x[a.i]) : ident_bits()};
+  }
+  static __device__ Part part_identity() { return {key_of(ident_bits()), -1, ident_bits()}; }
+  static __device__ Part merge_part(Part a, Part b) {
+    if (better(b.key, a.key) || (b.key == a.key && b.i < a.i)) return b;
     return a;
   }
-  static __device__ Part to_part(Acc a) { return a; }
-  static __device__ Part part_identity() { return identity(); }
-  static __device__ Part merge_part(Part a, Part b) { return merge(a, b); }
   static __device__ void store(OutPtrs o, Part p) {
     *static_cast<double*>(o.val) = __longlong_as_double(p.bits);
     if (WITH_LOC) *o.idx = p.i;
@@ -344,7 +385,20 @@ struct BitOp {
   static __device__ void store(OutPtrs o, Part p) { *static_cast<T*>(o.val) = p; }
 };
 
-// Ops that sum a whole chunk of a thread's full-vector loads at once.
+// Ops whose thread result reads the input back to become a partial.
+template <class Op, class = void>
+struct HasToPartX : std::false_type {};
+template <class Op>
+struct HasToPartX<Op, decltype(void(Op::to_part_x(std::declval<typename Op::Acc>(),
+                                                  std::declval<const typename Op::T*>())))>
+    : std::true_type {};
+template <class Op>
+__device__ __forceinline__ typename Op::Part part_of(typename Op::Acc a, const typename Op::T* x) {
+  if constexpr (HasToPartX<Op>::value) return Op::to_part_x(a, x);
+  else return Op::to_part(a);
+}
+
+// Ops that reduce a whole chunk of a thread's full-vector loads at once.
 template <class Op, class = void>
 struct IsChunked : std::false_type {};
 template <class Op>
@@ -396,7 +450,7 @@ reduce_kernel(const typename Op::T* __restrict__ x, const typename Op::T* __rest
         if (DOT) vy[j] = ld_vec(y + e);
       }
       if constexpr (!DOT && IsChunked<Op>::value) {
-        Op::add_chunk(acc, vx);
+        Op::add_chunk(acc, vx, base + size_t(tid) * C::VN, size_t(RBLOCK) * C::VN);
       } else {
 #pragma unroll
         for (int j = 0; j < C::NV; ++j) {
@@ -422,7 +476,7 @@ reduce_kernel(const typename Op::T* __restrict__ x, const typename Op::T* __rest
 #pragma unroll
             for (int k = 0; k < C::VN; ++k) vx[j].v[k] = x[e + k];
           }
-          Op::add_chunk(acc, vx);
+          Op::add_chunk(acc, vx, base + size_t(tid) * C::VN, size_t(RBLOCK) * C::VN);
           chunk_done = true;
         }
       }
@@ -441,13 +495,13 @@ reduce_kernel(const typename Op::T* __restrict__ x, const typename Op::T* __rest
       }
     }
     if (det) {
-      const Part r = block_reduce(Op::to_part(acc), Op::part_identity(),
+      const Part r = block_reduce(part_of<Op>(acc, x), Op::part_identity(),
                                   [](Part a, Part b) { return Op::merge_part(a, b); }, sh_part);
       if (tid == 0) parts[c] = r;
     }
   }
   if (!det) {
-    const Part r = block_reduce(Op::to_part(acc), Op::part_identity(),
+    const Part r = block_reduce(part_of<Op>(acc, x), Op::part_identity(),
                                 [](Part a, Part b) { return Op::merge_part(a, b); }, sh_part);
     if (tid == 0) parts[blockIdx.x] = r;
   }
