@@ -118,3 +118,59 @@ def test_copy_forms_leave_input(prims, orc):
     np.testing.assert_array_equal(to_host(ok), ek)
     np.testing.assert_array_equal(to_host(ov), ev)
     np.testing.assert_array_equal(to_host(dk), kf)
+
+
+# Mid-size sorts (2^21 + 4097 keys, 293 tiles) with special float values and
+# skewed key distributions.
+NG = (1 << 21) + 4097
+
+
+@pytest.mark.parametrize("kt", [np.uint32, np.int32, np.float32, np.uint64, np.int64, np.float64])
+def test_sort_2m_keys_bit_exact(prims, orc, kt):
+    for seed, dup in ((1, False), (2, True)):
+        x = _keys(kt, NG, seed, dup)
+        if np.dtype(kt).kind == "f":
+            # (NaN has no place under operator<; +-0.0 compare equal, so
+            # floats are compared as values)
+            x[:6] = [0.0, -0.0, np.inf, -np.inf, 1e-40, -1e-40]
+        for desc in (False, True):
+            d = to_dev(x)
+            prims.sort(d, descending=desc)
+            np.testing.assert_array_equal(to_host(d), orc.sort(x, descending=desc),
+                                          err_msg=f"{kt} dup={dup} desc={desc}")
+
+
+def test_sort_2m_out_of_place_and_offsets(prims, orc):
+    import torch
+    x = _keys(np.uint64, NG + 3, 5)
+    src = to_dev(x)
+    out = torch.empty_like(src)
+    prims.sort_copy(src, out)
+    np.testing.assert_array_equal(to_host(out), orc.sort(x))
+    np.testing.assert_array_equal(to_host(src), x)            # input untouched
+    # a view 1 element into the buffer (unaligned for the 16-byte loads)
+    y = _keys(np.uint32, NG + 1, 6)
+    d = to_dev(np.concatenate([np.zeros(1, np.uint32), y]))
+    prims.sort(d[1:])
+    np.testing.assert_array_equal(to_host(d)[1:], orc.sort(y))
+
+
+@pytest.mark.parametrize("case", ["one_group", "many_big", "mixed"])
+def test_sort_2m_skewed_keys(prims, orc, case):
+    """Skewed keys: most keys share their top bits (one digit value per
+    pass carries most of a tile), or a large share does."""
+    rng = np.random.default_rng(9)
+    n = NG
+    if case == "one_group":      # 64-bit keys below 2^40: every key in group 0
+        x = rng.integers(0, 1 << 40, n, dtype=np.uint64)
+    elif case == "many_big":     # 32-bit keys over 100 top-16 values
+        x = (rng.integers(0, 100, n, dtype=np.uint32) << np.uint32(16)) | \
+            rng.integers(0, 1 << 16, n, dtype=np.uint32)
+    else:                        # 40 % in one group, the rest spread
+        x = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+        sel = rng.random(n) < 0.4
+        x[sel] = (np.uint32(0x1234) << np.uint32(16)) | (x[sel] & np.uint32(0xFFFF))
+    for desc in (False, True):
+        d = to_dev(x)
+        prims.sort(d, descending=desc)
+        np.testing.assert_array_equal(to_host(d), orc.sort(x, descending=desc), err_msg=case)
