@@ -70,7 +70,13 @@ hist_kernel(const int32_t* __restrict__ x, size_t n, uint32_t nbins, uint32_t sb
     count_one(sh, R, rsel, v, sbins, gcounts, v < nbins);
   }
   __syncthreads();
-  for (uint32_t b = tid; b < sbins; b += HBLOCK) {
+  // flush: every block starts at its own offset in the bin range (warp
+  // aligned), so the blocks, which finish together, do not all hit the
+  // same global counters at the same time
+  const uint32_t off = uint32_t((size_t(blockIdx.x) * sbins / gridDim.x) & ~size_t(31));
+  for (uint32_t k = tid; k < sbins; k += HBLOCK) {
+    uint32_t b = k + off;
+    if (b >= sbins) b -= sbins;
     uint32_t c = 0;
     for (int r = 0; r < R; ++r) c += sh[size_t(b) * R + r];
     if (c) atomicAdd(gcounts + b, (unsigned long long)c);
