@@ -316,6 +316,71 @@ int b200_histogram_i32(const int32_t* x, size_t n, int32_t nbins, uint64_t* coun
                        b200_stream_t stream);
 
 /* ======================================================================
+ * Binned reductions -- MultiReduce{Sum,Min,Max,BitOr,BitAnd}<policy, T>
+ * (pattern/multi_reduce.hpp:68-190; combine rule per bin in
+ * pattern/detail/multi_reduce.hpp:172-402 and
+ * policy/sequential/multi_reduce.hpp:135; CUDA atomics in
+ * policy/cuda/multi_reduce.hpp:80-690).
+ * out[b] = op(out[b], vals[i]) for every i with bins[i] == b; bins outside
+ * [0, nbins) are skipped.  `out` holds the initial values (the MultiReduce
+ * constructor's init) and is combined into.  min keeps `if (v < val) val =
+ * v`, max `if (val < v) val = v`: NaN values never enter.  Integer and bit
+ * results are exact; floating-point sums depend on the atomic order.
+ * ====================================================================== */
+int b200_multi_reduce_sum_i32(const int32_t* bins, const int32_t* vals, size_t n, int32_t nbins,
+                              int32_t* out, b200_stream_t stream);
+int b200_multi_reduce_sum_i64(const int32_t* bins, const int64_t* vals, size_t n, int32_t nbins,
+                              int64_t* out, b200_stream_t stream);
+int b200_multi_reduce_sum_u32(const int32_t* bins, const uint32_t* vals, size_t n, int32_t nbins,
+                              uint32_t* out, b200_stream_t stream);
+int b200_multi_reduce_sum_u64(const int32_t* bins, const uint64_t* vals, size_t n, int32_t nbins,
+                              uint64_t* out, b200_stream_t stream);
+int b200_multi_reduce_sum_f32(const int32_t* bins, const float* vals, size_t n, int32_t nbins,
+                              float* out, b200_stream_t stream);
+int b200_multi_reduce_sum_f64(const int32_t* bins, const double* vals, size_t n, int32_t nbins,
+                              double* out, b200_stream_t stream);
+int b200_multi_reduce_min_i32(const int32_t* bins, const int32_t* vals, size_t n, int32_t nbins,
+                              int32_t* out, b200_stream_t stream);
+int b200_multi_reduce_min_i64(const int32_t* bins, const int64_t* vals, size_t n, int32_t nbins,
+                              int64_t* out, b200_stream_t stream);
+int b200_multi_reduce_min_u32(const int32_t* bins, const uint32_t* vals, size_t n, int32_t nbins,
+                              uint32_t* out, b200_stream_t stream);
+int b200_multi_reduce_min_u64(const int32_t* bins, const uint64_t* vals, size_t n, int32_t nbins,
+                              uint64_t* out, b200_stream_t stream);
+int b200_multi_reduce_min_f32(const int32_t* bins, const float* vals, size_t n, int32_t nbins,
+                              float* out, b200_stream_t stream);
+int b200_multi_reduce_min_f64(const int32_t* bins, const double* vals, size_t n, int32_t nbins,
+                              double* out, b200_stream_t stream);
+int b200_multi_reduce_max_i32(const int32_t* bins, const int32_t* vals, size_t n, int32_t nbins,
+                              int32_t* out, b200_stream_t stream);
+int b200_multi_reduce_max_i64(const int32_t* bins, const int64_t* vals, size_t n, int32_t nbins,
+                              int64_t* out, b200_stream_t stream);
+int b200_multi_reduce_max_u32(const int32_t* bins, const uint32_t* vals, size_t n, int32_t nbins,
+                              uint32_t* out, b200_stream_t stream);
+int b200_multi_reduce_max_u64(const int32_t* bins, const uint64_t* vals, size_t n, int32_t nbins,
+                              uint64_t* out, b200_stream_t stream);
+int b200_multi_reduce_max_f32(const int32_t* bins, const float* vals, size_t n, int32_t nbins,
+                              float* out, b200_stream_t stream);
+int b200_multi_reduce_max_f64(const int32_t* bins, const double* vals, size_t n, int32_t nbins,
+                              double* out, b200_stream_t stream);
+int b200_multi_reduce_bitor_i32(const int32_t* bins, const int32_t* vals, size_t n, int32_t nbins,
+                                int32_t* out, b200_stream_t stream);
+int b200_multi_reduce_bitor_i64(const int32_t* bins, const int64_t* vals, size_t n, int32_t nbins,
+                                int64_t* out, b200_stream_t stream);
+int b200_multi_reduce_bitor_u32(const int32_t* bins, const uint32_t* vals, size_t n, int32_t nbins,
+                                uint32_t* out, b200_stream_t stream);
+int b200_multi_reduce_bitor_u64(const int32_t* bins, const uint64_t* vals, size_t n, int32_t nbins,
+                                uint64_t* out, b200_stream_t stream);
+int b200_multi_reduce_bitand_i32(const int32_t* bins, const int32_t* vals, size_t n, int32_t nbins,
+                                 int32_t* out, b200_stream_t stream);
+int b200_multi_reduce_bitand_i64(const int32_t* bins, const int64_t* vals, size_t n, int32_t nbins,
+                                 int64_t* out, b200_stream_t stream);
+int b200_multi_reduce_bitand_u32(const int32_t* bins, const uint32_t* vals, size_t n, int32_t nbins,
+                                 uint32_t* out, b200_stream_t stream);
+int b200_multi_reduce_bitand_u64(const int32_t* bins, const uint64_t* vals, size_t n, int32_t nbins,
+                                 uint64_t* out, b200_stream_t stream);
+
+/* ======================================================================
  * Batched loops -- WorkPool/WorkGroup with many uneven loops
  * (pattern/WorkGroup.hpp:207-530; CUDA runners
  * policy/cuda/WorkGroup/WorkRunner.hpp:38-407, which launch once per loop

@@ -201,6 +201,18 @@ def histogram(x: np.ndarray, nbins: int, parallel: bool = False) -> np.ndarray:
     return counts
 
 
+def multi_reduce(op: str, bins: np.ndarray, vals: np.ndarray, out: np.ndarray) -> np.ndarray:
+    """MultiReduce{Sum,Min,Max,BitOr,BitAnd}: out[b] combined in place with
+    every vals[i] whose bins[i] == b, in index order (seq rule)."""
+    bins = np.ascontiguousarray(bins, dtype=np.int32)
+    vals = np.ascontiguousarray(vals)
+    assert out.dtype == vals.dtype and out.flags.c_contiguous
+    _fn(f"orc_multi_reduce_{op}_{_SFX[vals.dtype]}", None,
+        [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p])(
+        _p(bins), _p(vals), vals.size, out.size, _p(out))
+    return out
+
+
 # ------------------------------------------------------ exact arithmetic
 def exact_sum(x: np.ndarray) -> tuple[float, float]:
     """Exact sum as (hi, lo): hi = round(sum), lo = round(sum - hi)."""

@@ -581,6 +581,46 @@ void orc_omp_histogram_i32(const int32_t* x, int64_t n, int32_t nbins, uint64_t*
   }
 }
 
+// ---- MultiReduce{Sum,Min,Max,BitOr,BitAnd}: out[b] starts as given and
+// every element with bins[i] == b is combined in index order with the
+// reduce op's rule (policy/sequential/multi_reduce.hpp:135 combine ->
+// MultiReduceOp{}(m_data[bin], val)): sum val += v, min `if (v < val) val =
+// v`, max `if (val < v) val = v` (equal values keep the first, NaN never
+// enters), bit ops |= and &=.  Bins outside [0, nbins) are skipped.
+extern "C++" {
+template <class T, class F>
+static void multi_reduce(const int32_t* bins, const T* vals, int64_t n, int32_t nbins, T* out,
+                         F op) {
+  for (int64_t i = 0; i < n; ++i)
+    if (bins[i] >= 0 && bins[i] < nbins) op(out[bins[i]], vals[i]);
+}
+}
+#define ORC_MR(OP, SUF, T, BODY)                                                                 \
+  void orc_multi_reduce_##OP##_##SUF(const int32_t* bins, const T* vals, int64_t n,             \
+                                     int32_t nbins, T* out) {                                   \
+    multi_reduce<T>(bins, vals, n, nbins, out, [](T& val, T v) { BODY; });                      \
+  }
+#define ORC_MR_ALL(SUF, T)                                                                       \
+  ORC_MR(sum, SUF, T, val = T(val + v))                                                          \
+  ORC_MR(min, SUF, T, if (v < val) val = v)                                                      \
+  ORC_MR(max, SUF, T, if (val < v) val = v)
+ORC_MR_ALL(i32, int32_t)
+ORC_MR_ALL(i64, int64_t)
+ORC_MR_ALL(u32, uint32_t)
+ORC_MR_ALL(u64, uint64_t)
+ORC_MR_ALL(f32, float)
+ORC_MR_ALL(f64, double)
+ORC_MR(bitor, i32, int32_t, val |= v)
+ORC_MR(bitor, i64, int64_t, val |= v)
+ORC_MR(bitor, u32, uint32_t, val |= v)
+ORC_MR(bitor, u64, uint64_t, val |= v)
+ORC_MR(bitand, i32, int32_t, val &= v)
+ORC_MR(bitand, i64, int64_t, val &= v)
+ORC_MR(bitand, u32, uint32_t, val &= v)
+ORC_MR(bitand, u64, uint64_t, val &= v)
+#undef ORC_MR_ALL
+#undef ORC_MR
+
 // ---- exact sums: (hi, lo) with hi = round(sum), lo = round(sum - hi)
 void orc_exact_sum_f64(const double* x, int64_t n, double* hi, double* lo) {
   LongAcc a;

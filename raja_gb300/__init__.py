@@ -356,6 +356,63 @@ def histogram(x, nbins: int, counts=None, *, sync=True, stream=None):
     return counts
 
 
+_MR_OPS = {"sum": "sum", "plus": "sum", "min": "min", "minimum": "min", "max": "max",
+           "maximum": "max", "bitor": "bitor", "bit_or": "bitor", "bitand": "bitand",
+           "bit_and": "bitand"}
+
+
+def multi_reduce(op: str, bins, vals, nbins: int | None = None, *, out=None, init=None,
+                 sync=True, stream=None):
+    """RAJA::MultiReduce{Sum,Min,Max,BitOr,BitAnd}: out[b] = op(out[b], vals[i])
+    for every i with bins[i] == b (bins outside [0, nbins) skipped).
+
+    `out` (combined into) or a fresh tensor of nbins elements set to `init`
+    (default: the op's identity, as MultiReduce(num_bins) starts) is returned.
+    """
+    torch = _torch()
+    _check_dev(bins, vals)
+    if bins.dtype != torch.int32:
+        raise TypeError("multi_reduce takes int32 bins")
+    if bins.numel() != vals.numel():
+        raise ValueError("bins and vals differ in length")
+    kind = _MR_OPS[op]
+    sfx = _suffix(vals)
+    if kind.startswith("bit") and sfx[0] == "f":
+        raise TypeError("bit multi reductions take integer values")
+    if out is None:
+        if nbins is None:
+            raise ValueError("nbins or out is required")
+        bits = 8 * vals.element_size()
+        if init is None:   # the op's identity
+            if kind in ("sum", "bitor"):
+                init = 0
+            elif kind == "bitand":
+                init = -1
+            elif sfx[0] == "f":
+                fi = torch.finfo(vals.dtype)
+                init = fi.max if kind == "min" else -fi.max
+            elif sfx[0] == "u":
+                init = (1 << bits) - 1 if kind == "min" else 0
+            else:
+                info = torch.iinfo(vals.dtype)
+                init = info.max if kind == "min" else info.min
+        if sfx[0] == "u":   # unsigned values are held in a signed view
+            init = int(init) & ((1 << bits) - 1)
+            if init >= 1 << (bits - 1):
+                init -= 1 << bits
+            base = torch.int32 if bits == 32 else torch.int64
+            out = torch.full((int(nbins),), init, dtype=base, device=vals.device).view(vals.dtype)
+        else:
+            out = torch.full((int(nbins),), init, dtype=vals.dtype, device=vals.device)
+    elif out.dtype != vals.dtype:
+        raise TypeError("out and vals differ in dtype")
+    _check_dev(out)
+    _lib.call(f"b200_multi_reduce_{kind}_{sfx}", bins.data_ptr(), vals.data_ptr(), vals.numel(),
+              int(out.numel()), out.data_ptr(), _stream(stream))
+    _finish(sync, stream)
+    return out
+
+
 # ----------------------------------------------------------- instrumentation
 def prof_enable(on: bool = True) -> None:
     _lib.call("b200_prof_enable", int(bool(on)))

@@ -78,6 +78,9 @@ def _signatures() -> dict[str, tuple]:
         sig[f"b200_sort_pairs_{kv}"] = (_I, [_P, _P, _SZ, _I, _P])
     for kv in ("f32_i32", "u32_i32"):
         sig[f"b200_sort_pairs_copy_{kv}"] = (_I, [_P, _P, _P, _P, _SZ, _I, _P])
+    for t in ("i32", "i64", "u32", "u64", "f32", "f64"):
+        for op in ("sum", "min", "max") + (("bitor", "bitand") if t[0] != "f" else ()):
+            sig[f"b200_multi_reduce_{op}_{t}"] = (_I, [_P, _P, _SZ, C.c_int32, _P, _P])
     sig.update({
         "b200_batch_plan_create": (_I, [_P, _I, _P]),
         "b200_batch_plan_destroy": (_I, [_P]),

@@ -264,3 +264,27 @@ def test_omp_paths_agree_with_seq(orc):
     orc.axpy(2.5, xf, y, parallel=True)
     orc.axpy(2.5, xf, y2, parallel=False)
     np.testing.assert_array_equal(y, y2)
+
+
+def test_oracle_multi_reduce_vs_numpy_at():
+    """The oracle's MultiReduce restatement against numpy's unbuffered
+    ufunc.at (integers: order does not matter), out-of-range bins skipped."""
+    import oracle
+    rng = np.random.default_rng(41)
+    n, nbins = 20000, 37
+    bins = rng.integers(-2, nbins + 2, n).astype(np.int32)
+    ok = (bins >= 0) & (bins < nbins)
+    for dt in (np.int32, np.int64, np.uint32, np.uint64):
+        vals = rng.integers(0, 1 << 30, n).astype(dt)
+        for op, uf, init in (("sum", np.add, 0), ("min", np.minimum, np.iinfo(dt).max),
+                             ("max", np.maximum, np.iinfo(dt).min), ("bitor", np.bitwise_or, 0),
+                             ("bitand", np.bitwise_and, np.iinfo(dt).max)):
+            ref = np.full(nbins, init, dtype=dt)
+            uf.at(ref, bins[ok], vals[ok])
+            got = oracle.multi_reduce(op, bins, vals, np.full(nbins, init, dtype=dt))
+            np.testing.assert_array_equal(got, ref, err_msg=f"{op} {dt}")
+    # floats: min keeps the first of equal values and skips NaN
+    v = np.array([2.0, np.nan, 1.0, 1.0, -0.0, 0.0])
+    b = np.array([0, 0, 0, 1, 2, 2], np.int32)
+    got = oracle.multi_reduce("min", b, v, np.full(3, np.inf))
+    assert got[0] == 1.0 and got[1] == 1.0 and np.signbit(got[2])
