@@ -26,7 +26,9 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -46,6 +48,8 @@ struct b200_exec {
 template <int BLOCK = 256>
 using b200_exec_async = b200_exec<BLOCK, true>;
 struct b200_reduce {};
+struct b200_multi_reduce {};
+struct b200_atomic {};
 template <int BLOCK = 256, bool Async = false>
 struct b200_work {};
 struct b200_synchronize {};
@@ -166,7 +170,7 @@ __device__ inline void grid_combine(const DevSlot<T>& s, T v, Merge merge) {
   if (threadIdx.x == 0) {
     s.partials[blockIdx.x] = v;
     __threadfence();
-    last = atomicAdd(s.ticket, 1u) == gridDim.x - 1;
+    last = ::atomicAdd(s.ticket, 1u) == gridDim.x - 1;
   }
   __syncthreads();
   if (!last) return;
@@ -1036,5 +1040,279 @@ inline void synchronize<b200_synchronize>() {
   b200::check_cuda(cudaDeviceSynchronize(), "synchronize");
   b200::wait();
 }
+
+// --------------------------------------------------------------- atomics
+// b200_atomic: CUDA atomics in device code (min / max of floating types by
+// compare-and-swap with the `<` rule), GCC __atomic builtins on the host.
+// Each returns the value before the operation, as the reference's
+// cuda_atomic does (policy/cuda/atomic.hpp).
+namespace b200 {
+namespace atom {
+template <typename T>
+using Word = std::conditional_t<sizeof(T) == 4, unsigned int, unsigned long long>;
+template <typename T>
+RAJA_HOST_DEVICE inline Word<T> bits(T v) {
+  Word<T> w;
+  memcpy(&w, &v, sizeof(T));
+  return w;
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T from_bits(Word<T> w) {
+  T v;
+  memcpy(&v, &w, sizeof(T));
+  return v;
+}
+// generic read-modify-write by compare-and-swap: new value = f(old)
+template <typename T, typename F>
+RAJA_HOST_DEVICE inline T rmw(T* acc, F f) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte atomics");
+  Word<T>* p = reinterpret_cast<Word<T>*>(acc);
+#ifdef __CUDA_ARCH__
+  Word<T> cur = *reinterpret_cast<volatile Word<T>*>(p);
+  while (true) {
+    const Word<T> nv = bits<T>(f(from_bits<T>(cur)));
+    const Word<T> prev = ::atomicCAS(p, cur, nv);
+    if (prev == cur) return from_bits<T>(cur);
+    cur = prev;
+  }
+#else
+  Word<T> cur = __atomic_load_n(p, __ATOMIC_RELAXED);
+  while (true) {
+    const Word<T> nv = bits<T>(f(from_bits<T>(cur)));
+    if (__atomic_compare_exchange_n(p, &cur, nv, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED))
+      return from_bits<T>(cur);
+  }
+#endif
+}
+}  // namespace atom
+}  // namespace b200
+
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicLoad(b200_atomic, T* acc) {
+  return b200::atom::rmw(acc, [](T o) { return o; });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline void atomicStore(b200_atomic, T* acc, T v) {
+  b200::atom::rmw(acc, [v](T) { return v; });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicAdd(b200_atomic, T* acc, T v) {
+#ifdef __CUDA_ARCH__
+  if constexpr (std::is_same<T, int>::value || std::is_same<T, unsigned>::value ||
+                std::is_same<T, unsigned long long>::value || std::is_same<T, float>::value ||
+                std::is_same<T, double>::value)
+    return ::atomicAdd(acc, v);
+#endif
+  return b200::atom::rmw(acc, [v](T o) { return T(o + v); });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicSub(b200_atomic, T* acc, T v) {
+  return b200::atom::rmw(acc, [v](T o) { return T(o - v); });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicMin(b200_atomic, T* acc, T v) {
+#ifdef __CUDA_ARCH__
+  if constexpr (std::is_same<T, int>::value || std::is_same<T, unsigned>::value ||
+                std::is_same<T, long long>::value || std::is_same<T, unsigned long long>::value)
+    return ::atomicMin(acc, v);
+#endif
+  return b200::atom::rmw(acc, [v](T o) { return v < o ? v : o; });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicMax(b200_atomic, T* acc, T v) {
+#ifdef __CUDA_ARCH__
+  if constexpr (std::is_same<T, int>::value || std::is_same<T, unsigned>::value ||
+                std::is_same<T, long long>::value || std::is_same<T, unsigned long long>::value)
+    return ::atomicMax(acc, v);
+#endif
+  return b200::atom::rmw(acc, [v](T o) { return o < v ? v : o; });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicInc(b200_atomic, T* acc) {
+  return atomicAdd(b200_atomic{}, acc, T(1));
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicInc(b200_atomic, T* acc, T val) {
+  return b200::atom::rmw(acc, [val](T o) { return val <= o ? T(0) : T(o + T(1)); });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicDec(b200_atomic, T* acc) {
+  return atomicSub(b200_atomic{}, acc, T(1));
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicDec(b200_atomic, T* acc, T val) {
+  return b200::atom::rmw(acc, [val](T o) { return (o == T(0) || val < o) ? val : T(o - T(1)); });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicAnd(b200_atomic, T* acc, T v) {
+  return b200::atom::rmw(acc, [v](T o) { return T(o & v); });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicOr(b200_atomic, T* acc, T v) {
+  return b200::atom::rmw(acc, [v](T o) { return T(o | v); });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicXor(b200_atomic, T* acc, T v) {
+  return b200::atom::rmw(acc, [v](T o) { return T(o ^ v); });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicExchange(b200_atomic, T* acc, T v) {
+  return b200::atom::rmw(acc, [v](T) { return v; });
+}
+template <typename T>
+RAJA_HOST_DEVICE inline T atomicCAS(b200_atomic, T* acc, T compare, T v) {
+#ifdef __CUDA_ARCH__
+  using W = b200::atom::Word<T>;
+  return b200::atom::from_bits<T>(::atomicCAS(reinterpret_cast<W*>(acc), b200::atom::bits(compare),
+                                              b200::atom::bits(v)));
+#else
+  auto w = b200::atom::bits(compare);
+  __atomic_compare_exchange_n(reinterpret_cast<b200::atom::Word<T>*>(acc), &w,
+                              b200::atom::bits(v), false, __ATOMIC_RELAXED, __ATOMIC_RELAXED);
+  return b200::atom::from_bits<T>(w);
+#endif
+}
+
+// ---------------------------------------------------------- multi reduce
+// MultiReduce{Sum,Min,Max,BitOr,BitAnd}<b200_multi_reduce, T>: the bins
+// live in device memory, initialised to the op's identity; device code
+// combines into them with b200_atomic operations (the reference's
+// cuda_multi_reduce_atomic global path, policy/cuda/multi_reduce.hpp:
+// 208-470); get() waits for the b200 stream, reads them back and folds
+// them into the host-side init values.  Copies share the bins.  For binned
+// reductions over arrays, the library's b200_multi_reduce_* entry points
+// privatize the bins in shared memory.
+namespace b200 {
+namespace detail {
+template <typename T, typename Op>
+class DevMultiReduce {
+ public:
+  using value_type = T;
+  DevMultiReduce(size_t num_bins, T init) { setup(std::vector<T>(num_bins, init)); }
+  explicit DevMultiReduce(size_t num_bins) : DevMultiReduce(num_bins, Op::ident()) {}
+  template <typename Container, typename = decltype(std::declval<const Container&>().begin())>
+  explicit DevMultiReduce(const Container& c) {
+    setup(std::vector<T>(c.begin(), c.end()));
+  }
+  // copies (the loop body's capture, on the host and on the device) share
+  // the bins and own nothing
+  RAJA_HOST_DEVICE DevMultiReduce(const DevMultiReduce& o)
+      : st_(o.st_), dev_(o.dev_), n_(o.n_), owner_(false) {}
+  DevMultiReduce& operator=(const DevMultiReduce&) = delete;
+  RAJA_HOST_DEVICE ~DevMultiReduce() {
+#if !defined(__CUDA_ARCH__)
+    release();
+#endif
+  }
+  size_t size() const { return n_; }
+  T get(size_t bin) const {
+    sync();
+    return st_->host.at(bin);
+  }
+  template <typename Container>
+  void get_all(Container& c) const {
+    sync();
+    size_t b = 0;
+    for (auto& v : c) v = st_->host[b++];
+  }
+  void reset() { reset(n_, Op::ident()); }
+  void reset(size_t num_bins, T init = Op::ident()) {
+    release();
+    setup(std::vector<T>(num_bins, init));
+  }
+  RAJA_HOST_DEVICE void combine(size_t bin, T v) const { Op::atomic(dev_ + bin, v); }
+
+ private:
+  struct State {
+    std::vector<T> init, host;
+    T* dev = nullptr;
+  };
+  void setup(std::vector<T> init) {
+    n_ = init.size();
+    st_ = new State();
+    owner_ = true;
+    check_cuda(cudaMalloc(&st_->dev, std::max<size_t>(n_, 1) * sizeof(T)), "multi reduce bins");
+    dev_ = st_->dev;
+    std::vector<T> id(n_, Op::ident());
+    check_cuda(cudaMemcpy(dev_, id.data(), n_ * sizeof(T), cudaMemcpyHostToDevice), "multi reduce bins");
+    st_->host = init;
+    st_->init = std::move(init);
+  }
+  void release() {
+    if (owner_ && st_) {
+      cudaFree(st_->dev);
+      delete st_;
+    }
+    st_ = nullptr;
+    owner_ = false;
+  }
+  void sync() const {
+    wait();
+    std::vector<T> d(n_);
+    check_cuda(cudaMemcpy(d.data(), dev_, n_ * sizeof(T), cudaMemcpyDeviceToHost), "multi reduce get");
+    for (size_t b = 0; b < n_; ++b) {
+      T v = st_->init[b];
+      Op::fold(v, d[b]);
+      st_->host[b] = v;
+    }
+  }
+  State* st_ = nullptr;
+  T* dev_ = nullptr;
+  size_t n_ = 0;
+  bool owner_ = false;
+};
+
+template <typename T> struct DMrSum {
+  static T ident() { return T(0); }
+  RAJA_HOST_DEVICE static void atomic(T* p, T v) { atomicAdd(b200_atomic{}, p, v); }
+  static void fold(T& a, T v) { a += v; }
+};
+template <typename T> struct DMrMin {
+  static T ident() { return operators::limits<T>::max(); }
+  RAJA_HOST_DEVICE static void atomic(T* p, T v) { atomicMin(b200_atomic{}, p, v); }
+  static void fold(T& a, T v) { if (v < a) a = v; }
+};
+template <typename T> struct DMrMax {
+  static T ident() { return operators::limits<T>::min(); }
+  RAJA_HOST_DEVICE static void atomic(T* p, T v) { atomicMax(b200_atomic{}, p, v); }
+  static void fold(T& a, T v) { if (a < v) a = v; }
+};
+template <typename T> struct DMrOr {
+  static T ident() { return T(0); }
+  RAJA_HOST_DEVICE static void atomic(T* p, T v) { atomicOr(b200_atomic{}, p, v); }
+  static void fold(T& a, T v) { a |= v; }
+};
+template <typename T> struct DMrAnd {
+  static T ident() { return T(~T(0)); }
+  RAJA_HOST_DEVICE static void atomic(T* p, T v) { atomicAnd(b200_atomic{}, p, v); }
+  static void fold(T& a, T v) { a &= v; }
+};
+}  // namespace detail
+}  // namespace b200
+
+#define RAJA_B200_MULTI_REDUCER(CLS, OPK, METHOD)                                               \
+  template <typename T>                                                                         \
+  class CLS<b200_multi_reduce, T> : public b200::detail::DevMultiReduce<T, b200::detail::OPK<T>> { \
+    using B = b200::detail::DevMultiReduce<T, b200::detail::OPK<T>>;                            \
+                                                                                                \
+   public:                                                                                      \
+    using B::B;                                                                                 \
+    struct reference {                                                                          \
+      const B* mr;                                                                              \
+      size_t bin;                                                                               \
+      RAJA_HOST_DEVICE const reference& METHOD(T v) const {                                     \
+        mr->combine(bin, v);                                                                    \
+        return *this;                                                                           \
+      }                                                                                         \
+      T get() const { return mr->get(bin); }                                                    \
+    };                                                                                          \
+    RAJA_HOST_DEVICE reference operator[](size_t bin) const { return reference{this, bin}; }    \
+  };
+RAJA_B200_MULTI_REDUCER(MultiReduceSum, DMrSum, operator+=)
+RAJA_B200_MULTI_REDUCER(MultiReduceMin, DMrMin, min)
+RAJA_B200_MULTI_REDUCER(MultiReduceMax, DMrMax, max)
+RAJA_B200_MULTI_REDUCER(MultiReduceBitOr, DMrOr, operator|=)
+RAJA_B200_MULTI_REDUCER(MultiReduceBitAnd, DMrAnd, operator&=)
+#undef RAJA_B200_MULTI_REDUCER
 
 }  // namespace RAJA

@@ -180,6 +180,8 @@ struct seq_exec {};
 struct omp_parallel_for_exec {};
 struct seq_reduce {};
 struct omp_reduce {};
+struct seq_multi_reduce {};
+struct seq_atomic {};
 
 namespace expt {
 // ---- ValLoc / ValOp / KernelName (pattern/params/params_base.hpp:10-253)
@@ -413,6 +415,154 @@ class HostCombinable {
 RAJA_COMPAT_HOST_REDUCERS(seq_reduce)
 RAJA_COMPAT_HOST_REDUCERS(omp_reduce)
 #undef RAJA_COMPAT_HOST_REDUCERS
+
+// ---------------------------------------------------------- multi reduce
+// MultiReduce{Sum,Min,Max,BitOr,BitAnd}<POL, T> (pattern/multi_reduce.hpp:
+// 68-190, pattern/detail/multi_reduce.hpp:60-402): num_bins values, each
+// starting at init; mr[bin] += v / .min(v) / .max(v) / |= v / &= v combine
+// with the op's rule (min: `if (v < val) val = v`, max: `if (val < v) val =
+// v`); get(bin), get_all(container), reset(), size().  Copies (the loop
+// body's capture) combine into the same bins.
+template <typename POL, typename T> class MultiReduceSum;
+template <typename POL, typename T> class MultiReduceMin;
+template <typename POL, typename T> class MultiReduceMax;
+template <typename POL, typename T> class MultiReduceBitOr;
+template <typename POL, typename T> class MultiReduceBitAnd;
+
+namespace detail {
+template <typename T> struct MrSum { static T ident() { return T(0); } void operator()(T& a, T v) const { a += v; } };
+template <typename T> struct MrMin { static T ident() { return operators::limits<T>::max(); } void operator()(T& a, T v) const { if (v < a) a = v; } };
+template <typename T> struct MrMax { static T ident() { return operators::limits<T>::min(); } void operator()(T& a, T v) const { if (a < v) a = v; } };
+template <typename T> struct MrOr { static T ident() { return T(0); } void operator()(T& a, T v) const { a |= v; } };
+template <typename T> struct MrAnd { static T ident() { return T(~T(0)); } void operator()(T& a, T v) const { a &= v; } };
+
+template <typename T, typename Op>
+class HostMultiReduce {
+ public:
+  using value_type = T;
+  HostMultiReduce(size_t num_bins, T init) : data_(std::make_shared<std::vector<T>>(num_bins, init)) {}
+  explicit HostMultiReduce(size_t num_bins) : HostMultiReduce(num_bins, Op::ident()) {}
+  template <typename Container, typename = decltype(std::declval<const Container&>().begin())>
+  explicit HostMultiReduce(const Container& c)
+      : data_(std::make_shared<std::vector<T>>(c.begin(), c.end())) {}
+  size_t size() const { return data_->size(); }
+  T get(size_t bin) const { return (*data_)[bin]; }
+  template <typename Container>
+  void get_all(Container& c) const {
+    size_t b = 0;
+    for (auto& v : c) v = get(b++);
+  }
+  void reset() { std::fill(data_->begin(), data_->end(), Op::ident()); }
+  void reset(size_t num_bins, T init = Op::ident()) { data_->assign(num_bins, init); }
+  void combine(size_t bin, T v) const { Op{}((*data_)[bin], v); }
+
+ private:
+  std::shared_ptr<std::vector<T>> data_;
+};
+}  // namespace detail
+
+#define RAJA_COMPAT_HOST_MULTI_REDUCER(CLS, OPK, METHOD, RET)                                  \
+  template <typename T>                                                                        \
+  class CLS<seq_multi_reduce, T> : public detail::HostMultiReduce<T, detail::OPK<T>> {           \
+    using B = detail::HostMultiReduce<T, detail::OPK<T>>;                                      \
+                                                                                               \
+   public:                                                                                     \
+    using B::B;                                                                                \
+    struct reference {                                                                         \
+      const B* mr;                                                                             \
+      size_t bin;                                                                              \
+      RET METHOD(T v) const { mr->combine(bin, v); return *this; }                              \
+      T get() const { return mr->get(bin); }                                                   \
+    };                                                                                         \
+    reference operator[](size_t bin) const { return reference{this, bin}; }                    \
+  };
+RAJA_COMPAT_HOST_MULTI_REDUCER(MultiReduceSum, MrSum, operator+=, const reference&)
+RAJA_COMPAT_HOST_MULTI_REDUCER(MultiReduceMin, MrMin, min, const reference&)
+RAJA_COMPAT_HOST_MULTI_REDUCER(MultiReduceMax, MrMax, max, const reference&)
+RAJA_COMPAT_HOST_MULTI_REDUCER(MultiReduceBitOr, MrOr, operator|=, const reference&)
+RAJA_COMPAT_HOST_MULTI_REDUCER(MultiReduceBitAnd, MrAnd, operator&=, const reference&)
+#undef RAJA_COMPAT_HOST_MULTI_REDUCER
+
+// --------------------------------------------------------------- atomics
+// RAJA::atomicX<Policy>(acc, ...) dispatches to atomicX(Policy{}, acc, ...)
+// (pattern/atomic.hpp:90-286); seq_atomic is plain read-modify-write
+// (policy/sequential/atomic.hpp:37-170).  Each returns the value before the
+// operation.
+template <typename T> RAJA_HOST_DEVICE T atomicLoad(seq_atomic, T* acc) { return *acc; }
+template <typename T> RAJA_HOST_DEVICE void atomicStore(seq_atomic, T* acc, T v) { *acc = v; }
+template <typename T> RAJA_HOST_DEVICE T atomicAdd(seq_atomic, T* acc, T v) { T o = *acc; *acc = o + v; return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicSub(seq_atomic, T* acc, T v) { T o = *acc; *acc = o - v; return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicMin(seq_atomic, T* acc, T v) { T o = *acc; if (v < o) *acc = v; return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicMax(seq_atomic, T* acc, T v) { T o = *acc; if (o < v) *acc = v; return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicInc(seq_atomic, T* acc) { T o = *acc; *acc = o + T(1); return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicInc(seq_atomic, T* acc, T val) { T o = *acc; *acc = val <= o ? T(0) : o + T(1); return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicDec(seq_atomic, T* acc) { T o = *acc; *acc = o - T(1); return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicDec(seq_atomic, T* acc, T val) { T o = *acc; *acc = (o == T(0) || val < o) ? val : o - T(1); return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicAnd(seq_atomic, T* acc, T v) { T o = *acc; *acc = o & v; return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicOr(seq_atomic, T* acc, T v) { T o = *acc; *acc = o | v; return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicXor(seq_atomic, T* acc, T v) { T o = *acc; *acc = o ^ v; return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicExchange(seq_atomic, T* acc, T v) { T o = *acc; *acc = v; return o; }
+template <typename T> RAJA_HOST_DEVICE T atomicCAS(seq_atomic, T* acc, T compare, T v) { T o = *acc; if (o == compare) *acc = v; return o; }
+
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicLoad(T* acc) { return atomicLoad(Policy{}, acc); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE void atomicStore(T* acc, T v) { atomicStore(Policy{}, acc, v); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicAdd(T* acc, T v) { return atomicAdd(Policy{}, acc, v); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicSub(T* acc, T v) { return atomicSub(Policy{}, acc, v); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicMin(T* acc, T v) { return atomicMin(Policy{}, acc, v); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicMax(T* acc, T v) { return atomicMax(Policy{}, acc, v); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicInc(T* acc) { return atomicInc(Policy{}, acc); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicInc(T* acc, T val) { return atomicInc(Policy{}, acc, val); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicDec(T* acc) { return atomicDec(Policy{}, acc); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicDec(T* acc, T val) { return atomicDec(Policy{}, acc, val); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicAnd(T* acc, T v) { return atomicAnd(Policy{}, acc, v); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicOr(T* acc, T v) { return atomicOr(Policy{}, acc, v); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicXor(T* acc, T v) { return atomicXor(Policy{}, acc, v); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicExchange(T* acc, T v) { return atomicExchange(Policy{}, acc, v); }
+template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicCAS(T* acc, T compare, T v) { return atomicCAS(Policy{}, acc, compare, v); }
+
+// AtomicRef<T, Policy> (pattern/atomic.hpp:299-): a pointer with atomic
+// member operations; fetch_* return the previous value, the operators the
+// new one.
+template <typename T, typename Policy = seq_atomic>
+class AtomicRef {
+ public:
+  using value_type = T;
+  RAJA_HOST_DEVICE explicit AtomicRef(T* p) : p_(p) {}
+  RAJA_HOST_DEVICE T* getPointer() const { return p_; }
+  RAJA_HOST_DEVICE void store(T v) const { atomicStore(Policy{}, p_, v); }
+  RAJA_HOST_DEVICE T load() const { return atomicLoad(Policy{}, p_); }
+  RAJA_HOST_DEVICE operator T() const { return load(); }
+  RAJA_HOST_DEVICE T operator=(T v) const { store(v); return v; }
+  RAJA_HOST_DEVICE T exchange(T v) const { return atomicExchange(Policy{}, p_, v); }
+  RAJA_HOST_DEVICE T CAS(T compare, T v) const { return atomicCAS(Policy{}, p_, compare, v); }
+  RAJA_HOST_DEVICE bool compare_exchange_strong(T& expect, T v) const {
+    const T o = atomicCAS(Policy{}, p_, expect, v);
+    const bool ok = o == expect;
+    expect = o;
+    return ok;
+  }
+  RAJA_HOST_DEVICE T fetch_add(T v) const { return atomicAdd(Policy{}, p_, v); }
+  RAJA_HOST_DEVICE T fetch_sub(T v) const { return atomicSub(Policy{}, p_, v); }
+  RAJA_HOST_DEVICE T fetch_min(T v) const { return atomicMin(Policy{}, p_, v); }
+  RAJA_HOST_DEVICE T fetch_max(T v) const { return atomicMax(Policy{}, p_, v); }
+  RAJA_HOST_DEVICE T fetch_and(T v) const { return atomicAnd(Policy{}, p_, v); }
+  RAJA_HOST_DEVICE T fetch_or(T v) const { return atomicOr(Policy{}, p_, v); }
+  RAJA_HOST_DEVICE T fetch_xor(T v) const { return atomicXor(Policy{}, p_, v); }
+  RAJA_HOST_DEVICE T operator++() const { return atomicInc(Policy{}, p_) + T(1); }
+  RAJA_HOST_DEVICE T operator++(int) const { return atomicInc(Policy{}, p_); }
+  RAJA_HOST_DEVICE T operator--() const { return atomicDec(Policy{}, p_) - T(1); }
+  RAJA_HOST_DEVICE T operator--(int) const { return atomicDec(Policy{}, p_); }
+  RAJA_HOST_DEVICE T operator+=(T v) const { return atomicAdd(Policy{}, p_, v) + v; }
+  RAJA_HOST_DEVICE T operator-=(T v) const { return atomicSub(Policy{}, p_, v) - v; }
+  RAJA_HOST_DEVICE T operator&=(T v) const { return atomicAnd(Policy{}, p_, v) & v; }
+  RAJA_HOST_DEVICE T operator|=(T v) const { return atomicOr(Policy{}, p_, v) | v; }
+  RAJA_HOST_DEVICE T operator^=(T v) const { return atomicXor(Policy{}, p_, v) ^ v; }
+  RAJA_HOST_DEVICE T min(T v) const { const T o = atomicMin(Policy{}, p_, v); return v < o ? v : o; }
+  RAJA_HOST_DEVICE T max(T v) const { const T o = atomicMax(Policy{}, p_, v); return o < v ? v : o; }
+
+ private:
+  T* p_;
+};
 
 // ---------------------------------------------------------------- forall
 // Host implementations (policy/sequential/forall.hpp:58-102,

@@ -366,7 +366,92 @@ void workgroup_case(const char* tag) {
   cudaFree(r);
 }
 
+// MultiReduce on b200 against seq, and b200 atomics in device code
+void test_multi_reduce_and_atomics() {
+  const Index_type n = 200003;
+  const int nb = 37;
+  int* bins = nullptr;
+  double* vals = nullptr;
+  cudaMallocManaged(&bins, n * sizeof(int));
+  cudaMallocManaged(&vals, n * sizeof(double));
+  std::mt19937 rng(17);
+  for (Index_type i = 0; i < n; ++i) {
+    bins[i] = int(rng() % nb);
+    vals[i] = double(int(rng() % 2001) - 1000) / 8.0;  // exact sums
+  }
+  using exec = RAJA::b200_exec<256>;
+  RAJA::MultiReduceSum<RAJA::b200_multi_reduce, double> dsum(nb, 1.5);
+  RAJA::MultiReduceMin<RAJA::b200_multi_reduce, double> dmin(nb);
+  RAJA::MultiReduceMax<RAJA::b200_multi_reduce, double> dmax(nb);
+  RAJA::MultiReduceBitOr<RAJA::b200_multi_reduce, long long> dor(nb);
+  RAJA::MultiReduceBitAnd<RAJA::b200_multi_reduce, unsigned> dand(nb);
+  RAJA::forall<exec>(RAJA::RangeSegment(0, n), [=] RAJA_DEVICE(Index_type i) {
+    const int b = bins[i];
+    dsum[b] += vals[i];
+    dmin[b].min(vals[i]);
+    dmax[b].max(vals[i]);
+    dor[b] |= (long long)(i & 0xff) << (b % 8);
+    dand[b] &= ~(1u << (i % 13));
+  });
+  RAJA::MultiReduceSum<RAJA::seq_multi_reduce, double> hsum(nb, 1.5);
+  RAJA::MultiReduceMin<RAJA::seq_multi_reduce, double> hmin(nb);
+  RAJA::MultiReduceMax<RAJA::seq_multi_reduce, double> hmax(nb);
+  RAJA::MultiReduceBitOr<RAJA::seq_multi_reduce, long long> hor(nb);
+  RAJA::MultiReduceBitAnd<RAJA::seq_multi_reduce, unsigned> hand(nb);
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, n), [=](Index_type i) {
+    const int b = bins[i];
+    hsum[b] += vals[i];
+    hmin[b].min(vals[i]);
+    hmax[b].max(vals[i]);
+    hor[b] |= (long long)(i & 0xff) << (b % 8);
+    hand[b] &= ~(1u << (i % 13));
+  });
+  bool ok = true;
+  for (int b = 0; b < nb; ++b)
+    ok = ok && dsum.get(b) == hsum.get(b) && dmin.get(b) == hmin.get(b) &&
+         dmax[b].get() == hmax[b].get() && dor.get(b) == hor.get(b) && dand.get(b) == hand.get(b);
+  CHECK("multi_reduce_b200_vs_seq", ok);
+
+  // device atomics: a counter, a bounded wrap-around counter, a max by
+  // compare-and-swap (doubles), and an AtomicRef
+  unsigned long long* cnt = nullptr;
+  unsigned* wrap = nullptr;
+  double* dmx = nullptr;
+  int* ref = nullptr;
+  cudaMallocManaged(&cnt, sizeof(*cnt));
+  cudaMallocManaged(&wrap, sizeof(*wrap));
+  cudaMallocManaged(&dmx, sizeof(*dmx));
+  cudaMallocManaged(&ref, sizeof(*ref));
+  *cnt = 0;
+  *wrap = 0;
+  *dmx = -1e300;
+  *ref = 0;
+  RAJA::forall<exec>(RAJA::RangeSegment(0, n), [=] RAJA_DEVICE(Index_type i) {
+    RAJA::atomicAdd<RAJA::b200_atomic>(cnt, 1ull);
+    RAJA::atomicInc<RAJA::b200_atomic>(wrap, 999u);
+    RAJA::atomicMax<RAJA::b200_atomic>(dmx, vals[i]);
+    RAJA::AtomicRef<int, RAJA::b200_atomic> r(ref);
+    r += int(i % 3);
+  });
+  RAJA::b200::wait();
+  double hmx = -1e300;
+  long long hr = 0;
+  for (Index_type i = 0; i < n; ++i) {
+    hmx = hmx < vals[i] ? vals[i] : hmx;
+    hr += i % 3;
+  }
+  CHECK("atomics_b200", *cnt == (unsigned long long)n && *wrap == unsigned(n % 1000) &&
+                            *dmx == hmx && *ref == int(hr));
+  cudaFree(cnt);
+  cudaFree(wrap);
+  cudaFree(dmx);
+  cudaFree(ref);
+  cudaFree(bins);
+  cudaFree(vals);
+}
+
 int main() {
+  test_multi_reduce_and_atomics();
   test_reducers();
   test_forall_and_params();
   test_scans();

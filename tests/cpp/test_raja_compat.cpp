@@ -103,6 +103,59 @@ int main() {
   bool ok = true;
   for (int i = 0; i < 100; ++i) ok = ok && w[i] == ((i >= 10 && i < 60) ? i + 5 : 0);
   CHECK("workgroup_seq", ok);
+
+  // MultiReduce (seq): bins combined in index order with each op's rule
+  {
+    const int nb = 5;
+    RAJA::MultiReduceSum<RAJA::seq_multi_reduce, int> msum(nb);
+    RAJA::MultiReduceMin<RAJA::seq_multi_reduce, int> mmin(nb, 100);
+    RAJA::MultiReduceMax<RAJA::seq_multi_reduce, int> mmax(nb);
+    RAJA::MultiReduceBitOr<RAJA::seq_multi_reduce, int> mor(nb);
+    RAJA::MultiReduceBitAnd<RAJA::seq_multi_reduce, int> mand(nb);
+    std::vector<int> sum(nb, 0), mn(nb, 100), mx(nb, std::numeric_limits<int>::lowest()),
+        bo(nb, 0), ba(nb, -1);
+    RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 50), [=](Index_type i) {
+      const int b = int(i % nb), v = int((i * 37) % 23) - 7;
+      msum[b] += v;
+      mmin[b].min(v);
+      mmax[b].max(v);
+      mor[b] |= v;
+      mand[b] &= v;
+    });
+    for (int i = 0; i < 50; ++i) {
+      const int b = i % nb, v = (i * 37) % 23 - 7;
+      sum[b] += v;
+      mn[b] = v < mn[b] ? v : mn[b];
+      mx[b] = mx[b] < v ? v : mx[b];
+      bo[b] |= v;
+      ba[b] &= v;
+    }
+    bool okm = msum.size() == size_t(nb);
+    std::vector<int> all(nb);
+    msum.get_all(all);
+    for (int b = 0; b < nb; ++b)
+      okm = okm && all[b] == sum[b] && mmin.get(b) == mn[b] && mmax[b].get() == mx[b] &&
+            mor.get(b) == bo[b] && mand.get(b) == ba[b];
+    CHECK("multi_reduce_seq", okm);
+    msum.reset();
+    CHECK("multi_reduce_reset", msum.get(0) == 0 && msum.get(4) == 0);
+  }
+
+  // atomics (seq) and AtomicRef, including the bounded inc / dec rules
+  {
+    unsigned u = 3;
+    bool oka = RAJA::atomicInc<RAJA::seq_atomic>(&u, 3u) == 3u && u == 0u;
+    oka = oka && RAJA::atomicDec<RAJA::seq_atomic>(&u, 5u) == 0u && u == 5u;
+    oka = oka && RAJA::atomicCAS<RAJA::seq_atomic>(&u, 5u, 9u) == 5u && u == 9u;
+    oka = oka && RAJA::atomicCAS<RAJA::seq_atomic>(&u, 5u, 1u) == 9u && u == 9u;
+    int x = 10;
+    RAJA::AtomicRef<int, RAJA::seq_atomic> r(&x);
+    oka = oka && (r += 5) == 15 && r.fetch_sub(3) == 15 && r.load() == 12;
+    oka = oka && r.min(4) == 4 && r.max(20) == 20 && (r++) == 20 && x == 21;
+    oka = oka && RAJA::atomicExchange<RAJA::seq_atomic>(&x, 7) == 21 && x == 7;
+    oka = oka && RAJA::atomicXor<RAJA::seq_atomic>(&x, 5) == 7 && x == 2;
+    CHECK("atomics_seq", oka);
+  }
   printf("%d failures\n", g_fail);
   return g_fail;
 }
