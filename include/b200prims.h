@@ -82,7 +82,9 @@ const char* b200_last_error_string(void);
 
 /* Wait for `stream`, then read and clear the device status word of the
  * current device.  Returns B200_ERR_TIMEOUT if a bounded device wait (scan
- * or sort look-back) gave up since the last check.  Replaces
+ * or sort look-back) gave up since the last check.  The word is read in
+ * the stream's own order: work queued on other streams is not waited for
+ * (the word itself is shared by all streams of the device).  Replaces
  * cuda::synchronize / res.wait() (MemUtils_CUDA.hpp:205-247). */
 int b200_stream_synchronize(b200_stream_t stream);
 

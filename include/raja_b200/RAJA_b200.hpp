@@ -16,6 +16,9 @@
 //                                   one persistent launch
 //                                   (policy/cuda/WorkGroup/WorkRunner.hpp)
 //   RAJA::b200_synchronize          RAJA::synchronize<> target
+//   RAJA::resources::Cuda           stream resource for the b200 policies:
+//                                   forall / scan / sort / WorkGroup::run
+//                                   take it first and return EventProxy
 //
 // Include after a RAJA front-end (the real RAJA or raja_compat).  Lambda
 // loop bodies stay templated and are compiled into the application with
@@ -27,8 +30,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -542,6 +547,160 @@ inline void finish(const char* what) {
 }  // namespace detail
 }  // namespace b200
 
+// ------------------------------------------------------------ resources
+// resources::Cuda for the b200 policies: a CUDA stream on one device, with
+// the interface of camp's Cuda resource as RAJA uses it (allocate /
+// deallocate / memcpy / memset in stream order, get_event, wait, wait_for;
+// test/unit/resource/tests/*.hpp).  A default-constructed resource takes
+// the next stream of a per-device pool of 16 (blocking streams, so work on
+// the legacy default stream still orders with them); get_default() is the
+// thread's current b200 stream (the legacy default stream unless changed);
+// CudaFromStream wraps a stream the caller owns.  While a call runs on a
+// resource, the b200 policies launch on its stream.
+namespace resources {
+
+class CudaEvent {
+ public:
+  explicit CudaEvent(cudaStream_t s) {
+    cudaEvent_t e = nullptr;
+    b200::check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+    ev_ = std::shared_ptr<CUevent_st>(e, [](cudaEvent_t x) { cudaEventDestroy(x); });
+    b200::check_cuda(cudaEventRecord(e, s), "cudaEventRecord");
+  }
+  bool check() const { return cudaEventQuery(ev_.get()) == cudaSuccess; }
+  void wait() const { b200::check_cuda(cudaEventSynchronize(ev_.get()), "cudaEventSynchronize"); }
+  cudaEvent_t getCudaEvent_t() const { return ev_.get(); }
+
+ private:
+  std::shared_ptr<CUevent_st> ev_;
+};
+
+class Cuda {
+ public:
+  static constexpr int kPoolSize = 16;
+  Cuda() : Cuda(-1) {}
+  explicit Cuda(int group, int device = current_device()) : dev_(device) {
+    static std::atomic<unsigned> next{0};
+    const unsigned k = group >= 0 ? unsigned(group) % kPoolSize : next.fetch_add(1) % kPoolSize;
+    s_ = pool(device)[k];
+  }
+  static Cuda get_default() { return CudaFromStream(b200::stream()); }
+  static Cuda CudaFromStream(cudaStream_t s, int device = current_device()) {
+    Cuda c(s, device);
+    return c;
+  }
+  cudaStream_t get_stream() const { return s_; }
+  int get_device() const { return dev_; }
+  Platform get_platform() const { return Platform::cuda; }
+
+  template <typename T>
+  T* allocate(size_t n, MemoryAccess ma = MemoryAccess::Device) {
+    void* p = nullptr;
+    const size_t bytes = n * sizeof(T);
+    if (ma == MemoryAccess::Pinned)
+      b200::check_cuda(cudaMallocHost(&p, bytes), "resources::Cuda::allocate (pinned)");
+    else if (ma == MemoryAccess::Managed)
+      b200::check_cuda(cudaMallocManaged(&p, bytes), "resources::Cuda::allocate (managed)");
+    else
+      b200::check_cuda(cudaMalloc(&p, bytes), "resources::Cuda::allocate");
+    return static_cast<T*>(p);
+  }
+  void* calloc(size_t bytes, MemoryAccess ma = MemoryAccess::Device) {
+    void* p = allocate<char>(bytes, ma);
+    memset(p, 0, bytes);
+    return p;
+  }
+  // The kind of memory is read from the pointer, so a pointer from any of
+  // the three kinds of allocate() is freed correctly.
+  void deallocate(void* p, MemoryAccess = MemoryAccess::Unknown) {
+    if (!p) return;
+    cudaPointerAttributes a{};
+    b200::check_cuda(cudaPointerGetAttributes(&a, p), "resources::Cuda::deallocate");
+    if (a.type == cudaMemoryTypeHost)
+      b200::check_cuda(cudaFreeHost(p), "cudaFreeHost");
+    else
+      b200::check_cuda(cudaFree(p), "cudaFree");
+  }
+  void memcpy(void* dst, const void* src, size_t bytes) {
+    if (bytes) b200::check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s_), "resources::Cuda::memcpy");
+  }
+  void memset(void* p, int v, size_t bytes) {
+    if (bytes) b200::check_cuda(cudaMemsetAsync(p, v, bytes, s_), "resources::Cuda::memset");
+  }
+  CudaEvent get_event() { return CudaEvent(s_); }
+  Event get_event_erased() { return Event{CudaEvent(s_)}; }
+  // Waits for the stream and reports device-side errors of the b200
+  // kernels (bounded waits that gave up), like res.wait() + cudaErrchk.
+  void wait() { b200::check(b200_stream_synchronize(s_), "resources::Cuda::wait"); }
+  // A CUDA event becomes a stream dependency; any other event is waited
+  // for on the host.
+  void wait_for(Event* e) {
+    if (const CudaEvent* ce = e->try_get<CudaEvent>())
+      b200::check_cuda(cudaStreamWaitEvent(s_, ce->getCudaEvent_t(), 0), "cudaStreamWaitEvent");
+    else
+      e->wait();
+  }
+  friend bool operator==(const Cuda& a, const Cuda& b) { return a.s_ == b.s_ && a.dev_ == b.dev_; }
+  friend bool operator!=(const Cuda& a, const Cuda& b) { return !(a == b); }
+
+ private:
+  Cuda(cudaStream_t s, int device) : s_(s), dev_(device) {}
+  static int current_device() {
+    int d = 0;
+    b200::check_cuda(cudaGetDevice(&d), "cudaGetDevice");
+    return d;
+  }
+  static const cudaStream_t* pool(int device) {
+    static std::mutex mu;
+    static std::vector<std::vector<cudaStream_t>> pools;
+    std::lock_guard<std::mutex> lock(mu);
+    if (int(pools.size()) <= device) pools.resize(device + 1);
+    auto& p = pools[device];
+    if (p.empty()) {
+      int cur = 0;
+      b200::check_cuda(cudaGetDevice(&cur), "cudaGetDevice");
+      if (cur != device) b200::check_cuda(cudaSetDevice(device), "cudaSetDevice");
+      p.resize(kPoolSize);
+      for (auto& s : p) b200::check_cuda(cudaStreamCreate(&s), "cudaStreamCreate");
+      if (cur != device) b200::check_cuda(cudaSetDevice(cur), "cudaSetDevice");
+    }
+    return p.data();
+  }
+  cudaStream_t s_ = nullptr;
+  int dev_ = 0;
+};
+
+// Binding: the b200 policies read the thread's current stream; the guard
+// sets it to the resource's stream and restores the previous one.
+class StreamBinding {
+ public:
+  explicit StreamBinding(cudaStream_t s) : prev_(b200::stream()) { b200::stream() = s; }
+  StreamBinding(StreamBinding&& o) noexcept : prev_(o.prev_), active_(o.active_) { o.active_ = false; }
+  StreamBinding(const StreamBinding&) = delete;
+  StreamBinding& operator=(const StreamBinding&) = delete;
+  ~StreamBinding() {
+    if (active_) b200::stream() = prev_;
+  }
+
+ private:
+  cudaStream_t prev_;
+  bool active_ = true;
+};
+inline StreamBinding bind_resource(Cuda& r) { return StreamBinding(r.get_stream()); }
+
+template <>
+struct is_resource<Cuda> : std::true_type {};
+template <int BLOCK, bool Async>
+struct get_resource<b200_exec<BLOCK, Async>> {
+  using type = Cuda;
+};
+template <int BLOCK, bool Async>
+struct get_resource<b200_work<BLOCK, Async>> {
+  using type = Cuda;
+};
+
+}  // namespace resources
+
 template <int BLOCK, bool Async, class Body, class T>
 void forall_impl(b200_exec<BLOCK, Async>, const TypedRangeSegment<T>& r, Body&& body) {
   using B = std::decay_t<Body>;
@@ -989,8 +1148,13 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index,
       b200::check_cuda(cudaMemcpy(d + m_bodies_off, bytes.data(), bytes.size(), cudaMemcpyHostToDevice),
                        "WorkGroup bodies");
   }
-  WorkSite<policy, Index, xargs<>, Alloc> run() {
-    if (m_nloops == 0) return {};
+  using resource_type = resources::Cuda;
+  WorkSite<policy, Index, xargs<>, Alloc> run() { return run(resource_type::get_default()); }
+  // The loops run on the resource's stream (pattern/WorkGroup.hpp:357-370).
+  WorkSite<policy, Index, xargs<>, Alloc> run(resource_type r) {
+    WorkSite<policy, Index, xargs<>, Alloc> site(r);
+    if (m_nloops == 0) return site;
+    auto bound = bind_resource(r);
     cudaStream_t s = b200::stream();
     char* d = static_cast<char*>(m_dev);
     auto* loops = reinterpret_cast<const b200::detail::WgLoop*>(d + m_loops_off);
@@ -1013,7 +1177,7 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index,
     }
     b200::check_cuda(cudaGetLastError(), "WorkGroup run");
     if (!Async) b200::wait();
-    return {};
+    return site;
   }
   void clear() {}
 

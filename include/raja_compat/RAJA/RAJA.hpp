@@ -29,6 +29,8 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 #include <functional>
 #include <limits>
 #include <memory>
@@ -182,6 +184,213 @@ struct seq_reduce {};
 struct omp_reduce {};
 struct seq_multi_reduce {};
 struct seq_atomic {};
+
+// ------------------------------------------------------------ resources
+// RAJA::resources (util/resource.hpp:37-64) re-exports camp's resources
+// (the camp submodule, github.com/llnl/camp, not vendored in the reference
+// tree).  This restates the part the primitive path uses, following its
+// call sites in pattern/forall.hpp:545-627, pattern/scan.hpp:49-441,
+// pattern/sort.hpp:54-451 and the resource unit tests
+// (test/unit/resource/tests/*.hpp):
+//   - a concrete resource (Host here; back-ends add theirs) allocates,
+//     copies and sets memory in its own order, hands out events, waits
+//     for its own work (wait) or for an event (wait_for);
+//   - Resource and Event erase the concrete types; copies share the same
+//     underlying resource or event;
+//   - every forall / scan / sort returns EventProxy<Res>, which becomes an
+//     Event (recorded on the resource at that point) when converted.
+// A back-end is told which resource a call runs on through
+// bind_resource(res): the returned guard keeps the binding for the call.
+namespace resources {
+
+enum class Platform { undefined = 0, host = 1, cuda = 2 };
+enum class MemoryAccess { Unknown, Device, Pinned, Managed };
+
+struct EventProxyBase {};
+
+struct HostEvent {
+  bool check() const { return true; }
+  void wait() const {}
+};
+
+class Event {
+  struct Concept {
+    virtual ~Concept() = default;
+    virtual bool check() const = 0;
+    virtual void wait() const = 0;
+  };
+  template <typename E>
+  struct Model final : Concept {
+    explicit Model(E e) : ev(std::move(e)) {}
+    bool check() const override { return ev.check(); }
+    void wait() const override { ev.wait(); }
+    E ev;
+  };
+  std::shared_ptr<Concept> m_;
+
+ public:
+  Event() = default;  // an event that has already happened
+  template <typename E, typename std::enable_if<!std::is_same<std::decay_t<E>, Event>::value &&
+                                                    !std::is_base_of<EventProxyBase, std::decay_t<E>>::value,
+                                                int>::type = 0>
+  Event(E e) : m_(std::make_shared<Model<std::decay_t<E>>>(std::move(e))) {}
+  bool check() const { return !m_ || m_->check(); }
+  void wait() const {
+    if (m_) m_->wait();
+  }
+  template <typename E>
+  const E* try_get() const {
+    auto* m = dynamic_cast<const Model<E>*>(m_.get());
+    return m ? &m->ev : nullptr;
+  }
+  template <typename E>
+  E get() const {
+    const E* e = try_get<E>();
+    if (!e) throw std::runtime_error("resources::Event::get: the event is of another type");
+    return *e;
+  }
+};
+
+class Host {
+ public:
+  static Host get_default() { return Host{}; }
+  Platform get_platform() const { return Platform::host; }
+  template <typename T>
+  T* allocate(size_t n, MemoryAccess = MemoryAccess::Device) {
+    return static_cast<T*>(std::malloc(n * sizeof(T)));
+  }
+  void* calloc(size_t bytes, MemoryAccess = MemoryAccess::Device) { return std::calloc(1, bytes); }
+  void deallocate(void* p, MemoryAccess = MemoryAccess::Device) { std::free(p); }
+  void memcpy(void* dst, const void* src, size_t bytes) {
+    if (bytes) std::memcpy(dst, src, bytes);
+  }
+  void memset(void* p, int v, size_t bytes) {
+    if (bytes) std::memset(p, v, bytes);
+  }
+  HostEvent get_event() { return {}; }
+  Event get_event_erased() { return Event{HostEvent{}}; }
+  void wait() {}
+  void wait_for(Event* e) { e->wait(); }
+};
+
+// Host work binds nothing.
+struct NoBinding {};
+inline NoBinding bind_resource(Host&) { return {}; }
+
+class Resource {
+  struct Concept {
+    virtual ~Concept() = default;
+    virtual Platform platform() const = 0;
+    virtual void* alloc(size_t bytes, MemoryAccess ma) = 0;
+    virtual void* zalloc(size_t bytes, MemoryAccess ma) = 0;
+    virtual void dealloc(void* p, MemoryAccess ma) = 0;
+    virtual void copy(void* dst, const void* src, size_t bytes) = 0;
+    virtual void set(void* p, int v, size_t bytes) = 0;
+    virtual Event event() = 0;
+    virtual void wait() = 0;
+    virtual void wait_for(Event* e) = 0;
+    virtual std::shared_ptr<void> bind() = 0;
+  };
+  template <typename R>
+  struct Model final : Concept {
+    explicit Model(R res) : r(std::move(res)) {}
+    Platform platform() const override { return r.get_platform(); }
+    void* alloc(size_t bytes, MemoryAccess ma) override { return r.template allocate<char>(bytes, ma); }
+    void* zalloc(size_t bytes, MemoryAccess ma) override { return r.calloc(bytes, ma); }
+    void dealloc(void* p, MemoryAccess ma) override { r.deallocate(p, ma); }
+    void copy(void* dst, const void* src, size_t bytes) override { r.memcpy(dst, src, bytes); }
+    void set(void* p, int v, size_t bytes) override { r.memset(p, v, bytes); }
+    Event event() override { return r.get_event_erased(); }
+    void wait() override { r.wait(); }
+    void wait_for(Event* e) override { r.wait_for(e); }
+    std::shared_ptr<void> bind() override {
+      using G = decltype(bind_resource(r));
+      return std::make_shared<G>(bind_resource(r));
+    }
+    R r;
+  };
+  std::shared_ptr<Concept> m_;
+
+ public:
+  template <typename R, typename std::enable_if<!std::is_same<std::decay_t<R>, Resource>::value, int>::type = 0>
+  Resource(R r) : m_(std::make_shared<Model<std::decay_t<R>>>(std::move(r))) {}
+  Platform get_platform() const { return m_->platform(); }
+  template <typename T>
+  T* allocate(size_t n, MemoryAccess ma = MemoryAccess::Device) {
+    return static_cast<T*>(m_->alloc(n * sizeof(T), ma));
+  }
+  void* calloc(size_t bytes, MemoryAccess ma = MemoryAccess::Device) { return m_->zalloc(bytes, ma); }
+  void deallocate(void* p, MemoryAccess ma = MemoryAccess::Device) { m_->dealloc(p, ma); }
+  void memcpy(void* dst, const void* src, size_t bytes) { m_->copy(dst, src, bytes); }
+  void memset(void* p, int v, size_t bytes) { m_->set(p, v, bytes); }
+  Event get_event() { return m_->event(); }
+  Event get_event_erased() { return m_->event(); }
+  void wait() { m_->wait(); }
+  void wait_for(Event* e) { m_->wait_for(e); }
+  template <typename R>
+  R* try_get() {
+    auto* m = dynamic_cast<Model<R>*>(m_.get());
+    return m ? &m->r : nullptr;
+  }
+  template <typename R>
+  R get() {
+    R* r = try_get<R>();
+    if (!r) throw std::runtime_error("resources::Resource::get: the resource is of another type");
+    return *r;
+  }
+  friend std::shared_ptr<void> bind_resource(Resource& r) { return r.m_->bind(); }
+};
+
+// EventProxy<Res>: what an asynchronous call returns.  Converting it to an
+// Event (or to the resource's own event type) records an event on the
+// resource at that point; get() does the same.
+template <typename Res>
+class EventProxy : public EventProxyBase {
+  using native_event = decltype(std::declval<Res&>().get_event());
+
+ public:
+  explicit EventProxy(Res r) : r_(std::move(r)) {}
+  Event get() const { return r_.get_event_erased(); }
+  operator Event() const { return get(); }
+  template <typename E, typename std::enable_if<std::is_same<E, native_event>::value &&
+                                                    !std::is_same<E, Event>::value,
+                                                int>::type = 0>
+  operator E() const {
+    return r_.get_event();
+  }
+  Res resource() const { return r_; }
+
+ private:
+  mutable Res r_;
+};
+
+template <typename T>
+struct is_resource : std::false_type {};
+template <>
+struct is_resource<Host> : std::true_type {};
+template <>
+struct is_resource<Resource> : std::true_type {};
+
+// Resource type of an execution policy (util/resource.hpp:44-58); host
+// policies run on Host, back-ends specialise for theirs.
+template <typename Pol>
+struct get_resource {
+  using type = Host;
+};
+template <typename Pol>
+typename get_resource<Pol>::type get_default_resource() {
+  return get_resource<Pol>::type::get_default();
+}
+
+}  // namespace resources
+
+namespace detail {
+template <typename T>
+using enable_if_resource = typename std::enable_if<resources::is_resource<std::decay_t<T>>::value, int>::type;
+template <typename T>
+using enable_if_not_resource =
+    typename std::enable_if<!resources::is_resource<std::decay_t<T>>::value, int>::type;
+}  // namespace detail
 
 namespace expt {
 // ---- ValLoc / ValOp / KernelName (pattern/params/params_base.hpp:10-253)
@@ -663,12 +872,26 @@ void forall_split(Seg&& seg, Tup&& tup, std::index_sequence<I...>) {
 }
 }  // namespace detail
 
-// RAJA::forall<POLICY>(segment, [params...,] body)  (pattern/forall.hpp:545-627)
-template <typename Pol, typename Seg, typename... Args>
-void forall(Seg&& seg, Args&&... args) {
+// RAJA::forall<POLICY>([resource,] segment, [params...,] body)
+// (pattern/forall.hpp:545-627).  Without a resource the policy's default
+// resource is used.  The call runs with the resource bound and returns an
+// EventProxy on it.
+template <typename Pol, typename Res, typename Seg, typename... Args, detail::enable_if_resource<Res> = 0>
+resources::EventProxy<std::decay_t<Res>> forall(Res&& r, Seg&& seg, Args&&... args) {
   static_assert(sizeof...(Args) >= 1, "forall needs a loop body");
-  detail::forall_split<Pol>(std::forward<Seg>(seg), std::forward_as_tuple(std::forward<Args>(args)...),
-                            std::make_index_sequence<sizeof...(Args) - 1>{});
+  std::decay_t<Res> res = r;
+  {
+    auto bound = bind_resource(res);
+    (void)bound;
+    detail::forall_split<Pol>(std::forward<Seg>(seg), std::forward_as_tuple(std::forward<Args>(args)...),
+                              std::make_index_sequence<sizeof...(Args) - 1>{});
+  }
+  return resources::EventProxy<std::decay_t<Res>>(res);
+}
+template <typename Pol, typename Seg, typename... Args, detail::enable_if_not_resource<Seg> = 0>
+resources::EventProxy<typename resources::get_resource<Pol>::type> forall(Seg&& seg, Args&&... args) {
+  return forall<Pol>(resources::get_resource<Pol>::type::get_default(), std::forward<Seg>(seg),
+                     std::forward<Args>(args)...);
 }
 
 // ----------------------------------------------------------------- scans
@@ -699,28 +922,68 @@ void scan_exclusive(seq_exec, const T* b, const T* e, T* out, F f, T v) {
   }
 }
 
+// Each front-end has a form that takes the resource first
+// (pattern/scan.hpp:336-441) and returns an EventProxy on it; the form
+// without one uses the policy's default resource.
+#define RAJA_COMPAT_DEFAULT_RES(Pol) resources::get_resource<Pol>::type::get_default()
+#define RAJA_COMPAT_RES_T(Pol) resources::EventProxy<typename resources::get_resource<Pol>::type>
+
+template <typename Pol, typename Res, typename T, typename F = operators::plus<std::remove_const_t<T>>,
+          detail::enable_if_resource<Res> = 0>
+resources::EventProxy<Res> inclusive_scan(Res r, Span<T> in, Span<std::remove_const_t<T>> out, F f = F{}) {
+  auto bound = bind_resource(r);
+  (void)bound;
+  if (in.size() != 0)
+    scan_inclusive(Pol{}, static_cast<const std::remove_const_t<T>*>(in.begin()),
+                   static_cast<const std::remove_const_t<T>*>(in.end()), out.begin(), f);
+  return resources::EventProxy<Res>(r);
+}
+template <typename Pol, typename Res, typename T, typename F = operators::plus<std::remove_const_t<T>>,
+          detail::enable_if_resource<Res> = 0>
+resources::EventProxy<Res> exclusive_scan(Res r, Span<T> in, Span<std::remove_const_t<T>> out, F f = F{},
+                                          std::remove_const_t<T> v = F::identity()) {
+  auto bound = bind_resource(r);
+  (void)bound;
+  if (in.size() != 0)
+    scan_exclusive(Pol{}, static_cast<const std::remove_const_t<T>*>(in.begin()),
+                   static_cast<const std::remove_const_t<T>*>(in.end()), out.begin(), f, v);
+  return resources::EventProxy<Res>(r);
+}
+template <typename Pol, typename Res, typename T, typename F = operators::plus<T>,
+          detail::enable_if_resource<Res> = 0>
+resources::EventProxy<Res> inclusive_scan_inplace(Res r, Span<T> io, F f = F{}) {
+  auto bound = bind_resource(r);
+  (void)bound;
+  if (io.size() != 0)
+    scan_inclusive(Pol{}, static_cast<const T*>(io.begin()), static_cast<const T*>(io.end()), io.begin(), f);
+  return resources::EventProxy<Res>(r);
+}
+template <typename Pol, typename Res, typename T, typename F = operators::plus<T>,
+          detail::enable_if_resource<Res> = 0>
+resources::EventProxy<Res> exclusive_scan_inplace(Res r, Span<T> io, F f = F{}, T v = F::identity()) {
+  auto bound = bind_resource(r);
+  (void)bound;
+  if (io.size() != 0)
+    scan_exclusive(Pol{}, static_cast<const T*>(io.begin()), static_cast<const T*>(io.end()), io.begin(), f, v);
+  return resources::EventProxy<Res>(r);
+}
+
 template <typename Pol, typename T, typename F = operators::plus<std::remove_const_t<T>>>
-void inclusive_scan(Span<T> in, Span<std::remove_const_t<T>> out, F f = F{}) {
-  if (in.size() == 0) return;
-  scan_inclusive(Pol{}, static_cast<const std::remove_const_t<T>*>(in.begin()),
-                 static_cast<const std::remove_const_t<T>*>(in.end()), out.begin(), f);
+RAJA_COMPAT_RES_T(Pol) inclusive_scan(Span<T> in, Span<std::remove_const_t<T>> out, F f = F{}) {
+  return inclusive_scan<Pol>(RAJA_COMPAT_DEFAULT_RES(Pol), in, out, f);
 }
 template <typename Pol, typename T, typename F = operators::plus<std::remove_const_t<T>>>
-void exclusive_scan(Span<T> in, Span<std::remove_const_t<T>> out, F f = F{},
-                    std::remove_const_t<T> v = F::identity()) {
-  if (in.size() == 0) return;
-  scan_exclusive(Pol{}, static_cast<const std::remove_const_t<T>*>(in.begin()),
-                 static_cast<const std::remove_const_t<T>*>(in.end()), out.begin(), f, v);
+RAJA_COMPAT_RES_T(Pol) exclusive_scan(Span<T> in, Span<std::remove_const_t<T>> out, F f = F{},
+                                      std::remove_const_t<T> v = F::identity()) {
+  return exclusive_scan<Pol>(RAJA_COMPAT_DEFAULT_RES(Pol), in, out, f, v);
 }
 template <typename Pol, typename T, typename F = operators::plus<T>>
-void inclusive_scan_inplace(Span<T> io, F f = F{}) {
-  if (io.size() == 0) return;
-  scan_inclusive(Pol{}, static_cast<const T*>(io.begin()), static_cast<const T*>(io.end()), io.begin(), f);
+RAJA_COMPAT_RES_T(Pol) inclusive_scan_inplace(Span<T> io, F f = F{}) {
+  return inclusive_scan_inplace<Pol>(RAJA_COMPAT_DEFAULT_RES(Pol), io, f);
 }
 template <typename Pol, typename T, typename F = operators::plus<T>>
-void exclusive_scan_inplace(Span<T> io, F f = F{}, T v = F::identity()) {
-  if (io.size() == 0) return;
-  scan_exclusive(Pol{}, static_cast<const T*>(io.begin()), static_cast<const T*>(io.end()), io.begin(), f, v);
+RAJA_COMPAT_RES_T(Pol) exclusive_scan_inplace(Span<T> io, F f = F{}, T v = F::identity()) {
+  return exclusive_scan_inplace<Pol>(RAJA_COMPAT_DEFAULT_RES(Pol), io, f, v);
 }
 
 // ----------------------------------------------------------------- sorts
@@ -747,18 +1010,58 @@ void sort_stable_pairs(seq_exec, K* kb, K* ke, V* vb, C c) {
 template <typename K, typename V, typename C>
 void sort_unstable_pairs(seq_exec p, K* kb, K* ke, V* vb, C c) { sort_stable_pairs(p, kb, ke, vb, c); }
 
-template <typename Pol, typename T, typename C = operators::less<T>>
-void sort(Span<T> s, C c = C{}) { if (s.size() > 1) sort_unstable(Pol{}, s.begin(), s.end(), c); }
-template <typename Pol, typename T, typename C = operators::less<T>>
-void stable_sort(Span<T> s, C c = C{}) { if (s.size() > 1) sort_stable(Pol{}, s.begin(), s.end(), c); }
-template <typename Pol, typename K, typename V, typename C = operators::less<K>>
-void sort_pairs(Span<K> k, Span<V> v, C c = C{}) {
+// Resource-first forms as for the scans (pattern/sort.hpp:54-451).
+template <typename Pol, typename Res, typename T, typename C = operators::less<T>,
+          detail::enable_if_resource<Res> = 0>
+resources::EventProxy<Res> sort(Res r, Span<T> s, C c = C{}) {
+  auto bound = bind_resource(r);
+  (void)bound;
+  if (s.size() > 1) sort_unstable(Pol{}, s.begin(), s.end(), c);
+  return resources::EventProxy<Res>(r);
+}
+template <typename Pol, typename Res, typename T, typename C = operators::less<T>,
+          detail::enable_if_resource<Res> = 0>
+resources::EventProxy<Res> stable_sort(Res r, Span<T> s, C c = C{}) {
+  auto bound = bind_resource(r);
+  (void)bound;
+  if (s.size() > 1) sort_stable(Pol{}, s.begin(), s.end(), c);
+  return resources::EventProxy<Res>(r);
+}
+template <typename Pol, typename Res, typename K, typename V, typename C = operators::less<K>,
+          detail::enable_if_resource<Res> = 0>
+resources::EventProxy<Res> sort_pairs(Res r, Span<K> k, Span<V> v, C c = C{}) {
+  auto bound = bind_resource(r);
+  (void)bound;
   if (k.size() > 1) sort_unstable_pairs(Pol{}, k.begin(), k.end(), v.begin(), c);
+  return resources::EventProxy<Res>(r);
+}
+template <typename Pol, typename Res, typename K, typename V, typename C = operators::less<K>,
+          detail::enable_if_resource<Res> = 0>
+resources::EventProxy<Res> stable_sort_pairs(Res r, Span<K> k, Span<V> v, C c = C{}) {
+  auto bound = bind_resource(r);
+  (void)bound;
+  if (k.size() > 1) sort_stable_pairs(Pol{}, k.begin(), k.end(), v.begin(), c);
+  return resources::EventProxy<Res>(r);
+}
+
+template <typename Pol, typename T, typename C = operators::less<T>>
+RAJA_COMPAT_RES_T(Pol) sort(Span<T> s, C c = C{}) {
+  return sort<Pol>(RAJA_COMPAT_DEFAULT_RES(Pol), s, c);
+}
+template <typename Pol, typename T, typename C = operators::less<T>>
+RAJA_COMPAT_RES_T(Pol) stable_sort(Span<T> s, C c = C{}) {
+  return stable_sort<Pol>(RAJA_COMPAT_DEFAULT_RES(Pol), s, c);
 }
 template <typename Pol, typename K, typename V, typename C = operators::less<K>>
-void stable_sort_pairs(Span<K> k, Span<V> v, C c = C{}) {
-  if (k.size() > 1) sort_stable_pairs(Pol{}, k.begin(), k.end(), v.begin(), c);
+RAJA_COMPAT_RES_T(Pol) sort_pairs(Span<K> k, Span<V> v, C c = C{}) {
+  return sort_pairs<Pol>(RAJA_COMPAT_DEFAULT_RES(Pol), k, v, c);
 }
+template <typename Pol, typename K, typename V, typename C = operators::less<K>>
+RAJA_COMPAT_RES_T(Pol) stable_sort_pairs(Span<K> k, Span<V> v, C c = C{}) {
+  return stable_sort_pairs<Pol>(RAJA_COMPAT_DEFAULT_RES(Pol), k, v, c);
+}
+#undef RAJA_COMPAT_DEFAULT_RES
+#undef RAJA_COMPAT_RES_T
 
 // ------------------------------------------------------------- WorkGroup
 // pattern/WorkGroup.hpp:117-530.  Host runners execute the loops in
@@ -782,7 +1085,17 @@ class WorkPool;
 template <typename POL, typename Index, typename XArgs = xargs<>, typename Alloc = void>
 class WorkGroup;
 template <typename POL, typename Index, typename XArgs = xargs<>, typename Alloc = void>
-class WorkSite {};
+class WorkSite {
+ public:
+  using resource_type = typename resources::get_resource<typename POL::exec_policy>::type;
+  WorkSite() : m_resource(resource_type::get_default()) {}
+  explicit WorkSite(resource_type r) : m_resource(r) {}
+  resource_type get_resource() const { return m_resource; }
+  void clear() {}
+
+ private:
+  resource_type m_resource;
+};
 
 namespace detail {
 // Host runner: type-erased loops kept in enqueue order.
@@ -817,14 +1130,20 @@ template <typename EXEC, typename ORDER, typename STORAGE, typename Index, typen
 class WorkGroup<WorkGroupPolicy<EXEC, ORDER, STORAGE>, Index, xargs<>, Alloc> {
  public:
   using policy = WorkGroupPolicy<EXEC, ORDER, STORAGE>;
-  WorkSite<policy, Index, xargs<>, Alloc> run() {
+  using resource_type = typename resources::get_resource<EXEC>::type;
+  // run([resource]) (pattern/WorkGroup.hpp:357-370): the loops run on the
+  // resource, the policy's default one when none is given.
+  WorkSite<policy, Index, xargs<>, Alloc> run(resource_type r) {
+    auto bound = bind_resource(r);
+    (void)bound;
     if (std::is_same<ORDER, reverse_ordered>::value) {
       for (auto it = m_loops.rbegin(); it != m_loops.rend(); ++it) (*it)();
     } else {
       for (auto& f : m_loops) f();
     }
-    return {};
+    return WorkSite<policy, Index, xargs<>, Alloc>(r);
   }
+  WorkSite<policy, Index, xargs<>, Alloc> run() { return run(resource_type::get_default()); }
   void clear() { m_loops.clear(); }
   std::vector<std::function<void()>> m_loops;
 };

@@ -191,13 +191,16 @@ const char* b200_last_error_string(void) { return t_last_error.c_str(); }
 
 int b200_stream_synchronize(b200_stream_t stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  B200_CUDA(cudaStreamSynchronize(s));
   uint32_t* st = nullptr;
   B200_TRY(status_word(&st));
+  // Read the status word in the stream's own order, so that waiting for
+  // one stream does not also wait for work on the others.
   uint32_t h = 0;
-  B200_CUDA(cudaMemcpy(&h, st, sizeof(h), cudaMemcpyDeviceToHost));
+  B200_CUDA(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s));
+  B200_CUDA(cudaStreamSynchronize(s));
   if (h != 0) {
-    B200_CUDA(cudaMemset(st, 0, sizeof(uint32_t)));
+    B200_CUDA(cudaMemsetAsync(st, 0, sizeof(uint32_t), s));
+    B200_CUDA(cudaStreamSynchronize(s));
     return fail(B200_ERR_TIMEOUT,
                 "a bounded device wait gave up (status 0x%x: %s%s%s)", h,
                 (h & kStatusScanTimeout) ? "scan look-back " : "",

@@ -6,6 +6,7 @@
 //   N in {357, 32000}, plus/min/max, non-identity offsets), sort /
 //   stable_sort / sort_pairs, and test/functional/workgroup (a[i] += i + 5).
 // Prints one PASS/FAIL line per case; the exit status is the failure count.
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <random>
@@ -450,6 +451,208 @@ void test_multi_reduce_and_atomics() {
   cudaFree(vals);
 }
 
+// Resources and events (test/unit/resource/tests/*.hpp): stream-ordered
+// copies, cross-stream dependencies through events, joins, several
+// streams writing one array, sync vs async policies, and scans, sorts,
+// reducers and WorkGroup runs on a resource.
+__device__ inline void spin_cycles(long long c) {
+  const long long t0 = clock64();
+  while (clock64() - t0 < c) {
+  }
+}
+
+template <class Pol>
+void resource_semantics(const char* tag) {
+  namespace res = RAJA::resources;
+  char nm[96];
+  res::Host host;
+  {  // BasicAsyncSemantics
+    const int n = 10000000;
+    res::Cuda dev;
+    int* d = res::Resource{dev}.allocate<int>(n);
+    int* h = host.allocate<int>(n);
+    RAJA::forall<RAJA::seq_exec>(host, RAJA::RangeSegment(0, n), [=](Index_type i) { h[i] = int(i); });
+    dev.memcpy(d, h, sizeof(int) * n);
+    RAJA::forall<Pol>(dev, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) { d[i] = int(i) + 2; });
+    dev.memcpy(h, d, sizeof(int) * n);
+    dev.wait();
+    bool ok = true;
+    for (int i = 0; i < n; ++i) ok = ok && h[i] == i + 2;
+    snprintf(nm, sizeof nm, "resource_basic_async_%s", tag);
+    CHECK(nm, ok);
+    dev.deallocate(d);
+    host.deallocate(h);
+  }
+  {  // Depends
+    const int n = 10000;
+    res::Cuda dev1, dev2;
+    int* d1 = res::Resource{dev1}.allocate<int>(n);
+    int* d2 = res::Resource{dev2}.allocate<int>(n);
+    int* h = host.allocate<int>(n);
+    RAJA::forall<Pol>(dev1, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) { d1[i] = int(i); });
+    res::Event e = RAJA::forall<Pol>(dev2, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) {
+      spin_cycles(20000);
+      d2[i] = -1;
+    });
+    dev1.wait_for(&e);
+    RAJA::forall<Pol>(dev1, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) { d1[i] *= d2[i]; });
+    dev1.memcpy(h, d1, sizeof(int) * n);
+    dev1.wait();
+    bool ok = dev1 != dev2;
+    for (int i = 0; i < n; ++i) ok = ok && h[i] == -i;
+    snprintf(nm, sizeof nm, "resource_depends_%s", tag);
+    CHECK(nm, ok);
+    dev1.deallocate(d1);
+    dev2.deallocate(d2);
+    host.deallocate(h);
+  }
+  {  // JoinAsyncSemantics
+    const int n = 1000000;
+    res::Cuda dev1, dev2;
+    int* d = res::Resource{dev1}.allocate<int>(n);
+    int* h = host.allocate<int>(n);
+    RAJA::forall<RAJA::seq_exec>(host, RAJA::RangeSegment(0, n), [=](Index_type i) { h[i] = int(i); });
+    dev2.memcpy(d, h, sizeof(int) * n);
+    auto e1 = dev2.get_event_erased();
+    dev1.wait_for(&e1);
+    res::Event e2 = RAJA::forall<Pol>(dev1, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) { d[i] = int(i) + 2; });
+    dev2.wait_for(&e2);
+    dev2.memcpy(h, d, sizeof(int) * n);
+    dev2.wait();
+    bool ok = true;
+    for (int i = 0; i < n; ++i) ok = ok && h[i] == i + 2;
+    snprintf(nm, sizeof nm, "resource_join_%s", tag);
+    CHECK(nm, ok);
+    dev1.deallocate(d);
+    host.deallocate(h);
+  }
+  {  // MultiStream
+    const int n = 10000;
+    res::Cuda dev1, dev2;
+    int* d = res::Resource{dev1}.allocate<int>(n);
+    int* h = host.allocate<int>(n);
+    res::Event e1 = RAJA::forall<Pol>(dev1, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) {
+      if (i % 3 == 0) d[i] = int(i);
+    });
+    res::Event e2 = RAJA::forall<Pol>(dev2, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) {
+      if (i % 3 == 1) d[i] = int(i);
+    });
+    res::Event e3 = RAJA::forall<Pol>(dev2, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) {
+      if (i % 3 == 2) d[i] = int(i);
+    });
+    dev1.wait_for(&e2);
+    dev1.wait_for(&e3);
+    dev1.memcpy(h, d, sizeof(int) * n);
+    dev1.wait();
+    bool ok = e1.try_get<res::CudaEvent>() != nullptr;
+    for (int i = 0; i < n; ++i) ok = ok && h[i] == i;
+    snprintf(nm, sizeof nm, "resource_multistream_%s", tag);
+    CHECK(nm, ok);
+    dev1.deallocate(d);
+    host.deallocate(h);
+  }
+}
+
+// One spinning forall per resource, then a wait on each; seconds.
+template <class Pol>
+double timed_spins(RAJA::resources::Cuda* dev, int ns, long long cycles) {
+  const auto t0 = std::chrono::steady_clock::now();
+  for (int s = 0; s < ns; ++s)
+    RAJA::forall<Pol>(dev[s], RAJA::RangeSegment(0, 10000), [=] __device__(Index_type) { spin_cycles(cycles); });
+  for (int s = 0; s < ns; ++s) dev[s].wait();
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void test_resources() {
+  namespace res = RAJA::resources;
+  using async = RAJA::b200_exec_async<256>;
+  static_assert(std::is_same<res::get_resource<exec>::type, res::Cuda>::value, "b200 resource");
+  resource_semantics<async>("async");
+  resource_semantics<exec>("sync");
+
+  // a synchronous policy has finished when forall returns
+  {
+    const int n = 1 << 20;
+    res::Cuda dev;
+    int* m = dev.allocate<int>(n, res::MemoryAccess::Managed);
+    RAJA::forall<exec>(dev, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) {
+      spin_cycles(2000);
+      m[i] = 7 * int(i);
+    });
+    bool ok = true;
+    for (int i = 0; i < n; ++i) ok = ok && m[i] == 7 * i;
+    CHECK("resource_sync_policy_done_on_return", ok);
+    dev.deallocate(m);
+  }
+  // AsyncTime: eight resources, one ~2 ms kernel each.  Asynchronous
+  // launches overlap; synchronous ones run one after another.
+  {
+    constexpr int NS = 8;
+    res::Cuda dev[NS];
+    int clk_khz = 0;
+    cudaDeviceGetAttribute(&clk_khz, cudaDevAttrClockRate, 0);
+    const long long cycles = (long long)(clk_khz > 0 ? clk_khz : 2000000) * 2;  // about 2 ms
+    timed_spins<async>(dev, NS, cycles);  // warm-up
+    const double t_sync = timed_spins<exec>(dev, NS, cycles);
+    const double t_async = timed_spins<async>(dev, NS, cycles);
+    printf("async_time: sync %.2f ms, async %.2f ms\n", t_sync * 1e3, t_async * 1e3);
+    CHECK("resource_async_time", t_async < 0.5 * t_sync);
+  }
+  // scans, sorts and reducers on a resource; EventProxy to CudaEvent
+  {
+    const int n = 32000;
+    res::Cuda dev;
+    int* in = dev.allocate<int>(n, res::MemoryAccess::Managed);
+    int* out = dev.allocate<int>(n, res::MemoryAccess::Managed);
+    for (int i = 0; i < n; ++i) in[i] = (i * 7919) % 1000 - 500;
+    res::CudaEvent ce = RAJA::exclusive_scan<async>(dev, RAJA::make_span((const int*)in, n), RAJA::make_span(out, n),
+                                                    RAJA::operators::plus<int>{}, 5);
+    ce.wait();
+    bool ok = true;
+    long acc = 5;
+    for (int i = 0; i < n; ++i) {
+      ok = ok && out[i] == int(acc);
+      acc += in[i];
+    }
+    CHECK("resource_exclusive_scan_event", ok);
+    int* vals = dev.allocate<int>(n, res::MemoryAccess::Managed);
+    for (int i = 0; i < n; ++i) vals[i] = i;
+    res::Event se = RAJA::stable_sort_pairs<async>(res::Resource{dev}, RAJA::make_span(in, n), RAJA::make_span(vals, n));
+    se.wait();
+    ok = true;
+    for (int i = 1; i < n; ++i) ok = ok && (in[i - 1] < in[i] || (in[i - 1] == in[i] && vals[i - 1] < vals[i]));
+    CHECK("resource_stable_sort_pairs", ok);
+    RAJA::ReduceSum<red, long long> s(0);
+    RAJA::ReduceMin<red, int> mn(1 << 30);
+    RAJA::forall<exec>(dev, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) {
+      s += vals[i];
+      mn.min(in[i]);
+    });
+    CHECK("resource_reducers", s.get() == (long long)n * (n - 1) / 2 && mn.get() == in[0]);
+    dev.deallocate(in);
+    dev.deallocate(out);
+    dev.deallocate(vals);
+  }
+  // WorkGroup::run(resource)
+  {
+    const int n = 4096;
+    res::Cuda dev;
+    int* a = dev.allocate<int>(n, res::MemoryAccess::Managed);
+    for (int i = 0; i < n; ++i) a[i] = 0;
+    using wpol = RAJA::WorkGroupPolicy<RAJA::b200_work<256, true>, RAJA::unordered>;
+    RAJA::WorkPool<wpol, Index_type> pool;
+    pool.enqueue(RAJA::RangeSegment(0, n / 2), [=] __device__(Index_type i) { a[i] += int(i) + 5; });
+    pool.enqueue(RAJA::RangeSegment(n / 2, n), [=] __device__(Index_type i) { a[i] -= int(i); });
+    auto group = pool.instantiate();
+    auto site = group.run(dev);
+    site.get_resource().wait();
+    bool ok = site.get_resource() == dev;
+    for (int i = 0; i < n; ++i) ok = ok && a[i] == (i < n / 2 ? i + 5 : -i);
+    CHECK("resource_workgroup_run", ok);
+    dev.deallocate(a);
+  }
+}
+
 int main() {
   test_multi_reduce_and_atomics();
   test_reducers();
@@ -458,6 +661,7 @@ int main() {
   test_sorts();
   workgroup_case<RAJA::unordered>("unordered");
   workgroup_case<RAJA::ordered>("ordered");
+  test_resources();
   printf("%d failures\n", g_fail);
   return g_fail;
 }

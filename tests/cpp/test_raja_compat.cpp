@@ -156,6 +156,56 @@ int main() {
     oka = oka && RAJA::atomicXor<RAJA::seq_atomic>(&x, 5) == 7 && x == 2;
     CHECK("atomics_seq", oka);
   }
+  // resources on the host: Host, type-erased Resource and Event, EventProxy
+  // returned by forall / scan / sort (test/unit/resource/tests/*.hpp)
+  {
+    namespace res = RAJA::resources;
+    static_assert(std::is_same<res::get_resource<RAJA::seq_exec>::type, res::Host>::value, "host policy");
+    res::Host host;
+    const int n = 1000;
+    int* h = host.allocate<int>(n);
+    int* g = res::Resource{host}.allocate<int>(n);
+    host.memset(g, 0, sizeof(int) * n);
+    RAJA::forall<RAJA::seq_exec>(host, RAJA::RangeSegment(0, n), [=](Index_type i) { h[i] = int(i) + 2; });
+    res::Resource er{host};
+    er.memcpy(g, h, sizeof(int) * n);
+    res::Event e = RAJA::forall<RAJA::seq_exec>(er, RAJA::RangeSegment(0, n), [=](Index_type i) { g[i] *= 3; });
+    er.wait_for(&e);
+    er.wait();
+    bool okr = e.check() && er.get_platform() == res::Platform::host && er.try_get<res::Host>() != nullptr;
+    for (int i = 0; i < n; ++i) okr = okr && g[i] == 3 * (i + 2);
+    res::HostEvent he = RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 1), [](Index_type) {});
+    okr = okr && he.check();
+    res::Event pe = host.get_event_erased();
+    okr = okr && pe.try_get<res::HostEvent>() != nullptr && pe.try_get<int>() == nullptr;
+    bool threw = false;
+    try {
+      (void)pe.get<int>();
+    } catch (const std::runtime_error&) {
+      threw = true;
+    }
+    okr = okr && threw;
+    // scans and sorts on a resource
+    res::Event se = RAJA::inclusive_scan<RAJA::seq_exec>(host, RAJA::make_span((const int*)h, n),
+                                                         RAJA::make_span(g, n));
+    se.wait();
+    long acc = 0;
+    for (int i = 0; i < n; ++i) {
+      acc += i + 2;
+      okr = okr && g[i] == int(acc);
+    }
+    RAJA::stable_sort<RAJA::seq_exec>(er, RAJA::make_span(g, n), RAJA::operators::greater<int>{});
+    for (int i = 1; i < n; ++i) okr = okr && g[i - 1] >= g[i];
+    // WorkGroup::run(resource) hands the resource to the WorkSite
+    RAJA::WorkPool<RAJA::WorkGroupPolicy<RAJA::seq_exec, RAJA::ordered>, Index_type> pool2;
+    pool2.enqueue(RAJA::RangeSegment(0, n), [=](Index_type i) { h[i] = -int(i); });
+    auto g2 = pool2.instantiate();
+    auto site = g2.run(host);
+    okr = okr && site.get_resource().get_platform() == res::Platform::host && h[n - 1] == -(n - 1);
+    host.deallocate(h);
+    er.deallocate(g);
+    CHECK("resources_host", okr);
+  }
   printf("%d failures\n", g_fail);
   return g_fail;
 }
