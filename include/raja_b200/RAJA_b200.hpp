@@ -117,32 +117,47 @@ inline unsigned grid_for(Kernel k, int block, long long len) {
 }
 
 // ---- device combine helpers (block reduce + last-block ticket)
+// Threads and blocks are numbered linearly (x fastest), so the helpers
+// serve 1-D forall launches and the 1-3-D grids of RAJA::launch alike.
+__device__ inline unsigned lin_tid() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }
+__device__ inline unsigned lin_nthreads() { return blockDim.x * blockDim.y * blockDim.z; }
+__device__ inline unsigned lin_bid() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
+__device__ inline unsigned lin_nblocks() { return gridDim.x * gridDim.y * gridDim.z; }
+
+template <class T>
+__device__ inline T shfl_down_t(const T& v, int o, unsigned mask) {
+  static_assert(sizeof(T) % 4 == 0, "reducer value size");
+  unsigned w[sizeof(T) / 4];
+  memcpy(w, &v, sizeof(T));
+  for (int i = 0; i < int(sizeof(T) / 4); ++i) w[i] = __shfl_down_sync(mask, w[i], o);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+// Fold the first `valid` lanes of this warp into lane 0.  `present` lanes
+// of the warp exist (a block's last warp may be partial) and all of them
+// take part in the shuffles.
+template <class T, class Merge>
+__device__ inline T warp_fold(T v, int lane, int valid, int present, Merge merge) {
+  const unsigned mask = present >= 32 ? 0xffffffffu : ((1u << present) - 1u);
+  for (int o = 16; o > 0; o >>= 1) {
+    const T other = shfl_down_t(v, o, mask);
+    if (lane + o < valid) v = merge(v, other);
+  }
+  return v;
+}
+
 template <class T, class Merge>
 __device__ inline T block_reduce(T v, Merge merge) {
   __shared__ unsigned char sh_raw[32 * sizeof(T) + 16];
   T* sh = reinterpret_cast<T*>(sh_raw);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  for (int o = 16; o > 0; o >>= 1) {
-    T other;
-    unsigned w[sizeof(T) / 4];
-    memcpy(w, &v, sizeof(T));
-    for (int i = 0; i < int(sizeof(T) / 4); ++i) w[i] = __shfl_down_sync(0xffffffffu, w[i], o);
-    memcpy(&other, w, sizeof(T));
-    if (lane + o < 32) v = merge(v, other);
-  }
+  const int tid = int(lin_tid()), nt = int(lin_nthreads());
+  const int lane = tid & 31, warp = tid >> 5, nw = (nt + 31) >> 5;
+  const int present = nt - warp * 32 < 32 ? nt - warp * 32 : 32;
+  v = warp_fold(v, lane, present, present, merge);
   if (lane == 0) sh[warp] = v;
   __syncthreads();
-  if (warp == 0) {
-    v = sh[lane < nw ? lane : 0];
-    for (int o = 16; o > 0; o >>= 1) {
-      T other;
-      unsigned w[sizeof(T) / 4];
-      memcpy(w, &v, sizeof(T));
-      for (int i = 0; i < int(sizeof(T) / 4); ++i) w[i] = __shfl_down_sync(0xffffffffu, w[i], o);
-      memcpy(&other, w, sizeof(T));
-      if (lane + o < nw) v = merge(v, other);
-    }
-  }
+  if (warp == 0) v = warp_fold(sh[lane < nw ? lane : 0], lane, nw, present, merge);
   __syncthreads();
   return v;  // valid in thread 0
 }
@@ -171,43 +186,36 @@ __device__ inline T ld_cg(const T* p) {
 template <class T, class Merge>
 __device__ inline void grid_combine(const DevSlot<T>& s, T v, Merge merge) {
   __shared__ bool last;
+  const unsigned tid = lin_tid(), nt = lin_nthreads(), nb = lin_nblocks();
   v = block_reduce(v, merge);
-  if (threadIdx.x == 0) {
-    s.partials[blockIdx.x] = v;
+  if (tid == 0) {
+    s.partials[lin_bid()] = v;
     __threadfence();
-    last = ::atomicAdd(s.ticket, 1u) == gridDim.x - 1;
+    last = ::atomicAdd(s.ticket, 1u) == nb - 1;
   }
   __syncthreads();
   if (!last) return;
   __threadfence();
-  bool have = false;
+  // thread t folds partials t, t + nt, ...; the threads holding partials
+  // are a prefix 0 .. min(nb, nt) - 1, so only those merge below
   T r = v;
-  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+  for (unsigned b = tid; b < nb; b += nt) {
     const T p = ld_cg(s.partials + b);
-    r = have ? merge(r, p) : p;
-    have = true;
+    r = b == tid ? p : merge(r, p);
   }
-  // threads without a partial hold v, the last block's own partial:
-  // re-merging it is harmless for idempotent merges but not for sums, so
-  // those threads contribute the identity by skipping the merge below
   __shared__ unsigned char fin_raw[32 * sizeof(T) + 16];
   T* fin = reinterpret_cast<T*>(fin_raw);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  const unsigned nb = gridDim.x;
-  // warp-level fold of the threads that hold partials (threads < nb)
-  for (int o = 16; o > 0; o >>= 1) {
-    unsigned w[sizeof(T) / 4];
-    memcpy(w, &r, sizeof(T));
-    for (int i = 0; i < int(sizeof(T) / 4); ++i) w[i] = __shfl_down_sync(0xffffffffu, w[i], o);
-    T other;
-    memcpy(&other, w, sizeof(T));
-    if (lane + o < 32 && threadIdx.x + o < nb) r = merge(r, other);
-  }
-  if (lane == 0) fin[warp] = r;
+  const int lane = int(tid & 31), warp = int(tid >> 5);
+  const int holders = int(nb < nt ? nb : nt);
+  const int present = int(nt) - warp * 32 < 32 ? int(nt) - warp * 32 : 32;
+  int valid = holders - warp * 32;
+  valid = valid < 0 ? 0 : (valid > 32 ? 32 : valid);
+  r = warp_fold(r, lane, valid, present, merge);
+  if (lane == 0 && valid > 0) fin[warp] = r;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     T acc = fin[0];
-    for (int w = 1; w < nw && unsigned(w * 32) < nb; ++w) acc = merge(acc, fin[w]);
+    for (int w = 1; w * 32 < holders; ++w) acc = merge(acc, fin[w]);
     *s.result = acc;
     *s.ticket = 0u;
   }
@@ -357,11 +365,12 @@ class DevReducer {
   V fold() const {
     if (!shared_) return V{};
     for (const Pending& p : shared_->pending) {
-      check_cuda(cudaStreamSynchronize(p.stream), "reducer wait");
+      // stream-ordered read and free: other streams are not waited for
       V r;
-      check_cuda(cudaMemcpy(&r, p.result, sizeof(V), cudaMemcpyDeviceToHost), "reducer result");
+      check_cuda(cudaMemcpyAsync(&r, p.result, sizeof(V), cudaMemcpyDeviceToHost, p.stream), "reducer result");
+      check_cuda(cudaStreamSynchronize(p.stream), "reducer wait");
       shared_->init = K::fold_init(shared_->init, r);
-      cudaFree(p.block);
+      cudaFreeAsync(p.block, p.stream);
     }
     shared_->pending.clear();
     return shared_->init;
@@ -849,12 +858,15 @@ forall_params_kernel(Body body, T begin, long long len,
 }  // namespace detail
 }  // namespace b200
 
+// Read the launch results on stream s (the kernel has finished) and fold
+// them into the targets in parameter order: *target = op(*target, result).
 template <class Slots, size_t... I, class... Red>
-void resolve_params(const Slots& slots, std::index_sequence<I...>, Red&... reds) {
-  auto one = [](auto& red, const auto& slot) {
+void resolve_params(const Slots& slots, cudaStream_t s, std::index_sequence<I...>, Red&... reds) {
+  auto one = [s](auto& red, const auto& slot) {
     using RK = b200::detail::ParamKind<std::decay_t<decltype(red)>>;
     typename RK::type::V v;
-    b200::check_cuda(cudaMemcpy(&v, slot.result, sizeof(v), cudaMemcpyDeviceToHost), "param result");
+    b200::check_cuda(cudaMemcpyAsync(&v, slot.result, sizeof(v), cudaMemcpyDeviceToHost, s), "param result");
+    b200::check_cuda(cudaStreamSynchronize(s), "param result");
     red.combineTarget(RK::to_target(v));
   };
   (one(reds, b200::detail::dget<I>(slots)), ...);
@@ -875,10 +887,261 @@ void forall_params_impl(b200_exec<BLOCK, Async>, const TypedRangeSegment<T>& r, 
   k<<<g, BLOCK, 0, s>>>(body, r.b, len, slots);
   b200::check_cuda(cudaGetLastError(), "b200 forall params");
   b200::wait();  // param_resolve waits for the kernel, as the reference does
-  // resolve in parameter order: *target = op(*target, result)
-  resolve_params(slots, std::index_sequence_for<Red...>{}, reds...);
-  for (size_t i = 0; i < sizeof...(Red); ++i) cudaFree(blocks[i]);
+  resolve_params(slots, s, std::index_sequence_for<Red...>{}, reds...);
+  for (size_t i = 0; i < sizeof...(Red); ++i) cudaFreeAsync(blocks[i], s);
 }
+
+// ---------------------------------------------------------------- launch
+// RAJA::launch on the b200 policies (replaces cuda_launch_t and the CUDA
+// loop policies, policy/cuda/launch.hpp): one kernel of Teams x Threads
+// with LaunchParams::shared_mem_size bytes of dynamic shared memory; each
+// loop policy maps a segment onto one kind of index:
+//   b200_thread_{x,y,z}_{direct,loop}   threadIdx   (team-local)
+//   b200_block_{x,y,z}_{direct,loop}    blockIdx
+//   b200_global_{x,y,z}_{direct,loop}   blockIdx * blockDim + threadIdx
+//   b200_flatten_block_threads_{xy,xyz}_{direct,loop}
+//                                       threads of a team numbered x-first
+// "direct" runs index i on the i-th position if i < length; "loop" strides
+// by the number of positions.  The *_direct_unchecked names of the
+// reference map to the checked direct forms (same results whenever the
+// unchecked form is valid).  A host-compiled loop body runs sequentially.
+template <bool Async = false, int NUM_THREADS = 0>
+struct b200_launch_t {};
+
+template <int KIND, int D, bool LOOP>
+struct b200_loop_pol {};
+namespace b200 {
+namespace launch {
+enum Kind { kThread = 0, kBlock = 1, kGlobal = 2, kFlatThreads = 3 };
+struct Pos {
+  Index_type id;  // this thread's position
+  Index_type n;   // number of positions
+};
+__device__ inline unsigned tid3(int d) { return d == 0 ? threadIdx.x : (d == 1 ? threadIdx.y : threadIdx.z); }
+__device__ inline unsigned tdim3(int d) { return d == 0 ? blockDim.x : (d == 1 ? blockDim.y : blockDim.z); }
+__device__ inline unsigned bid3(int d) { return d == 0 ? blockIdx.x : (d == 1 ? blockIdx.y : blockIdx.z); }
+__device__ inline unsigned bdim3(int d) { return d == 0 ? gridDim.x : (d == 1 ? gridDim.y : gridDim.z); }
+template <int KIND, int D>
+__device__ inline Pos pos() {
+  if constexpr (KIND == kThread) {
+    return {Index_type(tid3(D)), Index_type(tdim3(D))};
+  } else if constexpr (KIND == kBlock) {
+    return {Index_type(bid3(D)), Index_type(bdim3(D))};
+  } else if constexpr (KIND == kGlobal) {
+    return {Index_type(bid3(D)) * tdim3(D) + tid3(D), Index_type(bdim3(D)) * tdim3(D)};
+  } else {
+    static_assert(D == 2 || D == 3, "flattened threads over xy or xyz");
+    const Index_type xy = Index_type(threadIdx.x) + Index_type(blockDim.x) * threadIdx.y;
+    if constexpr (D == 2) return {xy, Index_type(blockDim.x) * blockDim.y};
+    else return {xy + Index_type(blockDim.x) * blockDim.y * threadIdx.z,
+                 Index_type(blockDim.x) * blockDim.y * blockDim.z};
+  }
+}
+}  // namespace launch
+}  // namespace b200
+
+#define RAJA_B200_LOOP_POLS(NAME, KIND, D)                                \
+  using b200_##NAME##_direct = b200_loop_pol<KIND, D, false>;            \
+  using b200_##NAME##_direct_unchecked = b200_loop_pol<KIND, D, false>;  \
+  using b200_##NAME##_loop = b200_loop_pol<KIND, D, true>;
+RAJA_B200_LOOP_POLS(thread_x, 0, 0)
+RAJA_B200_LOOP_POLS(thread_y, 0, 1)
+RAJA_B200_LOOP_POLS(thread_z, 0, 2)
+RAJA_B200_LOOP_POLS(block_x, 1, 0)
+RAJA_B200_LOOP_POLS(block_y, 1, 1)
+RAJA_B200_LOOP_POLS(block_z, 1, 2)
+RAJA_B200_LOOP_POLS(global_x, 2, 0)
+RAJA_B200_LOOP_POLS(global_y, 2, 1)
+RAJA_B200_LOOP_POLS(global_z, 2, 2)
+RAJA_B200_LOOP_POLS(flatten_block_threads_xy, 3, 2)
+RAJA_B200_LOOP_POLS(flatten_block_threads_xyz, 3, 3)
+#undef RAJA_B200_LOOP_POLS
+using b200_global_thread_x = b200_global_x_direct;
+using b200_global_thread_y = b200_global_y_direct;
+using b200_global_thread_z = b200_global_z_direct;
+
+template <int KIND, int D, bool LOOP, typename SEGMENT>
+struct LoopExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
+  template <typename BODY>
+  RAJA_HOST_DEVICE static void exec(const LaunchContext& ctx, const SEGMENT& seg, const BODY& body) {
+#if defined(__CUDA_ARCH__)
+    (void)ctx;
+    const b200::launch::Pos p = b200::launch::pos<KIND, D>();
+    const Index_type n = detail::seg_len(seg);
+    if (LOOP) {
+      for (Index_type k = p.id; k < n; k += p.n) body(detail::seg_at(seg, k));
+    } else if (p.id < n) {
+      body(detail::seg_at(seg, p.id));
+    }
+#else
+    LoopExecute<seq_exec, SEGMENT>::exec(ctx, seg, body);
+#endif
+  }
+};
+template <int KIND, int D, bool LOOP, typename SEGMENT>
+struct LoopICountExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
+  template <typename BODY>
+  RAJA_HOST_DEVICE static void exec(const LaunchContext& ctx, const SEGMENT& seg, const BODY& body) {
+#if defined(__CUDA_ARCH__)
+    (void)ctx;
+    using I = std::decay_t<decltype(detail::seg_at(seg, 0))>;
+    const b200::launch::Pos p = b200::launch::pos<KIND, D>();
+    const Index_type n = detail::seg_len(seg);
+    if (LOOP) {
+      for (Index_type k = p.id; k < n; k += p.n) body(detail::seg_at(seg, k), I(k));
+    } else if (p.id < n) {
+      body(detail::seg_at(seg, p.id), I(p.id));
+    }
+#else
+    LoopICountExecute<seq_exec, SEGMENT>::exec(ctx, seg, body);
+#endif
+  }
+};
+template <int KIND, int D, bool LOOP, typename SEGMENT>
+struct TileExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
+  template <typename TILE_T, typename BODY>
+  RAJA_HOST_DEVICE static void exec(const LaunchContext& ctx, TILE_T ts, const SEGMENT& seg, const BODY& body) {
+#if defined(__CUDA_ARCH__)
+    (void)ctx;
+    const b200::launch::Pos p = b200::launch::pos<KIND, D>();
+    const Index_type t = Index_type(ts), nt = (detail::seg_len(seg) + t - 1) / t;
+    if (LOOP) {
+      for (Index_type k = p.id; k < nt; k += p.n) body(detail::seg_tile(seg, t, k));
+    } else if (p.id < nt) {
+      body(detail::seg_tile(seg, t, p.id));
+    }
+#else
+    TileExecute<seq_exec, SEGMENT>::exec(ctx, ts, seg, body);
+#endif
+  }
+};
+template <int KIND, int D, bool LOOP, typename SEGMENT>
+struct TileTCountExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
+  template <typename TILE_T, typename BODY>
+  RAJA_HOST_DEVICE static void exec(const LaunchContext& ctx, TILE_T ts, const SEGMENT& seg, const BODY& body) {
+#if defined(__CUDA_ARCH__)
+    (void)ctx;
+    using I = std::decay_t<decltype(detail::seg_at(seg, 0))>;
+    const b200::launch::Pos p = b200::launch::pos<KIND, D>();
+    const Index_type t = Index_type(ts), nt = (detail::seg_len(seg) + t - 1) / t;
+    if (LOOP) {
+      for (Index_type k = p.id; k < nt; k += p.n) body(detail::seg_tile(seg, t, k), I(k));
+    } else if (p.id < nt) {
+      body(detail::seg_tile(seg, t, p.id), I(p.id));
+    }
+#else
+    TileTCountExecute<seq_exec, SEGMENT>::exec(ctx, ts, seg, body);
+#endif
+  }
+};
+
+namespace b200 {
+namespace detail {
+// Every launch kernel names the dynamic shared memory the same way.
+#define RAJA_B200_LAUNCH_SMEM extern __shared__ __align__(16) unsigned char b200_launch_smem[]
+
+template <class Body>
+__global__ void launch_kernel(Body body_in) {
+  RAJA_B200_LAUNCH_SMEM;
+  Body body(body_in);  // per-thread copy: captured reducers privatise here
+  LaunchContext ctx;
+  ctx.shared_mem_ptr = b200_launch_smem;
+  body(ctx);
+}
+template <int NT, class Body>
+__global__ void __launch_bounds__(NT) launch_kernel_nt(Body body_in) {
+  RAJA_B200_LAUNCH_SMEM;
+  Body body(body_in);
+  LaunchContext ctx;
+  ctx.shared_mem_ptr = b200_launch_smem;
+  body(ctx);
+}
+template <class Body, class... R, size_t... I>
+__device__ inline void launch_params_body(Body& body, const DTuple<DevSlot<typename ParamKind<R>::type::V>...>& slots,
+                                          std::index_sequence<I...>) {
+  RAJA_B200_LAUNCH_SMEM;
+  LaunchContext ctx;
+  ctx.shared_mem_ptr = b200_launch_smem;
+  DTuple<typename R::valop_type...> vals{};
+  body(ctx, dget<I>(vals)...);
+  (combine_param<R>(dget<I>(slots), dget<I>(vals)), ...);
+}
+template <int NT, class Body, class... R>
+__global__ void __launch_bounds__(NT > 0 ? NT : 1024)
+launch_params_kernel(Body body_in, DTuple<DevSlot<typename ParamKind<R>::type::V>...> slots) {
+  Body body(body_in);
+  launch_params_body<Body, R...>(body, slots, std::index_sequence_for<R...>{});
+}
+#undef RAJA_B200_LAUNCH_SMEM
+
+struct LaunchShape {
+  dim3 grid, block;
+  size_t smem;
+  unsigned blocks;
+  bool empty;
+};
+template <int NT, class Kernel>
+inline LaunchShape launch_shape(const LaunchParams& p, Kernel k) {
+  LaunchShape sh;
+  const int* t = p.teams.value;
+  const int* th = p.threads.value;
+  sh.empty = t[0] <= 0 || t[1] <= 0 || t[2] <= 0 || th[0] <= 0 || th[1] <= 0 || th[2] <= 0;
+  if (sh.empty) return sh;
+  sh.grid = dim3(unsigned(t[0]), unsigned(t[1]), unsigned(t[2]));
+  sh.block = dim3(unsigned(th[0]), unsigned(th[1]), unsigned(th[2]));
+  const long long nthreads = (long long)th[0] * th[1] * th[2];
+  if (nthreads > 1024 || (NT > 0 && nthreads > NT))
+    throw std::runtime_error("b200 launch: " + std::to_string(nthreads) + " threads per team exceed the policy's " +
+                             std::to_string(NT > 0 ? NT : 1024));
+  sh.blocks = sh.grid.x * sh.grid.y * sh.grid.z;
+  sh.smem = p.shared_mem_size ? p.shared_mem_size + kLaunchSharedSlack : 0;
+  if (sh.smem > 48 * 1024)
+    check_cuda(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sh.smem)),
+               "b200 launch shared memory");
+  return sh;
+}
+}  // namespace detail
+}  // namespace b200
+
+template <bool Async, int NT>
+struct LaunchExecute<b200_launch_t<Async, NT>> {
+  template <typename Res, typename Body>
+  static void exec(Res, const LaunchParams& p, const Body& body) {
+    using B = std::decay_t<Body>;
+    void (*k)(B) = NT > 0 ? b200::detail::launch_kernel_nt<(NT > 0 ? NT : 1), B> : b200::detail::launch_kernel<B>;
+    const b200::detail::LaunchShape sh = b200::detail::launch_shape<NT>(p, k);
+    if (sh.empty) return;
+    cudaStream_t s = b200::stream();
+    B lb = b200::detail::LaunchCopy<B>::make(body, sh.blocks, s);
+    k<<<sh.grid, sh.block, sh.smem, s>>>(lb);
+    b200::detail::finish<Async>("b200 launch");
+  }
+  template <typename Res, typename Body, typename... Red>
+  static void exec_params(Res, const LaunchParams& p, const Body& body, Red&... reds) {
+    using B = std::decay_t<Body>;
+    using Slots = b200::detail::DTuple<b200::detail::DevSlot<typename b200::detail::ParamKind<Red>::type::V>...>;
+    auto k = b200::detail::launch_params_kernel<NT, B, Red...>;
+    const b200::detail::LaunchShape sh = b200::detail::launch_shape<NT>(p, k);
+    if (sh.empty) return;
+    cudaStream_t s = b200::stream();
+    void* blocks[sizeof...(Red) + 1] = {};
+    size_t bi = 0;
+    Slots slots{b200::detail::alloc_slot<typename b200::detail::ParamKind<Red>::type::V>(sh.blocks, s, &blocks[bi++])...};
+    B lb = b200::detail::LaunchCopy<B>::make(body, sh.blocks, s);
+    k<<<sh.grid, sh.block, sh.smem, s>>>(lb, slots);
+    b200::check_cuda(cudaGetLastError(), "b200 launch params");
+    b200::wait();  // the targets are combined after the kernel, as in the reference
+    resolve_params(slots, s, std::index_sequence_for<Red...>{}, reds...);
+    for (size_t i = 0; i < sizeof...(Red); ++i) cudaFreeAsync(blocks[i], s);
+  }
+};
+
+namespace resources {
+template <bool Async, int NT>
+struct get_resource<b200_launch_t<Async, NT>> {
+  using type = Cuda;
+};
+}  // namespace resources
 
 // ----------------------------------------------------------------- scans
 namespace b200 {

@@ -54,6 +54,12 @@
 #define RAJA_HOST
 #endif
 #define RAJA_INLINE inline
+// Team-shared arrays in RAJA::launch bodies (shared memory on the device).
+#if defined(__CUDA_ARCH__)
+#define RAJA_TEAM_SHARED __shared__
+#else
+#define RAJA_TEAM_SHARED
+#endif
 
 namespace RAJA {
 
@@ -136,8 +142,8 @@ template <typename T>
 struct TypedRangeStrideSegment {
   using value_type = T;
   T b, e, s;
-  TypedRangeStrideSegment(T begin, T end, T stride) : b(begin), e(end), s(stride) {}
-  T size() const {
+  RAJA_HOST_DEVICE TypedRangeStrideSegment(T begin, T end, T stride) : b(begin), e(end), s(stride) {}
+  RAJA_HOST_DEVICE T size() const {
     if (s > 0) return e > b ? (e - b + s - 1) / s : 0;
     return b > e ? (b - e + (-s) - 1) / (-s) : 0;
   }
@@ -151,8 +157,8 @@ struct TypedListSegment {
   using value_type = T;
   const T* data;
   Index_type len;
-  TypedListSegment(const T* d, Index_type n) : data(d), len(n) {}
-  Index_type size() const { return len; }
+  RAJA_HOST_DEVICE TypedListSegment(const T* d, Index_type n) : data(d), len(n) {}
+  RAJA_HOST_DEVICE Index_type size() const { return len; }
 };
 using ListSegment = TypedListSegment<Index_type>;
 
@@ -438,6 +444,8 @@ struct ValOp<ValLoc<T, I>, Op> {
   RAJA_HOST_DEVICE I getLoc() const { return val.loc; }
 };
 
+// A kernel name param (pattern/params/kernel_name.hpp:11-22: RAJA::Name
+// returns one); expt::Name is kept as a second spelling.
 struct KernelName {
   const char* name;
 };
@@ -487,6 +495,8 @@ ReduceLoc(T* target, I* index) {
   return {target, index};
 }
 }  // namespace expt
+
+inline expt::KernelName Name(const char* n) { return expt::KernelName{n}; }
 
 // operators::limits for ValLoc identities (pattern/detail/reduce.hpp:185-203)
 namespace operators {
@@ -824,7 +834,7 @@ void forall_params_impl(seq_exec, const TypedRangeSegment<T>& r, Body&& body, Re
 }
 
 namespace detail {
-// Dispatch of forall(seg, params..., body): kernel names (expt::Name) are
+// Dispatch of forall(seg, params..., body): kernel names (RAJA::Name) are
 // dropped wherever they appear (no plugin consumes them here); reducer
 // params are collected, in order, for forall_params_impl.
 template <typename Pol, typename Seg, typename Body, typename... Red>
@@ -893,6 +903,340 @@ resources::EventProxy<typename resources::get_resource<Pol>::type> forall(Seg&& 
   return forall<Pol>(resources::get_resource<Pol>::type::get_default(), std::forward<Seg>(seg),
                      std::forward<Args>(args)...);
 }
+
+// ---------------------------------------------------------------- launch
+// RAJA::launch (pattern/launch/launch_core.hpp:45-675): a kernel of
+// Teams x Threads with a LaunchContext for dynamic shared memory and
+// team barriers; loop / loop_icount / tile / tile_tcount map segments onto
+// the team and thread indices through loop policies.  LaunchPolicy and
+// LoopPolicy pair a host policy with a device one; a loop body compiled
+// for the device uses the device policy (launch_core.hpp:454-459).
+enum struct ExecPlace : int { HOST, DEVICE, NUM_PLACES };
+
+template <typename HOST_POLICY, typename DEVICE_POLICY = HOST_POLICY>
+struct LoopPolicy {
+  using host_policy_t = HOST_POLICY;
+  using device_policy_t = DEVICE_POLICY;
+};
+template <typename HOST_POLICY, typename DEVICE_POLICY = HOST_POLICY>
+struct LaunchPolicy {
+  using host_policy_t = HOST_POLICY;
+  using device_policy_t = DEVICE_POLICY;
+};
+
+struct Teams {
+  int value[3];
+  RAJA_HOST_DEVICE constexpr Teams() : value{1, 1, 1} {}
+  RAJA_HOST_DEVICE constexpr Teams(int i) : value{i, 1, 1} {}
+  RAJA_HOST_DEVICE constexpr Teams(int i, int j) : value{i, j, 1} {}
+  RAJA_HOST_DEVICE constexpr Teams(int i, int j, int k) : value{i, j, k} {}
+};
+struct Threads {
+  int value[3];
+  RAJA_HOST_DEVICE constexpr Threads() : value{1, 1, 1} {}
+  RAJA_HOST_DEVICE constexpr Threads(int i) : value{i, 1, 1} {}
+  RAJA_HOST_DEVICE constexpr Threads(int i, int j) : value{i, j, 1} {}
+  RAJA_HOST_DEVICE constexpr Threads(int i, int j, int k) : value{i, j, k} {}
+};
+struct Lanes {
+  int value;
+  RAJA_HOST_DEVICE constexpr Lanes() : value(0) {}
+  RAJA_HOST_DEVICE constexpr Lanes(int i) : value(i) {}
+};
+
+struct LaunchParams {
+  Teams teams;
+  Threads threads;
+  size_t shared_mem_size = 0;
+  LaunchParams() = default;
+  LaunchParams(Teams t, Threads th, size_t shmem = 0) : teams(t), threads(th), shared_mem_size(shmem) {}
+};
+
+// Bytes a launch reserves beyond LaunchParams::shared_mem_size, for the
+// alignment padding getSharedMemory adds between requests.
+constexpr size_t kLaunchSharedSlack = 256;
+
+class LaunchContext {
+ public:
+  size_t shared_mem_offset = 0;
+  void* shared_mem_ptr = nullptr;
+  RAJA_HOST_DEVICE LaunchContext() {}
+  // Bump allocation of `n` elements from the launch's dynamic shared
+  // memory, each request aligned to its type.
+  template <typename T>
+  RAJA_HOST_DEVICE T* getSharedMemory(size_t n) {
+    const size_t a = alignof(T);
+    shared_mem_offset = (shared_mem_offset + a - 1) / a * a;
+    T* p = reinterpret_cast<T*>(static_cast<char*>(shared_mem_ptr) + shared_mem_offset);
+    shared_mem_offset += n * sizeof(T);
+    return p;
+  }
+  RAJA_HOST_DEVICE void releaseSharedMemory() { shared_mem_offset = 0; }
+  RAJA_HOST_DEVICE void teamSync() {
+#if defined(__CUDA_ARCH__)
+    __syncthreads();
+#endif
+  }
+};
+
+#if defined(__CUDA_ARCH__)
+template <typename POLICY_LIST>
+using loop_policy = typename POLICY_LIST::device_policy_t;
+#else
+template <typename POLICY_LIST>
+using loop_policy = typename POLICY_LIST::host_policy_t;
+#endif
+
+// Element k of a segment, and its length, for loop executors.
+namespace detail {
+template <typename T>
+RAJA_HOST_DEVICE Index_type seg_len(const TypedRangeSegment<T>& s) { return Index_type(s.e - s.b); }
+template <typename T>
+RAJA_HOST_DEVICE T seg_at(const TypedRangeSegment<T>& s, Index_type k) { return T(s.b + T(k)); }
+template <typename T>
+RAJA_HOST_DEVICE Index_type seg_len(const TypedRangeStrideSegment<T>& s) { return Index_type(s.size()); }
+template <typename T>
+RAJA_HOST_DEVICE T seg_at(const TypedRangeStrideSegment<T>& s, Index_type k) { return T(s.b + T(k) * s.s); }
+template <typename T>
+RAJA_HOST_DEVICE Index_type seg_len(const TypedListSegment<T>& s) { return s.len; }
+template <typename T>
+RAJA_HOST_DEVICE T seg_at(const TypedListSegment<T>& s, Index_type k) { return s.data[k]; }
+// Tile t of size `ts` of a range segment (the last one may be short).
+template <typename T>
+RAJA_HOST_DEVICE TypedRangeSegment<T> seg_tile(const TypedRangeSegment<T>& s, Index_type ts, Index_type t) {
+  const Index_type lo = t * ts, n = seg_len(s);
+  return TypedRangeSegment<T>(T(s.b + T(lo)), T(s.b + T(lo + ts < n ? lo + ts : n)));
+}
+}  // namespace detail
+
+// Loop executors, specialised per loop policy (launch_core.hpp:461-465,
+// 560-564).  seq_exec runs every index in order on the calling thread.
+template <typename POLICY, typename SEGMENT>
+struct LoopExecute;
+template <typename POLICY, typename SEGMENT>
+struct LoopICountExecute;
+template <typename POLICY, typename SEGMENT>
+struct TileExecute;
+template <typename POLICY, typename SEGMENT>
+struct TileTCountExecute;
+
+template <typename SEGMENT>
+struct LoopExecute<seq_exec, SEGMENT> {
+  template <typename BODY>
+  RAJA_HOST_DEVICE static void exec(const LaunchContext&, const SEGMENT& seg, const BODY& body) {
+    const Index_type n = detail::seg_len(seg);
+    for (Index_type k = 0; k < n; ++k) body(detail::seg_at(seg, k));
+  }
+};
+template <typename SEGMENT>
+struct LoopICountExecute<seq_exec, SEGMENT> {
+  template <typename BODY>
+  RAJA_HOST_DEVICE static void exec(const LaunchContext&, const SEGMENT& seg, const BODY& body) {
+    using I = std::decay_t<decltype(detail::seg_at(seg, 0))>;
+    const Index_type n = detail::seg_len(seg);
+    for (Index_type k = 0; k < n; ++k) body(detail::seg_at(seg, k), I(k));
+  }
+};
+template <typename SEGMENT>
+struct TileExecute<seq_exec, SEGMENT> {
+  template <typename TILE_T, typename BODY>
+  RAJA_HOST_DEVICE static void exec(const LaunchContext&, TILE_T ts, const SEGMENT& seg, const BODY& body) {
+    const Index_type n = detail::seg_len(seg), t = Index_type(ts);
+    for (Index_type k = 0; k * t < n; ++k) body(detail::seg_tile(seg, t, k));
+  }
+};
+template <typename SEGMENT>
+struct TileTCountExecute<seq_exec, SEGMENT> {
+  template <typename TILE_T, typename BODY>
+  RAJA_HOST_DEVICE static void exec(const LaunchContext&, TILE_T ts, const SEGMENT& seg, const BODY& body) {
+    using I = std::decay_t<decltype(detail::seg_at(seg, 0))>;
+    const Index_type n = detail::seg_len(seg), t = Index_type(ts);
+    for (Index_type k = 0; k * t < n; ++k) body(detail::seg_tile(seg, t, k), I(k));
+  }
+};
+
+template <typename POLICY_LIST, typename CONTEXT, typename SEGMENT, typename BODY>
+RAJA_HOST_DEVICE void loop(const CONTEXT& ctx, const SEGMENT& seg, const BODY& body) {
+  LoopExecute<loop_policy<POLICY_LIST>, SEGMENT>::exec(ctx, seg, body);
+}
+template <typename POLICY_LIST, typename CONTEXT, typename SEGMENT, typename BODY>
+RAJA_HOST_DEVICE void loop_icount(const CONTEXT& ctx, const SEGMENT& seg, const BODY& body) {
+  LoopICountExecute<loop_policy<POLICY_LIST>, SEGMENT>::exec(ctx, seg, body);
+}
+template <typename POLICY_LIST, typename CONTEXT, typename TILE_T, typename SEGMENT, typename BODY>
+RAJA_HOST_DEVICE void tile(const CONTEXT& ctx, TILE_T tile_size, const SEGMENT& seg, const BODY& body) {
+  TileExecute<loop_policy<POLICY_LIST>, SEGMENT>::exec(ctx, tile_size, seg, body);
+}
+template <typename POLICY_LIST, typename CONTEXT, typename TILE_T, typename SEGMENT, typename BODY>
+RAJA_HOST_DEVICE void tile_tcount(const CONTEXT& ctx, TILE_T tile_size, const SEGMENT& seg, const BODY& body) {
+  TileTCountExecute<loop_policy<POLICY_LIST>, SEGMENT>::exec(ctx, tile_size, seg, body);
+}
+
+// Launch executors, specialised per launch policy.  exec(res, params,
+// body) runs the body with no reducer params; exec_params(res, params,
+// body, reds...) passes one ValOp per expt reducer and combines them into
+// the targets afterwards.
+template <typename LAUNCH_POLICY>
+struct LaunchExecute;
+
+struct seq_launch_t {};
+
+template <>
+struct LaunchExecute<seq_launch_t> {
+  template <typename Res, typename Body>
+  static void exec(Res, const LaunchParams& p, const Body& body) {
+    std::vector<std::max_align_t> shm((p.shared_mem_size + kLaunchSharedSlack) / sizeof(std::max_align_t) + 1);
+    LaunchContext ctx;
+    ctx.shared_mem_ptr = shm.data();
+    body(ctx);
+  }
+  template <typename Res, typename Body, typename... Red>
+  static void exec_params(Res, const LaunchParams& p, const Body& body, Red&... reds) {
+    std::vector<std::max_align_t> shm((p.shared_mem_size + kLaunchSharedSlack) / sizeof(std::max_align_t) + 1);
+    LaunchContext ctx;
+    ctx.shared_mem_ptr = shm.data();
+    std::tuple<typename Red::valop_type...> vals;
+    std::apply([&](auto&... v) { body(ctx, v...); }, vals);
+    std::apply([&](auto&... v) { (reds.combineTarget(v.val), ...); }, vals);
+  }
+};
+
+namespace resources {
+template <>
+struct get_resource<seq_launch_t> {
+  using type = Host;
+};
+}  // namespace resources
+
+namespace detail {
+// launch(res, params, [names / reducers ...,] body): names are dropped,
+// reducers collected in order (as for forall).
+template <typename LP, typename Res, typename Body, typename... Red>
+void launch_collect(Res& r, const LaunchParams& p, const Body& body, std::tuple<Red&...> reds) {
+  if constexpr (sizeof...(Red) == 0) {
+    LaunchExecute<LP>::exec(r, p, body);
+  } else {
+    std::apply([&](auto&... rd) { LaunchExecute<LP>::exec_params(r, p, body, rd...); }, reds);
+  }
+}
+template <typename LP, typename Res, typename Body, typename... Red, typename R0, typename... Rest>
+void launch_collect(Res& r, const LaunchParams& p, const Body& body, std::tuple<Red&...> reds, R0& r0,
+                    Rest&... rest) {
+  if constexpr (expt::detail::is_reducer<std::decay_t<R0>>::value) {
+    launch_collect<LP>(r, p, body, std::tuple_cat(reds, std::tie(r0)), rest...);
+  } else {
+    static_assert(std::is_same<std::decay_t<R0>, expt::KernelName>::value,
+                  "launch arguments between the params and the body are reducers or names");
+    launch_collect<LP>(r, p, body, reds, rest...);
+  }
+}
+template <typename LP, typename Res, typename Tup, size_t... I>
+void launch_split(Res& r, const LaunchParams& p, Tup&& tup, std::index_sequence<I...>) {
+  constexpr size_t N = std::tuple_size<std::decay_t<Tup>>::value;
+  launch_collect<LP>(r, p, std::get<N - 1>(tup), std::tuple<>(), std::get<I>(tup)...);
+}
+template <typename LP, typename Res, typename... Args>
+void launch_on(Res r, const LaunchParams& p, Args&&... args) {
+  static_assert(sizeof...(Args) >= 1, "launch needs a body");
+  auto bound = bind_resource(r);
+  (void)bound;
+  launch_split<LP>(r, p, std::forward_as_tuple(args...), std::make_index_sequence<sizeof...(Args) - 1>{});
+}
+}  // namespace detail
+
+// launch<POLICY>(params, [names / reducers ...,] body): runs the launch
+// policy's first (host_policy_t) entry on its default resource
+// (launch_core.hpp:249-289).
+template <typename POLICY_LIST, typename... Args>
+void launch(const LaunchParams& p, Args&&... args) {
+  using LP = typename POLICY_LIST::host_policy_t;
+  detail::launch_on<LP>(resources::get_resource<LP>::type::get_default(), p, std::forward<Args>(args)...);
+}
+// launch<POLICY>(place, params, ...): host or device policy chosen at run
+// time (launch_core.hpp:291-337).
+template <typename POLICY_LIST, typename... Args>
+void launch(ExecPlace place, const LaunchParams& p, Args&&... args) {
+  if (place == ExecPlace::HOST) {
+    using LP = typename POLICY_LIST::host_policy_t;
+    detail::launch_on<LP>(resources::get_resource<LP>::type::get_default(), p, std::forward<Args>(args)...);
+  } else if (place == ExecPlace::DEVICE) {
+    using LP = typename POLICY_LIST::device_policy_t;
+    detail::launch_on<LP>(resources::get_resource<LP>::type::get_default(), p, std::forward<Args>(args)...);
+  } else {
+    throw std::runtime_error("launch: unknown ExecPlace");
+  }
+}
+// launch<POLICY>(resource, params, ...): the resource's platform picks the
+// host or the device policy (launch_core.hpp:370-452).
+template <typename POLICY_LIST, typename... Args>
+resources::EventProxy<resources::Resource> launch(resources::Resource res, const LaunchParams& p,
+                                                  Args&&... args) {
+  if (res.get_platform() == resources::Platform::host) {
+    using LP = typename POLICY_LIST::host_policy_t;
+    detail::launch_on<LP>(res, p, std::forward<Args>(args)...);
+  } else {
+    using LP = typename POLICY_LIST::device_policy_t;
+    detail::launch_on<LP>(res, p, std::forward<Args>(args)...);
+  }
+  return resources::EventProxy<resources::Resource>(res);
+}
+
+// Resource for a run-time place (launch_core.hpp:339-369).
+template <typename T, typename U>
+resources::Resource Get_Runtime_Resource(T host_res, U device_res, ExecPlace place) {
+  if (place == ExecPlace::DEVICE) return resources::Resource(device_res);
+  return resources::Resource(host_res);
+}
+template <typename T>
+resources::Resource Get_Host_Resource(T host_res, ExecPlace place) {
+  if (place == ExecPlace::DEVICE) throw std::runtime_error("Get_Host_Resource: device is not enabled");
+  return resources::Resource(host_res);
+}
+
+// ------------------------------------------------------------ View/Layout
+// Row-major layouts and views (util/View.hpp, util/Layout.hpp): the last
+// index has stride one.
+template <size_t DIM, typename IdxT = Index_type, ptrdiff_t StrideOne = ptrdiff_t(DIM) - 1>
+struct Layout {
+  static_assert(StrideOne == ptrdiff_t(DIM) - 1, "only row-major layouts");
+  Index_type sizes[DIM];
+  Index_type strides[DIM];
+  template <typename... Ns>
+  RAJA_HOST_DEVICE Layout(Ns... ns) : sizes{Index_type(ns)...} {
+    static_assert(sizeof...(Ns) == DIM, "one size per dimension");
+    Index_type st = 1;
+    for (size_t d = DIM; d-- > 0;) {
+      strides[d] = st;
+      st *= sizes[d];
+    }
+  }
+  template <typename... Is>
+  RAJA_HOST_DEVICE Index_type operator()(Is... is) const {
+    static_assert(sizeof...(Is) == DIM, "one index per dimension");
+    const Index_type idx[DIM] = {Index_type(is)...};
+    Index_type off = 0;
+    for (size_t d = 0; d < DIM; ++d) off += idx[d] * strides[d];
+    return off;
+  }
+  RAJA_HOST_DEVICE Index_type size() const {
+    Index_type n = 1;
+    for (size_t d = 0; d < DIM; ++d) n *= sizes[d];
+    return n;
+  }
+};
+template <typename T, typename LayoutT>
+struct View {
+  T* data;
+  LayoutT layout;
+  template <typename... Ns>
+  RAJA_HOST_DEVICE View(T* p, Ns... ns) : data(p), layout(ns...) {}
+  RAJA_HOST_DEVICE View(T* p, const LayoutT& l) : data(p), layout(l) {}
+  template <typename... Is>
+  RAJA_HOST_DEVICE T& operator()(Is... is) const {
+    return data[layout(is...)];
+  }
+  RAJA_HOST_DEVICE void set_data(T* p) { data = p; }
+};
 
 // ----------------------------------------------------------------- scans
 // pattern/scan.hpp front-ends.  Back-ends overload scan_inclusive /

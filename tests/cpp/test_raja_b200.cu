@@ -183,7 +183,7 @@ void test_forall_and_params() {
   // expt::Reduce / ReduceLoc params: target = op(target, result)
   double s = 10.0, lo = 1e300, hi = -1e300, vmin = 1e300;
   Index_type imin = -1;
-  RAJA::forall<exec>(RAJA::RangeSegment(0, n), RAJA::expt::Name("expt_reduce"),
+  RAJA::forall<exec>(RAJA::RangeSegment(0, n), RAJA::Name("expt_reduce"),
                      RAJA::expt::Reduce<RAJA::operators::plus>(&s),
                      RAJA::expt::Reduce<RAJA::operators::minimum>(&lo),
                      RAJA::expt::Reduce<RAJA::operators::maximum>(&hi),
@@ -653,6 +653,251 @@ void test_resources() {
   }
 }
 
+// RAJA::launch on the b200 policies (test/functional/launch): nested
+// direct / loop policies over a 6-D View, tile_tcount + loop_icount,
+// dynamic (including > 48 KB) and static team shared memory, reducer
+// params against the host launch, run-time place switch, resources,
+// flattened thread policies and the three segment kinds.
+using dlaunch = RAJA::LaunchPolicy<RAJA::b200_launch_t<false>>;
+using hdlaunch = RAJA::LaunchPolicy<RAJA::seq_launch_t, RAJA::b200_launch_t<false>>;
+template <class P>
+using lp = RAJA::LoopPolicy<RAJA::seq_exec, P>;
+
+template <class TX, class TY, class TZ, class BX, class BY, class BZ>
+void launch_nested_case(const char* tag, int M) {
+  const RAJA::RangeSegment r1(0, 2 * M), r2(0, 3 * M), r3(0, 4 * M), r4(0, 4 * M), r5(0, 5 * M), r6(0, 6 * M);
+  const Index_type N1 = 2 * M, N2 = 3 * M, N3 = 4 * M, N4 = 4 * M, N5 = 5 * M, N6 = 6 * M;
+  const Index_type N = N1 * N2 * N3 * N4 * N5 * N6;
+  Index_type* a = managed<Index_type>(N);
+  for (Index_type i = 0; i < N; ++i) a[i] = 0;
+  RAJA::View<Index_type, RAJA::Layout<6>> Av(a, N6, N5, N4, N3, N2, N1);
+  RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(4, 5, 6), RAJA::Threads(2, 3, 4)),
+                        [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx) {
+    RAJA::loop<BZ>(ctx, r6, [&](Index_type bz) {
+      RAJA::loop<BY>(ctx, r5, [&](Index_type by) {
+        RAJA::loop<BX>(ctx, r4, [&](Index_type bx) {
+          RAJA::loop<TZ>(ctx, r3, [&](Index_type tz) {
+            RAJA::loop<TY>(ctx, r2, [&](Index_type ty) {
+              RAJA::loop<TX>(ctx, r1, [&](Index_type tx) {
+                const Index_type idx = tx + N1 * (ty + N2 * (tz + N3 * (bx + N4 * (by + N5 * bz))));
+                Av(bz, by, bx, tz, ty, tx) += idx;
+              });
+            });
+          });
+        });
+      });
+    });
+  });
+  bool ok = true;
+  for (Index_type i = 0; i < N; ++i) ok = ok && a[i] == i;
+  char nm[96];
+  snprintf(nm, sizeof nm, "launch_nested_%s", tag);
+  CHECK(nm, ok);
+  cudaFree(a);
+}
+
+template <class TEAM, class THREAD>
+void launch_tile_case(const char* tag, int M, int teams, int threads) {
+  constexpr int ts = 4;
+  const int NT = M * ts + 1;
+  int* tt = managed<int>(NT);
+  int* ii = managed<int>(NT);
+  for (int i = 0; i < NT; ++i) tt[i] = ii[i] = -1;
+  const RAJA::RangeSegment r(0, NT);
+  RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(teams), RAJA::Threads(threads)),
+                        [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx) {
+    RAJA::tile_tcount<TEAM>(ctx, ts, r, [&](const RAJA::RangeSegment& tile, Index_type bx) {
+      RAJA::loop_icount<THREAD>(ctx, tile, [&](Index_type tx, Index_type ix) {
+        tt[tx] = int(bx);
+        ii[tx] = int(ix);
+      });
+    });
+  });
+  bool ok = true;
+  for (int i = 0; i < NT; ++i) ok = ok && tt[i] == i / ts && ii[i] == i % ts;
+  char nm[96];
+  snprintf(nm, sizeof nm, "launch_tile_tcount_icount_%s", tag);
+  CHECK(nm, ok);
+  cudaFree(tt);
+  cudaFree(ii);
+}
+
+void launch_shared_case(const char* tag, int teams, int th, int per_thread) {
+  // each team stages `len` longs and ints in dynamic shared memory, then
+  // reads them back reversed after a team barrier
+  const int len = th * per_thread;
+  long* out = managed<long>(size_t(teams) * len);
+  const size_t shm = size_t(len) * (sizeof(long) + sizeof(int));
+  RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(teams), RAJA::Threads(th), shm),
+                        [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx) {
+    RAJA::loop<lp<RAJA::b200_block_x_direct>>(ctx, RAJA::RangeSegment(0, teams), [&](Index_type b) {
+      long* tile = ctx.getSharedMemory<long>(len);
+      int* itile = ctx.getSharedMemory<int>(len);
+      RAJA::loop<lp<RAJA::b200_thread_x_loop>>(ctx, RAJA::RangeSegment(0, len), [&](Index_type t) {
+        itile[t] = int(t);
+        tile[len - t - 1] = len - t - 1 + long(len) * b;
+      });
+      ctx.teamSync();
+      RAJA::loop<lp<RAJA::b200_thread_x_loop>>(ctx, RAJA::RangeSegment(0, len), [&](Index_type t) {
+        out[t + long(len) * b] = tile[t] + itile[t];
+      });
+      ctx.releaseSharedMemory();
+    });
+  });
+  bool ok = true;
+  for (int b = 0; b < teams; ++b)
+    for (int t = 0; t < len; ++t) ok = ok && out[t + long(len) * b] == long(t) + long(len) * b + t;
+  char nm[96];
+  snprintf(nm, sizeof nm, "launch_dynamic_shared_%s", tag);
+  CHECK(nm, ok);
+  cudaFree(out);
+}
+
+void test_launch() {
+  namespace res = RAJA::resources;
+  static_assert(std::is_same<res::get_resource<RAJA::b200_launch_t<true>>::type, res::Cuda>::value, "launch res");
+  launch_nested_case<lp<RAJA::b200_thread_x_direct>, lp<RAJA::b200_thread_y_direct>, lp<RAJA::b200_thread_z_direct>,
+                     lp<RAJA::b200_block_x_direct>, lp<RAJA::b200_block_y_direct>, lp<RAJA::b200_block_z_direct>>(
+      "direct", 1);
+  launch_nested_case<lp<RAJA::b200_thread_x_loop>, lp<RAJA::b200_thread_y_loop>, lp<RAJA::b200_thread_z_loop>,
+                     lp<RAJA::b200_block_x_loop>, lp<RAJA::b200_block_y_loop>, lp<RAJA::b200_block_z_loop>>("loop", 2);
+  launch_tile_case<lp<RAJA::b200_block_x_loop>, lp<RAJA::b200_thread_x_loop>>("loop", 5, 1, 3);
+  launch_tile_case<lp<RAJA::b200_block_x_direct>, lp<RAJA::b200_thread_x_direct>>("direct", 5, 6, 4);
+  launch_shared_case("5x32", 5, 32, 1);
+  launch_shared_case("3x256_96KB", 3, 256, 32);  // 8192 longs + ints: 96 KB of dynamic shared memory
+
+  // static team shared memory (test-launch-StaticMem.hpp)
+  {
+    constexpr int TH = 64;
+    const int teams = 7;
+    int* out = managed<int>(teams * TH);
+    RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(teams), RAJA::Threads(TH)),
+                          [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx) {
+      RAJA::loop<lp<RAJA::b200_block_x_direct>>(ctx, RAJA::RangeSegment(0, teams), [&](Index_type b) {
+        RAJA_TEAM_SHARED int tile[TH];
+        RAJA::loop<lp<RAJA::b200_thread_x_direct>>(ctx, RAJA::RangeSegment(0, TH), [&](Index_type t) {
+          tile[t] = int(t + TH * b);
+        });
+        ctx.teamSync();
+        RAJA::loop<lp<RAJA::b200_thread_x_direct>>(ctx, RAJA::RangeSegment(0, TH), [&](Index_type t) {
+          out[t + TH * b] = tile[TH - 1 - t];
+        });
+      });
+    });
+    bool ok = true;
+    for (int b = 0; b < teams; ++b)
+      for (int t = 0; t < TH; ++t) ok = ok && out[t + TH * b] == TH - 1 - t + TH * b;
+    CHECK("launch_static_shared", ok);
+    cudaFree(out);
+  }
+
+  // reducer params (test-launch-basic-param-expt-Reduce*.hpp): device
+  // against host through the run-time place switch
+  {
+    const int n = 1000003;
+    double* x = managed<double>(n);
+    int* bits = managed<int>(n);
+    std::mt19937 rng(11);
+    for (int i = 0; i < n; ++i) {
+      x[i] = double(int(rng() % 100));
+      bits[i] = int(rng()) | 0x11;
+    }
+    x[777777] = -5.0;
+    x[999999] = -5.0;
+    const int threads = 256, blocks = (n - 1) / threads + 1;
+    using VS = RAJA::expt::ValOp<double, RAJA::operators::plus>;
+    using VM = RAJA::expt::ValOp<double, RAJA::operators::minimum>;
+    using VX = RAJA::expt::ValOp<double, RAJA::operators::maximum>;
+    using VA = RAJA::expt::ValOp<int, RAJA::operators::bit_and>;
+    using VL = RAJA::expt::ValOp<RAJA::expt::ValLoc<double, Index_type>, RAJA::operators::minimum>;
+    struct R {
+      double sum, sum2, mn, mx;
+      int band;
+      double lv;
+      Index_type li;
+    } got[2];
+    const RAJA::ExecPlace places[2] = {RAJA::ExecPlace::DEVICE, RAJA::ExecPlace::HOST};
+    for (int k = 0; k < 2; ++k) {
+      R& r = got[k];
+      r = R{0.0, 2.0, 1e300, -1e300, -1, 1e300, -1};
+      RAJA::launch<hdlaunch>(
+          places[k], RAJA::LaunchParams(RAJA::Teams(blocks), RAJA::Threads(threads)),
+          RAJA::expt::Reduce<RAJA::operators::plus>(&r.sum), RAJA::expt::Reduce<RAJA::operators::plus>(&r.sum2),
+          RAJA::Name("LaunchReduceParams"), RAJA::expt::Reduce<RAJA::operators::minimum>(&r.mn),
+          RAJA::expt::Reduce<RAJA::operators::maximum>(&r.mx), RAJA::expt::Reduce<RAJA::operators::bit_and>(&r.band),
+          RAJA::expt::ReduceLoc<RAJA::operators::minimum>(&r.lv, &r.li),
+          [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx, VS & s, VS & s2, VM & m, VX & M, VA & a, VL & l) {
+            RAJA::loop<lp<RAJA::b200_global_thread_x>>(ctx, RAJA::RangeSegment(0, n), [&](Index_type i) {
+              s += x[i];
+              s2 += x[i];
+              m.min(x[i]);
+              M.max(x[i]);
+              a &= bits[i];
+              l.minloc(x[i], i);
+            });
+          });
+    }
+    const R& d = got[0];
+    const R& h = got[1];
+    CHECK("launch_reduce_params_vs_host", d.sum == h.sum && d.sum2 == h.sum + 2.0 && d.mn == h.mn && d.mx == h.mx &&
+                                              d.band == h.band && d.lv == -5.0 && d.li == 777777 && h.li == 777777);
+    // two launches accumulate into one target; fewer teams than needed with a loop policy
+    double s = 0.0;
+    for (int j = 0; j < 2; ++j)
+      RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(37), RAJA::Threads(128)),
+                            RAJA::expt::Reduce<RAJA::operators::plus>(&s),
+                            [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx, VS & v) {
+                              RAJA::loop<lp<RAJA::b200_global_x_loop>>(ctx, RAJA::RangeSegment(0, n),
+                                                                       [&](Index_type i) { v += x[i]; });
+                            });
+    CHECK("launch_reduce_two_loops", s == 2.0 * h.sum);
+    // a captured ReduceSum<b200_reduce> and a MultiReduce in a 2-D launch
+    RAJA::ReduceSum<red, double> rs(0.0);
+    RAJA::MultiReduceSum<RAJA::b200_multi_reduce, int> hist(4);
+    RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(19), RAJA::Threads(16, 8)),
+                          [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx) {
+      RAJA::tile<lp<RAJA::b200_block_x_loop>>(ctx, 4096, RAJA::RangeSegment(0, n), [&](const RAJA::RangeSegment& t) {
+        RAJA::loop<lp<RAJA::b200_flatten_block_threads_xy_loop>>(ctx, t, [&](Index_type i) {
+          rs += x[i];
+          hist[int(i & 3)] += 1;
+        });
+      });
+    });
+    int hb[4];
+    for (int b = 0; b < 4; ++b) hb[b] = hist.get(b);
+    CHECK("launch_captured_reducers_2d_flatten",
+          rs.get() == h.sum && hb[0] + hb[1] + hb[2] + hb[3] == n && hb[3] == n / 4);
+    cudaFree(x);
+    cudaFree(bits);
+  }
+
+  // resources: launch on a Resource returns an event; strided and list segments
+  {
+    const int n = 4099;
+    res::Cuda dev;
+    int* a = dev.allocate<int>(n, res::MemoryAccess::Managed);
+    Index_type* lst = dev.allocate<Index_type>(3, res::MemoryAccess::Managed);
+    lst[0] = 4098;  // even indices: the strided loop writes the odd ones
+    lst[1] = 8;
+    lst[2] = 0;
+    for (int i = 0; i < n; ++i) a[i] = 0;
+    res::Event e = RAJA::launch<RAJA::LaunchPolicy<RAJA::seq_launch_t, RAJA::b200_launch_t<true, 256>>>(
+        res::Resource{dev}, RAJA::LaunchParams(RAJA::Teams(8), RAJA::Threads(256)),
+        [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx) {
+          RAJA::loop<lp<RAJA::b200_global_x_loop>>(ctx, RAJA::RangeStrideSegment(1, n, 2),
+                                                   [&](Index_type i) { a[i] = int(i); });
+          RAJA::loop<lp<RAJA::b200_global_x_direct>>(ctx, RAJA::ListSegment(lst, 3),
+                                                     [&](Index_type i) { a[i] = -1; });
+        });
+    e.wait();
+    bool ok = e.try_get<res::CudaEvent>() != nullptr;
+    for (int i = 0; i < n; ++i) ok = ok && a[i] == ((i == 4098 || i == 8 || i == 0) ? -1 : (i & 1 ? i : 0));
+    CHECK("launch_resource_stride_list_segments", ok);
+    dev.deallocate(a);
+    dev.deallocate(lst);
+  }
+}
+
 int main() {
   test_multi_reduce_and_atomics();
   test_reducers();
@@ -662,6 +907,7 @@ int main() {
   workgroup_case<RAJA::unordered>("unordered");
   workgroup_case<RAJA::ordered>("ordered");
   test_resources();
+  test_launch();
   printf("%d failures\n", g_fail);
   return g_fail;
 }

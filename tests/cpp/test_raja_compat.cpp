@@ -80,9 +80,9 @@ int main() {
   CHECK("expt_reduce_host", t == 46.0);
   // kernel names may sit before, between or after the reducer params
   double t1 = 0.0, t2 = 100.0;
-  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 10), RAJA::expt::Name("a"),
-                               RAJA::expt::Reduce<RAJA::operators::plus>(&t1), RAJA::expt::Name("b"),
-                               RAJA::expt::Reduce<RAJA::operators::minimum>(&t2), RAJA::expt::Name("c"),
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 10), RAJA::Name("a"),
+                               RAJA::expt::Reduce<RAJA::operators::plus>(&t1), RAJA::Name("b"),
+                               RAJA::expt::Reduce<RAJA::operators::minimum>(&t2), RAJA::Name("c"),
                                [=](Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& s,
                                    RAJA::expt::ValOp<double, RAJA::operators::minimum>& m) {
                                  s += double(i);
@@ -90,7 +90,7 @@ int main() {
                                });
   CHECK("expt_reduce_names_anywhere", t1 == 45.0 && t2 == 3.0);
   int named = 0;
-  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 4), RAJA::expt::Name("only"),
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 4), RAJA::Name("only"),
                                [&](Index_type) { ++named; });
   CHECK("forall_name_only", named == 4);
   // WorkGroup (ordered): a[i] += i + 5 (test-workgroup-Unordered-Single.hpp)
@@ -205,6 +205,95 @@ int main() {
     host.deallocate(h);
     er.deallocate(g);
     CHECK("resources_host", okr);
+  }
+  // RAJA::launch on the host (test/functional/launch): nested loops over a
+  // View, dynamic shared memory with teamSync, tile_tcount + loop_icount,
+  // reducer params, run-time place and a resource
+  {
+    using lpol = RAJA::LaunchPolicy<RAJA::seq_launch_t>;
+    using loop = RAJA::LoopPolicy<RAJA::seq_exec>;
+    const int N1 = 2, N2 = 3, N3 = 4;
+    std::vector<int> a3(N1 * N2 * N3, 0);
+    RAJA::View<int, RAJA::Layout<3>> A(a3.data(), N3, N2, N1);
+    RAJA::launch<lpol>(RAJA::LaunchParams(RAJA::Teams(N3), RAJA::Threads(N2, N1)), [=](RAJA::LaunchContext ctx) {
+      RAJA::loop<loop>(ctx, RAJA::RangeSegment(0, N3), [&](Index_type z) {
+        RAJA::loop<loop>(ctx, RAJA::RangeSegment(0, N2), [&](Index_type y) {
+          RAJA::loop<loop>(ctx, RAJA::RangeSegment(0, N1), [&](Index_type x) {
+            A(z, y, x) += int(x + N1 * (y + N2 * z));
+          });
+        });
+      });
+    });
+    bool okl = true;
+    for (int i = 0; i < N1 * N2 * N3; ++i) okl = okl && a3[i] == i;
+    CHECK("launch_seq_nested_view", okl);
+
+    // dynamic shared memory: a reversed tile plus an int tile per team
+    const int teams = 5, th = 32;
+    std::vector<long> out(teams * th, 0);
+    long* op = out.data();
+    RAJA::launch<lpol>(RAJA::LaunchParams(RAJA::Teams(teams), RAJA::Threads(th), th * (sizeof(long) + sizeof(int))),
+                       [=](RAJA::LaunchContext ctx) {
+                         RAJA::loop<loop>(ctx, RAJA::RangeSegment(0, teams), [&](Index_type b) {
+                           long* tile = ctx.getSharedMemory<long>(th);
+                           int* itile = ctx.getSharedMemory<int>(th);
+                           RAJA::loop<loop>(ctx, RAJA::RangeSegment(0, th), [&](Index_type t) {
+                             itile[t] = int(t);
+                             tile[th - t - 1] = th - t - 1 + th * b;
+                           });
+                           ctx.teamSync();
+                           RAJA::loop<loop>(ctx, RAJA::RangeSegment(0, th), [&](Index_type t) {
+                             op[t + th * b] = tile[t] + itile[t];
+                           });
+                           ctx.releaseSharedMemory();
+                         });
+                       });
+    okl = true;
+    for (int b = 0; b < teams; ++b)
+      for (int t = 0; t < th; ++t) okl = okl && out[t + th * b] == long(t + th * b) + t;
+    CHECK("launch_seq_shared_mem", okl);
+
+    // tile_tcount + loop_icount: tile size 4 over 0..4M (test-launch-nested-Tile-iCount-tCount-Loop.hpp)
+    const int M = 5, ts = 4, NT = M * ts + 1;
+    std::vector<int> tt(NT, -1), ii(NT, -1);
+    int* ttp = tt.data();
+    int* iip = ii.data();
+    RAJA::launch<lpol>(RAJA::LaunchParams(RAJA::Teams(1), RAJA::Threads(3)), [=](RAJA::LaunchContext ctx) {
+      RAJA::tile_tcount<loop>(ctx, ts, RAJA::RangeSegment(0, NT), [&](const RAJA::RangeSegment& tile, Index_type bx) {
+        RAJA::loop_icount<loop>(ctx, tile, [&](Index_type tx, Index_type ix) {
+          ttp[tx] = int(bx);
+          iip[tx] = int(ix);
+        });
+      });
+    });
+    okl = true;
+    for (int i = 0; i < NT; ++i) okl = okl && tt[i] == i / ts && ii[i] == i % ts;
+    CHECK("launch_seq_tile_tcount_icount", okl);
+
+    // reducer params and a kernel name, run-time place, resource
+    double s = 2.0;
+    int mn = 1000;
+    RAJA::launch<RAJA::LaunchPolicy<RAJA::seq_launch_t, RAJA::seq_launch_t>>(
+        RAJA::ExecPlace::HOST, RAJA::LaunchParams(RAJA::Teams(4), RAJA::Threads(64)),
+        RAJA::expt::Reduce<RAJA::operators::plus>(&s), RAJA::Name("launch_reduce"),
+        RAJA::expt::Reduce<RAJA::operators::minimum>(&mn),
+        [=](RAJA::LaunchContext ctx, RAJA::expt::ValOp<double, RAJA::operators::plus>& vs,
+            RAJA::expt::ValOp<int, RAJA::operators::minimum>& vm) {
+          RAJA::loop<loop>(ctx, RAJA::RangeStrideSegment(0, 100, 3), [&](Index_type i) {
+            vs += double(i);
+            vm.min(int(i) + 7);
+          });
+        });
+    CHECK("launch_seq_reduce_params", s == 2.0 + 1683.0 && mn == 7);
+    RAJA::resources::Host host;
+    RAJA::resources::Event le = RAJA::launch<lpol>(
+        RAJA::resources::Resource{host}, RAJA::LaunchParams(RAJA::Teams(1), RAJA::Threads(1)),
+        [=](RAJA::LaunchContext ctx) {
+          const Index_type idx[3] = {5, 1, 3};
+          RAJA::loop<loop>(ctx, RAJA::ListSegment(idx, 3), [&](Index_type i) { op[i] = -1; });
+        });
+    le.wait();
+    CHECK("launch_seq_resource_list_segment", out[5] == -1 && out[1] == -1 && out[3] == -1 && out[2] != -1);
   }
   printf("%d failures\n", g_fail);
   return g_fail;
