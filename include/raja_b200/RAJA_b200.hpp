@@ -97,6 +97,7 @@ struct LaunchCtx {
   bool active = false;
   unsigned grid = 0;
   cudaStream_t stream = nullptr;
+  unsigned long long launch_id = 0;  // new for every launch copy
 };
 inline LaunchCtx& ctx() {
   static thread_local LaunchCtx c;
@@ -149,7 +150,9 @@ __device__ inline T warp_fold(T v, int lane, int valid, int present, Merge merge
 
 template <class T, class Merge>
 __device__ inline T block_reduce(T v, Merge merge) {
-  __shared__ unsigned char sh_raw[32 * sizeof(T) + 16];
+  static_assert(alignof(T) <= 16, "reducer values are aligned to at most 16 bytes");
+  // typed views of byte buffers need the alignment of T (values up to 16 B)
+  __shared__ __align__(16) unsigned char sh_raw[32 * sizeof(T) + 16];
   T* sh = reinterpret_cast<T*>(sh_raw);
   const int tid = int(lin_tid()), nt = int(lin_nthreads());
   const int lane = tid & 31, warp = tid >> 5, nw = (nt + 31) >> 5;
@@ -203,7 +206,7 @@ __device__ inline void grid_combine(const DevSlot<T>& s, T v, Merge merge) {
     const T p = ld_cg(s.partials + b);
     r = b == tid ? p : merge(r, p);
   }
-  __shared__ unsigned char fin_raw[32 * sizeof(T) + 16];
+  __shared__ __align__(16) unsigned char fin_raw[32 * sizeof(T) + 16];
   T* fin = reinterpret_cast<T*>(fin_raw);
   const int lane = int(tid & 31), warp = int(tid >> 5);
   const int holders = int(nb < nt ? nb : nt);
@@ -313,6 +316,11 @@ class DevReducer {
   struct Shared {
     V init;
     std::vector<Pending> pending;
+    // The slot of the launch being copied: copying a __host__ __device__
+    // lambda's closure copy-constructs its captures more than once, and
+    // every such copy of one launch must share one slot.
+    unsigned long long slot_launch = 0;
+    DevSlot<V> slot{nullptr, nullptr, nullptr};
   };
   Shared* shared_ = nullptr;
   bool original_ = false;
@@ -333,9 +341,13 @@ class DevReducer {
     shared_ = o.shared_;
     LaunchCtx& c = ctx();
     if (c.active && !o.launch_copy_) {
-      void* block = nullptr;
-      slot_ = alloc_slot<V>(c.grid, c.stream, &block);
-      shared_->pending.push_back(Pending{block, slot_.result, c.stream});
+      if (shared_->slot_launch != c.launch_id) {
+        void* block = nullptr;
+        shared_->slot = alloc_slot<V>(c.grid, c.stream, &block);
+        shared_->slot_launch = c.launch_id;
+        shared_->pending.push_back(Pending{block, shared_->slot.result, c.stream});
+      }
+      slot_ = shared_->slot;
       launch_copy_ = true;
     } else {
       slot_ = o.slot_;
@@ -536,6 +548,7 @@ struct LaunchCopy {
     c.active = true;
     c.grid = grid;
     c.stream = s;
+    ++c.launch_id;
     try {
       Body copy(b);
       c.active = false;

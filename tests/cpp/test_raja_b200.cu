@@ -865,8 +865,29 @@ void test_launch() {
     });
     int hb[4];
     for (int b = 0; b < 4; ++b) hb[b] = hist.get(b);
-    CHECK("launch_captured_reducers_2d_flatten",
-          rs.get() == h.sum && hb[0] + hb[1] + hb[2] + hb[3] == n && hb[3] == n / 4);
+    const double rsv = rs.get();
+    printf("captured 2d: rs %.1f (host %.1f) hist %d %d %d %d\n", rsv, h.sum, hb[0], hb[1], hb[2], hb[3]);
+    CHECK("launch_captured_reducesum_2d_flatten", rsv == h.sum);
+    CHECK("launch_captured_multireduce_2d_flatten", hb[0] + hb[1] + hb[2] + hb[3] == n && hb[3] == n / 4);
+    // the same captured reducer with 1-D teams of threads
+    RAJA::ReduceSum<red, double> rs1(0.0);
+    RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(23), RAJA::Threads(128)),
+                          [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx) {
+      RAJA::loop<lp<RAJA::b200_global_x_loop>>(ctx, RAJA::RangeSegment(0, n), [&](Index_type i) { rs1 += x[i]; });
+    });
+    const double rs1v = rs1.get();
+    printf("captured 1d: rs %.1f (host %.1f)\n", rs1v, h.sum);
+    CHECK("launch_captured_reducesum_1d", rs1v == h.sum);
+    // forall with a __host__ __device__ body: its closure copies the
+    // captured reducer more than once on the host, still one result per launch
+    RAJA::ReduceSum<red, double> rs2(1.0);
+    RAJA::ReduceMinLoc<red, double, Index_type> ml2(1e300, -1);
+    for (int j = 0; j < 2; ++j)
+      RAJA::forall<exec>(RAJA::RangeSegment(0, n), [=] RAJA_HOST_DEVICE(Index_type i) {
+        rs2 += x[i];
+        ml2.minloc(x[i], i);
+      });
+    CHECK("forall_hd_lambda_reducers", rs2.get() == 1.0 + 2.0 * h.sum && ml2.get() == -5.0 && ml2.getLoc() == 777777);
     cudaFree(x);
     cudaFree(bits);
   }
@@ -899,6 +920,7 @@ void test_launch() {
 }
 
 int main() {
+  setvbuf(stdout, nullptr, _IONBF, 0);  // every PASS line reaches the log even if the run aborts
   test_multi_reduce_and_atomics();
   test_reducers();
   test_forall_and_params();
