@@ -13,7 +13,7 @@
 //      every 8-bit digit position at once (per-warp shared counters); it
 //      also zeroes the first pass's look-back status words;
 //   2. bins_kernel: exclusive scan of each histogram -> global digit bases;
-//   3. one onesweep_kernel per digit: a tile of 256 threads x 24-28 keys is
+//   3. one onesweep_kernel per digit: a tile of 384 threads x 16-24 keys is
 //      loaded with coalesced warp-striped reads, ranked in registers with a
 //      warp-level multisplit built from eight ballots per key (on this GPU
 //      __match_any_sync costs ~80 cycles per warp, the ballots a few), its
@@ -37,17 +37,23 @@
 namespace b200 {
 namespace {
 
-constexpr int RB = 256;       // threads per tile
-// Keys per thread of a onesweep tile, by shape (measured on GB300 at 2^28:
-// 28 is best for 32-bit keys alone, 24 for 64-bit keys and for pairs;
-// 16, 20 and 32 are slower).
-template <class K, bool HAS_V>
-struct SweepShape {
-  static constexpr int KPT = (sizeof(K) == 4 && !HAS_V) ? 28 : 24;
-  static constexpr int TILE = RB * KPT;
-};
+constexpr int RB = 256;       // threads per block of the histogram kernel
 constexpr int RADIX = 256;
 constexpr int WARPS = RB / 32;
+// Threads and keys per thread of a onesweep tile, by shape, measured on
+// GB300 at 2^28: 384 threads with 24 keys each for 32-bit keys alone (9216
+// per tile) and 16 each otherwise (6144 per tile, three blocks per SM for
+// 64-bit keys).  256 threads x 28 / 24 keys is 1% slower for 64-bit keys
+// and pairs; 512 threads leave two blocks per SM and are 20% slower.  The
+// first RADIX threads own one digit each in the per-digit phase.
+template <class K, bool HAS_V>
+struct SweepShape {
+  static constexpr int RB = 384;
+  static constexpr int WARPS = RB / 32;
+  static constexpr int KPT = (sizeof(K) == 4 && !HAS_V) ? 24 : 16;
+  static constexpr int TILE = RB * KPT;
+  static_assert(RB >= RADIX && RB % 32 == 0 && KPT % 4 == 0, "whole digit warps, four digits per register");
+};
 
 template <class K>
 struct KeyBits {
@@ -224,24 +230,25 @@ struct SweepSmem {
   alignas(128) K kin[TILE];                       // the tile as loaded (TMA)
   alignas(128) V vin[HAS_V ? TILE : 1];
   uint16_t idx[TILE];                             // tile position of the i-th key in digit order
-  uint32_t wcnt[WARPS][RADIX];                    // per-warp digit counts, then running starts
+  uint32_t wcnt[SweepShape<K, HAS_V>::WARPS][RADIX];  // per-warp digit counts, then running starts
   ST gdst[RADIX];                                 // global dst = gdst[d] + local position
-  uint32_t wtot[WARPS];
+  uint32_t wtot[RADIX / 32];
   uint64_t bar;
   uint32_t tile;
 };
 
 // Blocks per SM the shared memory allows (228 KB per SM, 1 KB reserved per
-// block), at most five (48 registers, no spills); the register budget is
-// cut to match.
+// block), at most five and at most 2048 threads (48 registers, no spills);
+// the register budget is cut to match.
 template <class K, class V, bool HAS_V, class ST>
 constexpr int sweep_min_blocks() {
   constexpr int b = 233472 / int(sizeof(SweepSmem<K, V, HAS_V, ST>) + 1024);
-  return b < 1 ? 1 : (b > 5 ? 5 : b);
+  constexpr int cap = 2048 / SweepShape<K, HAS_V>::RB < 5 ? 2048 / SweepShape<K, HAS_V>::RB : 5;
+  return b < 1 ? 1 : (b > cap ? cap : b);
 }
 
 template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST>
-__global__ void __launch_bounds__(RB, (sweep_min_blocks<K, V, HAS_V, ST>()))
+__global__ void __launch_bounds__(SweepShape<K, HAS_V>::RB, (sweep_min_blocks<K, V, HAS_V, ST>()))
 onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __restrict__ vin,
                 V* __restrict__ vout, size_t n, int shift, int desc,
                 const uint32_t* __restrict__ bins, ST* __restrict__ status,
@@ -251,11 +258,13 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   using U = typename KB::U;
   using S = Status<ST>;
   constexpr int KPT = SweepShape<K, HAS_V>::KPT, TILE = SweepShape<K, HAS_V>::TILE;
+  constexpr int SRB = SweepShape<K, HAS_V>::RB, SW = SweepShape<K, HAS_V>::WARPS;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SweepSmem<K, V, HAS_V, ST>& sm = *reinterpret_cast<SweepSmem<K, V, HAS_V, ST>*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool downer = SRB == RADIX || tid < RADIX;  // owns digit tid in the per-digit phase
 #pragma unroll
-  for (int w = 0; w < WARPS; ++w) sm.wcnt[w][tid] = 0;
+  for (int i = tid; i < SW * RADIX; i += SRB) (&sm.wcnt[0][0])[i] = 0;
   if (tid == 0) {
     sm.tile = atomicAdd(tile_counter, 1u);
     mbar_init(&sm.bar, 1);
@@ -280,14 +289,14 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   } else {
     // partial (last) tile: padding keys sort after every real key
     const K padk = FIRST ? KB::pad(desc != 0) : KB::cook(~U(0));
-    for (int e = tid; e < TILE; e += RB) {
+    for (int e = tid; e < TILE; e += SRB) {
       sm.kin[e] = (e < lim) ? kin[tbase + e] : padk;
       if (HAS_V && e < lim) sm.vin[e] = vin[tbase + e];
     }
     __syncthreads();
   }
   // this tile's row of the next pass's status words starts at zero
-  if (!LAST) status_next[tile * RADIX + tid] = ST(0);
+  if (!LAST && downer) status_next[tile * RADIX + tid] = ST(0);
 
   // key e of the tile in order-preserving form (padding is all ones)
   auto ukey = [&](int e) -> U {
@@ -315,35 +324,39 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   }
   __syncthreads();
 
-  // ---- per-digit counts: thread d owns digit d
-  const int d = tid;
-  uint32_t cnt = 0;
-#pragma unroll
-  for (int w = 0; w < WARPS; ++w) {
-    const uint32_t c = sm.wcnt[w][d];
-    sm.wcnt[w][d] = cnt;  // exclusive offset of warp w inside digit d
-    cnt += c;
-  }
+  // ---- per-digit counts: thread d < RADIX owns digit d (whole warps, so
+  // the shuffles below see full warps)
+  const int d = downer ? tid : 0;
+  uint32_t cnt = 0, inc = 0;
   ST* my_status = status + tile * RADIX + d;
-  if (tile == 0) st_relaxed(my_status, ST(S::INCL | (ST(bins[d]) + cnt)));
-  else st_relaxed(my_status, ST(S::AGG | ST(cnt)));
-
-  // block exclusive scan of the counts -> local digit starts
-  uint32_t inc = cnt;
+  if (downer) {
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += t;
+    for (int w = 0; w < SW; ++w) {
+      const uint32_t c = sm.wcnt[w][d];
+      sm.wcnt[w][d] = cnt;  // exclusive offset of warp w inside digit d
+      cnt += c;
+    }
+    if (tile == 0) st_relaxed(my_status, ST(S::INCL | (ST(bins[d]) + cnt)));
+    else st_relaxed(my_status, ST(S::AGG | ST(cnt)));
+
+    // block exclusive scan of the counts -> local digit starts
+    inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) sm.wtot[warp] = inc;
   }
-  if (lane == 31) sm.wtot[warp] = inc;
   __syncthreads();
   uint32_t lstart = inc - cnt;
+  if (downer) {
 #pragma unroll
-  for (int w = 0; w < WARPS - 1; ++w)
-    if (w < warp) lstart += sm.wtot[w];
+    for (int w = 0; w < RADIX / 32 - 1; ++w)
+      if (w < warp) lstart += sm.wtot[w];
 #pragma unroll
-  for (int w = 0; w < WARPS; ++w) sm.wcnt[w][d] += lstart;  // tile-local start of (warp, digit)
-
+    for (int w = 0; w < SW; ++w) sm.wcnt[w][d] += lstart;  // tile-local start of (warp, digit)
+  }
   __syncthreads();
 
   // ---- warp-level multisplit ranking, scattered straight into digit order
@@ -374,8 +387,9 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   // loads of one window are independent, then consumed in order until an
   // inclusive count is found.  A not-yet-published tile stops the
   // consumption; the wait is bounded.
-  ST gstart;
-  if (tile == 0) {
+  ST gstart = 0;
+  if (!downer) {
+  } else if (tile == 0) {
     gstart = ST(bins[d]);
   } else {
     constexpr int LBW = 8;
@@ -410,7 +424,7 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
     gstart = acc;
     st_relaxed(my_status, ST(S::INCL | (acc + cnt)));
   }
-  sm.gdst[d] = gstart - ST(lstart);
+  if (downer) sm.gdst[d] = gstart - ST(lstart);
   __syncthreads();
 
   // ---- write out in runs (one digit's run is contiguous in global): the
@@ -419,7 +433,7 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   // key's destination lies in [0, n).
 #pragma unroll
   for (int j = 0; j < KPT; ++j) {
-    const int i = j * RB + tid;
+    const int i = j * SRB + tid;
     const int e = sm.idx[i];
     if (e < lim) {
       const U uk = ukey(e);
@@ -449,7 +463,8 @@ int launch_sweep_t(const char* name, size_t tiles, cudaStream_t s, const K* src,
     B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(SM))));
     attr = true;
   }
-  B200_LAUNCH(name, kern, (unsigned)tiles, RB, sizeof(SM), s, src, dst, vsrc, vdst, n, shift, desc,
+  constexpr int threads = SweepShape<K, HAS_V>::RB;
+  B200_LAUNCH(name, kern, (unsigned)tiles, threads, sizeof(SM), s, src, dst, vsrc, vdst, n, shift, desc,
               bins, status, status_next, counter, err, lim, tma_ok);
   return B200_OK;
 }

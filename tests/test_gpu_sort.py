@@ -11,8 +11,8 @@ from conftest import to_dev, to_host
 pytestmark = pytest.mark.gpu
 
 G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-# tiles hold 7168 keys for 32-bit keys alone (256 threads x 28), 6144 otherwise
-SIZES = [0, 1, 2, 3, 100, 4097, 6143, 6144, 6145, 7167, 7168, 7169, 14337, 100003,
+# tiles hold 9216 keys for 32-bit keys alone (384 threads x 24), 6144 otherwise
+SIZES = [0, 1, 2, 3, 100, 4097, 6143, 6144, 6145, 9215, 9216, 9217, 12289, 18433, 100003,
          (1 << 20) + 5]
 
 
