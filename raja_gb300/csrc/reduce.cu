@@ -292,9 +292,10 @@ struct Extremum {
 // operator<).  NaNs are skipped (operator< never selects them): a chunk is
 // tested once for an all-ones exponent, and only chunks holding an
 // infinity or a NaN take the per-element test.  Per thread only the key
-// and the index are carried; the value's own bits are read back from the
-// input at the index once, when the thread's result becomes a partial, so
-// -0.0 keeps its sign.  Ties resolve to the lowest index as above.
+// and the index are carried; the value's bits are rebuilt from the key when
+// the thread's result becomes a partial, except for a zero winner, whose
+// bits are read back from the input so that -0.0 keeps its sign.  Ties
+// resolve to the lowest index as above.
 template <bool MIN, bool WITH_LOC>
 struct ExtremumF64 {
   using T = double;
@@ -356,8 +357,15 @@ struct ExtremumF64 {
         if (better(key, a.key)) { a.key = key; a.i = (long long)(e0 + j * stride + k); }
       }
   }
+  // The bits of the winner from its key: key_of is one-to-one except that
+  // +0.0 and -0.0 both map to key 0, so only a zero winner is read back
+  // from the input (to keep its sign).
+  static __device__ __forceinline__ long long bits_of_key(long long k) {
+    return k >= 0 ? k : ((k - 1) ^ 0x7fffffffffffffffll);
+  }
   static __device__ Part to_part_x(Acc a, const double* x) {
-    return {a.key, a.i, a.i >= 0 ? __double_as_longlong(x[a.i]) : ident_bits()};
+    if (a.i < 0) return {a.key, a.i, ident_bits()};
+    return {a.key, a.i, a.key != 0 ? bits_of_key(a.key) : __double_as_longlong(x[a.i])};
   }
   static __device__ Part part_identity() { return {key_of(ident_bits()), -1, ident_bits()}; }
   static __device__ Part merge_part(Part a, Part b) {
