@@ -27,6 +27,7 @@
 #pragma once
 
 #include <algorithm>
+#include <array>
 #include <cstddef>
 #include <cstdint>
 #include <cstdlib>
@@ -1201,9 +1202,17 @@ struct Layout {
   static_assert(StrideOne == ptrdiff_t(DIM) - 1, "only row-major layouts");
   Index_type sizes[DIM];
   Index_type strides[DIM];
-  template <typename... Ns>
+  template <typename... Ns, typename std::enable_if<sizeof...(Ns) == DIM &&
+                                                        (std::is_integral<Ns>::value && ...),
+                                                    int>::type = 0>
   RAJA_HOST_DEVICE Layout(Ns... ns) : sizes{Index_type(ns)...} {
-    static_assert(sizeof...(Ns) == DIM, "one size per dimension");
+    set_strides();
+  }
+  explicit Layout(const std::array<Index_type, DIM>& s) {
+    for (size_t d = 0; d < DIM; ++d) sizes[d] = s[d];
+    set_strides();
+  }
+  RAJA_HOST_DEVICE void set_strides() {
     Index_type st = 1;
     for (size_t d = DIM; d-- > 0;) {
       strides[d] = st;
@@ -1224,11 +1233,46 @@ struct Layout {
     return n;
   }
 };
+// Offset layouts (util/OffsetLayout.hpp:40-244): dimension d runs over
+// [begin[d], end[d]), stored row-major from begin.
+template <size_t DIM, typename IdxT = Index_type>
+struct OffsetLayout {
+  Layout<DIM, IdxT> base;
+  Index_type offsets[DIM];
+  OffsetLayout(const std::array<Index_type, DIM>& begin, const std::array<Index_type, DIM>& end)
+      : base(sizes_of(begin, end)) {
+    for (size_t d = 0; d < DIM; ++d) offsets[d] = begin[d];
+  }
+  template <typename... Is>
+  RAJA_HOST_DEVICE Index_type operator()(Is... is) const {
+    static_assert(sizeof...(Is) == DIM, "one index per dimension");
+    const Index_type idx[DIM] = {Index_type(is)...};
+    Index_type off = 0;
+    for (size_t d = 0; d < DIM; ++d) off += (idx[d] - offsets[d]) * base.strides[d];
+    return off;
+  }
+  RAJA_HOST_DEVICE Index_type size() const { return base.size(); }
+
+ private:
+  static std::array<Index_type, DIM> sizes_of(const std::array<Index_type, DIM>& b,
+                                               const std::array<Index_type, DIM>& e) {
+    std::array<Index_type, DIM> s{};
+    for (size_t d = 0; d < DIM; ++d) s[d] = e[d] - b[d];
+    return s;
+  }
+};
+template <size_t DIM, typename IdxT = Index_type>
+OffsetLayout<DIM, IdxT> make_offset_layout(const std::array<Index_type, DIM>& begin,
+                                           const std::array<Index_type, DIM>& end) {
+  return OffsetLayout<DIM, IdxT>(begin, end);
+}
+
 template <typename T, typename LayoutT>
 struct View {
   T* data;
   LayoutT layout;
-  template <typename... Ns>
+  template <typename... Ns,
+            typename std::enable_if<(sizeof...(Ns) > 0) && (std::is_integral<Ns>::value && ...), int>::type = 0>
   RAJA_HOST_DEVICE View(T* p, Ns... ns) : data(p), layout(ns...) {}
   RAJA_HOST_DEVICE View(T* p, const LayoutT& l) : data(p), layout(l) {}
   template <typename... Is>

@@ -919,6 +919,90 @@ void test_launch() {
   }
 }
 
+// 7-point Jacobi through RAJA::launch over Views with an OffsetLayout
+// (interior [0, N), halo at -1 and N), max residual by an expt::Reduce
+// param: the device launch against the same body run by the host launch,
+// bit-exact, over several sweeps.  The operation order follows the oracle's
+// sweep: ((x pair) + (y pair)) + (z pair), then * (1/6); the product and
+// the residual's difference are rounded separately on both sides.
+RAJA_HOST_DEVICE inline double mul_rn(double a, double b) {
+#if defined(__CUDA_ARCH__)
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+RAJA_HOST_DEVICE inline double sub_rn(double a, double b) {
+#if defined(__CUDA_ARCH__)
+  return __dsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+
+double jacobi_launch(RAJA::ExecPlace place, int Nx, int Ny, int Nz, double* u, double* unew) {
+  using pol = RAJA::LaunchPolicy<RAJA::seq_launch_t, RAJA::b200_launch_t<false>>;
+  using kpol = RAJA::LoopPolicy<RAJA::seq_exec, RAJA::b200_block_x_direct>;
+  using jtile = RAJA::LoopPolicy<RAJA::seq_exec, RAJA::b200_block_y_direct>;
+  using jpol = RAJA::LoopPolicy<RAJA::seq_exec, RAJA::b200_thread_y_direct>;
+  using ipol = RAJA::LoopPolicy<RAJA::seq_exec, RAJA::b200_thread_x_loop>;
+  const auto lay = RAJA::make_offset_layout<3>({{-1, -1, -1}}, {{Nz + 1, Ny + 1, Nx + 1}});
+  RAJA::View<double, RAJA::OffsetLayout<3>> U(u, lay), Un(unew, lay);
+  constexpr int JT = 4;
+  double rmax = 0.0;
+  RAJA::launch<pol>(place, RAJA::LaunchParams(RAJA::Teams(Nz, (Ny + JT - 1) / JT), RAJA::Threads(32, JT)),
+                    RAJA::expt::Reduce<RAJA::operators::maximum>(&rmax),
+                    [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx,
+                                         RAJA::expt::ValOp<double, RAJA::operators::maximum>& r) {
+    RAJA::loop<kpol>(ctx, RAJA::RangeSegment(0, Nz), [&](Index_type k) {
+      RAJA::tile<jtile>(ctx, JT, RAJA::RangeSegment(0, Ny), [&](const RAJA::RangeSegment& jt) {
+        RAJA::loop<jpol>(ctx, jt, [&](Index_type j) {
+          RAJA::loop<ipol>(ctx, RAJA::RangeSegment(0, Nx), [&](Index_type i) {
+            double acc = U(k, j, i - 1) + U(k, j, i + 1);
+            acc += U(k, j - 1, i) + U(k, j + 1, i);
+            acc += U(k - 1, j, i) + U(k + 1, j, i);
+            const double v = mul_rn(acc, 1.0 / 6.0);
+            Un(k, j, i) = v;
+            r.max(fabs(sub_rn(v, U(k, j, i))));
+          });
+        });
+      });
+    });
+  });
+  return rmax;
+}
+
+void test_launch_jacobi() {
+  const int dims[2][3] = {{64, 64, 64}, {130, 37, 21}};
+  for (const auto& d : dims) {
+    const int Nx = d[0], Ny = d[1], Nz = d[2];
+    const size_t tot = size_t(Nx + 2) * (Ny + 2) * (Nz + 2);
+    double* ud = managed<double>(tot);
+    double* vd = managed<double>(tot);
+    std::vector<double> uh(tot), vh(tot);
+    std::mt19937_64 rng(5);
+    std::uniform_real_distribution<double> dist(-1.0, 1.0);
+    for (size_t q = 0; q < tot; ++q) ud[q] = vd[q] = uh[q] = vh[q] = dist(rng);
+    double rd = 0.0, rh = 0.0;
+    for (int sweep = 0; sweep < 6; ++sweep) {
+      double* a = (sweep & 1) ? vd : ud;
+      double* b = (sweep & 1) ? ud : vd;
+      double* ah = (sweep & 1) ? vh.data() : uh.data();
+      double* bh = (sweep & 1) ? uh.data() : vh.data();
+      rd = jacobi_launch(RAJA::ExecPlace::DEVICE, Nx, Ny, Nz, a, b);
+      rh = jacobi_launch(RAJA::ExecPlace::HOST, Nx, Ny, Nz, ah, bh);
+    }
+    bool ok = rd == rh && rd > 0.0;
+    for (size_t q = 0; q < tot; ++q) ok = ok && ud[q] == uh[q] && vd[q] == vh[q];
+    char nm[96];
+    snprintf(nm, sizeof nm, "launch_jacobi_offset_view_%dx%dx%d", Nx, Ny, Nz);
+    printf("%s: residual device %.17g host %.17g\n", nm, rd, rh);
+    CHECK(nm, ok);
+    cudaFree(ud);
+    cudaFree(vd);
+  }
+}
+
 int main() {
   setvbuf(stdout, nullptr, _IONBF, 0);  // every PASS line reaches the log even if the run aborts
   test_multi_reduce_and_atomics();
@@ -930,6 +1014,7 @@ int main() {
   workgroup_case<RAJA::ordered>("ordered");
   test_resources();
   test_launch();
+  test_launch_jacobi();
   printf("%d failures\n", g_fail);
   return g_fail;
 }
