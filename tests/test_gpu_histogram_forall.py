@@ -35,6 +35,25 @@ def test_histogram_bit_exact(prims, orc, nbins):
                                           orc.histogram(x[1:], nbins).astype(np.int64))
 
 
+@pytest.mark.parametrize("nbins", [65536, 70001, 114000])
+def test_histogram_hot_bins_many_bins(prims, orc, nbins):
+    """More bins than fit in shared memory as 32-bit counts (the rest are
+    counted in global memory): two adjacent hot bins take ~100k hits per
+    block, the last bin and scattered others a few."""
+    import torch
+    n = 1 << 24
+    g = torch.Generator(device="cuda")
+    g.manual_seed(nbins)
+    x = torch.randint(0, nbins, (n,), generator=g, device="cuda", dtype=torch.int32)
+    hot = torch.rand(n, generator=g, device="cuda") < 0.9
+    x = torch.where(hot, torch.where(torch.arange(n, device="cuda") % 3 == 0, 41, 40), x).to(torch.int32)
+    x[::1000] = nbins - 1
+    xh = x.cpu().numpy()
+    exp = orc.histogram(xh, nbins).astype(np.int64)
+    assert exp[40] > 1 << 22 and exp[41] > 1 << 21
+    np.testing.assert_array_equal(to_host(prims.histogram(x, nbins)), exp)
+
+
 def test_histogram_accumulates(prims):
     import torch
     x = torch.randint(0, 16, (100000,), dtype=torch.int32, device="cuda")
