@@ -174,3 +174,74 @@ def test_sort_2m_skewed_keys(prims, orc, case):
         d = to_dev(x)
         prims.sort(d, descending=desc)
         np.testing.assert_array_equal(to_host(d), orc.sort(x, descending=desc), err_msg=case)
+
+
+# 2^26 and 2^27 keys (2^28 is covered by the full-size tests): uniform
+# keys, keys with few distinct top bits, and stable f32/i32 pairs with many
+# equal keys, +-0.0 and infinities, ascending and descending, in place and
+# out of place.  The reference is a stable torch sort of an
+# order-preserving int64 key.
+NL = [(1 << 26) + 777, (1 << 27) + 5]
+
+
+def _ord64(t):
+    import torch
+    if t.dtype == torch.uint32:
+        return t.view(torch.int32).to(torch.int64) & 0xFFFFFFFF
+    if t.dtype == torch.float32:
+        b = t.view(torch.int32).to(torch.int64)
+        return torch.where(b < 0, b ^ 0x7FFFFFFF, b)
+    if t.dtype == torch.uint64:
+        return t.view(torch.int64) ^ (-2 ** 63)
+    raise TypeError(t.dtype)
+
+
+def _large_input(kind, n, gen):
+    import torch
+    dev = "cuda"
+    if kind.startswith("u32"):
+        k = torch.randint(-2 ** 31, 2 ** 31, (n,), generator=gen, device=dev, dtype=torch.int32)
+        if kind.endswith("skew"):            # every key below 2^16
+            k = k & 0xFFFF
+        return k.view(torch.uint32), None
+    if kind.startswith("u64"):
+        k = torch.randint(-2 ** 63, 2 ** 63 - 1, (n,), generator=gen, device=dev, dtype=torch.int64)
+        if kind.endswith("skew"):            # keys below 2^40
+            k = k & ((1 << 40) - 1)
+        return k.view(torch.uint64), None
+    k = torch.randn(n, generator=gen, device=dev, dtype=torch.float32)
+    k[: n // 8] = torch.round(k[: n // 8] * 4) / 4   # many equal keys
+    k[1::997] = 0.0
+    k[2::997] = -0.0
+    k[3::4099] = float("inf")
+    k[4::4099] = float("-inf")
+    if kind.endswith("skew"):                # keys in [1, 2): 128 top-16 values
+        k = 1.0 + torch.rand(n, generator=gen, device=dev, dtype=torch.float32)
+        k[: n // 4] = 1.5
+    return k, torch.arange(n, device=dev, dtype=torch.int32)
+
+
+@pytest.mark.parametrize("n", NL)
+@pytest.mark.parametrize("kind", ["u32", "u64", "pairs", "u32_skew", "u64_skew", "pairs_skew"])
+def test_sort_large_sizes_exact(prims, n, kind):
+    import torch
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(n + sum(map(ord, kind)))
+    k, v = _large_input(kind, n, gen)
+    sint = torch.int32 if k.element_size() == 4 else torch.int64   # same-width signed view
+    for desc in (False, True):
+        perm = torch.sort(_ord64(k), descending=desc, stable=True).indices
+        want = k.view(sint)[perm]
+        if v is None:
+            if desc:
+                got = k.clone()
+                prims.sort(got, descending=True)               # in place
+            else:
+                got = torch.empty_like(k)
+                prims.sort_copy(k, got)                        # out of place
+            assert torch.equal(got.view(sint), want), (kind, desc)
+        else:
+            ko, vo = k.clone(), v.clone()
+            prims.sort_pairs(ko, vo, descending=desc)
+            assert torch.equal(ko.view(sint), want), (kind, desc)
+            assert torch.equal(vo, v[perm]), (kind, desc)        # stable: values in input order
