@@ -850,22 +850,23 @@ __device__ inline void combine_param(const DevSlot<typename ParamKind<R>::type::
   grid_combine(slot, ParamKind<R>::from_valop(v), [](typename K::V a, typename K::V b) { return K::merge(a, b); });
 }
 
-template <int BLOCK, class Body, class T, class... R, size_t... I>
-__device__ inline void params_body(Body& body, T begin, long long len,
+// Any segment kind: element i is RAJA::detail::seg_at(seg, i).
+template <int BLOCK, class Body, class Seg, class... R, size_t... I>
+__device__ inline void params_body(Body& body, const Seg& seg, long long len,
                                    const DTuple<DevSlot<typename ParamKind<R>::type::V>...>& slots,
                                    std::index_sequence<I...>) {
   DTuple<typename R::valop_type...> vals{};
   const long long stride = (long long)gridDim.x * BLOCK;
   for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < len; i += stride)
-    body(T(begin + T(i)), dget<I>(vals)...);
+    body(::RAJA::detail::seg_at(seg, Index_type(i)), dget<I>(vals)...);
   (combine_param<R>(dget<I>(slots), dget<I>(vals)), ...);
 }
 
-template <int BLOCK, class Body, class T, class... R>
+template <int BLOCK, class Body, class Seg, class... R>
 __global__ void __launch_bounds__(BLOCK)
-forall_params_kernel(Body body, T begin, long long len,
+forall_params_kernel(Body body, Seg seg, long long len,
                      DTuple<DevSlot<typename ParamKind<R>::type::V>...> slots) {
-  params_body<BLOCK, Body, T, R...>(body, begin, len, slots, std::index_sequence_for<R...>{});
+  params_body<BLOCK, Body, Seg, R...>(body, seg, len, slots, std::index_sequence_for<R...>{});
 }
 
 }  // namespace detail
@@ -885,19 +886,19 @@ void resolve_params(const Slots& slots, cudaStream_t s, std::index_sequence<I...
   (one(reds, b200::detail::dget<I>(slots)), ...);
 }
 
-template <int BLOCK, bool Async, class T, class Body, class... Red>
-void forall_params_impl(b200_exec<BLOCK, Async>, const TypedRangeSegment<T>& r, Body&& body,
-                        Red&... reds) {
+template <int BLOCK, bool Async, class Seg, class Body, class... Red,
+          class = decltype(::RAJA::detail::seg_len(std::declval<const Seg&>()))>
+void forall_params_impl(b200_exec<BLOCK, Async>, const Seg& r, Body&& body, Red&... reds) {
   using B = std::decay_t<Body>;
   using Slots = b200::detail::DTuple<b200::detail::DevSlot<typename b200::detail::ParamKind<Red>::type::V>...>;
-  const long long len = (long long)r.size();
-  auto k = b200::detail::forall_params_kernel<BLOCK, B, T, Red...>;
+  const long long len = (long long)::RAJA::detail::seg_len(r);
+  auto k = b200::detail::forall_params_kernel<BLOCK, B, Seg, Red...>;
   const unsigned g = b200::detail::grid_for(k, BLOCK, len > 0 ? len : 1);
   cudaStream_t s = b200::stream();
   void* blocks[sizeof...(Red) + 1] = {};
   size_t bi = 0;
   Slots slots{b200::detail::alloc_slot<typename b200::detail::ParamKind<Red>::type::V>(g, s, &blocks[bi++])...};
-  k<<<g, BLOCK, 0, s>>>(body, r.b, len, slots);
+  k<<<g, BLOCK, 0, s>>>(body, r, len, slots);
   b200::check_cuda(cudaGetLastError(), "b200 forall params");
   b200::wait();  // param_resolve waits for the kernel, as the reference does
   resolve_params(slots, s, std::index_sequence_for<Red...>{}, reds...);

@@ -172,6 +172,28 @@ struct TypedIndexSet {
   size_t getNumSegments() const { return segs.size(); }
 };
 
+// Element k of a segment, and its length (loop executors, forall params).
+namespace detail {
+template <typename T>
+RAJA_HOST_DEVICE Index_type seg_len(const TypedRangeSegment<T>& s) { return Index_type(s.e - s.b); }
+template <typename T>
+RAJA_HOST_DEVICE T seg_at(const TypedRangeSegment<T>& s, Index_type k) { return T(s.b + T(k)); }
+template <typename T>
+RAJA_HOST_DEVICE Index_type seg_len(const TypedRangeStrideSegment<T>& s) { return Index_type(s.size()); }
+template <typename T>
+RAJA_HOST_DEVICE T seg_at(const TypedRangeStrideSegment<T>& s, Index_type k) { return T(s.b + T(k) * s.s); }
+template <typename T>
+RAJA_HOST_DEVICE Index_type seg_len(const TypedListSegment<T>& s) { return s.len; }
+template <typename T>
+RAJA_HOST_DEVICE T seg_at(const TypedListSegment<T>& s, Index_type k) { return s.data[k]; }
+// Tile t of size `ts` of a range segment (the last one may be short).
+template <typename T>
+RAJA_HOST_DEVICE TypedRangeSegment<T> seg_tile(const TypedRangeSegment<T>& s, Index_type ts, Index_type t) {
+  const Index_type lo = t * ts, n = seg_len(s);
+  return TypedRangeSegment<T>(T(s.b + T(lo)), T(s.b + T(lo + ts < n ? lo + ts : n)));
+}
+}  // namespace detail
+
 // ---------------------------------------------------------------- spans
 template <typename T>
 struct Span {
@@ -825,11 +847,13 @@ void forall_impl(Pol p, const TypedIndexSet<T>& is, Body&& body) {
 // forall with expt params on host: each param gets a ValOp local starting
 // at its identity; after the loop the target is combined (param_resolve,
 // policy/sequential/params/reduce.hpp:42-46).
-template <typename T, typename Body, typename... Red>
-void forall_params_impl(seq_exec, const TypedRangeSegment<T>& r, Body&& body, Red&... reds) {
+template <typename Seg, typename Body, typename... Red,
+          typename = decltype(detail::seg_len(std::declval<const Seg&>()))>
+void forall_params_impl(seq_exec, const Seg& r, Body&& body, Red&... reds) {
   std::tuple<typename Red::valop_type...> vals;
+  const Index_type n = detail::seg_len(r);
   std::apply([&](auto&... v) {
-    for (T i = r.b; i < r.e; ++i) body(i, v...);
+    for (Index_type k = 0; k < n; ++k) body(detail::seg_at(r, k), v...);
   }, vals);
   std::apply([&](auto&... v) { (reds.combineTarget(v.val), ...); }, vals);
 }
@@ -988,27 +1012,6 @@ template <typename POLICY_LIST>
 using loop_policy = typename POLICY_LIST::host_policy_t;
 #endif
 
-// Element k of a segment, and its length, for loop executors.
-namespace detail {
-template <typename T>
-RAJA_HOST_DEVICE Index_type seg_len(const TypedRangeSegment<T>& s) { return Index_type(s.e - s.b); }
-template <typename T>
-RAJA_HOST_DEVICE T seg_at(const TypedRangeSegment<T>& s, Index_type k) { return T(s.b + T(k)); }
-template <typename T>
-RAJA_HOST_DEVICE Index_type seg_len(const TypedRangeStrideSegment<T>& s) { return Index_type(s.size()); }
-template <typename T>
-RAJA_HOST_DEVICE T seg_at(const TypedRangeStrideSegment<T>& s, Index_type k) { return T(s.b + T(k) * s.s); }
-template <typename T>
-RAJA_HOST_DEVICE Index_type seg_len(const TypedListSegment<T>& s) { return s.len; }
-template <typename T>
-RAJA_HOST_DEVICE T seg_at(const TypedListSegment<T>& s, Index_type k) { return s.data[k]; }
-// Tile t of size `ts` of a range segment (the last one may be short).
-template <typename T>
-RAJA_HOST_DEVICE TypedRangeSegment<T> seg_tile(const TypedRangeSegment<T>& s, Index_type ts, Index_type t) {
-  const Index_type lo = t * ts, n = seg_len(s);
-  return TypedRangeSegment<T>(T(s.b + T(lo)), T(s.b + T(lo + ts < n ? lo + ts : n)));
-}
-}  // namespace detail
 
 // Loop executors, specialised per loop policy (launch_core.hpp:461-465,
 // 560-564).  seq_exec runs every index in order on the calling thread.

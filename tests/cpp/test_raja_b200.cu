@@ -1003,6 +1003,49 @@ void test_launch_jacobi() {
   }
 }
 
+// expt::Reduce params over strided and list segments, device vs seq
+void test_params_segments() {
+  const int n = 200003;
+  double* x = managed<double>(n);
+  for (int i = 0; i < n; ++i) x[i] = double((i * 7919) % 1000) - 500.0;
+  x[123457] = -777.0;
+  Index_type* lst = managed<Index_type>(5000);
+  for (int i = 0; i < 5000; ++i) lst[i] = Index_type((i * 40009) % n);
+  using VS = RAJA::expt::ValOp<double, RAJA::operators::plus>;
+  using VL = RAJA::expt::ValOp<RAJA::expt::ValLoc<double, Index_type>, RAJA::operators::minimum>;
+  double res[2][4];
+  Index_type loc[2][2];
+  for (int dev = 0; dev < 2; ++dev) {
+    double s1 = 0.0, v1 = 1e300, s2 = 0.0, v2 = 1e300;
+    Index_type i1 = -1, i2 = -1;
+    auto body = [=] RAJA_HOST_DEVICE(Index_type i, VS& s, VL& m) {
+      s += x[i];
+      m.minloc(x[i], i);
+    };
+    if (dev) {
+      RAJA::forall<exec>(RAJA::RangeStrideSegment(1, n, 2), RAJA::expt::Reduce<RAJA::operators::plus>(&s1),
+                         RAJA::expt::ReduceLoc<RAJA::operators::minimum>(&v1, &i1), body);
+      RAJA::forall<exec>(RAJA::ListSegment(lst, 5000), RAJA::expt::Reduce<RAJA::operators::plus>(&s2),
+                         RAJA::expt::ReduceLoc<RAJA::operators::minimum>(&v2, &i2), body);
+    } else {
+      RAJA::forall<RAJA::seq_exec>(RAJA::RangeStrideSegment(1, n, 2), RAJA::expt::Reduce<RAJA::operators::plus>(&s1),
+                                   RAJA::expt::ReduceLoc<RAJA::operators::minimum>(&v1, &i1), body);
+      RAJA::forall<RAJA::seq_exec>(RAJA::ListSegment(lst, 5000), RAJA::expt::Reduce<RAJA::operators::plus>(&s2),
+                                   RAJA::expt::ReduceLoc<RAJA::operators::minimum>(&v2, &i2), body);
+    }
+    res[dev][0] = s1; res[dev][1] = v1; res[dev][2] = s2; res[dev][3] = v2;
+    loc[dev][0] = i1; loc[dev][1] = i2;
+  }
+  // integer-valued doubles: the sums are exact in any order; MinLoc keeps
+  // the lowest index of the stride segment, the first list position's
+  // index on the device only up to ties, so values are compared there
+  CHECK("expt_reduce_stride_list_b200",
+        res[1][0] == res[0][0] && res[1][1] == res[0][1] && loc[1][0] == loc[0][0] && loc[0][0] == 123457 &&
+        res[1][2] == res[0][2] && res[1][3] == res[0][3]);
+  cudaFree(x);
+  cudaFree(lst);
+}
+
 int main() {
   setvbuf(stdout, nullptr, _IONBF, 0);  // every PASS line reaches the log even if the run aborts
   test_multi_reduce_and_atomics();
@@ -1015,6 +1058,7 @@ int main() {
   test_resources();
   test_launch();
   test_launch_jacobi();
+  test_params_segments();
   printf("%d failures\n", g_fail);
   return g_fail;
 }

@@ -89,6 +89,26 @@ int main() {
                                  m.min(double(i) + 3.0);
                                });
   CHECK("expt_reduce_names_anywhere", t1 == 45.0 && t2 == 3.0);
+  // params over strided and list segments (test-forall-basic-param-expt-ReduceSum.hpp segments)
+  {
+    double ts = 0.0, tm = 1e9;
+    RAJA::forall<RAJA::seq_exec>(RAJA::RangeStrideSegment(3, 1029, 3), RAJA::expt::Reduce<RAJA::operators::plus>(&ts),
+                                 RAJA::expt::Reduce<RAJA::operators::minimum>(&tm),
+                                 [=](Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& s,
+                                     RAJA::expt::ValOp<double, RAJA::operators::minimum>& m) {
+                                   s += double(i);
+                                   m.min(double(1000 - i));
+                                 });
+    double want = 0.0;
+    for (int i = 3; i < 1029; i += 3) want += i;
+    const Index_type lst[4] = {7, 2, 11, 5};
+    double tl = 0.0;
+    RAJA::forall<RAJA::seq_exec>(RAJA::ListSegment(lst, 4), RAJA::expt::Reduce<RAJA::operators::plus>(&tl),
+                                 [=](Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& s) {
+                                   s += double(i * i);
+                                 });
+    CHECK("expt_reduce_stride_list_segments", ts == want && tm == double(1000 - 1026) && tl == 49.0 + 4 + 121 + 25);
+  }
   int named = 0;
   RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 4), RAJA::Name("only"),
                                [&](Index_type) { ++named; });
