@@ -295,7 +295,8 @@ def run_reference(args, rank: int, world: int):
 
 def config_block(args, n_override=None):
     n = n_override or (1 << args.log2n)
-    return {"workload": "bandwidth sweep (BASELINE configs[1]) at N=2^%d per primitive"
+    return {"workload": "primitive bandwidth sweep (reductions, MinLoc/MaxLoc, int64 scan, sorts, "
+                        "histograms) at N=2^%d per primitive"
                         % (n.bit_length() - 1),
             "n": n, "primitives": [p for p, _ in primitive_table(n)],
             "l2_flush": "none: every input is larger than the 129 MB L2",

@@ -118,8 +118,8 @@ int b200_prof_read(char* names, size_t name_stride, uint64_t* launches,
  * forall -- fixed-type bodies of the RAJA::forall hot loop
  * (policy/cuda/forall.hpp:371-655, kernel forallp_cuda_kernel).  Arbitrary
  * lambda bodies go through the templated b200_exec policy in
- * include/raja_b200/forall.hpp; these entry points cover the loop bodies
- * the benchmark configurations name.
+ * include/raja_b200/RAJA_b200.hpp; these entry points cover the fixed
+ * daxpy / fp32 axpy loop bodies.
  * ====================================================================== */
 
 /* y[i] += a * x[i]  for i in [0, n) */
@@ -157,7 +157,8 @@ int b200_reduce_sum_u32(const uint32_t* x, size_t n, int mode, uint32_t* out,
 int b200_reduce_sum_u64(const uint64_t* x, size_t n, int mode, uint64_t* out,
                         b200_stream_t stream);
 
-/* dot = sum_i x[i]*y[i]  (ReduceSum of products, BASELINE configs 1 and 3) */
+/* dot = sum_i x[i]*y[i]  (ReduceSum of products; the daxpy/dot and the
+ * ill-conditioned fp32 accuracy workloads) */
 int b200_dot_f32(const float* x, const float* y, size_t n, int mode,
                  double* out, b200_stream_t stream);
 int b200_dot_f64(const double* x, const double* y, size_t n, int mode,
