@@ -416,8 +416,9 @@ def main():
     if not args.no_extras:
         del inputs, outs
         torch.cuda.empty_cache()
-        for nm, fn in (("batched_workgroup_cfg4", bench_batched), ("jacobi_cfg5", bench_jacobi),
-                       ("accuracy_cfg3", bench_accuracy)):
+        for nm, fn in (("forall_daxpy_dot", bench_forall_dot),
+                       ("batched_workgroup_4096_loops", bench_batched), ("jacobi_256_meshes", bench_jacobi),
+                       ("accuracy_ill_conditioned", bench_accuracy)):
             try:
                 extras[nm] = fn(lib)
             except Exception as e:  # report, do not lose the headline line
@@ -503,6 +504,48 @@ def exact_prefix_f64(v):
     for k in range(cum.shape[1] - 1, -1, -1):   # most significant limb first
         out += torch.ldexp(cum[:, k].double(), torch.tensor(32 * k + emin, device=v.device))
     return out
+
+
+def bench_forall_dot(lib, reps=20, seed=6):
+    """The forall daxpy body y += 2.5 x (24 B per element) and the dot
+    product (16 B per element in FP64, 8 B in FP32) at 2^28 and 2^20
+    elements, CUDA events over `reps` back-to-back calls (every input is
+    larger than the L2 at 2^28; at 2^20 the data stays in L2)."""
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    s = torch.cuda.current_stream().cuda_stream
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    res = {}
+    peak = load_peaks().get("hbm_gbs")
+    for log2n in (28, 20):
+        n = 1 << log2n
+        x = torch.rand(n, generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+        y = torch.rand(n, generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+        xf, yf = x.float(), y.float()
+        calls = (("daxpy_f64", 24 * n, lambda: lib.b200_forall_axpy_f64(2.5, x.data_ptr(), y.data_ptr(), n, s)),
+                 ("dot_f64", 16 * n, lambda: lib.b200_dot_f64(x.data_ptr(), y.data_ptr(), n, 0, out.data_ptr(), s)),
+                 ("dot_f32", 8 * n, lambda: lib.b200_dot_f32(xf.data_ptr(), yf.data_ptr(), n, 0, out.data_ptr(), s)))
+        for nm, nbytes, f in calls:
+            for _ in range(3):
+                f()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                rc = f()
+                if rc != 0:
+                    raise RuntimeError(f"{nm}: status {rc}")
+            b.record()
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b) / reps
+            gbs = nbytes / ms / 1e6
+            res[f"{nm}_n2p{log2n}_ms"] = round(ms, 4)
+            res[f"{nm}_n2p{log2n}_gbs"] = round(gbs, 1)
+            if peak and log2n == 28:
+                res[f"{nm}_n2p{log2n}_frac_of_measured_hbm"] = round(gbs / peak, 3)
+        del x, y, xf, yf
+    return res
 
 
 def bench_accuracy(lib, seed=3):
