@@ -42,6 +42,10 @@
 
 #include "../b200prims.h"
 
+#if defined(RAJA_ENABLE_NVTX)
+#include <nvtx3/nvToolsExt.h>
+#endif
+
 namespace RAJA {
 
 // ------------------------------------------------------------ policies
@@ -569,6 +573,43 @@ inline void finish(const char* what) {
 }  // namespace detail
 }  // namespace b200
 
+// --------------------------------------------------------- kernel names
+// A RAJA::Name param on a b200 loop or launch opens an NVTX range of that
+// name around the launch when built with RAJA_ENABLE_NVTX (as the CUDA
+// back-end does, policy/cuda/params/kernel_name.hpp:33-70), and is kept as
+// the thread's last kernel name either way.
+namespace b200 {
+inline const char*& last_kernel_name() {
+  static thread_local const char* n = nullptr;
+  return n;
+}
+class NameScope {
+ public:
+  explicit NameScope(const char* n) : on_(n != nullptr) {
+    if (!on_) return;
+    last_kernel_name() = n;
+#if defined(RAJA_ENABLE_NVTX)
+    nvtxRangePushA(n);
+#endif
+  }
+  NameScope(NameScope&& o) noexcept : on_(o.on_) { o.on_ = false; }
+  NameScope(const NameScope&) = delete;
+  NameScope& operator=(const NameScope&) = delete;
+  ~NameScope() {
+#if defined(RAJA_ENABLE_NVTX)
+    if (on_) nvtxRangePop();
+#endif
+  }
+
+ private:
+  bool on_;
+};
+}  // namespace b200
+template <int BLOCK, bool Async>
+b200::NameScope kernel_name_scope(const b200_exec<BLOCK, Async>&, const char* n) {
+  return b200::NameScope(n);
+}
+
 // ------------------------------------------------------------ resources
 // resources::Cuda for the b200 policies: a CUDA stream on one device, with
 // the interface of camp's Cuda resource as RAJA uses it (allocate /
@@ -921,6 +962,10 @@ void forall_params_impl(b200_exec<BLOCK, Async>, const Seg& r, Body&& body, Red&
 // unchecked form is valid).  A host-compiled loop body runs sequentially.
 template <bool Async = false, int NUM_THREADS = 0>
 struct b200_launch_t {};
+template <bool Async, int NUM_THREADS>
+b200::NameScope kernel_name_scope(const b200_launch_t<Async, NUM_THREADS>&, const char* n) {
+  return b200::NameScope(n);
+}
 
 template <int KIND, int D, bool LOOP>
 struct b200_loop_pol {};

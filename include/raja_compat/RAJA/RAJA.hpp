@@ -858,6 +858,25 @@ void forall_params_impl(seq_exec, const Seg& r, Body&& body, Red&... reds) {
   std::apply([&](auto&... v) { (reds.combineTarget(v.val), ...); }, vals);
 }
 
+// Kernel names (RAJA::Name) bracket the loop they name.  The front-end
+// finds the first name among the params and asks the policy for a scope
+// (kernel_name_scope, found by argument-dependent lookup): host policies
+// take none, as in the reference, whose CUDA back-end pushes an NVTX range
+// (policy/cuda/params/kernel_name.hpp:33-70).
+struct NoNameScope {};
+template <typename Pol>
+NoNameScope kernel_name_scope(const Pol&, const char*) {
+  return {};
+}
+namespace detail {
+inline const char* find_name() { return nullptr; }
+template <typename P0, typename... Ps>
+const char* find_name(const P0& p0, const Ps&... ps) {
+  if constexpr (std::is_same<std::decay_t<P0>, expt::KernelName>::value) return p0.name;
+  else return find_name(ps...);
+}
+}  // namespace detail
+
 namespace detail {
 // Dispatch of forall(seg, params..., body): kernel names (RAJA::Name) are
 // dropped wherever they appear (no plugin consumes them here); reducer
@@ -894,6 +913,8 @@ void forall_collect(Pol p, Seg&& seg, Body&& body, std::tuple<Red&...> reds, R0&
 
 template <typename Pol, typename Seg, typename Body, typename... Params>
 void forall_with(Pol p, Seg&& seg, Body&& body, Params&&... params) {
+  auto named = kernel_name_scope(p, find_name(params...));
+  (void)named;
   if constexpr ((expt::detail::is_reducer<std::decay_t<Params>>::value || ... || false)) {
     forall_collect(p, std::forward<Seg>(seg), std::forward<Body>(body), std::tuple<>(), params...);
   } else {
@@ -1144,6 +1165,8 @@ void launch_on(Res r, const LaunchParams& p, Args&&... args) {
   static_assert(sizeof...(Args) >= 1, "launch needs a body");
   auto bound = bind_resource(r);
   (void)bound;
+  auto named = kernel_name_scope(LP{}, find_name(args...));
+  (void)named;
   launch_split<LP>(r, p, std::forward_as_tuple(args...), std::make_index_sequence<sizeof...(Args) - 1>{});
 }
 }  // namespace detail

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <random>
+#include <string>
 #include <vector>
 
 #include "RAJA/RAJA.hpp"
@@ -1039,6 +1040,18 @@ void test_params_segments() {
   // integer-valued doubles: the sums are exact in any order; MinLoc keeps
   // the lowest index of the stride segment, the first list position's
   // index on the device only up to ties, so values are compared there
+  // a kernel name reaches the b200 launch (NVTX range under RAJA_ENABLE_NVTX)
+  RAJA::b200::last_kernel_name() = nullptr;
+  double sn = 0.0;
+  RAJA::forall<exec>(RAJA::RangeSegment(0, 1000), RAJA::Name("b200_named_loop"),
+                     RAJA::expt::Reduce<RAJA::operators::plus>(&sn),
+                     [=] RAJA_HOST_DEVICE(Index_type i, VS& s) { s += double(i); });
+  const char* seen = RAJA::b200::last_kernel_name();
+  RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(1), RAJA::Threads(32)), RAJA::Name("b200_named_launch"),
+                        [=] RAJA_HOST_DEVICE(RAJA::LaunchContext) {});
+  const char* seen2 = RAJA::b200::last_kernel_name();
+  CHECK("kernel_name_reaches_b200", sn == 499500.0 && seen && std::string(seen) == "b200_named_loop" && seen2 &&
+                                        std::string(seen2) == "b200_named_launch");
   CHECK("expt_reduce_stride_list_b200",
         res[1][0] == res[0][0] && res[1][1] == res[0][1] && loc[1][0] == loc[0][0] && loc[0][0] == 123457 &&
         res[1][2] == res[0][2] && res[1][3] == res[0][3]);

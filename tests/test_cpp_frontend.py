@@ -30,7 +30,8 @@ def test_b200_policies_against_seq(tmp_path):
     lib = b.build()
     nvcc = b.nvcc()
     exe = str(tmp_path / "test_raja_b200")
-    r = _run([nvcc, "-std=c++17", "--extended-lambda", "--expt-relaxed-constexpr", "-O2", *b.ARCH, *INC,
+    r = _run([nvcc, "-std=c++17", "--extended-lambda", "--expt-relaxed-constexpr", "-O2", "-DRAJA_ENABLE_NVTX",
+              *b.ARCH, *INC,
               f"{ROOT}/tests/cpp/test_raja_b200.cu", "-o", exe, f"-L{os.path.dirname(lib)}", "-lb200prims",
               f"-Xlinker", f"-rpath={os.path.dirname(lib)}"])
     assert r.returncode == 0, r.stderr[-4000:]
