@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <random>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -1059,6 +1060,90 @@ void test_params_segments() {
   cudaFree(lst);
 }
 
+// Empty and tiny inputs through the RAJA API on the b200 policies: empty
+// segments leave reducers at their init values and params targets
+// unchanged; launches with zero teams do nothing; scans and sorts of
+// length 0, 1 and 2; an empty WorkGroup; waiting on an unused resource.
+void test_edge_cases() {
+  bool ok = true;
+  int* a = managed<int>(4);
+  a[0] = 5; a[1] = -3; a[2] = 7; a[3] = 1;
+  {
+    RAJA::ReduceSum<red, int> s(11);
+    RAJA::ReduceMinLoc<red, int, Index_type> m(100, -1);
+    RAJA::forall<exec>(RAJA::RangeSegment(4, 4), [=] RAJA_HOST_DEVICE(Index_type i) {
+      s += a[i];
+      m.minloc(a[i], i);
+    });
+    RAJA::forall<exec>(RAJA::RangeStrideSegment(0, 0, 2), [=] RAJA_HOST_DEVICE(Index_type i) { s += a[i]; });
+    RAJA::forall<exec>(RAJA::ListSegment(nullptr, 0), [=] RAJA_HOST_DEVICE(Index_type i) { s += a[i]; });
+    ok = ok && s.get() == 11 && m.get() == 100 && m.getLoc() == -1;
+    double t = 2.5;
+    RAJA::forall<exec>(RAJA::RangeSegment(0, 0), RAJA::expt::Reduce<RAJA::operators::plus>(&t),
+                       [=] RAJA_HOST_DEVICE(Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& v) {
+                         v += double(a[i]);
+                       });
+    ok = ok && t == 2.5;
+  }
+  CHECK("edge_empty_segments_b200", ok);
+  ok = true;
+  {
+    double t = 1.0;
+    RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(0), RAJA::Threads(32)),
+                          RAJA::expt::Reduce<RAJA::operators::plus>(&t),
+                          [=] RAJA_HOST_DEVICE(RAJA::LaunchContext ctx,
+                                               RAJA::expt::ValOp<double, RAJA::operators::plus>& v) {
+                            RAJA::loop<lp<RAJA::b200_global_thread_x>>(ctx, RAJA::RangeSegment(0, 4),
+                                                                       [&](Index_type i) { v += 1.0; });
+                          });
+    RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(4), RAJA::Threads(0)),
+                          [=] RAJA_HOST_DEVICE(RAJA::LaunchContext) { a[0] = 99; });
+    ok = ok && t == 1.0 && a[0] == 5;
+    bool threw = false;
+    try {
+      RAJA::launch<dlaunch>(RAJA::LaunchParams(RAJA::Teams(1), RAJA::Threads(64, 32)),
+                            [=] RAJA_HOST_DEVICE(RAJA::LaunchContext) {});
+    } catch (const std::runtime_error&) {
+      threw = true;  // 2048 threads per team
+    }
+    ok = ok && threw;
+  }
+  CHECK("edge_launch_empty_and_oversized", ok);
+  ok = true;
+  {
+    int* o = managed<int>(4);
+    o[0] = o[1] = o[2] = o[3] = -9;
+    RAJA::inclusive_scan<exec>(RAJA::make_span((const int*)a, 0), RAJA::make_span(o, 0));
+    ok = ok && o[0] == -9;
+    RAJA::exclusive_scan<exec>(RAJA::make_span((const int*)a, 1), RAJA::make_span(o, 1),
+                               RAJA::operators::plus<int>{}, 4);
+    ok = ok && o[0] == 4 && o[1] == -9;
+    RAJA::inclusive_scan<exec>(RAJA::make_span((const int*)a, 2), RAJA::make_span(o, 2),
+                               RAJA::operators::minimum<int>{});
+    ok = ok && o[0] == 5 && o[1] == -3;
+    RAJA::stable_sort<exec>(RAJA::make_span(a, 0));
+    RAJA::stable_sort<exec>(RAJA::make_span(a, 1));
+    ok = ok && a[0] == 5;
+    int* v = managed<int>(2);
+    v[0] = 10; v[1] = 20;
+    RAJA::stable_sort_pairs<exec>(RAJA::make_span(a, 2), RAJA::make_span(v, 2));
+    ok = ok && a[0] == -3 && a[1] == 5 && v[0] == 20 && v[1] == 10;
+    cudaFree(o);
+    cudaFree(v);
+  }
+  CHECK("edge_scan_sort_lengths_0_1_2", ok);
+  {
+    using wpol = RAJA::WorkGroupPolicy<RAJA::b200_work<256, false>, RAJA::unordered>;
+    RAJA::WorkPool<wpol, Index_type> pool;
+    auto group = pool.instantiate();
+    auto site = group.run();
+    RAJA::resources::Cuda fresh;
+    fresh.wait();
+    CHECK("edge_empty_workgroup_and_idle_resource", pool.num_loops() == 0);
+  }
+  cudaFree(a);
+}
+
 int main() {
   setvbuf(stdout, nullptr, _IONBF, 0);  // every PASS line reaches the log even if the run aborts
   test_multi_reduce_and_atomics();
@@ -1072,6 +1157,7 @@ int main() {
   test_launch();
   test_launch_jacobi();
   test_params_segments();
+  test_edge_cases();
   printf("%d failures\n", g_fail);
   return g_fail;
 }
