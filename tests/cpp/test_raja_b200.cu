@@ -1144,6 +1144,64 @@ void test_edge_cases() {
   cudaFree(a);
 }
 
+// Bandwidth of the lambda-body paths (printed, not asserted): daxpy through
+// forall<b200_exec_async>, a ReduceSum<b200_reduce> dot, an expt::Reduce
+// dot, and daxpy through RAJA::launch, at 2^27 doubles (above the L2).
+void perf_lambda_paths() {
+  const Index_type n = Index_type(1) << 27;
+  double *x = nullptr, *y = nullptr;
+  if (cudaMalloc(&x, n * sizeof(double)) != cudaSuccess || cudaMalloc(&y, n * sizeof(double)) != cudaSuccess) {
+    printf("perf: allocation failed\n");
+    return;
+  }
+  cudaMemset(x, 0, n * sizeof(double));
+  cudaMemset(y, 0, n * sizeof(double));
+  using async = RAJA::b200_exec_async<256>;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  auto timed = [&](const char* what, double bytes, int reps, auto&& f) {
+    f();
+    cudaDeviceSynchronize();
+    cudaEventRecord(a, 0);
+    for (int r = 0; r < reps; ++r) f();
+    cudaEventRecord(b, 0);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    ms /= reps;
+    printf("perf: %-34s %8.4f ms  %7.1f GB/s\n", what, ms, bytes / (ms * 1e6));
+  };
+  timed("forall daxpy (lambda, async)", 24.0 * n, 10, [&] {
+    RAJA::forall<async>(RAJA::RangeSegment(0, n), [=] __device__(Index_type i) { y[i] += 2.5 * x[i]; });
+  });
+  timed("ReduceSum dot (lambda)", 16.0 * n, 5, [&] {
+    RAJA::ReduceSum<red, double> d(0.0);
+    RAJA::forall<async>(RAJA::RangeSegment(0, n), [=] __device__(Index_type i) { d += x[i] * y[i]; });
+    (void)d.get();
+  });
+  timed("expt::Reduce dot (lambda)", 16.0 * n, 5, [&] {
+    double d = 0.0;
+    RAJA::forall<async>(RAJA::RangeSegment(0, n), RAJA::expt::Reduce<RAJA::operators::plus>(&d),
+                        [=] __device__(Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& v) {
+                          v += x[i] * y[i];
+                        });
+  });
+  using alaunch = RAJA::LaunchPolicy<RAJA::b200_launch_t<true>>;
+  timed("launch daxpy (global thread loop)", 24.0 * n, 10, [&] {
+    RAJA::launch<alaunch>(RAJA::LaunchParams(RAJA::Teams(152 * 8), RAJA::Threads(256)),
+                          [=] __device__(RAJA::LaunchContext ctx) {
+      RAJA::loop<RAJA::LoopPolicy<RAJA::b200_global_x_loop>>(ctx, RAJA::RangeSegment(0, n),
+                                                              [&](Index_type i) { y[i] += 2.5 * x[i]; });
+    });
+  });
+  cudaDeviceSynchronize();
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(x);
+  cudaFree(y);
+}
+
 int main() {
   setvbuf(stdout, nullptr, _IONBF, 0);  // every PASS line reaches the log even if the run aborts
   test_multi_reduce_and_atomics();
@@ -1158,6 +1216,7 @@ int main() {
   test_launch_jacobi();
   test_params_segments();
   test_edge_cases();
+  perf_lambda_paths();
   printf("%d failures\n", g_fail);
   return g_fail;
 }
