@@ -1308,6 +1308,37 @@ struct View {
   RAJA_HOST_DEVICE void set_data(T* p) { data = p; }
 };
 
+// ---------------------------------------------------------- forall_Icount
+// forall_Icount<POLICY>(segment, icount, body): body(icount + k, seg[k])
+// for k in [0, len) (pattern/forall.hpp:102-124, 227-276); over an
+// IndexSet the count runs on across the segments, one forall per segment.
+namespace detail {
+template <typename Seg, typename Body>
+struct IcountAdapter {
+  Seg seg;
+  Body body;
+  Index_type icount;
+  template <typename I>
+  RAJA_HOST_DEVICE void operator()(I k) const {
+    body(Index_type(icount + Index_type(k)), seg_at(seg, Index_type(k)));
+  }
+};
+}  // namespace detail
+template <typename Pol, typename Seg, typename Body,
+          typename = decltype(detail::seg_len(std::declval<const std::decay_t<Seg>&>()))>
+void forall_Icount(Seg&& seg, Index_type icount, Body&& body) {
+  detail::IcountAdapter<std::decay_t<Seg>, std::decay_t<Body>> ad{seg, body, icount};
+  forall<Pol>(TypedRangeSegment<Index_type>(0, detail::seg_len(seg)), ad);
+}
+template <typename Pol, typename T, typename Body>
+void forall_Icount(const TypedIndexSet<T>& is, Body&& body) {
+  Index_type ic = 0;
+  for (const auto& s : is.segs) {
+    forall_Icount<Pol>(s, ic, body);
+    ic += detail::seg_len(s);
+  }
+}
+
 // ----------------------------------------------------------------- scans
 // pattern/scan.hpp front-ends.  Back-ends overload scan_inclusive /
 // scan_exclusive in namespace RAJA on their policy type; the front-end

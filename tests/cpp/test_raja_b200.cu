@@ -1133,6 +1133,32 @@ void test_edge_cases() {
   }
   CHECK("edge_scan_sort_lengths_0_1_2", ok);
   {
+    // forall_Icount on b200 over an IndexSet and a list segment, with a
+    // captured reducer
+    RAJA::TypedIndexSet<Index_type> is;
+    is.push_back(RAJA::RangeSegment(0, 5000));
+    is.push_back(RAJA::RangeSegment(7000, 7003));
+    is.push_back(RAJA::RangeSegment(9000, 12000));
+    Index_type* w = managed<Index_type>(8003);
+    for (int i = 0; i < 8003; ++i) w[i] = -1;
+    RAJA::ReduceSum<red, long long> cnt(0);
+    RAJA::forall_Icount<exec>(is, [=] RAJA_HOST_DEVICE(Index_type ic, Index_type idx) {
+      w[ic] = idx;
+      cnt += 1;
+    });
+    bool okc = cnt.get() == 8003;
+    for (int i = 0; i < 8003; ++i)
+      okc = okc && w[i] == (i < 5000 ? i : (i < 5003 ? 7000 + (i - 5000) : 9000 + (i - 5003)));
+    Index_type* lst = managed<Index_type>(4);
+    lst[0] = 40; lst[1] = 3; lst[2] = 17; lst[3] = 8;
+    RAJA::forall_Icount<exec>(RAJA::ListSegment(lst, 4), Index_type(100),
+                              [=] RAJA_HOST_DEVICE(Index_type ic, Index_type idx) { w[ic - 100] = idx * 2; });
+    okc = okc && w[0] == 80 && w[1] == 6 && w[2] == 34 && w[3] == 16;
+    CHECK("forall_icount_b200", okc);
+    cudaFree(w);
+    cudaFree(lst);
+  }
+  {
     using wpol = RAJA::WorkGroupPolicy<RAJA::b200_work<256, false>, RAJA::unordered>;
     RAJA::WorkPool<wpol, Index_type> pool;
     auto group = pool.instantiate();

@@ -109,6 +109,22 @@ int main() {
                                  });
     CHECK("expt_reduce_stride_list_segments", ts == want && tm == double(1000 - 1026) && tl == 49.0 + 4 + 121 + 25);
   }
+  // forall_Icount over a segment and over an IndexSet (test-forall-IcountIndexSet.hpp)
+  {
+    RAJA::TypedIndexSet<Index_type> is;
+    is.push_back(RAJA::RangeSegment(0, 5));
+    is.push_back(RAJA::RangeSegment(10, 13));
+    is.push_back(RAJA::RangeSegment(20, 24));
+    std::vector<Index_type> got(12, -1);
+    Index_type* gp = got.data();
+    RAJA::forall_Icount<RAJA::seq_exec>(is, [=](Index_type ic, Index_type idx) { gp[ic] = idx; });
+    const std::vector<Index_type> want{0, 1, 2, 3, 4, 10, 11, 12, 20, 21, 22, 23};
+    std::vector<Index_type> g2(3, -1);
+    Index_type* g2p = g2.data();
+    RAJA::forall_Icount<RAJA::seq_exec>(RAJA::RangeStrideSegment(5, 11, 2), Index_type(0),
+                                        [=](Index_type ic, Index_type idx) { g2p[ic] = idx; });
+    CHECK("forall_icount_indexset_and_stride", got == want && g2 == std::vector<Index_type>({5, 7, 9}));
+  }
   int named = 0;
   RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 4), RAJA::Name("only"),
                                [&](Index_type) { ++named; });
