@@ -800,39 +800,56 @@ void forall_impl(b200_exec<BLOCK, Async>, const TypedListSegment<T>& l, Body&& b
   k<<<g, BLOCK, 0, s>>>(lb, l.data, len);
   b200::detail::finish<Async>("b200 forall");
 }
-// IndexSet: one launch for all segments (the reference launches each
-// segment separately, policy/cuda/forall.hpp:675-706).
-template <int BLOCK, bool Async, class Body, class T>
-void forall_impl(b200_exec<BLOCK, Async>, const TypedIndexSet<T>& is, Body&& body) {
+// IndexSet: when every segment is a range, one launch covers them all (the
+// reference launches each segment separately, policy/cuda/forall.hpp:675-706);
+// otherwise the segments run one after another, each with its own launch.
+template <int BLOCK, bool Async, class Body, class... Segs>
+void forall_impl(b200_exec<BLOCK, Async> pol, const TypedIndexSet<Segs...>& is, Body&& body) {
+  using T = typename TypedIndexSet<Segs...>::value_type;
+  using Range = TypedRangeSegment<T>;
   using B = std::decay_t<Body>;
-  const int nseg = int(is.segs.size());
+  const auto& segs = is.segments();
+  const int nseg = int(segs.size());
   if (nseg == 0) return;
-  std::vector<T> begins(nseg);
-  std::vector<long long> prefix(nseg + 1, 0);
-  for (int i = 0; i < nseg; ++i) {
-    begins[i] = is.segs[i].b;
-    prefix[i + 1] = prefix[i] + (long long)is.segs[i].size();
+  bool all_range = true;
+  for (const auto& v : segs)
+    all_range = all_range && std::visit([](const auto& g) { return std::is_same<std::decay_t<decltype(g)>, Range>::value; }, v);
+  if constexpr (!one_of<Range, Segs...>::value) {
+    all_range = false;
   }
-  const long long total = prefix[nseg];
-  if (total == 0) return;
-  cudaStream_t s = b200::stream();
-  void* tbl = nullptr;
-  const size_t bb = ((nseg * sizeof(T) + 255) / 256) * 256;
-  b200::check_cuda(cudaMallocAsync(&tbl, bb + (nseg + 1) * sizeof(long long), s), "indexset table");
-  T* d_begins = static_cast<T*>(tbl);
-  long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + bb);
-  b200::check_cuda(cudaMemcpyAsync(d_begins, begins.data(), nseg * sizeof(T), cudaMemcpyHostToDevice, s),
-                   "indexset table");
-  b200::check_cuda(cudaMemcpyAsync(d_prefix, prefix.data(), (nseg + 1) * sizeof(long long),
-                                   cudaMemcpyHostToDevice, s),
-                   "indexset table");
-  auto k = b200::detail::forall_indexset_kernel<BLOCK, B, T>;
-  const unsigned g = b200::detail::grid_for(k, BLOCK, total);
-  B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
-  k<<<g, BLOCK, 0, s>>>(lb, d_begins, d_prefix, nseg, total);
-  b200::check_cuda(cudaGetLastError(), "b200 forall indexset");
-  b200::check_cuda(cudaFreeAsync(tbl, s), "indexset table");
-  if (!Async) b200::wait();
+  if (!all_range) {
+    for (const auto& v : segs) std::visit([&](const auto& g) { forall_impl(pol, g, body); }, v);
+    return;
+  }
+  if constexpr (one_of<Range, Segs...>::value) {
+    std::vector<T> begins(nseg);
+    std::vector<long long> prefix(nseg + 1, 0);
+    for (int i = 0; i < nseg; ++i) {
+      const Range& r = std::get<Range>(segs[i]);
+      begins[i] = r.b;
+      prefix[i + 1] = prefix[i] + (long long)r.size();
+    }
+    const long long total = prefix[nseg];
+    if (total == 0) return;
+    cudaStream_t s = b200::stream();
+    void* tbl = nullptr;
+    const size_t bb = ((nseg * sizeof(T) + 255) / 256) * 256;
+    b200::check_cuda(cudaMallocAsync(&tbl, bb + (nseg + 1) * sizeof(long long), s), "indexset table");
+    T* d_begins = static_cast<T*>(tbl);
+    long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + bb);
+    b200::check_cuda(cudaMemcpyAsync(d_begins, begins.data(), nseg * sizeof(T), cudaMemcpyHostToDevice, s),
+                     "indexset table");
+    b200::check_cuda(cudaMemcpyAsync(d_prefix, prefix.data(), (nseg + 1) * sizeof(long long),
+                                     cudaMemcpyHostToDevice, s),
+                     "indexset table");
+    auto k = b200::detail::forall_indexset_kernel<BLOCK, B, T>;
+    const unsigned g = b200::detail::grid_for(k, BLOCK, total);
+    B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
+    k<<<g, BLOCK, 0, s>>>(lb, d_begins, d_prefix, nseg, total);
+    b200::check_cuda(cudaGetLastError(), "b200 forall indexset");
+    b200::check_cuda(cudaFreeAsync(tbl, s), "indexset table");
+    if (!Async) b200::wait();
+  }
 }
 
 // ------------------------------------------------------ forall with params

@@ -39,6 +39,7 @@
 #include <tuple>
 #include <type_traits>
 #include <utility>
+#include <variant>
 #include <vector>
 
 #if defined(_OPENMP)
@@ -163,14 +164,54 @@ struct TypedListSegment {
 };
 using ListSegment = TypedListSegment<Index_type>;
 
-// IndexSet of range segments (index/IndexSet.hpp:87-364); forall over it
-// runs every segment, in order for the host policies.
-template <typename T>
-struct TypedIndexSet {
-  std::vector<TypedRangeSegment<T>> segs;
-  void push_back(TypedRangeSegment<T> s) { segs.push_back(s); }
-  size_t getNumSegments() const { return segs.size(); }
+// IndexSet (index/IndexSet.hpp:50-630): an ordered list of segments of the
+// listed types (range, strided, list) over one index type, e.g.
+// TypedIndexSet<RangeSegment, ListSegment>.  forall runs the segments in
+// order; forall_Icount numbers the indices across them.
+template <typename S, typename... Ts>
+struct one_of : std::bool_constant<(std::is_same<S, Ts>::value || ...)> {};
+template <typename... SegmentTypes>
+class TypedIndexSet {
+  static_assert(sizeof...(SegmentTypes) >= 1, "an IndexSet lists its segment types");
+  using first_segment = std::tuple_element_t<0, std::tuple<SegmentTypes...>>;
+
+ public:
+  using value_type = typename first_segment::value_type;
+  using segment_variant = std::variant<SegmentTypes...>;
+  template <typename S>
+  void push_back(const S& seg) {
+    static_assert(one_of<S, SegmentTypes...>::value, "segment type not listed in the IndexSet");
+    segs_.emplace_back(seg);
+  }
+  template <typename S>
+  void push_front(const S& seg) {
+    static_assert(one_of<S, SegmentTypes...>::value, "segment type not listed in the IndexSet");
+    segs_.insert(segs_.begin(), segment_variant(seg));
+  }
+  size_t getNumSegments() const { return segs_.size(); }
+  // total number of indices
+  size_t getLength() const {
+    size_t n = 0;
+    for (const auto& v : segs_) n += size_t(std::visit([](const auto& g) { return Index_type(g.size()); }, v));
+    return n;
+  }
+  // position of segment i's first index in the whole traversal
+  Index_type getStartingIcount(size_t i) const {
+    Index_type n = 0;
+    for (size_t k = 0; k < i && k < segs_.size(); ++k)
+      n += std::visit([](const auto& g) { return Index_type(g.size()); }, segs_[k]);
+    return n;
+  }
+  template <typename S>
+  const S& getSegment(size_t i) const {
+    return std::get<S>(segs_.at(i));
+  }
+  const std::vector<segment_variant>& segments() const { return segs_; }
+
+ private:
+  std::vector<segment_variant> segs_;
 };
+using IndexSet = TypedIndexSet<RangeSegment, ListSegment, RangeStrideSegment>;
 
 // Element k of a segment, and its length (loop executors, forall params).
 namespace detail {
@@ -839,9 +880,9 @@ void forall_impl(omp_parallel_for_exec, const TypedRangeSegment<T>& r, Body&& bo
   forall_impl(seq_exec{}, r, body);
 #endif
 }
-template <typename Pol, typename Body, typename T>
-void forall_impl(Pol p, const TypedIndexSet<T>& is, Body&& body) {
-  for (const auto& s : is.segs) forall_impl(p, s, body);
+template <typename Pol, typename Body, typename... Segs>
+void forall_impl(Pol p, const TypedIndexSet<Segs...>& is, Body&& body) {
+  for (const auto& s : is.segments()) std::visit([&](const auto& seg) { forall_impl(p, seg, body); }, s);
 }
 
 // forall with expt params on host: each param gets a ValOp local starting
@@ -1330,13 +1371,14 @@ void forall_Icount(Seg&& seg, Index_type icount, Body&& body) {
   detail::IcountAdapter<std::decay_t<Seg>, std::decay_t<Body>> ad{seg, body, icount};
   forall<Pol>(TypedRangeSegment<Index_type>(0, detail::seg_len(seg)), ad);
 }
-template <typename Pol, typename T, typename Body>
-void forall_Icount(const TypedIndexSet<T>& is, Body&& body) {
+template <typename Pol, typename... Segs, typename Body>
+void forall_Icount(const TypedIndexSet<Segs...>& is, Body&& body) {
   Index_type ic = 0;
-  for (const auto& s : is.segs) {
-    forall_Icount<Pol>(s, ic, body);
-    ic += detail::seg_len(s);
-  }
+  for (const auto& s : is.segments())
+    std::visit([&](const auto& seg) {
+      forall_Icount<Pol>(seg, ic, body);
+      ic += detail::seg_len(seg);
+    }, s);
 }
 
 // ----------------------------------------------------------------- scans

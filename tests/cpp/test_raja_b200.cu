@@ -217,7 +217,7 @@ void test_forall_and_params() {
   CHECK("expt_reduceloc_min", vmin == hvmin && imin == himin);
 
   // IndexSet: all segments in one launch
-  RAJA::TypedIndexSet<Index_type> is;
+  RAJA::TypedIndexSet<RAJA::RangeSegment> is;
   is.push_back(RAJA::RangeSegment(0, 100));
   is.push_back(RAJA::RangeSegment(1000, 5000));
   is.push_back(RAJA::RangeSegment(7, 7));
@@ -1135,7 +1135,7 @@ void test_edge_cases() {
   {
     // forall_Icount on b200 over an IndexSet and a list segment, with a
     // captured reducer
-    RAJA::TypedIndexSet<Index_type> is;
+    RAJA::TypedIndexSet<RAJA::RangeSegment> is;
     is.push_back(RAJA::RangeSegment(0, 5000));
     is.push_back(RAJA::RangeSegment(7000, 7003));
     is.push_back(RAJA::RangeSegment(9000, 12000));
@@ -1155,6 +1155,27 @@ void test_edge_cases() {
                               [=] RAJA_HOST_DEVICE(Index_type ic, Index_type idx) { w[ic - 100] = idx * 2; });
     okc = okc && w[0] == 80 && w[1] == 6 && w[2] == 34 && w[3] == 16;
     CHECK("forall_icount_b200", okc);
+    // a mixed IndexSet on b200: per-segment launches, reducer across them
+    Index_type* ml = managed<Index_type>(3);
+    ml[0] = 6000; ml[1] = 5; ml[2] = 6500;
+    RAJA::IndexSet mis;
+    mis.push_back(RAJA::RangeSegment(0, 3000));
+    mis.push_back(RAJA::ListSegment(ml, 3));
+    mis.push_back(RAJA::RangeStrideSegment(7000, 8000, 7));
+    for (int i = 0; i < 8003; ++i) w[i] = -1;
+    RAJA::ReduceSum<red, long long> msum(0);
+    RAJA::forall<exec>(mis, [=] RAJA_HOST_DEVICE(Index_type i) { msum += i; });
+    RAJA::forall_Icount<exec>(mis, [=] RAJA_HOST_DEVICE(Index_type ic, Index_type i) { w[ic] = i; });
+    long long want = 0;
+    std::vector<Index_type> order;
+    for (Index_type i = 0; i < 3000; ++i) order.push_back(i);
+    order.push_back(6000); order.push_back(5); order.push_back(6500);
+    for (Index_type i = 7000; i < 8000; i += 7) order.push_back(i);
+    for (Index_type i : order) want += i;
+    bool okm = msum.get() == want && mis.getLength() == order.size();
+    for (size_t k = 0; k < order.size(); ++k) okm = okm && w[k] == order[k];
+    CHECK("indexset_mixed_b200", okm);
+    cudaFree(ml);
     cudaFree(w);
     cudaFree(lst);
   }

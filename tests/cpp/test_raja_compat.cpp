@@ -111,7 +111,7 @@ int main() {
   }
   // forall_Icount over a segment and over an IndexSet (test-forall-IcountIndexSet.hpp)
   {
-    RAJA::TypedIndexSet<Index_type> is;
+    RAJA::TypedIndexSet<RAJA::RangeSegment> is;
     is.push_back(RAJA::RangeSegment(0, 5));
     is.push_back(RAJA::RangeSegment(10, 13));
     is.push_back(RAJA::RangeSegment(20, 24));
@@ -124,6 +124,24 @@ int main() {
     RAJA::forall_Icount<RAJA::seq_exec>(RAJA::RangeStrideSegment(5, 11, 2), Index_type(0),
                                         [=](Index_type ic, Index_type idx) { g2p[ic] = idx; });
     CHECK("forall_icount_indexset_and_stride", got == want && g2 == std::vector<Index_type>({5, 7, 9}));
+  }
+  // a mixed IndexSet: range, list and strided segments (buildIndexSet in the
+  // reference's IndexSet tests); traversal order and counts
+  {
+    const Index_type lst[3] = {50, 41, 47};
+    RAJA::IndexSet is;
+    is.push_back(RAJA::RangeSegment(0, 4));
+    is.push_back(RAJA::ListSegment(lst, 3));
+    is.push_back(RAJA::RangeStrideSegment(60, 69, 3));
+    is.push_front(RAJA::RangeSegment(100, 102));
+    std::vector<Index_type> seen, ics;
+    RAJA::forall<RAJA::seq_exec>(is, [&](Index_type i) { seen.push_back(i); });
+    RAJA::forall_Icount<RAJA::seq_exec>(is, [&](Index_type ic, Index_type i) { ics.push_back(ic * 1000 + i); });
+    const std::vector<Index_type> want{100, 101, 0, 1, 2, 3, 50, 41, 47, 60, 63, 66};
+    bool oki = seen == want && is.getNumSegments() == 4 && is.getLength() == 12 && is.getStartingIcount(2) == 6;
+    for (size_t k = 0; k < ics.size(); ++k) oki = oki && ics[k] == Index_type(k) * 1000 + want[k];
+    oki = oki && is.getSegment<RAJA::ListSegment>(2).size() == 3;
+    CHECK("indexset_mixed_segments", oki && ics.size() == 12);
   }
   int named = 0;
   RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 4), RAJA::Name("only"),
