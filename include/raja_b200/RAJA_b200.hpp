@@ -447,6 +447,7 @@ class ReduceBitOr<b200_reduce, T> : public b200::detail::DevReducer<b200::detail
   RAJA_HOST_DEVICE const ReduceBitOr& operator|=(T v) const { this->val_ |= v; return *this; }
   T get() const { return this->fold(); }
   operator T() const { return get(); }
+  void reset(T v) { this->reset_value(v); }
 };
 template <typename T>
 class ReduceBitAnd<b200_reduce, T> : public b200::detail::DevReducer<b200::detail::AndK<T>> {
@@ -458,6 +459,7 @@ class ReduceBitAnd<b200_reduce, T> : public b200::detail::DevReducer<b200::detai
   RAJA_HOST_DEVICE const ReduceBitAnd& operator&=(T v) const { this->val_ &= v; return *this; }
   T get() const { return this->fold(); }
   operator T() const { return get(); }
+  void reset(T v) { this->reset_value(v); }
 };
 // MinLoc / MaxLoc: the first extreme (lowest location among equal values),
 // and the init pair wins ties (pattern/detail/reduce.hpp:287-358).

@@ -33,6 +33,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <iterator>
 #include <limits>
 #include <memory>
 #include <stdexcept>
@@ -131,24 +132,65 @@ struct greater {
 }  // namespace operators
 
 // ------------------------------------------------------------- segments
+// Random-access iterator over the values start, start + step, ... (the role
+// of Iterators::numeric_iterator / strided_numeric_iterator,
+// index/RangeSegment.hpp, index/RangeStrideSegment.hpp).
+template <typename T>
+struct NumericIterator {
+  using iterator_category = std::random_access_iterator_tag;
+  using value_type = T;
+  using difference_type = Index_type;
+  using pointer = const T*;
+  using reference = T;
+  T v, step;
+  RAJA_HOST_DEVICE T operator*() const { return v; }
+  RAJA_HOST_DEVICE T operator[](difference_type k) const { return T(v + T(k) * step); }
+  RAJA_HOST_DEVICE NumericIterator& operator++() { v += step; return *this; }
+  RAJA_HOST_DEVICE NumericIterator operator++(int) { NumericIterator t = *this; v += step; return t; }
+  RAJA_HOST_DEVICE NumericIterator& operator--() { v -= step; return *this; }
+  RAJA_HOST_DEVICE NumericIterator& operator+=(difference_type k) { v += T(k) * step; return *this; }
+  RAJA_HOST_DEVICE NumericIterator& operator-=(difference_type k) { v -= T(k) * step; return *this; }
+  RAJA_HOST_DEVICE NumericIterator operator+(difference_type k) const { return {T(v + T(k) * step), step}; }
+  RAJA_HOST_DEVICE NumericIterator operator-(difference_type k) const { return {T(v - T(k) * step), step}; }
+  RAJA_HOST_DEVICE difference_type operator-(const NumericIterator& o) const {
+    return difference_type((v - o.v) / step);
+  }
+  RAJA_HOST_DEVICE bool operator==(const NumericIterator& o) const { return v == o.v; }
+  RAJA_HOST_DEVICE bool operator!=(const NumericIterator& o) const { return v != o.v; }
+  RAJA_HOST_DEVICE bool operator<(const NumericIterator& o) const { return (o - *this) > 0; }
+};
+
 template <typename T>
 struct TypedRangeSegment {
   using value_type = T;
+  using iterator = NumericIterator<T>;
   T b, e;
   RAJA_HOST_DEVICE TypedRangeSegment(T begin, T end) : b(begin), e(end < begin ? begin : end) {}
   RAJA_HOST_DEVICE T size() const { return e - b; }
+  RAJA_HOST_DEVICE iterator begin() const { return {b, T(1)}; }
+  RAJA_HOST_DEVICE iterator end() const { return {e, T(1)}; }
+  // the sub-range [begin + off, begin + off + len), clipped to this one
+  RAJA_HOST_DEVICE TypedRangeSegment slice(T off, T len) const {
+    const T lo = b + off < e ? T(b + off) : e;
+    const T hi = lo + len < e ? T(lo + len) : e;
+    return TypedRangeSegment(lo, hi);
+  }
+  RAJA_HOST_DEVICE bool operator==(const TypedRangeSegment& o) const { return b == o.b && e == o.e; }
 };
 using RangeSegment = TypedRangeSegment<Index_type>;
 
 template <typename T>
 struct TypedRangeStrideSegment {
   using value_type = T;
+  using iterator = NumericIterator<T>;
   T b, e, s;
   RAJA_HOST_DEVICE TypedRangeStrideSegment(T begin, T end, T stride) : b(begin), e(end), s(stride) {}
   RAJA_HOST_DEVICE T size() const {
     if (s > 0) return e > b ? (e - b + s - 1) / s : 0;
     return b > e ? (b - e + (-s) - 1) / (-s) : 0;
   }
+  RAJA_HOST_DEVICE iterator begin() const { return {b, s}; }
+  RAJA_HOST_DEVICE iterator end() const { return {T(b + size() * s), s}; }
 };
 using RangeStrideSegment = TypedRangeStrideSegment<Index_type>;
 
@@ -161,6 +203,8 @@ struct TypedListSegment {
   Index_type len;
   RAJA_HOST_DEVICE TypedListSegment(const T* d, Index_type n) : data(d), len(n) {}
   RAJA_HOST_DEVICE Index_type size() const { return len; }
+  RAJA_HOST_DEVICE const T* begin() const { return data; }
+  RAJA_HOST_DEVICE const T* end() const { return data + len; }
 };
 using ListSegment = TypedListSegment<Index_type>;
 

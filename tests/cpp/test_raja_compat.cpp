@@ -143,6 +143,17 @@ int main() {
     oki = oki && is.getSegment<RAJA::ListSegment>(2).size() == 3;
     CHECK("indexset_mixed_segments", oki && ics.size() == 12);
   }
+  // segment iterators and slices (index/RangeSegment.hpp)
+  {
+    RAJA::RangeSegment r(3, 10);
+    RAJA::RangeStrideSegment rs(2, 11, 3);
+    const std::vector<Index_type> vr(r.begin(), r.end()), vs(rs.begin(), rs.end());
+    const RAJA::RangeSegment sl = r.slice(2, 10);
+    CHECK("segment_iterators_slice",
+          r.end() - r.begin() == 7 && *r.begin() == 3 && r.begin()[2] == 5 &&
+              vr == std::vector<Index_type>({3, 4, 5, 6, 7, 8, 9}) && vs == std::vector<Index_type>({2, 5, 8}) &&
+              rs.end() - rs.begin() == 3 && sl == RAJA::RangeSegment(5, 10));
+  }
   int named = 0;
   RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 4), RAJA::Name("only"),
                                [&](Index_type) { ++named; });
