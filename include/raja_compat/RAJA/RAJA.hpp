@@ -293,7 +293,19 @@ Span<T> make_span(T* p, Index_type n) { return Span<T>{p, n}; }
 
 // ------------------------------------------------------------ policies
 struct seq_exec {};
+struct simd_exec {};  // policy/simd/policy.hpp:41: the sequential loop, vectorised by the compiler
 struct omp_parallel_for_exec {};
+// OpenMP loop schedules (policy/openmp/policy.hpp:238-252); a chunk size of
+// 0 leaves it to the runtime
+enum class omp_schedule { static_, dynamic_, guided_ };
+template <omp_schedule S, int Chunk>
+struct omp_parallel_for_schedule_exec {};
+template <int Chunk = 0>
+using omp_parallel_for_static_exec = omp_parallel_for_schedule_exec<omp_schedule::static_, Chunk>;
+template <int Chunk = 0>
+using omp_parallel_for_dynamic_exec = omp_parallel_for_schedule_exec<omp_schedule::dynamic_, Chunk>;
+template <int Chunk = 0>
+using omp_parallel_for_guided_exec = omp_parallel_for_schedule_exec<omp_schedule::guided_, Chunk>;
 struct seq_reduce {};
 struct omp_reduce {};
 struct seq_multi_reduce {};
@@ -922,6 +934,45 @@ void forall_impl(omp_parallel_for_exec, const TypedRangeSegment<T>& r, Body&& bo
   }
 #else
   forall_impl(seq_exec{}, r, body);
+#endif
+}
+// simd_exec: the sequential loop (any segment kind)
+template <typename Seg, typename Body, typename = decltype(detail::seg_len(std::declval<const Seg&>()))>
+void forall_impl(simd_exec, const Seg& seg, Body&& body) {
+  auto b = body;
+  const Index_type n = detail::seg_len(seg);
+#pragma omp simd
+  for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+}
+// scheduled OpenMP loops over any segment kind; the body is copied once per
+// thread, as for omp_parallel_for_exec
+template <omp_schedule S, int Chunk, typename Seg, typename Body,
+          typename = decltype(detail::seg_len(std::declval<const Seg&>()))>
+void forall_impl(omp_parallel_for_schedule_exec<S, Chunk>, const Seg& seg, Body&& body) {
+  const Index_type n = detail::seg_len(seg);
+#if defined(_OPENMP)
+#pragma omp parallel
+  {
+    auto b = body;
+    if (S == omp_schedule::static_) {
+      if (Chunk > 0) {
+#pragma omp for schedule(static, Chunk > 0 ? Chunk : 1)
+        for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+      } else {
+#pragma omp for schedule(static)
+        for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+      }
+    } else if (S == omp_schedule::dynamic_) {
+#pragma omp for schedule(dynamic, Chunk > 0 ? Chunk : 1)
+      for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+    } else {
+#pragma omp for schedule(guided, Chunk > 0 ? Chunk : 1)
+      for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+    }
+  }
+#else
+  auto b = body;
+  for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
 #endif
 }
 template <typename Pol, typename Body, typename... Segs>

@@ -154,6 +154,17 @@ int main() {
               vr == std::vector<Index_type>({3, 4, 5, 6, 7, 8, 9}) && vs == std::vector<Index_type>({2, 5, 8}) &&
               rs.end() - rs.begin() == 3 && sl == RAJA::RangeSegment(5, 10));
   }
+  // simd and scheduled OpenMP policies agree with seq (resource-forall example policies)
+  {
+    std::vector<long> r0(1000, 0), r1(1000, 0), r2(1000, 0), r3(1000, 0);
+    long *p0 = r0.data(), *p1 = r1.data(), *p2 = r2.data(), *p3 = r3.data();
+    RAJA::forall<RAJA::simd_exec>(RAJA::RangeSegment(0, 1000), [=](Index_type i) { p0[i] = 3 * i; });
+    RAJA::forall<RAJA::omp_parallel_for_static_exec<>>(RAJA::RangeSegment(0, 1000), [=](Index_type i) { p1[i] = 3 * i; });
+    RAJA::forall<RAJA::omp_parallel_for_dynamic_exec<16>>(RAJA::RangeStrideSegment(0, 1000, 1),
+                                                          [=](Index_type i) { p2[i] = 3 * i; });
+    RAJA::forall<RAJA::omp_parallel_for_guided_exec<8>>(RAJA::RangeSegment(0, 1000), [=](Index_type i) { p3[i] = 3 * i; });
+    CHECK("simd_and_scheduled_omp_policies", r0 == r1 && r1 == r2 && r2 == r3 && r3[999] == 2997);
+  }
   int named = 0;
   RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 4), RAJA::Name("only"),
                                [&](Index_type) { ++named; });
