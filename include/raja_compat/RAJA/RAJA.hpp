@@ -941,7 +941,9 @@ template <typename Seg, typename Body, typename = decltype(detail::seg_len(std::
 void forall_impl(simd_exec, const Seg& seg, Body&& body) {
   auto b = body;
   const Index_type n = detail::seg_len(seg);
+#if defined(_OPENMP)
 #pragma omp simd
+#endif
   for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
 }
 // scheduled OpenMP loops over any segment kind; the body is copied once per
