@@ -53,7 +53,7 @@ def _check(prims, orc, op, dt, n, nbins, seed, init=None):
 @pytest.mark.parametrize("dt", TYPES)
 @pytest.mark.parametrize("op", ["sum", "min", "max"])
 def test_multi_reduce_matches_seq(prims, orc, op, dt):
-    for i, (n, nbins) in enumerate(((1, 1), (100003, 1), (100003, 7), (100003, 256),
+    for i, (n, nbins) in enumerate(((0, 5), (1, 1), (100003, 1), (100003, 7), (100003, 256),
                                     (1 << 20, 5000), (1 << 20, 65536), (300007, 200000))):
         _check(prims, orc, op, dt, n, nbins, 10 * i + 1)
 
