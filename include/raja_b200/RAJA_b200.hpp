@@ -1415,14 +1415,17 @@ wg_one_kernel(const WgLoop* loops, int which, const unsigned char* bodies) {
 }  // namespace detail
 }  // namespace b200
 
-template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename Index, typename Alloc>
-class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, xargs<>, Alloc>;
+template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
+class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc>;
 
-template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename Index, typename Alloc>
-class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, xargs<>, Alloc> {
+template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
+class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc> {
  public:
-  using policy = WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>;
+  using policy = WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>;
   using group_type = WorkGroup<policy, Index, xargs<>, Alloc>;
+  WorkPool() = default;
+  template <typename A>
+  explicit WorkPool(const A&) {}  // the allocator: device storage comes from cudaMalloc
   template <typename T, typename Body>
   void enqueue(TypedRangeSegment<T> seg, Body body) {
     static_assert(std::is_trivially_copyable<Body>::value,
@@ -1445,10 +1448,10 @@ class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, 
   std::vector<unsigned char> m_bytes;
 };
 
-template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename Index, typename Alloc>
-class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, xargs<>, Alloc> {
+template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
+class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc> {
  public:
-  using policy = WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>;
+  using policy = WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>;
   WorkGroup() = default;
   WorkGroup(const WorkGroup&) = delete;
   WorkGroup(WorkGroup&& o) noexcept { *this = std::move(o); }
@@ -1529,9 +1532,9 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index,
   size_t m_loops_off = 0, m_tiles_off = 0, m_bodies_off = 0;
 };
 
-template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename Index, typename Alloc>
-typename WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, xargs<>, Alloc>::group_type
-WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE>, Index, xargs<>, Alloc>::instantiate() {
+template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
+typename WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc>::group_type
+WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc>::instantiate() {
   group_type g;
   g.setup(m_loops, m_bytes);
   m_loops.clear();

@@ -1656,7 +1656,15 @@ struct unordered {};
 struct array_of_pointers {};
 struct ragged_array_of_objects {};
 struct constant_stride_array_of_objects {};
-template <typename EXEC, typename ORDER = ordered, typename STORAGE = ragged_array_of_objects>
+// dispatch policies (policy/WorkGroup.hpp): how a runner calls the stored
+// loops; every b200 and host runner here calls them directly, so the
+// choice is accepted and has no effect
+struct indirect_function_call_dispatch {};
+struct indirect_virtual_function_dispatch {};
+template <typename... Callables>
+struct direct_dispatch {};
+template <typename EXEC, typename ORDER = ordered, typename STORAGE = ragged_array_of_objects,
+          typename DISPATCH = indirect_function_call_dispatch>
 struct WorkGroupPolicy {
   using exec_policy = EXEC;
   using order_policy = ORDER;
@@ -1689,10 +1697,13 @@ struct HostLoops {
 };
 }  // namespace detail
 
-template <typename EXEC, typename ORDER, typename STORAGE, typename Index, typename Alloc>
-class WorkPool<WorkGroupPolicy<EXEC, ORDER, STORAGE>, Index, xargs<>, Alloc> {
+template <typename EXEC, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
+class WorkPool<WorkGroupPolicy<EXEC, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc> {
  public:
-  using policy = WorkGroupPolicy<EXEC, ORDER, STORAGE>;
+  using policy = WorkGroupPolicy<EXEC, ORDER, STORAGE, DISPATCH>;
+  WorkPool() = default;
+  template <typename A>
+  explicit WorkPool(const A&) {}  // the allocator (pattern/WorkGroup.hpp:272-300); host loops need none
   template <typename Seg, typename Body>
   void enqueue(Seg seg, Body body) {
     m_loops.push_back([seg, body]() { forall<EXEC>(seg, body); });
@@ -1710,10 +1721,10 @@ class WorkPool<WorkGroupPolicy<EXEC, ORDER, STORAGE>, Index, xargs<>, Alloc> {
   std::vector<std::function<void()>> m_loops;
 };
 
-template <typename EXEC, typename ORDER, typename STORAGE, typename Index, typename Alloc>
-class WorkGroup<WorkGroupPolicy<EXEC, ORDER, STORAGE>, Index, xargs<>, Alloc> {
+template <typename EXEC, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
+class WorkGroup<WorkGroupPolicy<EXEC, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc> {
  public:
-  using policy = WorkGroupPolicy<EXEC, ORDER, STORAGE>;
+  using policy = WorkGroupPolicy<EXEC, ORDER, STORAGE, DISPATCH>;
   using resource_type = typename resources::get_resource<EXEC>::type;
   // run([resource]) (pattern/WorkGroup.hpp:357-370): the loops run on the
   // resource, the policy's default one when none is given.

@@ -9,6 +9,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <memory>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -370,6 +371,29 @@ void workgroup_case(const char* tag) {
 }
 
 // MultiReduce on b200 against seq, and b200 atomics in device code
+// WorkGroup with a dispatch policy and an allocator; pool reuse after
+// instantiate and a group run twice (test-workgroup-*-MultipleReuse.hpp)
+void test_workgroup_reuse() {
+  const int n = 5000;
+  int* a = managed<int>(2 * n);
+  for (int i = 0; i < 2 * n; ++i) a[i] = 0;
+  using wpol = RAJA::WorkGroupPolicy<RAJA::b200_work<256>, RAJA::unordered, RAJA::ragged_array_of_objects,
+                                     RAJA::indirect_function_call_dispatch>;
+  RAJA::WorkPool<wpol, Index_type, RAJA::xargs<>, std::allocator<char>> pool(std::allocator<char>{});
+  bool ok = true;
+  for (int reuse = 0; reuse < 2; ++reuse) {
+    pool.enqueue(RAJA::RangeSegment(0, n), [=] __device__(Index_type i) { a[i] += 1; });
+    pool.enqueue(RAJA::RangeSegment(n, 2 * n), [=] __device__(Index_type i) { a[i] += 10; });
+    auto group = pool.instantiate();
+    ok = ok && pool.num_loops() == 0;
+    group.run();
+    group.run();
+  }
+  for (int i = 0; i < 2 * n; ++i) ok = ok && a[i] == (i < n ? 4 : 40);
+  CHECK("workgroup_b200_dispatch_allocator_reuse", ok);
+  cudaFree(a);
+}
+
 void test_multi_reduce_and_atomics() {
   const Index_type n = 200003;
   const int nb = 37;
@@ -1251,6 +1275,7 @@ void perf_lambda_paths() {
 
 int main() {
   setvbuf(stdout, nullptr, _IONBF, 0);  // every PASS line reaches the log even if the run aborts
+  test_workgroup_reuse();
   test_multi_reduce_and_atomics();
   test_reducers();
   test_forall_and_params();

@@ -1,6 +1,7 @@
 // Host-only checks of the raja_compat front-end (seq_exec / omp policies)
 // against the known answers of the reference's functional tests.
 #include <cstdio>
+#include <memory>
 #include <numeric>
 #include <vector>
 
@@ -164,6 +165,26 @@ int main() {
                                                           [=](Index_type i) { p2[i] = 3 * i; });
     RAJA::forall<RAJA::omp_parallel_for_guided_exec<8>>(RAJA::RangeSegment(0, 1000), [=](Index_type i) { p3[i] = 3 * i; });
     CHECK("simd_and_scheduled_omp_policies", r0 == r1 && r1 == r2 && r2 == r3 && r3[999] == 2997);
+  }
+  // WorkGroup with a dispatch policy and an allocator, pool and group reuse
+  // (test-workgroup-*-MultipleReuse.hpp)
+  {
+    using wpol = RAJA::WorkGroupPolicy<RAJA::seq_exec, RAJA::reverse_ordered, RAJA::array_of_pointers,
+                                       RAJA::indirect_function_call_dispatch>;
+    RAJA::WorkPool<wpol, Index_type, RAJA::xargs<>, std::allocator<char>> pool(std::allocator<char>{});
+    std::vector<int> w2(40, 0);
+    int* w2p = w2.data();
+    bool okw = true;
+    for (int reuse = 0; reuse < 2; ++reuse) {
+      pool.enqueue(RAJA::RangeSegment(0, 20), [=](Index_type i) { w2p[i] += 1; });
+      pool.enqueue(RAJA::RangeSegment(20, 40), [=](Index_type i) { w2p[i] += 10; });
+      auto grp = pool.instantiate();
+      okw = okw && pool.num_loops() == 0;
+      grp.run();
+      grp.run();  // a group runs again
+    }
+    for (int i = 0; i < 40; ++i) okw = okw && w2[i] == (i < 20 ? 4 : 40);
+    CHECK("workgroup_dispatch_allocator_reuse", okw);
   }
   int named = 0;
   RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 4), RAJA::Name("only"),
