@@ -255,6 +255,23 @@ def cpu_model() -> str:
 
 
 # ------------------------------------------------------------- reference
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest x over all ranks (x itself on one rank): every rank's
+    timed region ends at the slowest rank."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_gbs(world: int, bytes_per_step: float, steps: int, ms: float) -> float:
+    """Whole-job GB/s: every rank processes its own step (weak scaling), so
+    the job moves world x bytes per step in the slowest rank's time."""
+    return world * bytes_per_step * steps / (ms / 1e3) / 1e9
+
+
 def run_reference(args, rank: int, world: int):
     if rank != 0:
         return
@@ -365,13 +382,9 @@ def main():
         dist.barrier()
     clk = clocks.stop()
     raja_gb300.synchronize()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
     ms_per_step = ms / args.steps
-    value = world * step_bytes * args.steps / (ms / 1e3) / 1e9
+    value = aggregate_gbs(world, step_bytes, args.steps, ms)
     launches_per_step = None
 
     # ---- per-primitive breakdown and per-kernel times (CUDA events on the
@@ -977,13 +990,9 @@ def run_e2e(args, lib, inputs, outs, n, stream, table, dist):
     stream.wait_stream(h2d_s)
     b.record(stream)
     torch.cuda.synchronize()
-    ms = a.elapsed_time(b)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(a.elapsed_time(b), dist, "cuda")
     world = dist.get_world_size() if dist else 1
-    value = world * sum(table.values()) * args.e2e_steps / (ms / 1e3) / 1e9
+    value = aggregate_gbs(world, sum(table.values()), args.e2e_steps, ms)
     return {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
             "ms_per_step": round(ms / args.e2e_steps, 3),
