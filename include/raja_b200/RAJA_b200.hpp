@@ -82,14 +82,26 @@ inline void check(int rc, const char* what) {
 // that gave up), like res.wait() + cudaErrchk.
 inline void wait() { check(b200_stream_synchronize(stream()), "b200 synchronize"); }
 
+// Devices a process may use (per-device caches are this long).
+constexpr int kMaxDevices = 64;
+
+inline int current_device_index() {
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) throw std::runtime_error("b200: device index out of range");
+  return dev;
+}
+
+// SM count of the current device, queried once per device.
 inline int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
-    check_cuda(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev), "sm count");
+  static std::atomic<int> n[kMaxDevices] = {};
+  const int dev = current_device_index();
+  int v = n[dev].load(std::memory_order_acquire);
+  if (v == 0) {
+    check_cuda(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev), "sm count");
+    n[dev].store(v, std::memory_order_release);
   }
-  return n;
+  return v;
 }
 
 namespace detail {
@@ -108,13 +120,21 @@ inline LaunchCtx& ctx() {
   return c;
 }
 
-// Grid for a kernel: one block per BLOCK elements, capped at the resident
-// blocks of the whole GPU (the loop grid-strides beyond that).
-template <class Kernel>
-inline unsigned grid_for(Kernel k, int block, long long len) {
-  int bps = 0;
-  check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, block, 0), "occupancy");
-  long long cap = (long long)sm_count() * (bps > 0 ? bps : 1);
+// Grid for a kernel that always runs `block` threads: one block per `block`
+// elements, capped at the resident blocks of the whole GPU (the loop
+// grid-strides beyond that).  The occupancy query runs once per (kernel,
+// device), as RAJA's CUDA back-end caches it after the first launch.
+template <auto Kernel>
+inline unsigned grid_for(int block, long long len) {
+  static std::atomic<long long> resident[kMaxDevices] = {};
+  const int dev = current_device_index();
+  long long cap = resident[dev].load(std::memory_order_acquire);
+  if (cap == 0) {
+    int bps = 0;
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, Kernel, block, 0), "occupancy");
+    cap = (long long)sm_count() * (bps > 0 ? bps : 1);
+    resident[dev].store(cap, std::memory_order_release);
+  }
   long long g = (len + block - 1) / block;
   if (g > cap) g = cap;
   if (g < 1) g = 1;
@@ -772,7 +792,7 @@ void forall_impl(b200_exec<BLOCK, Async>, const TypedRangeSegment<T>& r, Body&& 
   const long long len = (long long)r.size();
   if (len <= 0) return;
   auto k = b200::detail::forall_range_kernel<BLOCK, B, T>;
-  const unsigned g = b200::detail::grid_for(k, BLOCK, len);
+  const unsigned g = b200::detail::grid_for<b200::detail::forall_range_kernel<BLOCK, B, T>>(BLOCK, len);
   cudaStream_t s = b200::stream();
   B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
   k<<<g, BLOCK, 0, s>>>(lb, r.b, len);
@@ -784,7 +804,7 @@ void forall_impl(b200_exec<BLOCK, Async>, const TypedRangeStrideSegment<T>& r, B
   const long long len = (long long)r.size();
   if (len <= 0) return;
   auto k = b200::detail::forall_stride_kernel<BLOCK, B, T>;
-  const unsigned g = b200::detail::grid_for(k, BLOCK, len);
+  const unsigned g = b200::detail::grid_for<b200::detail::forall_stride_kernel<BLOCK, B, T>>(BLOCK, len);
   cudaStream_t s = b200::stream();
   B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
   k<<<g, BLOCK, 0, s>>>(lb, r.b, r.s, len);
@@ -796,7 +816,7 @@ void forall_impl(b200_exec<BLOCK, Async>, const TypedListSegment<T>& l, Body&& b
   const long long len = (long long)l.size();
   if (len <= 0) return;
   auto k = b200::detail::forall_list_kernel<BLOCK, B, T>;
-  const unsigned g = b200::detail::grid_for(k, BLOCK, len);
+  const unsigned g = b200::detail::grid_for<b200::detail::forall_list_kernel<BLOCK, B, T>>(BLOCK, len);
   cudaStream_t s = b200::stream();
   B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
   k<<<g, BLOCK, 0, s>>>(lb, l.data, len);
@@ -845,7 +865,7 @@ void forall_impl(b200_exec<BLOCK, Async> pol, const TypedIndexSet<Segs...>& is, 
                                      cudaMemcpyHostToDevice, s),
                      "indexset table");
     auto k = b200::detail::forall_indexset_kernel<BLOCK, B, T>;
-    const unsigned g = b200::detail::grid_for(k, BLOCK, total);
+    const unsigned g = b200::detail::grid_for<b200::detail::forall_indexset_kernel<BLOCK, B, T>>(BLOCK, total);
     B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
     k<<<g, BLOCK, 0, s>>>(lb, d_begins, d_prefix, nseg, total);
     b200::check_cuda(cudaGetLastError(), "b200 forall indexset");
@@ -953,7 +973,8 @@ void forall_params_impl(b200_exec<BLOCK, Async>, const Seg& r, Body&& body, Red&
   using Slots = b200::detail::DTuple<b200::detail::DevSlot<typename b200::detail::ParamKind<Red>::type::V>...>;
   const long long len = (long long)::RAJA::detail::seg_len(r);
   auto k = b200::detail::forall_params_kernel<BLOCK, B, Seg, Red...>;
-  const unsigned g = b200::detail::grid_for(k, BLOCK, len > 0 ? len : 1);
+  const unsigned g =
+      b200::detail::grid_for<b200::detail::forall_params_kernel<BLOCK, B, Seg, Red...>>(BLOCK, len > 0 ? len : 1);
   cudaStream_t s = b200::stream();
   void* blocks[sizeof...(Red) + 1] = {};
   size_t bi = 0;
@@ -1370,16 +1391,21 @@ template <class Body>
 __global__ void wg_get_fn(wg_fn* out) {
   *out = wg_run<Body>;
 }
+// The address is per device, so it is cached per device.
 template <class Body>
 inline wg_fn wg_fn_of() {
-  static wg_fn fp = nullptr;
+  static std::atomic<wg_fn> cache[kMaxDevices] = {};
+  const int dev = current_device_index();
+  wg_fn fp = cache[dev].load(std::memory_order_acquire);
   if (!fp) {
     wg_fn* d = nullptr;
     check_cuda(cudaMalloc(&d, sizeof(wg_fn)), "WorkPool dispatcher");
     wg_get_fn<Body><<<1, 1>>>(d);
-    check_cuda(cudaGetLastError(), "WorkPool dispatcher");
-    check_cuda(cudaMemcpy(&fp, d, sizeof(fp), cudaMemcpyDeviceToHost), "WorkPool dispatcher");
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(&fp, d, sizeof(fp), cudaMemcpyDeviceToHost);
     cudaFree(d);
+    check_cuda(e, "WorkPool dispatcher");
+    cache[dev].store(fp, std::memory_order_release);
   }
   return fp;
 }
@@ -1507,7 +1533,7 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
     if (std::is_same<ORDER, unordered>::value) {
       if (m_ntiles > 0) {
         auto k = b200::detail::wg_kernel<BLOCK>;
-        const unsigned g = b200::detail::grid_for(k, BLOCK, m_ntiles * BLOCK);
+        const unsigned g = b200::detail::grid_for<b200::detail::wg_kernel<BLOCK>>(BLOCK, m_ntiles * BLOCK);
         k<<<g, BLOCK, 0, s>>>(tiles, m_ntiles, loops, bodies);
       }
     } else {
@@ -1515,7 +1541,7 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
       auto k = b200::detail::wg_one_kernel<BLOCK>;
       for (int i = 0; i < m_nloops; ++i) {
         const int which = std::is_same<ORDER, reverse_ordered>::value ? m_nloops - 1 - i : i;
-        const unsigned g = b200::detail::grid_for(k, BLOCK, 1ll << 22);
+        const unsigned g = b200::detail::grid_for<b200::detail::wg_one_kernel<BLOCK>>(BLOCK, 1ll << 22);
         k<<<g, BLOCK, 0, s>>>(loops, which, bodies);
       }
     }

@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -24,6 +25,9 @@ int fail(int code, const char* fmt, ...);
 int cuda_check(cudaError_t e, const char* what);
 // Clear the message of the calling thread (called on success paths).
 void clear_error();
+
+// Devices a process may use (the per-device tables are this long).
+constexpr int kMaxDevices = 64;
 
 struct DeviceProps {
   int device = -1;
@@ -107,6 +111,44 @@ struct Sizer {
     int _b200_rc = (call);             \
     if (_b200_rc != B200_OK) return _b200_rc; \
   } while (0)
+
+// Once-per-(kernel, device) launch setup: the dynamic shared-memory opt-in
+// (a per-device function attribute) and the resident blocks per SM.  Each
+// kernel keeps one `static KernelSetup`; concurrent first calls from
+// several host threads may both run the setup, which is idempotent.
+struct KernelSetup {
+  std::atomic<int> bps[kMaxDevices] = {};   // 0 until the device's first launch
+};
+template <class K>
+int kernel_setup(KernelSetup& ks, const DeviceProps& props, K kern, int block, size_t dyn_smem,
+                 int* bps) {
+  int v = ks.bps[props.device].load(std::memory_order_acquire);
+  if (v == 0) {
+    if (dyn_smem > 0)
+      B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn_smem)));
+    int b = 0;
+    B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, block, dyn_smem));
+    v = b > 0 ? b : 1;
+    ks.bps[props.device].store(v, std::memory_order_release);
+  }
+  *bps = v;
+  return B200_OK;
+}
+
+// Dynamic shared-memory opt-in, once per device, for a kernel whose size
+// varies per launch: set to the largest size it is ever launched with, so
+// that concurrent launches of different sizes never race on the attribute.
+struct SmemOptIn {
+  std::atomic<bool> done[kMaxDevices] = {};
+};
+template <class K>
+int smem_optin(SmemOptIn& so, const DeviceProps& props, K kern, size_t max_smem) {
+  if (!so.done[props.device].load(std::memory_order_acquire)) {
+    B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(max_smem)));
+    so.done[props.device].store(true, std::memory_order_release);
+  }
+  return B200_OK;
+}
 
 // ---------------------------------------------------------------- device
 

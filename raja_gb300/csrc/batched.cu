@@ -227,15 +227,11 @@ loop_axpy_sum_kernel(float a, const float* __restrict__ x, float* __restrict__ y
 template <int BLOCK, int ITEMS>
 int launch_batched(b200_batch_plan_s* p, float a, const float* const* xs, float* const* ys,
                    double* sums, int comp, cudaStream_t s) {
-  static int bps = 0;
+  static KernelSetup ks;
   DeviceProps props;
   B200_TRY(device_props(&props));
-  if (bps == 0) {
-    int b = 0;
-    B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_axpy_sum_kernel<BLOCK, ITEMS>,
-                                                            BLOCK, 0));
-    bps = b > 0 ? b : 1;
-  }
+  int bps = 0;
+  B200_TRY(kernel_setup(ks, props, batched_axpy_sum_kernel<BLOCK, ITEMS>, BLOCK, 0, &bps));
   int64_t grid = int64_t(props.sms) * bps;
   if (grid > p->ntiles) grid = p->ntiles;
   if (grid < 1) grid = 1;
@@ -660,14 +656,11 @@ int b200_loop_axpy_sum_f32(float a, const float* x, float* y, size_t n, double* 
   if (n > 0 && (!x || !y)) return fail(B200_ERR_ARG, "%s: null pointer", name);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   constexpr int BLOCK = 256, ITEMS = 8, TILE = BLOCK * ITEMS;
-  static int bps = 0;
+  static KernelSetup ks;
   DeviceProps props;
   B200_TRY(device_props(&props));
-  if (bps == 0) {
-    int b = 0;
-    B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, loop_axpy_sum_kernel<BLOCK, ITEMS>, BLOCK, 0));
-    bps = b > 0 ? b : 1;
-  }
+  int bps = 0;
+  B200_TRY(kernel_setup(ks, props, loop_axpy_sum_kernel<BLOCK, ITEMS>, BLOCK, 0, &bps));
   int64_t grid = (int64_t(n) + TILE - 1) / TILE;
   if (grid > int64_t(props.sms) * bps) grid = int64_t(props.sms) * bps;
   if (grid < 1) grid = 1;

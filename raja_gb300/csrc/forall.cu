@@ -54,14 +54,11 @@ template <class T>
 int run_axpy(const char* name, T a, const T* x, T* y, size_t n, b200_stream_t stream) {
   if (n == 0) return B200_OK;
   if (!x || !y) return fail(B200_ERR_ARG, "%s: null pointer", name);
-  static int bps = 0;
+  static KernelSetup ks;
   DeviceProps p;
   B200_TRY(device_props(&p));
-  if (bps == 0) {
-    int b = 0;
-    B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, axpy_kernel<T>, FBLOCK, 0));
-    bps = b > 0 ? b : 1;
-  }
+  int bps = 0;
+  B200_TRY(kernel_setup(ks, p, axpy_kernel<T>, FBLOCK, 0, &bps));
   const bool vec_ok = reinterpret_cast<uintptr_t>(x) % 16 == 0 &&
                       reinterpret_cast<uintptr_t>(y) % 16 == 0;
   const size_t work = vec_ok ? (n * sizeof(T) + 15) / 16 : n;

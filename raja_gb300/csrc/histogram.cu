@@ -107,8 +107,9 @@ extern "C" int b200_histogram_i32(const int32_t* x, size_t n, int32_t nbins, uin
   uint32_t sbins = uint32_t(nbins);
   if (size_t(sbins) * R > cap_words) sbins = uint32_t(cap_words / R);
   const size_t smem = size_t(sbins) * R * 4;
+  static SmemOptIn so;
+  B200_TRY(smem_optin(so, p, hist_kernel, cap_words * 4));
   int bps = 0;
-  B200_CUDA(cudaFuncSetAttribute(hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, hist_kernel, HBLOCK, smem));
   if (bps < 1) bps = 1;
   size_t grid = size_t(p.sms) * bps;

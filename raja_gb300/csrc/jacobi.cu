@@ -181,18 +181,6 @@ jacobi_mesh_kernel(int nx, int ny, int nz, const double* __restrict__ u, double*
   flush_resid(rb.bits(), resid, sh);
 }
 
-// Resident blocks per SM of a JBLOCK-thread kernel (1 if the query fails;
-// a launch error is then reported by the launch itself).
-template <class K>
-int blocks_per_sm(K kern) {
-  int b = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, JBLOCK, 0) != cudaSuccess) {
-    (void)cudaGetLastError();
-    return 1;
-  }
-  return b > 0 ? b : 1;
-}
-
 int check_jplan(b200_jacobi_plan_s* p, const char* name) {
   if (!p) return fail(B200_ERR_ARG, "%s: null plan", name);
   int dev = 0;
@@ -289,11 +277,13 @@ int b200_jacobi_sweep_f64(b200_jacobi_plan p, const double* u, double* unew, con
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   B200_CUDA(cudaMemsetAsync(resid, 0, p->nmeshes * sizeof(double), s));
   if (p->ntiles == 0) return B200_OK;
-  static const int bps[2] = {blocks_per_sm(jacobi_kernel<false>), blocks_per_sm(jacobi_kernel<true>)};
+  static KernelSetup ks[2];
   DeviceProps props;
   B200_TRY(device_props(&props));
   const auto kern = f ? jacobi_kernel<true> : jacobi_kernel<false>;
-  int64_t grid = int64_t(props.sms) * bps[f ? 1 : 0];
+  int bps = 0;
+  B200_TRY(kernel_setup(ks[f ? 1 : 0], props, kern, JBLOCK, 0, &bps));
+  int64_t grid = int64_t(props.sms) * bps;
   if (grid > p->ntiles) grid = p->ntiles;
   B200_LAUNCH(name, kern, unsigned(grid), JBLOCK, 0, s, p->d_tiles, p->ntiles, p->d_dims,
               p->d_off, u, unew, f, reinterpret_cast<unsigned long long*>(resid));
@@ -308,14 +298,15 @@ int b200_jacobi_mesh_sweep_f64(int nx, int ny, int nz, const double* u, double* 
   if (!u || !unew || !resid || u == unew) return fail(B200_ERR_ARG, "%s: bad pointers", name);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   B200_CUDA(cudaMemsetAsync(resid, 0, sizeof(double), s));
-  static const int bps[2] = {blocks_per_sm(jacobi_mesh_kernel<false>),
-                             blocks_per_sm(jacobi_mesh_kernel<true>)};
+  static KernelSetup ks[2];
   DeviceProps props;
   B200_TRY(device_props(&props));
   const auto kern = f ? jacobi_mesh_kernel<true> : jacobi_mesh_kernel<false>;
+  int bps = 0;
+  B200_TRY(kernel_setup(ks[f ? 1 : 0], props, kern, JBLOCK, 0, &bps));
   const int64_t cnt = int64_t(nx - 2) * (ny - 2) * (nz - 2);
   int64_t grid = (cnt + JBLOCK - 1) / JBLOCK;
-  if (grid > int64_t(props.sms) * bps[f ? 1 : 0]) grid = int64_t(props.sms) * bps[f ? 1 : 0];
+  if (grid > int64_t(props.sms) * bps) grid = int64_t(props.sms) * bps;
   B200_LAUNCH(name, kern, unsigned(grid), JBLOCK, 0, s, nx, ny, nz, u, unew, f,
               reinterpret_cast<unsigned long long*>(resid));
   clear_error();

@@ -230,7 +230,8 @@ int run_multi_reduce(const char* name, const int32_t* bins, const T* vals, size_
   const uint32_t sbins = uint32_t(std::min<size_t>(size_t(nbins), cap));
   const size_t smem = size_t(sbins) * sizeof(S);
   auto kern = multi_reduce_kernel<Op, T>;
-  B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  static SmemOptIn so;
+  B200_TRY(smem_optin(so, p, kern, cap * sizeof(S)));
   int bps = 0;
   B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, MBLOCK, smem));
   if (bps < 1) bps = 1;

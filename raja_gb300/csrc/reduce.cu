@@ -536,14 +536,11 @@ reduce_kernel(const typename Op::T* __restrict__ x, const typename Op::T* __rest
 
 template <class Op, bool DOT>
 int grid_for(size_t n, int* grid) {
-  static int blocks_per_sm = 0;
+  static KernelSetup ks;
   DeviceProps props;
   B200_TRY(device_props(&props));
-  if (blocks_per_sm == 0) {
-    int b = 0;
-    B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, reduce_kernel<Op, DOT>, RBLOCK, 0));
-    blocks_per_sm = b > 0 ? b : 1;
-  }
+  int blocks_per_sm = 0;
+  B200_TRY(kernel_setup(ks, props, reduce_kernel<Op, DOT>, RBLOCK, 0, &blocks_per_sm));
   const size_t nchunks = (n + Chunk<typename Op::T>::SIZE - 1) / Chunk<typename Op::T>::SIZE;
   size_t g = size_t(props.sms) * size_t(blocks_per_sm);
   if (g > nchunks) g = nchunks;

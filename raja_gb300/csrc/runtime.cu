@@ -26,7 +26,6 @@ namespace b200 {
 namespace {
 thread_local std::string t_last_error;
 std::mutex g_mu;
-constexpr int kMaxDevices = 64;
 DeviceProps g_props[kMaxDevices];
 uint32_t* g_status[kMaxDevices] = {};
 std::atomic<uint32_t> g_spin_limit{0};

@@ -521,12 +521,11 @@ int launch_scan(const char* name, unsigned grid, cudaStream_t s, const typename 
                 typename Op::T* out, size_t n, typename Op::T init, int tma_ok, int vec_out,
                 uint64_t* words, uint32_t* counter, uint32_t* status, uint32_t lim) {
   auto kern = scan_kernel<Op, EXCL>;
-  static bool attr = false;
-  if (!attr) {
-    B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   int(sizeof(ScanSmem<Op>))));
-    attr = true;
-  }
+  static KernelSetup ks;
+  DeviceProps props;
+  B200_TRY(device_props(&props));
+  int bps = 0;
+  B200_TRY(kernel_setup(ks, props, kern, SBLOCK, sizeof(ScanSmem<Op>), &bps));
   B200_LAUNCH(name, kern, grid, SBLOCK, sizeof(ScanSmem<Op>), s, in, out, n, init, tma_ok, vec_out,
               words, counter, status, lim);
   return B200_OK;

@@ -458,12 +458,12 @@ int launch_sweep_t(const char* name, size_t tiles, cudaStream_t s, const K* src,
                      (!HAS_V || reinterpret_cast<uintptr_t>(vsrc) % 16 == 0);
   using SM = SweepSmem<K, V, HAS_V, ST>;
   auto kern = onesweep_kernel<K, V, HAS_V, ST, FIRST, LAST>;
-  static bool attr = false;
-  if (!attr) {
-    B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(SM))));
-    attr = true;
-  }
   constexpr int threads = SweepShape<K, HAS_V>::RB;
+  static KernelSetup ks;
+  DeviceProps props;
+  B200_TRY(device_props(&props));
+  int bps = 0;
+  B200_TRY(kernel_setup(ks, props, kern, threads, sizeof(SM), &bps));
   B200_LAUNCH(name, kern, (unsigned)tiles, threads, sizeof(SM), s, src, dst, vsrc, vdst, n, shift, desc,
               bins, status, status_next, counter, err, lim, tma_ok);
   return B200_OK;
@@ -533,13 +533,9 @@ int run_sort(const char* name, const K* kin, K* kout, const V* vin, V* vout, siz
   B200_TRY(device_props(&props));
   {
     const size_t smem = size_t(WARPS) * P * RADIX * sizeof(uint32_t);
-    static int bps = 0;
-    if (bps == 0) {
-      B200_CUDA(cudaFuncSetAttribute(hist_kernel<K, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-      int b = 0;
-      B200_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, hist_kernel<K, P>, RB, smem));
-      bps = b > 0 ? b : 1;
-    }
+    static KernelSetup ks;
+    int bps = 0;
+    B200_TRY(kernel_setup(ks, props, hist_kernel<K, P>, RB, smem, &bps));
     size_t g = size_t(props.sms) * bps;
     const size_t need = (n + RB - 1) / RB;
     if (g > need) g = need;
