@@ -80,13 +80,20 @@ int b200_abi_version(void);
 /* Message for the last failing call on this host thread ("" if none). */
 const char* b200_last_error_string(void);
 
-/* Wait for `stream`, then read and clear the device status word of the
- * current device.  Returns B200_ERR_TIMEOUT if a bounded device wait (scan
- * or sort look-back) gave up since the last check.  The word is read in
- * the stream's own order: work queued on other streams is not waited for
- * (the word itself is shared by all streams of the device).  Replaces
- * cuda::synchronize / res.wait() (MemUtils_CUDA.hpp:205-247). */
+/* Wait for `stream`, then read and clear the status word of the current
+ * device.  Returns B200_ERR_TIMEOUT if a bounded device wait (scan or sort
+ * look-back) gave up since the last check.  Work queued on other streams is
+ * not waited for; the word itself is shared by all streams of the device.
+ * It lives in mapped pinned host memory, so the check costs no copy.
+ * Replaces cuda::synchronize / res.wait() (MemUtils_CUDA.hpp:205-247). */
 int b200_stream_synchronize(b200_stream_t stream);
+
+/* Host address of the current device's status word (a uint32_t in mapped
+ * pinned memory that is 0 while no bounded device wait has given up).  A
+ * caller that synchronises a stream itself reads it afterwards instead of
+ * calling b200_stream_synchronize(); on a non-zero value,
+ * b200_stream_synchronize() reports and clears it. */
+int b200_status_word_address(const uint32_t** out);
 
 /* Test hook: upper bound on polling iterations of every device-side wait
  * (0 restores the default).  Used to exercise the timeout path without a

@@ -248,16 +248,98 @@ __device__ inline void grid_combine(const DevSlot<T>& s, T v, Merge merge) {
   }
 }
 
-// Allocate one launch's slot on the stream: partials, ticket, result.
+// Stream-ordered pool of the current device for the C++ layer's per-launch
+// device memory (reducer partials, IndexSet tables).  Its release threshold
+// is unbounded: the device's default pool returns freed memory at every
+// synchronisation, and re-mapping it cost ~100 us per call on GB300.
+inline cudaMemPool_t launch_pool() {
+  static std::atomic<cudaMemPool_t> pools[kMaxDevices] = {};
+  static std::mutex mu;
+  const int dev = current_device_index();
+  cudaMemPool_t p = pools[dev].load(std::memory_order_acquire);
+  if (!p) {
+    std::lock_guard<std::mutex> lk(mu);
+    p = pools[dev].load(std::memory_order_relaxed);
+    if (!p) {
+      cudaMemPoolProps props{};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      check_cuda(cudaMemPoolCreate(&p, &props), "launch memory pool");
+      uint64_t keep = ~uint64_t(0);
+      check_cuda(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep), "launch memory pool");
+      pools[dev].store(p, std::memory_order_release);
+    }
+  }
+  return p;
+}
+inline void* launch_alloc(size_t bytes, cudaStream_t s, const char* what) {
+  void* p = nullptr;
+  check_cuda(cudaMallocFromPoolAsync(&p, bytes, launch_pool(), s), what);
+  return p;
+}
+
+// A reducer result cell: 32 bytes of mapped pinned host memory.  The last
+// block of the launch stores the result through `dev`; the host reads
+// `host` after synchronising the stream, with no copy.
+struct ResultCell {
+  void* host = nullptr;
+  void* dev = nullptr;
+};
+struct CellPool {
+  std::mutex mu;
+  std::vector<ResultCell> free;
+};
+inline CellPool& cell_pool() {
+  static CellPool* pool = new CellPool;  // never destroyed: cells may be read until exit
+  return *pool;
+}
+inline ResultCell acquire_cell() {
+  CellPool& pool = cell_pool();
+  std::lock_guard<std::mutex> lk(pool.mu);
+  if (pool.free.empty()) {
+    constexpr size_t kCells = 256, kCell = 32;
+    void* h = nullptr;
+    check_cuda(cudaHostAlloc(&h, kCells * kCell, cudaHostAllocMapped | cudaHostAllocPortable), "reducer result cells");
+    void* d = nullptr;
+    check_cuda(cudaHostGetDevicePointer(&d, h, 0), "reducer result cells");
+    for (size_t i = kCells; i-- > 0;)
+      pool.free.push_back(ResultCell{static_cast<char*>(h) + i * kCell, static_cast<char*>(d) + i * kCell});
+  }
+  const ResultCell c = pool.free.back();
+  pool.free.pop_back();
+  return c;
+}
+inline void release_cell(const ResultCell& c) {
+  if (!c.host) return;
+  CellPool& pool = cell_pool();
+  std::lock_guard<std::mutex> lk(pool.mu);
+  pool.free.push_back(c);
+}
+
+// Memory behind one launch's reducer slot.
+struct SlotMem {
+  void* block = nullptr;  // partials and ticket (launch pool)
+  ResultCell cell;        // the result
+};
 template <class T>
-inline DevSlot<T> alloc_slot(unsigned grid, cudaStream_t s, void** block) {
+inline T read_cell(const ResultCell& c) {
+  static_assert(sizeof(T) <= 32, "reducer value larger than a result cell");
+  T v;
+  std::memcpy(&v, c.host, sizeof(T));
+  return v;
+}
+
+// Allocate one launch's slot on the stream: partials and ticket in device
+// memory, the result in a mapped host cell.
+template <class T>
+inline DevSlot<T> alloc_slot(unsigned grid, cudaStream_t s, SlotMem* mem) {
   const size_t pbytes = ((size_t(grid) * sizeof(T) + 255) / 256) * 256;
-  const size_t bytes = pbytes + 256 + sizeof(T);
-  check_cuda(cudaMallocAsync(block, bytes, s), "reducer slot");
-  char* b = static_cast<char*>(*block);
+  mem->block = launch_alloc(pbytes + 256, s, "reducer slot");
+  char* b = static_cast<char*>(mem->block);
   check_cuda(cudaMemsetAsync(b + pbytes, 0, sizeof(unsigned), s), "reducer ticket");
-  return DevSlot<T>{reinterpret_cast<T*>(b), reinterpret_cast<unsigned*>(b + pbytes),
-                    reinterpret_cast<T*>(b + pbytes + 256)};
+  mem->cell = acquire_cell();
+  return DevSlot<T>{reinterpret_cast<T*>(b), reinterpret_cast<unsigned*>(b + pbytes), static_cast<T*>(mem->cell.dev)};
 }
 
 // ---- ValLoc with lowest-index tie-break (device merges)
@@ -333,8 +415,7 @@ class DevReducer {
 
  protected:
   struct Pending {
-    void* block;
-    V* result;
+    SlotMem mem;
     cudaStream_t stream;
   };
   struct Shared {
@@ -366,10 +447,10 @@ class DevReducer {
     LaunchCtx& c = ctx();
     if (c.active && !o.launch_copy_) {
       if (shared_->slot_launch != c.launch_id) {
-        void* block = nullptr;
-        shared_->slot = alloc_slot<V>(c.grid, c.stream, &block);
+        SlotMem mem;
+        shared_->slot = alloc_slot<V>(c.grid, c.stream, &mem);
         shared_->slot_launch = c.launch_id;
-        shared_->pending.push_back(Pending{block, shared_->slot.result, c.stream});
+        shared_->pending.push_back(Pending{mem, c.stream});
       }
       slot_ = shared_->slot;
       launch_copy_ = true;
@@ -398,17 +479,23 @@ class DevReducer {
   RAJA_HOST_DEVICE void combine(const V& v) const { val_ = K::merge(val_, v); }
 
   // Fold the pending launch results into init, in launch order.
+  // One synchronisation per stream with pending launches (other streams are
+  // not waited for); the results are then read from their host cells.
   V fold() const {
     if (!shared_) return V{};
-    for (const Pending& p : shared_->pending) {
-      // stream-ordered read and free: other streams are not waited for
-      V r;
-      check_cuda(cudaMemcpyAsync(&r, p.result, sizeof(V), cudaMemcpyDeviceToHost, p.stream), "reducer result");
+    std::vector<Pending>& pend = shared_->pending;
+    std::vector<cudaStream_t> waited;
+    for (const Pending& p : pend) {
+      if (std::find(waited.begin(), waited.end(), p.stream) != waited.end()) continue;
       check_cuda(cudaStreamSynchronize(p.stream), "reducer wait");
-      shared_->init = K::fold_init(shared_->init, r);
-      cudaFreeAsync(p.block, p.stream);
+      waited.push_back(p.stream);
     }
-    shared_->pending.clear();
+    for (const Pending& p : pend) {
+      shared_->init = K::fold_init(shared_->init, read_cell<V>(p.mem.cell));
+      release_cell(p.mem.cell);
+      cudaFreeAsync(p.mem.block, p.stream);
+    }
+    pend.clear();
     return shared_->init;
   }
   void reset_value(V v) {
@@ -856,7 +943,7 @@ void forall_impl(b200_exec<BLOCK, Async> pol, const TypedIndexSet<Segs...>& is, 
     cudaStream_t s = b200::stream();
     void* tbl = nullptr;
     const size_t bb = ((nseg * sizeof(T) + 255) / 256) * 256;
-    b200::check_cuda(cudaMallocAsync(&tbl, bb + (nseg + 1) * sizeof(long long), s), "indexset table");
+    tbl = b200::detail::launch_alloc(bb + (nseg + 1) * sizeof(long long), s, "indexset table");
     T* d_begins = static_cast<T*>(tbl);
     long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + bb);
     b200::check_cuda(cudaMemcpyAsync(d_begins, begins.data(), nseg * sizeof(T), cudaMemcpyHostToDevice, s),
@@ -952,18 +1039,33 @@ forall_params_kernel(Body body, Seg seg, long long len,
 }  // namespace detail
 }  // namespace b200
 
-// Read the launch results on stream s (the kernel has finished) and fold
-// them into the targets in parameter order: *target = op(*target, result).
-template <class Slots, size_t... I, class... Red>
-void resolve_params(const Slots& slots, cudaStream_t s, std::index_sequence<I...>, Red&... reds) {
-  auto one = [s](auto& red, const auto& slot) {
+// Wait for the launch on stream s and fold its results into the targets in
+// parameter order: *target = op(*target, result).  One synchronisation
+// covers the launch; the results (host cells, one per parameter in `mem`)
+// and the status word (mapped host memory) are then read directly.
+// Returns false, with the targets untouched, when a bounded device wait
+// gave up; b200::wait() then reports it.
+template <class... Red>
+bool resolve_params(const b200::detail::SlotMem* mem, cudaStream_t s, Red&... reds) {
+  const uint32_t* status = nullptr;
+  b200::check(b200_status_word_address(&status), "b200 status word");
+  b200::check_cuda(cudaStreamSynchronize(s), "param result");
+  if (__atomic_load_n(status, __ATOMIC_ACQUIRE) != 0) return false;
+  size_t i = 0;
+  auto take = [&](auto& red) {
     using RK = b200::detail::ParamKind<std::decay_t<decltype(red)>>;
-    typename RK::type::V v;
-    b200::check_cuda(cudaMemcpyAsync(&v, slot.result, sizeof(v), cudaMemcpyDeviceToHost, s), "param result");
-    b200::check_cuda(cudaStreamSynchronize(s), "param result");
-    red.combineTarget(RK::to_target(v));
+    red.combineTarget(RK::to_target(b200::detail::read_cell<typename RK::type::V>(mem[i++].cell)));
   };
-  (one(reds, b200::detail::dget<I>(slots)), ...);
+  (take(reds), ...);
+  return true;
+}
+// Return the slot memory of a finished launch: cells to their pool, device
+// blocks to the launch pool in the stream's order.
+inline void release_slots(const b200::detail::SlotMem* mem, size_t n, cudaStream_t s) {
+  for (size_t i = 0; i < n; ++i) {
+    b200::detail::release_cell(mem[i].cell);
+    if (mem[i].block) cudaFreeAsync(mem[i].block, s);
+  }
 }
 
 template <int BLOCK, bool Async, class Seg, class Body, class... Red,
@@ -976,14 +1078,15 @@ void forall_params_impl(b200_exec<BLOCK, Async>, const Seg& r, Body&& body, Red&
   const unsigned g =
       b200::detail::grid_for<b200::detail::forall_params_kernel<BLOCK, B, Seg, Red...>>(BLOCK, len > 0 ? len : 1);
   cudaStream_t s = b200::stream();
-  void* blocks[sizeof...(Red) + 1] = {};
+  b200::detail::SlotMem mem[sizeof...(Red) + 1];
   size_t bi = 0;
-  Slots slots{b200::detail::alloc_slot<typename b200::detail::ParamKind<Red>::type::V>(g, s, &blocks[bi++])...};
+  Slots slots{b200::detail::alloc_slot<typename b200::detail::ParamKind<Red>::type::V>(g, s, &mem[bi++])...};
   k<<<g, BLOCK, 0, s>>>(body, r, len, slots);
   b200::check_cuda(cudaGetLastError(), "b200 forall params");
-  b200::wait();  // param_resolve waits for the kernel, as the reference does
-  resolve_params(slots, s, std::index_sequence_for<Red...>{}, reds...);
-  for (size_t i = 0; i < sizeof...(Red); ++i) cudaFreeAsync(blocks[i], s);
+  // param_resolve waits for the kernel, as the reference does
+  const bool ok = resolve_params(mem, s, reds...);
+  release_slots(mem, sizeof...(Red), s);
+  if (!ok) b200::wait();  // reports the device status and throws
 }
 
 // ---------------------------------------------------------------- launch
@@ -1223,15 +1326,16 @@ struct LaunchExecute<b200_launch_t<Async, NT>> {
     const b200::detail::LaunchShape sh = b200::detail::launch_shape<NT>(p, k);
     if (sh.empty) return;
     cudaStream_t s = b200::stream();
-    void* blocks[sizeof...(Red) + 1] = {};
+    b200::detail::SlotMem mem[sizeof...(Red) + 1];
     size_t bi = 0;
-    Slots slots{b200::detail::alloc_slot<typename b200::detail::ParamKind<Red>::type::V>(sh.blocks, s, &blocks[bi++])...};
+    Slots slots{b200::detail::alloc_slot<typename b200::detail::ParamKind<Red>::type::V>(sh.blocks, s, &mem[bi++])...};
     B lb = b200::detail::LaunchCopy<B>::make(body, sh.blocks, s);
     k<<<sh.grid, sh.block, sh.smem, s>>>(lb, slots);
     b200::check_cuda(cudaGetLastError(), "b200 launch params");
-    b200::wait();  // the targets are combined after the kernel, as in the reference
-    resolve_params(slots, s, std::index_sequence_for<Red...>{}, reds...);
-    for (size_t i = 0; i < sizeof...(Red); ++i) cudaFreeAsync(blocks[i], s);
+    // the targets are combined after the kernel, as in the reference
+    const bool ok = resolve_params(mem, s, reds...);
+    release_slots(mem, sizeof...(Red), s);
+    if (!ok) b200::wait();  // reports the device status and throws
   }
 };
 

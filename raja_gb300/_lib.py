@@ -44,6 +44,7 @@ def _signatures() -> dict[str, tuple]:
         "b200_abi_version": (_I, []),
         "b200_last_error_string": (C.c_char_p, []),
         "b200_stream_synchronize": (_I, [_P]),
+        "b200_status_word_address": (_I, [_P]),
         "b200_set_spin_limit": (_I, [C.c_uint64]),
         "b200_selftest_scan_timeout": (_I, [_P]),
         "b200_device_info": (_I, [_P, _P, _P]),

@@ -27,7 +27,8 @@ namespace {
 thread_local std::string t_last_error;
 std::mutex g_mu;
 DeviceProps g_props[kMaxDevices];
-uint32_t* g_status[kMaxDevices] = {};
+uint32_t* g_status[kMaxDevices] = {};       // device address of the status word
+uint32_t* g_status_host[kMaxDevices] = {};  // its host address (mapped pinned memory)
 std::atomic<uint32_t> g_spin_limit{0};
 constexpr uint32_t kDefaultSpinLimit = 1u << 22;  // ~0.4 s of polling
 
@@ -101,20 +102,33 @@ int device_props(DeviceProps* out) {
   return B200_OK;
 }
 
-int status_word(uint32_t** out) {
+// The status word lives in mapped pinned host memory: kernels OR error bits
+// into it through its device address (only when a bounded wait gives up),
+// and a host thread reads it directly once the stream has synchronised.
+// Reading a device word instead costs a copy-engine operation (about 3 us
+// more per synchronisation on GB300).
+namespace {
+int status_words(uint32_t** dev_out, uint32_t** host_out) {
   int dev = 0;
   B200_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(B200_ERR_ARG, "device %d out of range", dev);
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_status[dev]) {
-    uint32_t* p = nullptr;
-    B200_CUDA(cudaMalloc(&p, 256));
-    B200_CUDA(cudaMemset(p, 0, 256));
-    g_status[dev] = p;
+    void* h = nullptr;
+    B200_CUDA(cudaHostAlloc(&h, 256, cudaHostAllocMapped | cudaHostAllocPortable));
+    std::memset(h, 0, 256);
+    void* d = nullptr;
+    B200_CUDA(cudaHostGetDevicePointer(&d, h, 0));
+    g_status_host[dev] = static_cast<uint32_t*>(h);
+    g_status[dev] = static_cast<uint32_t*>(d);
   }
-  *out = g_status[dev];
+  if (dev_out) *dev_out = g_status[dev];
+  if (host_out) *host_out = g_status_host[dev];
   return B200_OK;
 }
+}  // namespace
+
+int status_word(uint32_t** out) { return status_words(out, nullptr); }
 
 uint32_t spin_limit() {
   uint32_t v = g_spin_limit.load();
@@ -190,22 +204,28 @@ const char* b200_last_error_string(void) { return t_last_error.c_str(); }
 
 int b200_stream_synchronize(b200_stream_t stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  uint32_t* st = nullptr;
-  B200_TRY(status_word(&st));
-  // Read the status word in the stream's own order, so that waiting for
-  // one stream does not also wait for work on the others.
-  uint32_t h = 0;
-  B200_CUDA(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s));
+  uint32_t* host = nullptr;
+  B200_TRY(status_words(nullptr, &host));
+  // Only this stream is waited for; the word itself is shared by all
+  // streams of the device, so an error raised by another stream's kernel
+  // before this point is reported here too.
   B200_CUDA(cudaStreamSynchronize(s));
+  const uint32_t h = __atomic_exchange_n(host, 0u, __ATOMIC_ACQ_REL);
   if (h != 0) {
-    B200_CUDA(cudaMemsetAsync(st, 0, sizeof(uint32_t), s));
-    B200_CUDA(cudaStreamSynchronize(s));
     return fail(B200_ERR_TIMEOUT,
                 "a bounded device wait gave up (status 0x%x: %s%s%s)", h,
                 (h & kStatusScanTimeout) ? "scan look-back " : "",
                 (h & kStatusSortTimeout) ? "sort look-back " : "",
                 (h & kStatusSegTimeout) ? "batched/segmented look-back " : "");
   }
+  return B200_OK;
+}
+
+int b200_status_word_address(const uint32_t** out) {
+  if (!out) return fail(B200_ERR_ARG, "b200_status_word_address: null out");
+  uint32_t* host = nullptr;
+  B200_TRY(status_words(nullptr, &host));
+  *out = host;
   return B200_OK;
 }
 

@@ -1267,6 +1267,42 @@ void perf_lambda_paths() {
     });
   });
   cudaDeviceSynchronize();
+
+  // Per-call cost at a size where launch and combine latency dominate
+  // (4096 elements): host time to submit an async forall, and the full
+  // round trip of the synchronous forms.
+  const Index_type m = 4096;
+  auto per_call = [&](const char* what, int reps, auto&& f) {
+    f();
+    cudaDeviceSynchronize();
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int r = 0; r < reps; ++r) f();
+    const auto t1 = std::chrono::steady_clock::now();
+    cudaDeviceSynchronize();
+    const auto t2 = std::chrono::steady_clock::now();
+    const double host = std::chrono::duration<double, std::micro>(t1 - t0).count() / reps;
+    const double all = std::chrono::duration<double, std::micro>(t2 - t0).count() / reps;
+    printf("perf: %-34s %8.2f us host  %8.2f us per call\n", what, host, all);
+  };
+  per_call("forall 4096 (async)", 2000, [&] {
+    RAJA::forall<async>(RAJA::RangeSegment(0, m), [=] __device__(Index_type i) { y[i] += 2.5 * x[i]; });
+  });
+  per_call("forall 4096 (sync)", 2000, [&] {
+    RAJA::forall<RAJA::b200_exec<256>>(RAJA::RangeSegment(0, m), [=] __device__(Index_type i) { y[i] += 2.5 * x[i]; });
+  });
+  per_call("ReduceSum 4096 + get()", 2000, [&] {
+    RAJA::ReduceSum<red, double> d(0.0);
+    RAJA::forall<async>(RAJA::RangeSegment(0, m), [=] __device__(Index_type i) { d += x[i] * y[i]; });
+    (void)d.get();
+  });
+  per_call("expt::Reduce 4096 (sync)", 2000, [&] {
+    double d = 0.0;
+    RAJA::forall<RAJA::b200_exec<256>>(RAJA::RangeSegment(0, m), RAJA::expt::Reduce<RAJA::operators::plus>(&d),
+                                       [=] __device__(Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& v) {
+                                         v += x[i] * y[i];
+                                       });
+  });
+  cudaDeviceSynchronize();
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   cudaFree(x);
