@@ -148,6 +148,45 @@ __device__ __forceinline__ double tile_axpy_sum(float a, const float* __restrict
   return double(s) + double(c);
 }
 
+// Fold one block's partial of a run of tiles [r0, r1) of `loop` into the
+// per-loop result.  The partial goes to the slot of the run's first tile and
+// zeros to the others, so that the loop's slots always hold one value per
+// tile; the block that completes the loop's tile count folds the slots in
+// tile order.  The runs are fixed by the grid, so the sum is deterministic.
+template <int BLOCK>
+__device__ __forceinline__ void flush_loop_run(double p, int loop, int64_t r0, int64_t r1,
+                                               const int64_t* __restrict__ loop_tile0,
+                                               double* __restrict__ sums, double* __restrict__ tile_part,
+                                               uint32_t* __restrict__ loop_cnt, double* sh, bool* last) {
+  p = block_sum<BLOCK>(p, sh);
+  const int64_t t0 = loop_tile0[loop];
+  const int64_t nt = loop_tile0[loop + 1] - t0;
+  for (int64_t k = r0 + threadIdx.x; k < r1; k += BLOCK) tile_part[k] = (k == r0) ? p : 0.0;
+  __threadfence();  // every writer publishes its slots before the ticket
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t prev = atomicAdd(loop_cnt + loop, uint32_t(r1 - r0));
+    *last = (int64_t(prev) + (r1 - r0) == nt);
+  }
+  __syncthreads();
+  if (*last) {
+    __threadfence();
+    double q = 0.0;
+    for (int64_t k = threadIdx.x; k < nt; k += BLOCK) q += __ldcg(tile_part + t0 + k);
+    q = block_sum<BLOCK>(q, sh);
+    if (threadIdx.x == 0) {
+      sums[loop] = q;
+      loop_cnt[loop] = 0u;
+    }
+  }
+  __syncthreads();
+}
+
+// All loops in one launch.  Each block takes a contiguous run of the tile
+// table (tiles are equal-sized, so the runs are balanced), prefetches the
+// next tile's descriptor, and keeps its partial sum in registers across the
+// tiles of one loop: the block reduction and the per-loop ticket run once
+// per loop the block touches instead of once per tile.
 template <int BLOCK, int ITEMS>
 __global__ void __launch_bounds__(BLOCK)
 batched_axpy_sum_kernel(const int32_t* __restrict__ tile_loop,
@@ -159,35 +198,34 @@ batched_axpy_sum_kernel(const int32_t* __restrict__ tile_loop,
   constexpr int TILE = BLOCK * ITEMS;
   __shared__ double sh[32];
   __shared__ bool last;
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int loop = tile_loop[t];
-    const int64_t t0 = loop_tile0[loop];
-    const int64_t nt = loop_tile0[loop + 1] - t0;
-    const int64_t len = loop_len[loop];
+  const int64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+  const int64_t b0 = int64_t(blockIdx.x) * per;
+  const int64_t b1 = b0 + per < ntiles ? b0 + per : ntiles;
+  if (b0 >= b1) return;                            // block-uniform
+  int cur = -1;                                    // loop of the running partial
+  int64_t run0 = b0, t0 = 0, len = 0;
+  const float* x = nullptr;
+  float* y = nullptr;
+  double acc = 0.0;
+  int nxt = tile_loop[b0];
+  for (int64_t t = b0; t < b1; ++t) {
+    const int loop = nxt;
+    if (t + 1 < b1) nxt = tile_loop[t + 1];         // one tile ahead
+    if (loop != cur) {                             // block-uniform
+      if (cur >= 0) flush_loop_run<BLOCK>(acc, cur, run0, t, loop_tile0, sums, tile_part, loop_cnt, sh, &last);
+      cur = loop;
+      run0 = t;
+      acc = 0.0;
+      t0 = loop_tile0[loop];
+      len = loop_len[loop];
+      x = xs[loop];
+      y = ys[loop];
+    }
     const int64_t lo = (t - t0) * TILE;
     const int64_t hi = min(lo + TILE, len);
-    double p = tile_axpy_sum<BLOCK, ITEMS>(a, xs[loop], ys[loop], lo, hi, comp != 0);
-    p = block_sum<BLOCK>(p, sh);
-    if (threadIdx.x == 0) {
-      tile_part[t] = p;
-      __threadfence();
-      const uint32_t prev = atomicAdd(loop_cnt + loop, 1u);
-      last = (prev == uint32_t(nt - 1));
-    }
-    __syncthreads();
-    if (last) {
-      // fold this loop's tile partials in tile order (deterministic)
-      __threadfence();
-      double q = 0.0;
-      for (int64_t k = threadIdx.x; k < nt; k += BLOCK) q += __ldcg(tile_part + t0 + k);
-      q = block_sum<BLOCK>(q, sh);
-      if (threadIdx.x == 0) {
-        sums[loop] = q;
-        loop_cnt[loop] = 0u;
-      }
-    }
-    __syncthreads();
+    acc += tile_axpy_sum<BLOCK, ITEMS>(a, x, y, lo, hi, comp != 0);
   }
+  flush_loop_run<BLOCK>(acc, cur, run0, b1, loop_tile0, sums, tile_part, loop_cnt, sh, &last);
 }
 
 // One fused axpy + sum over a single loop (the per-loop launch that the
