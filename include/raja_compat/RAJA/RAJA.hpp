@@ -310,6 +310,7 @@ struct seq_reduce {};
 struct omp_reduce {};
 struct seq_multi_reduce {};
 struct seq_atomic {};
+struct omp_atomic {};
 
 // ------------------------------------------------------------ resources
 // RAJA::resources (util/resource.hpp:37-64) re-exports camp's resources
@@ -843,6 +844,39 @@ template <typename T> RAJA_HOST_DEVICE T atomicXor(seq_atomic, T* acc, T v) { T 
 template <typename T> RAJA_HOST_DEVICE T atomicExchange(seq_atomic, T* acc, T v) { T o = *acc; *acc = v; return o; }
 template <typename T> RAJA_HOST_DEVICE T atomicCAS(seq_atomic, T* acc, T compare, T v) { T o = *acc; if (o == compare) *acc = v; return o; }
 
+// omp_atomic (policy/openmp/atomic.hpp:37-93): host atomics, safe under
+// omp_parallel_for_exec.  Every operation is a compare-exchange loop on the
+// value's bits with the compiler's __atomic builtins, so it covers
+// floating-point types too.  Host code only.
+namespace detail {
+template <typename T, typename F>
+inline T host_atomic_update(T* acc, F next) {
+  T old;
+  __atomic_load(acc, &old, __ATOMIC_RELAXED);
+  T want = next(old);
+  while (!__atomic_compare_exchange(acc, &old, &want, true, __ATOMIC_SEQ_CST, __ATOMIC_RELAXED)) want = next(old);
+  return old;
+}
+}  // namespace detail
+template <typename T> inline T atomicLoad(omp_atomic, T* acc) { T v; __atomic_load(acc, &v, __ATOMIC_SEQ_CST); return v; }
+template <typename T> inline void atomicStore(omp_atomic, T* acc, T v) { __atomic_store(acc, &v, __ATOMIC_SEQ_CST); }
+template <typename T> inline T atomicAdd(omp_atomic, T* acc, T v) { return detail::host_atomic_update(acc, [v](T o) { return T(o + v); }); }
+template <typename T> inline T atomicSub(omp_atomic, T* acc, T v) { return detail::host_atomic_update(acc, [v](T o) { return T(o - v); }); }
+template <typename T> inline T atomicMin(omp_atomic, T* acc, T v) { return detail::host_atomic_update(acc, [v](T o) { return v < o ? v : o; }); }
+template <typename T> inline T atomicMax(omp_atomic, T* acc, T v) { return detail::host_atomic_update(acc, [v](T o) { return o < v ? v : o; }); }
+template <typename T> inline T atomicInc(omp_atomic, T* acc) { return detail::host_atomic_update(acc, [](T o) { return T(o + T(1)); }); }
+template <typename T> inline T atomicInc(omp_atomic, T* acc, T val) { return detail::host_atomic_update(acc, [val](T o) { return val <= o ? T(0) : T(o + T(1)); }); }
+template <typename T> inline T atomicDec(omp_atomic, T* acc) { return detail::host_atomic_update(acc, [](T o) { return T(o - T(1)); }); }
+template <typename T> inline T atomicDec(omp_atomic, T* acc, T val) { return detail::host_atomic_update(acc, [val](T o) { return (o == T(0) || val < o) ? val : T(o - T(1)); }); }
+template <typename T> inline T atomicAnd(omp_atomic, T* acc, T v) { return detail::host_atomic_update(acc, [v](T o) { return T(o & v); }); }
+template <typename T> inline T atomicOr(omp_atomic, T* acc, T v) { return detail::host_atomic_update(acc, [v](T o) { return T(o | v); }); }
+template <typename T> inline T atomicXor(omp_atomic, T* acc, T v) { return detail::host_atomic_update(acc, [v](T o) { return T(o ^ v); }); }
+template <typename T> inline T atomicExchange(omp_atomic, T* acc, T v) { T o; __atomic_exchange(acc, &v, &o, __ATOMIC_SEQ_CST); return o; }
+template <typename T> inline T atomicCAS(omp_atomic, T* acc, T compare, T v) {
+  __atomic_compare_exchange(acc, &compare, &v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST);
+  return compare;  // the value found: equal to the old compare when the swap happened
+}
+
 template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicLoad(T* acc) { return atomicLoad(Policy{}, acc); }
 template <typename Policy, typename T> RAJA_HOST_DEVICE void atomicStore(T* acc, T v) { atomicStore(Policy{}, acc, v); }
 template <typename Policy, typename T> RAJA_HOST_DEVICE T atomicAdd(T* acc, T v) { return atomicAdd(Policy{}, acc, v); }
@@ -977,6 +1011,74 @@ void forall_impl(omp_parallel_for_schedule_exec<S, Chunk>, const Seg& seg, Body&
   for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
 #endif
 }
+
+// Work-sharing loops for use inside RAJA::region<omp_parallel_region>
+// (policy/openmp/policy.hpp: omp_for_exec, omp_for_static_exec,
+// omp_for_nowait_static_exec): an `omp for` with no parallel region of its
+// own, so the threads of the enclosing region share the iterations.
+// Outside a region the calling thread runs them all.
+struct omp_for_exec {};
+template <int Chunk = 0>
+struct omp_for_static_exec {};
+template <int Chunk = 0>
+struct omp_for_nowait_static_exec {};
+namespace detail {
+template <bool NOWAIT, int Chunk, typename Seg, typename Body>
+void omp_for_loop(const Seg& seg, const Body& body) {
+  const Index_type n = detail::seg_len(seg);
+  auto b = body;
+#if defined(_OPENMP)
+  if (NOWAIT) {
+#pragma omp for schedule(static, Chunk > 0 ? Chunk : 1) nowait
+    for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+  } else if (Chunk > 0) {
+#pragma omp for schedule(static, Chunk > 0 ? Chunk : 1)
+    for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+  } else {
+#pragma omp for schedule(static)
+    for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+  }
+#else
+  for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+#endif
+}
+}  // namespace detail
+template <typename Seg, typename Body, typename = decltype(detail::seg_len(std::declval<const Seg&>()))>
+void forall_impl(omp_for_exec, const Seg& seg, Body&& body) {
+  detail::omp_for_loop<false, 0>(seg, body);
+}
+template <int Chunk, typename Seg, typename Body, typename = decltype(detail::seg_len(std::declval<const Seg&>()))>
+void forall_impl(omp_for_static_exec<Chunk>, const Seg& seg, Body&& body) {
+  detail::omp_for_loop<false, Chunk>(seg, body);
+}
+template <int Chunk, typename Seg, typename Body, typename = decltype(detail::seg_len(std::declval<const Seg&>()))>
+void forall_impl(omp_for_nowait_static_exec<Chunk>, const Seg& seg, Body&& body) {
+  detail::omp_for_loop<true, Chunk>(seg, body);
+}
+
+// RAJA::region<Pol>(body) (pattern/region.hpp, policy/sequential/region.hpp,
+// policy/openmp/region.hpp): seq_region runs body once; omp_parallel_region
+// runs it on every thread of one OpenMP parallel region, where the omp_for
+// loops above share out their iterations.
+struct seq_region {};
+struct omp_parallel_region {};
+template <typename Pol, typename Body>
+void region(Body&& body) {
+  if constexpr (std::is_same<Pol, omp_parallel_region>::value) {
+#if defined(_OPENMP)
+#pragma omp parallel
+    {
+      body();
+    }
+#else
+    body();
+#endif
+  } else {
+    static_assert(std::is_same<Pol, seq_region>::value, "region policy: seq_region or omp_parallel_region");
+    body();
+  }
+}
+
 template <typename Pol, typename Body, typename... Segs>
 void forall_impl(Pol p, const TypedIndexSet<Segs...>& is, Body&& body) {
   for (const auto& s : is.segments()) std::visit([&](const auto& seg) { forall_impl(p, seg, body); }, s);
@@ -1086,6 +1188,62 @@ template <typename Pol, typename Seg, typename... Args, detail::enable_if_not_re
 resources::EventProxy<typename resources::get_resource<Pol>::type> forall(Seg&& seg, Args&&... args) {
   return forall<Pol>(resources::get_resource<Pol>::type::get_default(), std::forward<Seg>(seg),
                      std::forward<Args>(args)...);
+}
+
+}  // namespace RAJA
+
+// The policy list of RAJA::dynamic_forall (camp::list in the reference;
+// only the list itself is needed here).
+namespace camp {
+template <typename... Ts>
+struct list {};
+}  // namespace camp
+
+namespace RAJA {
+
+// RAJA::dynamic_forall<camp::list<P0, P1, ...>>([resource,] pol, segment,
+// [params...,] body) runs forall<P_pol> (pattern/forall.hpp:704-825, an
+// experimental interface there).  A `pol` outside the list throws, as
+// RAJA_ABORT_OR_THROW does with exceptions enabled.  The resource form
+// passes resource.get<resource type of P_pol>() and returns an EventProxy
+// on the type-erased resource.
+namespace detail {
+template <typename List>
+struct policy_list;
+template <typename... Pols>
+struct policy_list<camp::list<Pols...>> {
+  static constexpr int size = int(sizeof...(Pols));
+  template <typename F>
+  static void pick(int pol, F&& f) {
+    int idx = 0;
+    bool ran = false;
+    (void)std::initializer_list<int>{
+        ((idx++ == pol && !ran) ? (f(static_cast<Pols*>(nullptr)), ran = true, 0) : 0)...};
+  }
+};
+}  // namespace detail
+
+template <typename POLICY_LIST, typename Seg, typename... Args>
+void dynamic_forall(const int pol, Seg&& seg, Args&&... args) {
+  using L = detail::policy_list<POLICY_LIST>;
+  static_assert(L::size > 0, "RAJA policy list must not be empty");
+  if (pol < 0 || pol >= L::size) throw std::runtime_error("RAJA::dynamic_forall: policy enum not supported");
+  L::pick(pol, [&](auto* p) {
+    using P = std::remove_pointer_t<decltype(p)>;
+    forall<P>(seg, args...);
+  });
+}
+template <typename POLICY_LIST, typename Seg, typename... Args>
+resources::EventProxy<resources::Resource> dynamic_forall(resources::Resource r, const int pol, Seg&& seg,
+                                                          Args&&... args) {
+  using L = detail::policy_list<POLICY_LIST>;
+  static_assert(L::size > 0, "RAJA policy list must not be empty");
+  if (pol < 0 || pol >= L::size) throw std::runtime_error("RAJA::dynamic_forall: policy value out of range");
+  L::pick(pol, [&](auto* p) {
+    using P = std::remove_pointer_t<decltype(p)>;
+    forall<P>(r.template get<typename resources::get_resource<P>::type>(), seg, args...);
+  });
+  return resources::EventProxy<resources::Resource>(r);
 }
 
 // ---------------------------------------------------------------- launch
@@ -1359,11 +1517,35 @@ resources::Resource Get_Host_Resource(T host_res, ExecPlace place) {
 }
 
 // ------------------------------------------------------------ View/Layout
-// Row-major layouts and views (util/View.hpp, util/Layout.hpp): the last
-// index has stride one.
-template <size_t DIM, typename IdxT = Index_type, ptrdiff_t StrideOne = ptrdiff_t(DIM) - 1>
+// Layouts and views (util/View.hpp, util/Layout.hpp, util/PermutedLayout.hpp).
+// A layout holds the extent and stride of every dimension.  By default the
+// last index has stride one (row-major); make_permuted_layout orders the
+// strides by a permutation whose last entry is the stride-one dimension.
+// StrideOne names that dimension for the reader (-1: not stated), as in
+// RAJA; the strides themselves are kept at run time.
+
+// Permutations of the dimensions (util/Permutations.hpp), as index
+// sequences.
+using PERM_I = std::index_sequence<0>;
+using PERM_IJ = std::index_sequence<0, 1>;
+using PERM_JI = std::index_sequence<1, 0>;
+using PERM_IJK = std::index_sequence<0, 1, 2>;
+using PERM_IKJ = std::index_sequence<0, 2, 1>;
+using PERM_JIK = std::index_sequence<1, 0, 2>;
+using PERM_JKI = std::index_sequence<1, 2, 0>;
+using PERM_KIJ = std::index_sequence<2, 0, 1>;
+using PERM_KJI = std::index_sequence<2, 1, 0>;
+// as_array<Perm>::get(): the permutation as an array.
+template <typename Perm>
+struct as_array;
+template <size_t... P>
+struct as_array<std::index_sequence<P...>> {
+  static std::array<Index_type, sizeof...(P)> get() { return {{Index_type(P)...}}; }
+};
+
+template <size_t DIM, typename IdxT = Index_type, ptrdiff_t StrideOne = -1>
 struct Layout {
-  static_assert(StrideOne == ptrdiff_t(DIM) - 1, "only row-major layouts");
+  static_assert(StrideOne >= -1 && StrideOne < ptrdiff_t(DIM), "stride-one dimension out of range");
   Index_type sizes[DIM];
   Index_type strides[DIM];
   template <typename... Ns, typename std::enable_if<sizeof...(Ns) == DIM &&
@@ -1375,6 +1557,15 @@ struct Layout {
   explicit Layout(const std::array<Index_type, DIM>& s) {
     for (size_t d = 0; d < DIM; ++d) sizes[d] = s[d];
     set_strides();
+  }
+  // Strides in the order of `perm`: perm[DIM-1] has stride one.
+  Layout(const std::array<Index_type, DIM>& s, const std::array<Index_type, DIM>& perm) {
+    for (size_t d = 0; d < DIM; ++d) sizes[d] = s[d];
+    Index_type st = 1;
+    for (size_t k = DIM; k-- > 0;) {
+      strides[perm[k]] = st;
+      st *= sizes[perm[k]];
+    }
   }
   RAJA_HOST_DEVICE void set_strides() {
     Index_type st = 1;
@@ -1391,12 +1582,25 @@ struct Layout {
     for (size_t d = 0; d < DIM; ++d) off += idx[d] * strides[d];
     return off;
   }
+  // The indices of a linear offset (the inverse of operator()).
+  template <typename... Is>
+  RAJA_HOST_DEVICE void toIndices(Index_type linear, Is&... is) const {
+    static_assert(sizeof...(Is) == DIM, "one index per dimension");
+    size_t d = 0;
+    ((is = static_cast<std::decay_t<Is>>(sizes[d] ? (linear / strides[d]) % sizes[d] : 0), ++d), ...);
+  }
   RAJA_HOST_DEVICE Index_type size() const {
     Index_type n = 1;
     for (size_t d = 0; d < DIM; ++d) n *= sizes[d];
     return n;
   }
+  RAJA_HOST_DEVICE Index_type size_noproj() const { return size(); }
 };
+template <size_t DIM, typename IdxT = Index_type>
+Layout<DIM, IdxT> make_permuted_layout(const std::array<Index_type, DIM>& sizes,
+                                       const std::array<Index_type, DIM>& perm) {
+  return Layout<DIM, IdxT>(sizes, perm);
+}
 // Offset layouts (util/OffsetLayout.hpp:40-244): dimension d runs over
 // [begin[d], end[d]), stored row-major from begin.
 template <size_t DIM, typename IdxT = Index_type>
@@ -1433,6 +1637,9 @@ OffsetLayout<DIM, IdxT> make_offset_layout(const std::array<Index_type, DIM>& be
 
 template <typename T, typename LayoutT>
 struct View {
+  using value_type = T;
+  using pointer_type = T*;
+  using layout_type = LayoutT;
   T* data;
   LayoutT layout;
   template <typename... Ns,
@@ -1445,6 +1652,98 @@ struct View {
   }
   RAJA_HOST_DEVICE void set_data(T* p) { data = p; }
 };
+
+// Views whose elements are AtomicRefs (util/View.hpp:272-326):
+// make_atomic_view<Policy>(view)(i, j) += v is an atomic update.  With
+// seq_atomic the element reference is returned as it is.
+template <typename ViewType, typename AtomicPolicy>
+struct AtomicViewWrapper {
+  using base_type = ViewType;
+  using pointer_type = typename ViewType::pointer_type;
+  using value_type = typename ViewType::value_type;
+  using atomic_type = AtomicRef<value_type, AtomicPolicy>;
+  base_type base_;
+  explicit AtomicViewWrapper(const ViewType& v) : base_(v) {}
+  void set_data(pointer_type p) { base_.set_data(p); }
+  template <typename... Is>
+  RAJA_HOST_DEVICE atomic_type operator()(Is... is) const {
+    return atomic_type(&base_(is...));
+  }
+};
+template <typename ViewType>
+struct AtomicViewWrapper<ViewType, seq_atomic> {
+  using base_type = ViewType;
+  using pointer_type = typename ViewType::pointer_type;
+  using value_type = typename ViewType::value_type;
+  base_type base_;
+  explicit AtomicViewWrapper(const ViewType& v) : base_(v) {}
+  void set_data(pointer_type p) { base_.set_data(p); }
+  template <typename... Is>
+  RAJA_HOST_DEVICE value_type& operator()(Is... is) const {
+    return base_(is...);
+  }
+};
+template <typename AtomicPolicy, typename ViewType>
+AtomicViewWrapper<ViewType, AtomicPolicy> make_atomic_view(const ViewType& view) {
+  return AtomicViewWrapper<ViewType, AtomicPolicy>(view);
+}
+
+// ------------------------------------------------------- CombiningAdapter
+// A lambda of D indices run as a 1-D loop (util/CombiningAdapter.hpp:80-275):
+// linear index k maps through the layout to offsets within each range, and
+// the body receives begin_d + offset_d for every dimension:
+//   auto ad = make_CombiningAdapter(body, irange, jrange);
+//   forall<pol>(ad.getRange(), ad);
+// The layout is row-major (the last range fastest) or, for
+// make_PermutedCombiningAdapter<Perm>, ordered by Perm.
+template <typename Lambda, typename IdxLin, typename... IdxTs>
+struct CombiningAdapter {
+  static constexpr size_t D = sizeof...(IdxTs);
+  using RangeLinear = TypedRangeSegment<IdxLin>;
+  Lambda m_lambda;
+  Layout<D, IdxLin> m_layout;
+  Index_type m_begin[D];
+
+  CombiningAdapter(Lambda l, const Layout<D, IdxLin>& layout, const std::array<Index_type, D>& begin)
+      : m_lambda(std::move(l)), m_layout(layout) {
+    for (size_t d = 0; d < D; ++d) m_begin[d] = begin[d];
+  }
+  RAJA_HOST_DEVICE auto operator()(IdxLin linear) const { return call(linear, std::index_sequence_for<IdxTs...>{}); }
+  RAJA_HOST_DEVICE IdxLin size() const { return static_cast<IdxLin>(m_layout.size_noproj()); }
+  RAJA_HOST_DEVICE RangeLinear getRange() const { return RangeLinear(static_cast<IdxLin>(0), size()); }
+
+ private:
+  template <size_t... I>
+  RAJA_HOST_DEVICE auto call(IdxLin linear, std::index_sequence<I...>) const {
+    Index_type idx[D];
+    m_layout.toIndices(static_cast<Index_type>(linear), idx[I]...);
+    return m_lambda(static_cast<IdxTs>(m_begin[I] + idx[I])...);
+  }
+};
+
+namespace detail {
+template <typename Lambda, typename... IdxTs>
+auto combining_adapter(Lambda&& lambda, const std::array<Index_type, sizeof...(IdxTs)>* perm,
+                       const TypedRangeSegment<IdxTs>&... segs) {
+  using IdxLin = typename std::common_type<IdxTs...>::type;
+  constexpr size_t D = sizeof...(IdxTs);
+  const std::array<Index_type, D> sizes{{Index_type(segs.size())...}};
+  const std::array<Index_type, D> begin{{(segs.size() ? Index_type(*segs.begin()) : Index_type(0))...}};
+  Layout<D, IdxLin> layout = perm ? Layout<D, IdxLin>(sizes, *perm) : Layout<D, IdxLin>(sizes);
+  return CombiningAdapter<std::decay_t<Lambda>, IdxLin, IdxTs...>(std::forward<Lambda>(lambda), layout, begin);
+}
+}  // namespace detail
+
+template <typename Lambda, typename... IdxTs>
+auto make_CombiningAdapter(Lambda&& lambda, const TypedRangeSegment<IdxTs>&... segs) {
+  return detail::combining_adapter(std::forward<Lambda>(lambda), nullptr, segs...);
+}
+template <typename Perm, typename Lambda, typename... IdxTs>
+auto make_PermutedCombiningAdapter(Lambda&& lambda, const TypedRangeSegment<IdxTs>&... segs) {
+  const auto perm = as_array<Perm>::get();
+  static_assert(std::tuple_size<decltype(perm)>::value == sizeof...(IdxTs), "one permutation entry per range");
+  return detail::combining_adapter(std::forward<Lambda>(lambda), &perm, segs...);
+}
 
 // ---------------------------------------------------------- forall_Icount
 // forall_Icount<POLICY>(segment, icount, body): body(icount + k, seg[k])

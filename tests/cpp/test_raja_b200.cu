@@ -1218,6 +1218,77 @@ void test_edge_cases() {
 // Bandwidth of the lambda-body paths (printed, not asserted): daxpy through
 // forall<b200_exec_async>, a ReduceSum<b200_reduce> dot, an expt::Reduce
 // dot, and daxpy through RAJA::launch, at 2^27 doubles (above the L2).
+// dynamic_forall with a b200 entry, CombiningAdapter (plain and permuted)
+// and an atomic view on b200 policies, checked against the host loops.
+void test_forall_adapters() {
+  using pols = camp::list<RAJA::seq_exec, exec>;
+  bool ok = true;
+  Index_type* w = managed<Index_type>(1000);
+  for (int pol = 0; pol < 2; ++pol) {
+    for (int i = 0; i < 1000; ++i) w[i] = -1;
+    RAJA::dynamic_forall<pols>(pol, RAJA::TypedRangeSegment<Index_type>(5, 1005),
+                               [=] RAJA_HOST_DEVICE(Index_type i) { w[i - 5] = i; });
+    cudaDeviceSynchronize();
+    for (int i = 0; i < 1000; ++i) ok = ok && w[i] == i + 5;
+  }
+  CHECK("dynamic_forall_seq_and_b200", ok);
+
+  const int f0 = -7, l0 = 120, f1 = 3, l1 = 260, f2 = 1, l2 = 9;
+  const int N0 = l0 - f0, N1 = l1 - f1, N2 = l2 - f2;
+  int* c = managed<int>(size_t(N0) * N1 * N2 + 1);
+  for (int k = 0; k <= N0 * N1 * N2; ++k) c[k] = 0;
+  auto a3 = RAJA::make_CombiningAdapter(
+      [=] RAJA_HOST_DEVICE(int i0, int i1, int i2) {
+        if (i0 >= f0 && i0 < l0 && i1 >= f1 && i1 < l1 && i2 >= f2 && i2 < l2)
+          c[((i0 - f0) * N1 + (i1 - f1)) * N2 + (i2 - f2)] += ((i0 - f0) * N1 + (i1 - f1)) * N2 + (i2 - f2);
+        else
+          RAJA::atomicAdd<RAJA::b200_atomic>(c + N0 * N1 * N2, 1);
+      },
+      RAJA::TypedRangeSegment<int>(f0, l0), RAJA::TypedRangeSegment<int>(f1, l1), RAJA::TypedRangeSegment<int>(f2, l2));
+  RAJA::forall<exec>(a3.getRange(), a3);
+  cudaDeviceSynchronize();
+  ok = a3.size() == N0 * N1 * N2 && c[N0 * N1 * N2] == 0;
+  for (int k = 0; k < N0 * N1 * N2; ++k) ok = ok && c[k] == k;
+  CHECK("combining_adapter_3d_b200", ok);
+
+  // permuted (PERM_JI: the first range fastest): each linear index writes its (i, j)
+  int* pi = managed<int>(size_t(N0) * N1);
+  auto ap = RAJA::make_PermutedCombiningAdapter<RAJA::PERM_JI>(
+      [=] RAJA_HOST_DEVICE(int i0, int i1) { pi[(i1 - f1) * N0 + (i0 - f0)] = i0 * 1000 + i1; },
+      RAJA::TypedRangeSegment<int>(f0, l0), RAJA::TypedRangeSegment<int>(f1, l1));
+  RAJA::forall<exec>(ap.getRange(), ap);
+  cudaDeviceSynchronize();
+  ok = true;
+  for (int lin = 0; lin < N0 * N1; ++lin) {
+    const int i0 = f0 + lin % N0, i1 = f1 + lin / N0;
+    ok = ok && pi[lin] == i0 * 1000 + i1;
+  }
+  CHECK("permuted_combining_adapter_b200", ok);
+
+  // atomic view: a 2-D histogram with b200_atomic against the host count
+  int* h = managed<int>(8 * 16);
+  for (int k = 0; k < 128; ++k) h[k] = 0;
+  RAJA::View<int, RAJA::Layout<2>> hv(h, 8, 16);
+  auto av = RAJA::make_atomic_view<RAJA::b200_atomic>(hv);
+  RAJA::forall<exec>(RAJA::RangeSegment(0, 1 << 20), [=] RAJA_HOST_DEVICE(Index_type k) {
+    const Index_type x = (k * 2654435761ll) & 0xffff;
+    av(x % 8, (x / 8) % 16) += 1;
+  });
+  cudaDeviceSynchronize();
+  std::vector<int> ref(128, 0);
+  for (Index_type k = 0; k < (1 << 20); ++k) {
+    const Index_type x = (k * 2654435761ll) & 0xffff;
+    ref[(x % 8) * 16 + (x / 8) % 16] += 1;
+  }
+  ok = true;
+  for (int k = 0; k < 128; ++k) ok = ok && h[k] == ref[k];
+  CHECK("atomic_view_b200", ok);
+  cudaFree(w);
+  cudaFree(c);
+  cudaFree(pi);
+  cudaFree(h);
+}
+
 void perf_lambda_paths() {
   const Index_type n = Index_type(1) << 27;
   double *x = nullptr, *y = nullptr;
@@ -1324,6 +1395,7 @@ int main() {
   test_launch_jacobi();
   test_params_segments();
   test_edge_cases();
+  test_forall_adapters();
   perf_lambda_paths();
   printf("%d failures\n", g_fail);
   return g_fail;

@@ -1,6 +1,8 @@
 // Host-only checks of the raja_compat front-end (seq_exec / omp policies)
 // against the known answers of the reference's functional tests.
+#include <algorithm>
 #include <cstdio>
+#include <stdexcept>
 #include <memory>
 #include <numeric>
 #include <vector>
@@ -14,6 +16,155 @@ static int g_fail = 0;
     if (cond) printf("PASS %s\n", name);                   \
     else { printf("FAIL %s (line %d)\n", name, __LINE__); ++g_fail; } \
   } while (0)
+
+// dynamic_forall, CombiningAdapter, permuted layouts, atomic views,
+// omp_atomic and regions (test/functional/dynamic_forall,
+// forall/CombiningAdapter, forall/atomic-view, forall/region,
+// unit/view-layout).
+static void forall_adapters_and_regions() {
+  using pols = camp::list<RAJA::seq_exec, RAJA::omp_parallel_for_exec, RAJA::simd_exec>;
+  for (int pol = 0; pol < 3; ++pol) {
+    std::vector<Index_type> w(100, -1);
+    Index_type* wp = w.data();
+    RAJA::dynamic_forall<pols>(pol, RAJA::TypedRangeSegment<Index_type>(7, 107),
+                               [=](Index_type i) { wp[i - 7] = i; });
+    bool ok = true;
+    for (Index_type i = 0; i < 100; ++i) ok = ok && w[i] == i + 7;
+    CHECK("dynamic_forall_range", ok);
+  }
+  {
+    int zero = 0;
+    int* zp = &zero;
+    RAJA::dynamic_forall<pols>(1, RAJA::TypedRangeSegment<int>(5, 5), [=](int) { ++*zp; });
+    bool threw = false;
+    try {
+      RAJA::dynamic_forall<pols>(3, RAJA::RangeSegment(0, 4), [=](Index_type) {});
+    } catch (const std::runtime_error&) {
+      threw = true;
+    }
+    std::vector<int> w(10, 0);
+    int* wp = w.data();
+    RAJA::resources::Resource host{RAJA::resources::Host::get_default()};
+    auto ev = RAJA::dynamic_forall<pols>(host, 0, RAJA::RangeSegment(0, 10), [=](Index_type i) { wp[i] = 3; });
+    ev.get().wait();
+    CHECK("dynamic_forall_empty_range_and_bad_policy", zero == 0 && threw);
+    CHECK("dynamic_forall_resource", std::accumulate(w.begin(), w.end(), 0) == 30);
+  }
+  // CombiningAdapter 1-D, 2-D, 3-D with non-zero begins (and an empty range)
+  {
+    const int f0 = -3, l0 = 5, f1 = 2, l1 = 9, f2 = 1, l2 = 4;
+    const int N0 = l0 - f0, N1 = l1 - f1, N2 = l2 - f2;
+    std::vector<int> w(N0 * N1 * N2 + 1, 0);
+    int* wp = w.data();
+    auto a2 = RAJA::make_CombiningAdapter(
+        [=](int i0, int i1) {
+          if (i0 >= f0 && i0 < l0 && i1 >= f1 && i1 < l1) wp[(i0 - f0) * N1 + (i1 - f1)] += (i0 - f0) * N1 + (i1 - f1);
+          else wp[N0 * N1 * N2]++;
+        },
+        RAJA::TypedRangeSegment<int>(f0, l0), RAJA::TypedRangeSegment<int>(f1, l1));
+    RAJA::forall<RAJA::omp_parallel_for_exec>(a2.getRange(), a2);
+    bool ok = a2.size() == N0 * N1 && w[N0 * N1 * N2] == 0;
+    for (int k = 0; k < N0 * N1; ++k) ok = ok && w[k] == k;
+    CHECK("combining_adapter_2d", ok);
+    std::fill(w.begin(), w.end(), 0);
+    auto a3 = RAJA::make_CombiningAdapter([=](int i0, int i1, int i2) { wp[((i0 - f0) * N1 + (i1 - f1)) * N2 + (i2 - f2)] += 1; },
+                                          RAJA::TypedRangeSegment<int>(f0, l0), RAJA::TypedRangeSegment<int>(f1, l1),
+                                          RAJA::TypedRangeSegment<int>(f2, l2));
+    RAJA::forall<RAJA::seq_exec>(a3.getRange(), a3);
+    ok = a3.size() == N0 * N1 * N2;
+    for (int k = 0; k < N0 * N1 * N2; ++k) ok = ok && w[k] == 1;
+    CHECK("combining_adapter_3d", ok);
+    int calls = 0;
+    int* cp = &calls;
+    auto a1 = RAJA::make_CombiningAdapter([=](int i) { *cp += i; }, RAJA::TypedRangeSegment<int>(10, 13));
+    RAJA::forall<RAJA::seq_exec>(a1.getRange(), a1);
+    auto ae = RAJA::make_CombiningAdapter([=](int, int) { *cp += 1000; }, RAJA::TypedRangeSegment<int>(0, 4),
+                                          RAJA::TypedRangeSegment<int>(3, 3));
+    RAJA::forall<RAJA::seq_exec>(ae.getRange(), ae);
+    CHECK("combining_adapter_1d_and_empty", calls == 33 && ae.size() == 0);
+    // permuted: PERM_JI makes the first range the fastest
+    std::vector<int> order;
+    auto ap = RAJA::make_PermutedCombiningAdapter<RAJA::PERM_JI>([&](int i, int j) { order.push_back(10 * i + j); },
+                                                                 RAJA::TypedRangeSegment<int>(0, 3),
+                                                                 RAJA::TypedRangeSegment<int>(0, 2));
+    RAJA::forall<RAJA::seq_exec>(ap.getRange(), ap);
+    CHECK("permuted_combining_adapter_order", (order == std::vector<int>{0, 10, 20, 1, 11, 21}));
+  }
+  // permuted layouts: strides and toIndices round trip
+  {
+    auto L = RAJA::make_permuted_layout<3>({{4, 5, 6}}, RAJA::as_array<RAJA::PERM_KIJ>::get());
+    // PERM_KIJ: j has stride 1, then i, then k
+    bool ok = L.strides[1] == 1 && L.strides[0] == 5 && L.strides[2] == 20 && L.size() == 120;
+    for (Index_type lin = 0; lin < 120; ++lin) {
+      int i = -1, j = -1, k = -1;
+      L.toIndices(lin, i, j, k);
+      ok = ok && L(i, j, k) == lin && i < 4 && j < 5 && k < 6;
+    }
+    RAJA::Layout<2> rm(3, 7);
+    Index_type i = 0, j = 0;
+    rm.toIndices(17, i, j);
+    CHECK("permuted_layout_strides_and_to_indices", ok && i == 2 && j == 3 && rm(i, j) == 17);
+  }
+  // atomic views: a histogram through make_atomic_view under an omp loop
+  {
+    std::vector<int> bins(7, 0);
+    RAJA::View<int, RAJA::Layout<1>> v(bins.data(), 7);
+    auto av = RAJA::make_atomic_view<RAJA::omp_atomic>(v);
+    RAJA::forall<RAJA::omp_parallel_for_exec>(RAJA::RangeSegment(0, 7000), [=](Index_type k) { av(k % 7) += 1; });
+    std::vector<double> fb(3, 0.0);
+    RAJA::View<double, RAJA::Layout<1>> fv(fb.data(), 3);
+    auto sv = RAJA::make_atomic_view<RAJA::seq_atomic>(fv);
+    RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 30), [=](Index_type k) { sv(k % 3) += 0.5; });
+    bool ok = fb[0] == 5.0 && fb[1] == 5.0 && fb[2] == 5.0;
+    for (int b : bins) ok = ok && b == 1000;
+    CHECK("atomic_view_omp_and_seq", ok);
+  }
+  // omp_atomic under an omp loop: min / max / bounded inc / CAS on floats
+  {
+    double mn = 1e9, mx = -1e9, fsum = 0.0;
+    unsigned wrap = 0;
+    int cas_hits = 0;
+    int flag = 0;
+    double* pmn = &mn; double* pmx = &mx; double* pfs = &fsum;
+    unsigned* pw = &wrap; int* ph = &cas_hits; int* pf = &flag;
+    RAJA::forall<RAJA::omp_parallel_for_exec>(RAJA::RangeSegment(0, 10000), [=](Index_type k) {
+      const double x = double((k * 7919) % 10007) - 5000.0;
+      RAJA::atomicMin<RAJA::omp_atomic>(pmn, x);
+      RAJA::atomicMax<RAJA::omp_atomic>(pmx, x);
+      RAJA::atomicAdd<RAJA::omp_atomic>(pfs, 0.25);
+      RAJA::atomicInc<RAJA::omp_atomic>(pw, 9u);
+      if (RAJA::atomicCAS<RAJA::omp_atomic>(pf, 0, 1) == 0) RAJA::atomicAdd<RAJA::omp_atomic>(ph, 1);
+    });
+    double rmn = 1e9, rmx = -1e9;
+    for (Index_type k = 0; k < 10000; ++k) {
+      const double x = double((k * 7919) % 10007) - 5000.0;
+      rmn = std::min(rmn, x);
+      rmx = std::max(rmx, x);
+    }
+    CHECK("omp_atomic_min_max_add_inc_cas", mn == rmn && mx == rmx && fsum == 2500.0 && wrap == 10000u % 10u &&
+                                                cas_hits == 1 && flag == 1);
+  }
+  // regions: two loops inside one region (test-forall-region.hpp)
+  {
+    std::vector<int> idx(1000);
+    std::iota(idx.begin(), idx.end(), 0);
+    RAJA::TypedListSegment<int> lseg(idx.data(), 1000);
+    std::vector<int> w(1000, 0), w2(1000, 0);
+    int* wp = w.data();
+    int* wp2 = w2.data();
+    RAJA::region<RAJA::seq_region>([=]() {
+      RAJA::forall<RAJA::seq_exec>(RAJA::TypedRangeSegment<int>(0, 1000), [=](int i) { wp[i] += 1; });
+      RAJA::forall<RAJA::seq_exec>(lseg, [=](int i) { wp[i] += 2; });
+    });
+    RAJA::region<RAJA::omp_parallel_region>([=]() {
+      RAJA::forall<RAJA::omp_for_nowait_static_exec<>>(RAJA::TypedRangeSegment<int>(0, 1000), [=](int i) { wp2[i] += 1; });
+      RAJA::forall<RAJA::omp_for_nowait_static_exec<>>(lseg, [=](int i) { wp2[i] += 2; });
+    });
+    bool ok = true;
+    for (int i = 0; i < 1000; ++i) ok = ok && w[i] == 3 && w2[i] == 3;
+    CHECK("region_seq_and_omp", ok);
+  }
+}
 
 int main() {
   // ReduceSum with init 0 and 2; reset and two loops (test-forall-basic-ReduceSum.hpp)
@@ -392,6 +543,7 @@ int main() {
     le.wait();
     CHECK("launch_seq_resource_list_segment", out[5] == -1 && out[1] == -1 && out[3] == -1 && out[2] != -1);
   }
+  forall_adapters_and_regions();
   printf("%d failures\n", g_fail);
   return g_fail;
 }
