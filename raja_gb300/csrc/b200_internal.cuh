@@ -153,6 +153,8 @@ int smem_optin(SmemOptIn& so, const DeviceProps& props, K kern, size_t max_smem)
 // ---------------------------------------------------------------- device
 
 // Error codes ORed into the status word (bit positions name the waiter).
+// The word is mapped host memory that the host clears with an atomic
+// exchange, so kernels set bits with system-scope atomics.
 constexpr uint32_t kStatusScanTimeout = 1u << 0;
 constexpr uint32_t kStatusSortTimeout = 1u << 1;
 constexpr uint32_t kStatusSegTimeout = 1u << 2;

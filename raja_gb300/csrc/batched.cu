@@ -479,7 +479,7 @@ segscan_kernel(const int32_t* in, int32_t* out, int64_t n, const int64_t* __rest
         if (im) break;
         pred -= 32;
       }
-      if (timed_out && lane == 0) atomicOr(status, kStatusSegTimeout);
+      if (timed_out && lane == 0) atomicOr_system(status, kStatusSegTimeout);
       prefix = acc;
       if (lane == 0) {
         incls[tile] = seg_comb(prefix, tile_agg);

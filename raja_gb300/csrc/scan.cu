@@ -293,7 +293,7 @@ scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op
   const bool full = base + TS <= n;
   if (tma_ok && full) {
     if (!mbar_wait(&sm.bar, 0, spin_limit)) {
-      if (tid == 0) atomicOr(status, kStatusTmaTimeout);
+      if (tid == 0) atomicOr_system(status, kStatusTmaTimeout);
       mbar_wait(&sm.bar, 0, spin_limit);  // let the copy land before the block exits
     }
   } else {
@@ -465,7 +465,7 @@ scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op
         load_window(pred - (long long)lane * LBJ);
       }
       if (lane == 0) {
-        if (timed_out) atomicOr(status, kStatusScanTimeout);
+        if (timed_out) atomicOr_system(status, kStatusScanTimeout);
         SW::publish(words + tile * SW::NW, FLAG_INCL, Op::ccomb(acc, tile_agg));
         sm.prefix = acc;
       }

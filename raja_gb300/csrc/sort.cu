@@ -283,7 +283,7 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   const int lim = (tbase + TILE <= n) ? TILE : int(n - tbase);  // valid keys in this tile
   if (tma_ok && lim == TILE) {
     if (!mbar_wait(&sm.bar, 0, spin_limit)) {
-      if (tid == 0) atomicOr(err, kStatusTmaTimeout);
+      if (tid == 0) atomicOr_system(err, kStatusTmaTimeout);
       mbar_wait(&sm.bar, 0, spin_limit);  // let the copy land before the block exits
     }
   } else {
@@ -415,7 +415,7 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
       t -= used;
       if (used < LBW) {
         if (++spins > spin_limit) {
-          atomicOr(err, kStatusSortTimeout);
+          atomicOr_system(err, kStatusSortTimeout);
           break;
         }
         __nanosleep(100);
