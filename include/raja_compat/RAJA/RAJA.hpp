@@ -1117,9 +1117,93 @@ const char* find_name(const P0& p0, const Ps&... ps) {
 }
 }  // namespace detail
 
+// ------------------------------------------------------------- plugins
+// Launch hooks (util/PluginStrategy.hpp:20-37, util/PluginContext.hpp,
+// util/plugins.hpp:34-64, util/Registry.hpp): plugins registered with
+//   static RAJA::util::PluginRegistry::add<MyPlugin> P("name", "description");
+// see preCapture / postCapture around the front-end's copy of the loop body
+// and preLaunch / postLaunch around the launch, in registration order, with
+// the policy's platform and the kernel name (pattern/forall.hpp:567-582).
+// With no plugin registered the front-end skips the hooks and the copy.
+using Platform = resources::Platform;
+namespace util {
+struct PluginOptions {
+  std::string str;
+};
+struct PluginContext {
+  PluginContext(Platform p, std::string name) : platform(p), kernel_name(std::move(name)) {}
+  Platform platform;
+  std::string kernel_name;
+};
+class PluginStrategy {
+ public:
+  virtual ~PluginStrategy() = default;
+  virtual void init(const PluginOptions&) {}
+  virtual void preCapture(const PluginContext&) {}
+  virtual void postCapture(const PluginContext&) {}
+  virtual void preLaunch(const PluginContext&) {}
+  virtual void postLaunch(const PluginContext&) {}
+  virtual void finalize() {}
+};
+// A process-wide list of named objects of type T, filled by static
+// registration objects (add<U>) before main runs.
+template <typename T>
+class Registry {
+ public:
+  class entry {
+   public:
+    entry(std::string n, std::string d, std::shared_ptr<T> p) : name_(std::move(n)), desc_(std::move(d)), p_(std::move(p)) {}
+    const std::string& getName() const { return name_; }
+    const std::string& getDesc() const { return desc_; }
+    T* get() const { return p_.get(); }
+
+   private:
+    std::string name_, desc_;
+    std::shared_ptr<T> p_;
+  };
+  using iterator = typename std::vector<entry>::const_iterator;
+  template <typename U>
+  struct add {
+    add(const char* name, const char* desc) { entries().emplace_back(name, desc, std::make_shared<U>()); }
+  };
+  static iterator begin() { return entries().cbegin(); }
+  static iterator end() { return entries().cend(); }
+  static bool empty() { return entries().empty(); }
+
+ private:
+  static std::vector<entry>& entries() {
+    static std::vector<entry> v;
+    return v;
+  }
+};
+using PluginRegistry = Registry<PluginStrategy>;
+
+template <typename Policy>
+PluginContext make_context(std::string name) {
+  return PluginContext(resources::get_resource<Policy>::type::get_default().get_platform(), std::move(name));
+}
+// The front-end's copy of the loop body, between the capture hooks.
+template <typename T>
+std::remove_reference_t<T> trigger_updates_before(T&& item) {
+  return item;
+}
+inline void callPreCapturePlugins(const PluginContext& p) {
+  for (auto it = PluginRegistry::begin(); it != PluginRegistry::end(); ++it) it->get()->preCapture(p);
+}
+inline void callPostCapturePlugins(const PluginContext& p) {
+  for (auto it = PluginRegistry::begin(); it != PluginRegistry::end(); ++it) it->get()->postCapture(p);
+}
+inline void callPreLaunchPlugins(const PluginContext& p) {
+  for (auto it = PluginRegistry::begin(); it != PluginRegistry::end(); ++it) it->get()->preLaunch(p);
+}
+inline void callPostLaunchPlugins(const PluginContext& p) {
+  for (auto it = PluginRegistry::begin(); it != PluginRegistry::end(); ++it) it->get()->postLaunch(p);
+}
+}  // namespace util
+
 namespace detail {
-// Dispatch of forall(seg, params..., body): kernel names (RAJA::Name) are
-// dropped wherever they appear (no plugin consumes them here); reducer
+// Dispatch of forall(seg, params..., body): the kernel name (RAJA::Name)
+// opens the policy's name scope and labels the plugin context; reducer
 // params are collected, in order, for forall_params_impl.
 template <typename Pol, typename Seg, typename Body, typename... Red>
 void forall_collect(Pol p, Seg&& seg, Body&& body, std::tuple<Red&...> reds);
@@ -1152,14 +1236,29 @@ void forall_collect(Pol p, Seg&& seg, Body&& body, std::tuple<Red&...> reds, R0&
 }
 
 template <typename Pol, typename Seg, typename Body, typename... Params>
-void forall_with(Pol p, Seg&& seg, Body&& body, Params&&... params) {
-  auto named = kernel_name_scope(p, find_name(params...));
-  (void)named;
+void forall_dispatch(Pol p, Seg&& seg, Body&& body, Params&&... params) {
   if constexpr ((expt::detail::is_reducer<std::decay_t<Params>>::value || ... || false)) {
     forall_collect(p, std::forward<Seg>(seg), std::forward<Body>(body), std::tuple<>(), params...);
   } else {
     forall_impl(p, std::forward<Seg>(seg), std::forward<Body>(body));
   }
+}
+template <typename Pol, typename Seg, typename Body, typename... Params>
+void forall_with(Pol p, Seg&& seg, Body&& body, Params&&... params) {
+  const char* name = find_name(params...);
+  auto named = kernel_name_scope(p, name);
+  (void)named;
+  if (util::PluginRegistry::empty()) {
+    forall_dispatch(p, std::forward<Seg>(seg), std::forward<Body>(body), params...);
+    return;
+  }
+  const util::PluginContext ctx = util::make_context<Pol>(name ? name : "");
+  util::callPreCapturePlugins(ctx);
+  auto captured = util::trigger_updates_before(body);
+  util::callPostCapturePlugins(ctx);
+  util::callPreLaunchPlugins(ctx);
+  forall_dispatch(p, std::forward<Seg>(seg), captured, params...);
+  util::callPostLaunchPlugins(ctx);
 }
 template <typename Pol, typename Seg, typename Tup, size_t... I>
 void forall_split(Seg&& seg, Tup&& tup, std::index_sequence<I...>) {

@@ -3,7 +3,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <stdexcept>
+#include <string>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <vector>
 
@@ -16,6 +18,78 @@ static int g_fail = 0;
     if (cond) printf("PASS %s\n", name);                   \
     else { printf("FAIL %s (line %d)\n", name, __LINE__); ++g_fail; } \
   } while (0)
+
+// A counting plugin (test/integration/plugin/plugin_to_test.cpp): hooks
+// must pair up, with the loop's platform, around every forall.  Registered
+// statically, so every forall below runs through the hooks.
+struct PluginCounts {
+  int pre_capture = 0, post_capture = 0, pre_launch = 0, post_launch = 0;
+  RAJA::Platform capture_active = RAJA::Platform::undefined, launch_active = RAJA::Platform::undefined;
+  bool paired = true;
+  std::string last_name;
+};
+static PluginCounts g_plugin;
+static std::mutex g_plugin_mu;  // foralls inside an OpenMP region call the hooks from every thread
+class CounterPlugin : public RAJA::util::PluginStrategy {
+ public:
+  void preCapture(const RAJA::util::PluginContext& p) override {
+    std::lock_guard<std::mutex> lk(g_plugin_mu);
+    g_plugin.paired = g_plugin.paired && g_plugin.capture_active == RAJA::Platform::undefined;
+    ++g_plugin.pre_capture;
+    g_plugin.capture_active = p.platform;
+    g_plugin.last_name = p.kernel_name;
+  }
+  void postCapture(const RAJA::util::PluginContext& p) override {
+    std::lock_guard<std::mutex> lk(g_plugin_mu);
+    g_plugin.paired = g_plugin.paired && g_plugin.capture_active == p.platform;
+    ++g_plugin.post_capture;
+    g_plugin.capture_active = RAJA::Platform::undefined;
+  }
+  void preLaunch(const RAJA::util::PluginContext& p) override {
+    std::lock_guard<std::mutex> lk(g_plugin_mu);
+    g_plugin.paired = g_plugin.paired && g_plugin.launch_active == RAJA::Platform::undefined;
+    ++g_plugin.pre_launch;
+    g_plugin.launch_active = p.platform;
+  }
+  void postLaunch(const RAJA::util::PluginContext& p) override {
+    std::lock_guard<std::mutex> lk(g_plugin_mu);
+    g_plugin.paired = g_plugin.paired && g_plugin.launch_active == p.platform;
+    ++g_plugin.post_launch;
+    g_plugin.launch_active = RAJA::Platform::undefined;
+  }
+};
+static RAJA::util::PluginRegistry::add<CounterPlugin> g_counter_plugin("counter-plugin", "Counter");
+
+// test-plugin-forall.hpp: ten one-iteration loops, each seeing the capture
+// and launch hooks active with the host platform while it runs.
+static void plugin_hooks() {
+  // earlier loops include foralls issued from every thread of an OpenMP
+  // region, whose hooks interleave; pairing is checked from here on
+  g_plugin.paired = true;
+  g_plugin.capture_active = g_plugin.launch_active = RAJA::Platform::undefined;
+  const PluginCounts before = g_plugin;
+  std::vector<int> seen(10, 0);
+  int* sp = seen.data();
+  for (int i = 0; i < 10; ++i) {
+    RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(i, i + 1), [=](Index_type k) {
+      sp[k] = (g_plugin.launch_active == RAJA::Platform::host) ? g_plugin.pre_launch - before.pre_launch : -1;
+    });
+  }
+  bool ok = true;
+  for (int i = 0; i < 10; ++i) ok = ok && seen[i] == i + 1;
+  CHECK("plugin_launch_active_during_loop", ok);
+  CHECK("plugin_counts_pair_up", g_plugin.pre_capture - before.pre_capture == 10 &&
+                                     g_plugin.post_capture - before.post_capture == 10 &&
+                                     g_plugin.pre_launch - before.pre_launch == 10 &&
+                                     g_plugin.post_launch - before.post_launch == 10 && g_plugin.paired &&
+                                     g_plugin.capture_active == RAJA::Platform::undefined &&
+                                     g_plugin.launch_active == RAJA::Platform::undefined);
+  double t = 0.0;
+  RAJA::forall<RAJA::seq_exec>(RAJA::RangeSegment(0, 4), RAJA::Name("named_loop"),
+                               RAJA::expt::Reduce<RAJA::operators::plus>(&t),
+                               [=](Index_type k, RAJA::expt::ValOp<double, RAJA::operators::plus>& v) { v += double(k); });
+  CHECK("plugin_sees_kernel_name", g_plugin.last_name == "named_loop" && t == 6.0);
+}
 
 // dynamic_forall, CombiningAdapter, permuted layouts, atomic views,
 // omp_atomic and regions (test/functional/dynamic_forall,
@@ -544,6 +618,7 @@ int main() {
     CHECK("launch_seq_resource_list_segment", out[5] == -1 && out[1] == -1 && out[3] == -1 && out[2] != -1);
   }
   forall_adapters_and_regions();
+  plugin_hooks();
   printf("%d failures\n", g_fail);
   return g_fail;
 }
