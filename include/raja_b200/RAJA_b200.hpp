@@ -1560,11 +1560,17 @@ class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH
   void enqueue(TypedRangeSegment<T> seg, Body body) {
     static_assert(std::is_trivially_copyable<Body>::value,
                   "b200_work loop bodies must be trivially copyable device lambdas");
+    // with plugins registered, the capture hooks bracket the body copy
+    // (pattern/WorkGroup.hpp:287-296)
+    const bool hooks = !util::PluginRegistry::empty();
+    const util::PluginContext ctx(Platform::cuda, std::string());
+    if (hooks) util::callPreCapturePlugins(ctx);
     const b200::detail::wg_fn fp = b200::detail::wg_fn_of<Body>();
     const size_t off = (m_bytes.size() + 15) / 16 * 16;
     m_bytes.resize(off + sizeof(Body));
     std::memcpy(m_bytes.data() + off, &body, sizeof(Body));
     m_loops.push_back(b200::detail::WgLoop{fp, (long long)seg.b, (long long)seg.size(), off});
+    if (hooks) util::callPostCapturePlugins(ctx);
   }
   void reserve(size_t n, size_t bytes) {
     m_loops.reserve(n);
@@ -1629,6 +1635,11 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
     WorkSite<policy, Index, xargs<>, Alloc> site(r);
     if (m_nloops == 0) return site;
     auto bound = bind_resource(r);
+    // with plugins registered, the launch hooks bracket the run
+    // (pattern/WorkGroup.hpp:515-528)
+    const bool hooks = !util::PluginRegistry::empty();
+    const util::PluginContext ctx(Platform::cuda, std::string());
+    if (hooks) util::callPreLaunchPlugins(ctx);
     cudaStream_t s = b200::stream();
     char* d = static_cast<char*>(m_dev);
     auto* loops = reinterpret_cast<const b200::detail::WgLoop*>(d + m_loops_off);
@@ -1651,6 +1662,7 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
     }
     b200::check_cuda(cudaGetLastError(), "WorkGroup run");
     if (!Async) b200::wait();
+    if (hooks) util::callPostLaunchPlugins(ctx);
     return site;
   }
   void clear() {}

@@ -1555,14 +1555,33 @@ void launch_split(Res& r, const LaunchParams& p, Tup&& tup, std::index_sequence<
   constexpr size_t N = std::tuple_size<std::decay_t<Tup>>::value;
   launch_collect<LP>(r, p, std::get<N - 1>(tup), std::tuple<>(), std::get<I>(tup)...);
 }
+template <typename LP, typename Res, typename Body, typename Tup, size_t... I>
+void launch_split_body(Res& r, const LaunchParams& p, const Body& body, Tup&& tup, std::index_sequence<I...>) {
+  launch_collect<LP>(r, p, body, std::tuple<>(), std::get<I>(tup)...);
+}
+// With plugins registered, the capture hooks bracket a copy of the body and
+// the launch hooks bracket the launch (launch_core.hpp:264-286).
 template <typename LP, typename Res, typename... Args>
 void launch_on(Res r, const LaunchParams& p, Args&&... args) {
   static_assert(sizeof...(Args) >= 1, "launch needs a body");
   auto bound = bind_resource(r);
   (void)bound;
-  auto named = kernel_name_scope(LP{}, find_name(args...));
+  const char* name = find_name(args...);
+  auto named = kernel_name_scope(LP{}, name);
   (void)named;
-  launch_split<LP>(r, p, std::forward_as_tuple(args...), std::make_index_sequence<sizeof...(Args) - 1>{});
+  auto tup = std::forward_as_tuple(args...);
+  constexpr size_t N = sizeof...(Args);
+  if (util::PluginRegistry::empty()) {
+    launch_split<LP>(r, p, tup, std::make_index_sequence<N - 1>{});
+    return;
+  }
+  const util::PluginContext ctx = util::make_context<LP>(name ? name : "");
+  util::callPreCapturePlugins(ctx);
+  auto captured = util::trigger_updates_before(std::get<N - 1>(tup));
+  util::callPostCapturePlugins(ctx);
+  util::callPreLaunchPlugins(ctx);
+  launch_split_body<LP>(r, p, captured, tup, std::make_index_sequence<N - 1>{});
+  util::callPostLaunchPlugins(ctx);
 }
 }  // namespace detail
 
@@ -2102,9 +2121,20 @@ class WorkPool<WorkGroupPolicy<EXEC, ORDER, STORAGE, DISPATCH>, Index, xargs<>, 
   WorkPool() = default;
   template <typename A>
   explicit WorkPool(const A&) {}  // the allocator (pattern/WorkGroup.hpp:272-300); host loops need none
+  // The loops run through forall_impl at run(), inside the group's launch
+  // hooks; with plugins registered, each enqueue brackets the body copy with
+  // the capture hooks (pattern/WorkGroup.hpp:287-296).
   template <typename Seg, typename Body>
   void enqueue(Seg seg, Body body) {
-    m_loops.push_back([seg, body]() { forall<EXEC>(seg, body); });
+    if (util::PluginRegistry::empty()) {
+      m_loops.push_back([seg, body]() { forall_impl(EXEC{}, seg, body); });
+      return;
+    }
+    const util::PluginContext ctx = util::make_context<EXEC>(std::string());
+    util::callPreCapturePlugins(ctx);
+    auto captured = util::trigger_updates_before(body);
+    m_loops.push_back([seg, captured]() { forall_impl(EXEC{}, seg, captured); });
+    util::callPostCapturePlugins(ctx);
   }
   void reserve(size_t n, size_t) { m_loops.reserve(n); }
   size_t num_loops() const { return m_loops.size(); }
@@ -2126,14 +2156,20 @@ class WorkGroup<WorkGroupPolicy<EXEC, ORDER, STORAGE, DISPATCH>, Index, xargs<>,
   using resource_type = typename resources::get_resource<EXEC>::type;
   // run([resource]) (pattern/WorkGroup.hpp:357-370): the loops run on the
   // resource, the policy's default one when none is given.
+  // With plugins registered, the launch hooks bracket the whole run
+  // (pattern/WorkGroup.hpp:515-528).
   WorkSite<policy, Index, xargs<>, Alloc> run(resource_type r) {
     auto bound = bind_resource(r);
     (void)bound;
+    const bool hooks = !util::PluginRegistry::empty();
+    const util::PluginContext ctx = util::make_context<EXEC>(std::string());
+    if (hooks) util::callPreLaunchPlugins(ctx);
     if (std::is_same<ORDER, reverse_ordered>::value) {
       for (auto it = m_loops.rbegin(); it != m_loops.rend(); ++it) (*it)();
     } else {
       for (auto& f : m_loops) f();
     }
+    if (hooks) util::callPostLaunchPlugins(ctx);
     return WorkSite<policy, Index, xargs<>, Alloc>(r);
   }
   WorkSite<policy, Index, xargs<>, Alloc> run() { return run(resource_type::get_default()); }

@@ -89,6 +89,35 @@ static void plugin_hooks() {
                                RAJA::expt::Reduce<RAJA::operators::plus>(&t),
                                [=](Index_type k, RAJA::expt::ValOp<double, RAJA::operators::plus>& v) { v += double(k); });
   CHECK("plugin_sees_kernel_name", g_plugin.last_name == "named_loop" && t == 6.0);
+
+  // launch (test-plugin-launch.hpp): one capture and one launch per call
+  PluginCounts b = g_plugin;
+  int launch_seen = 0;
+  int* ls = &launch_seen;
+  RAJA::launch<RAJA::LaunchPolicy<RAJA::seq_launch_t>>(RAJA::LaunchParams(RAJA::Teams(1), RAJA::Threads(1)),
+                                                        [=](RAJA::LaunchContext) {
+                                                          *ls = g_plugin.launch_active == RAJA::Platform::host;
+                                                        });
+  CHECK("plugin_launch_hooks", launch_seen == 1 && g_plugin.pre_capture - b.pre_capture == 1 &&
+                                   g_plugin.pre_launch - b.pre_launch == 1 &&
+                                   g_plugin.post_launch - b.post_launch == 1 && g_plugin.paired);
+
+  // WorkGroup (test-plugin-workgroup.hpp): a capture per enqueue, one launch per run
+  b = g_plugin;
+  std::vector<int> wseen(10, 0);
+  int* wsp = wseen.data();
+  RAJA::WorkPool<RAJA::WorkGroupPolicy<RAJA::seq_exec, RAJA::ordered>, Index_type> pool;
+  for (int i = 0; i < 10; ++i)
+    pool.enqueue(RAJA::TypedRangeSegment<Index_type>(i, i + 1),
+                 [=](Index_type k) { wsp[k] = g_plugin.launch_active == RAJA::Platform::host ? 1 : -1; });
+  const bool after_enqueue = g_plugin.pre_capture - b.pre_capture == 10 &&
+                             g_plugin.post_capture - b.post_capture == 10 && g_plugin.pre_launch == b.pre_launch;
+  auto group = pool.instantiate();
+  group.run();
+  ok = after_enqueue && g_plugin.pre_launch - b.pre_launch == 1 && g_plugin.post_launch - b.post_launch == 1 &&
+            g_plugin.pre_capture - b.pre_capture == 10 && g_plugin.paired;
+  for (int v : wseen) ok = ok && v == 1;
+  CHECK("plugin_workgroup_hooks", ok);
 }
 
 // dynamic_forall, CombiningAdapter, permuted layouts, atomic views,
