@@ -1863,6 +1863,72 @@ auto make_PermutedCombiningAdapter(Lambda&& lambda, const TypedRangeSegment<IdxT
   return detail::combining_adapter(std::forward<Lambda>(lambda), &perm, segs...);
 }
 
+// ------------------------------------------------------ IndexSet builders
+// buildIndexSetAligned (index/IndexSetBuilders.hpp:56-62, algorithm in
+// src/AlignedRangeIndexSetBuilders.cpp): splits an index array into range
+// segments and list segments.  Walking the array, a range starts at a value
+// v with v % range_align == 0 whose successor is v + 1, and runs while the
+// indices stay consecutive; the indices between ranges form list segments.
+// The split is kept only if its encoded size (2 per range, 1 + length per
+// list, 1 to terminate) is below length * (range_align - 1) / range_align;
+// otherwise, and whenever length <= range_min_length, the whole array is one
+// list segment.  The list segments point into indices_in, which must stay
+// alive and readable where the loops run (the reference copies them into
+// work_res's memory).
+inline void buildIndexSetAligned(TypedIndexSet<RangeSegment, ListSegment>& iset, resources::Resource work_res,
+                                 const Index_type* const indices_in, Index_type length, Index_type range_min_length,
+                                 Index_type range_align) {
+  (void)work_res;
+  if (length <= 0) return;
+  if (length <= range_min_length) {
+    iset.push_back(ListSegment(indices_in, length));
+    return;
+  }
+  struct Piece {
+    bool range;
+    Index_type first;  // range: first value; list: first position in indices_in
+    Index_type len;
+  };
+  std::vector<Piece> pieces;
+  if (length == 1) {
+    pieces.push_back({false, 0, 1});
+  } else {
+    const Index_type* x = indices_in;
+    bool in_range = x[1] == x[0] + 1 && x[0] % range_align == 0;
+    Index_type first = in_range ? x[0] : 0, count = 0;
+    for (Index_type ii = 1; ii < length; ++ii) {
+      const Index_type prev = x[ii - 1];
+      if (x[ii] == prev + 1) {
+        if (!in_range && prev % range_align == 0) {   // a list ends where an aligned run starts
+          if (count != 0) pieces.push_back({false, first, count});
+          in_range = true;
+          first = prev;
+          count = 0;
+        }
+        ++count;
+      } else if (in_range) {                          // the run ends with prev
+        pieces.push_back({true, first, count + 1});
+        in_range = false;
+        first = ii;
+        count = 0;
+      } else {
+        ++count;
+      }
+    }
+    pieces.push_back({in_range, first, count + 1});
+  }
+  Index_type cost = 1;
+  for (const Piece& p : pieces) cost += p.range ? 2 : 1 + p.len;
+  if (cost < (length * (range_align - 1)) / range_align) {
+    for (const Piece& p : pieces) {
+      if (p.range) iset.push_back(RangeSegment(p.first, p.first + p.len));
+      else iset.push_back(ListSegment(indices_in + p.first, p.len));
+    }
+  } else {
+    iset.push_back(ListSegment(indices_in, length));
+  }
+}
+
 // ---------------------------------------------------------- forall_Icount
 // forall_Icount<POLICY>(segment, icount, body): body(icount + k, seg[k])
 // for k in [0, len) (pattern/forall.hpp:102-124, 227-276); over an

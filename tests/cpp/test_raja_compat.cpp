@@ -120,6 +120,47 @@ static void plugin_hooks() {
   CHECK("plugin_workgroup_hooks", ok);
 }
 
+// buildIndexSetAligned (test/functional/indexset-build/test-aligned-indexset.cpp)
+static void indexset_builders() {
+  std::vector<Index_type> idx(16);
+  std::iota(idx.begin(), idx.end(), 0);
+  idx.push_back(17);
+  idx.push_back(18);
+  for (Index_type i = 20; i < 28; ++i) idx.push_back(i);
+  idx.push_back(29);
+  idx.push_back(30);
+  idx.push_back(31);
+  RAJA::resources::Resource res{RAJA::resources::Host::get_default()};
+  RAJA::TypedIndexSet<RAJA::RangeSegment, RAJA::ListSegment> iset;
+  RAJA::buildIndexSetAligned(iset, res, idx.data(), Index_type(idx.size()), 8, 2);
+  using RS = RAJA::RangeSegment;
+  using LS = RAJA::ListSegment;
+  bool ok = iset.getLength() == idx.size() && iset.getNumSegments() == 5;
+  ok = ok && iset.getSegment<RS>(0).size() == 16 && *iset.getSegment<RS>(0).begin() == 0;
+  ok = ok && iset.getSegment<LS>(1).size() == 2 && *iset.getSegment<LS>(1).begin() == 17;
+  ok = ok && iset.getSegment<RS>(2).size() == 8 && *iset.getSegment<RS>(2).begin() == 20;
+  ok = ok && iset.getSegment<LS>(3).size() == 1 && *iset.getSegment<LS>(3).begin() == 29;
+  ok = ok && iset.getSegment<RS>(4).size() == 2 && *iset.getSegment<RS>(4).begin() == 30;
+  CHECK("index_set_aligned_reference_case", ok);
+  // the segments visit exactly the input indices, in order
+  std::vector<Index_type> seen;
+  RAJA::forall<RAJA::seq_exec>(iset, [&](Index_type i) { seen.push_back(i); });
+  CHECK("index_set_aligned_order", seen == idx);
+  // short input, or a split that saves too little: one list segment
+  RAJA::TypedIndexSet<RAJA::RangeSegment, RAJA::ListSegment> s1, s2, s3;
+  RAJA::buildIndexSetAligned(s1, res, idx.data(), 8, 8, 2);
+  std::vector<Index_type> scattered;
+  for (Index_type i = 0; i < 40; ++i) scattered.push_back(3 * i + 1);
+  RAJA::buildIndexSetAligned(s2, res, scattered.data(), 40, 8, 2);
+  std::vector<Index_type> dense(1000);
+  std::iota(dense.begin(), dense.end(), 64);
+  RAJA::buildIndexSetAligned(s3, res, dense.data(), 1000, 8, 32);
+  CHECK("index_set_aligned_short_and_scattered", s1.getNumSegments() == 1 && s1.getLength() == 8 &&
+                                                      s2.getNumSegments() == 1 && s2.getLength() == 40);
+  CHECK("index_set_aligned_dense_is_one_range",
+        s3.getNumSegments() == 1 && s3.getSegment<RS>(0).size() == 1000 && *s3.getSegment<RS>(0).begin() == 64);
+}
+
 // dynamic_forall, CombiningAdapter, permuted layouts, atomic views,
 // omp_atomic and regions (test/functional/dynamic_forall,
 // forall/CombiningAdapter, forall/atomic-view, forall/region,
@@ -648,6 +689,7 @@ int main() {
   }
   forall_adapters_and_regions();
   plugin_hooks();
+  indexset_builders();
   printf("%d failures\n", g_fail);
   return g_fail;
 }
