@@ -876,7 +876,7 @@ struct get_resource<b200_work<BLOCK, Async>> {
 template <int BLOCK, bool Async, class Body, class T>
 void forall_impl(b200_exec<BLOCK, Async>, const TypedRangeSegment<T>& r, Body&& body) {
   using B = std::decay_t<Body>;
-  const long long len = (long long)r.size();
+  const long long len = (long long)stripIndexType(r.size());
   if (len <= 0) return;
   auto k = b200::detail::forall_range_kernel<BLOCK, B, T>;
   const unsigned g = b200::detail::grid_for<b200::detail::forall_range_kernel<BLOCK, B, T>>(BLOCK, len);
@@ -888,7 +888,7 @@ void forall_impl(b200_exec<BLOCK, Async>, const TypedRangeSegment<T>& r, Body&& 
 template <int BLOCK, bool Async, class Body, class T>
 void forall_impl(b200_exec<BLOCK, Async>, const TypedRangeStrideSegment<T>& r, Body&& body) {
   using B = std::decay_t<Body>;
-  const long long len = (long long)r.size();
+  const long long len = (long long)stripIndexType(r.size());
   if (len <= 0) return;
   auto k = b200::detail::forall_stride_kernel<BLOCK, B, T>;
   const unsigned g = b200::detail::grid_for<b200::detail::forall_stride_kernel<BLOCK, B, T>>(BLOCK, len);
@@ -936,7 +936,7 @@ void forall_impl(b200_exec<BLOCK, Async> pol, const TypedIndexSet<Segs...>& is, 
     for (int i = 0; i < nseg; ++i) {
       const Range& r = std::get<Range>(segs[i]);
       begins[i] = r.b;
-      prefix[i + 1] = prefix[i] + (long long)r.size();
+      prefix[i + 1] = prefix[i] + (long long)stripIndexType(r.size());
     }
     const long long total = prefix[nseg];
     if (total == 0) return;

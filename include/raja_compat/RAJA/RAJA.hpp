@@ -131,6 +131,109 @@ struct greater {
 
 }  // namespace operators
 
+// ---------------------------------------------------- strongly typed indices
+// IndexValue<TYPE, VALUE> (index/IndexValue.hpp:34-415): an index wrapped in
+// its own type, so that indices of different spaces do not mix.  TYPE is
+// the derived class that RAJA_INDEX_VALUE / RAJA_INDEX_VALUE_T declare; the
+// arithmetic and comparisons take another TYPE or a raw VALUE and return
+// TYPE; *x and stripIndexType(x) give the raw value (there is no implicit
+// conversion to an integer).
+template <typename TYPE, typename VALUE = Index_type>
+class IndexValue {
+ public:
+  using value_type = VALUE;
+  RAJA_HOST_DEVICE constexpr IndexValue() : value(0) {}
+  RAJA_HOST_DEVICE constexpr explicit IndexValue(VALUE v) : value(v) {}
+  RAJA_HOST_DEVICE VALUE& operator*() { return value; }
+  RAJA_HOST_DEVICE constexpr const VALUE& operator*() const { return value; }
+
+  RAJA_HOST_DEVICE TYPE& operator++() { ++value; return self(); }
+  RAJA_HOST_DEVICE TYPE operator++(int) { TYPE t = self(); ++value; return t; }
+  RAJA_HOST_DEVICE TYPE& operator--() { --value; return self(); }
+  RAJA_HOST_DEVICE TYPE operator--(int) { TYPE t = self(); --value; return t; }
+
+#define RAJA_COMPAT_INDEX_ARITH(OP)                                                              \
+  RAJA_HOST_DEVICE TYPE operator OP(VALUE a) const { return TYPE(VALUE(value OP a)); }           \
+  RAJA_HOST_DEVICE TYPE operator OP(TYPE a) const { return TYPE(VALUE(value OP a.value)); }      \
+  RAJA_HOST_DEVICE TYPE& operator OP##=(VALUE a) { value = VALUE(value OP a); return self(); }    \
+  RAJA_HOST_DEVICE TYPE& operator OP##=(TYPE a) { value = VALUE(value OP a.value); return self(); }
+  RAJA_COMPAT_INDEX_ARITH(+)
+  RAJA_COMPAT_INDEX_ARITH(-)
+  RAJA_COMPAT_INDEX_ARITH(*)
+  RAJA_COMPAT_INDEX_ARITH(/)
+#undef RAJA_COMPAT_INDEX_ARITH
+  RAJA_HOST_DEVICE TYPE operator%(VALUE a) const { return TYPE(VALUE(value % a)); }
+  RAJA_HOST_DEVICE TYPE operator%(TYPE a) const { return TYPE(VALUE(value % a.value)); }
+
+#define RAJA_COMPAT_INDEX_CMP(OP)                                                 \
+  RAJA_HOST_DEVICE bool operator OP(VALUE a) const { return value OP a; }         \
+  RAJA_HOST_DEVICE bool operator OP(TYPE a) const { return value OP a.value; }
+  RAJA_COMPAT_INDEX_CMP(<)
+  RAJA_COMPAT_INDEX_CMP(<=)
+  RAJA_COMPAT_INDEX_CMP(>)
+  RAJA_COMPAT_INDEX_CMP(>=)
+  RAJA_COMPAT_INDEX_CMP(==)
+  RAJA_COMPAT_INDEX_CMP(!=)
+#undef RAJA_COMPAT_INDEX_CMP
+
+ protected:
+  VALUE value;
+
+ private:
+  RAJA_HOST_DEVICE TYPE& self() { return static_cast<TYPE&>(*this); }
+  RAJA_HOST_DEVICE const TYPE& self() const { return static_cast<const TYPE&>(*this); }
+};
+
+namespace detail {
+template <typename T, typename = void>
+struct is_index_value : std::false_type {};
+template <typename T>
+struct is_index_value<T, std::void_t<typename T::IndexValueType>> : std::true_type {};
+template <typename T, bool = is_index_value<T>::value>
+struct strip_index {
+  using type = T;
+};
+template <typename T>
+struct strip_index<T, true> {
+  using type = typename T::value_type;
+};
+}  // namespace detail
+// The raw value of an index (the value itself for integer indices).
+template <typename T>
+using strip_index_type_t = typename detail::strip_index<T>::type;
+template <typename T>
+RAJA_HOST_DEVICE constexpr strip_index_type_t<T> stripIndexType(const T& v) {
+  if constexpr (detail::is_index_value<T>::value) return *v;
+  else return v;
+}
+// convertIndex<TO>(from): the raw value of `from` as index type TO.
+template <typename TO, typename FROM>
+RAJA_HOST_DEVICE constexpr TO convertIndex(const FROM& v) {
+  return TO(static_cast<strip_index_type_t<TO>>(stripIndexType(v)));
+}
+
+}  // namespace RAJA
+
+// Declare a strongly typed index TYPE over Index_type (or over IDXT).
+#define RAJA_INDEX_VALUE(TYPE, NAME)                                                  \
+  class TYPE : public ::RAJA::IndexValue<TYPE> {                                      \
+   public:                                                                            \
+    using IndexValueType = TYPE;                                                      \
+    RAJA_HOST_DEVICE TYPE() : ::RAJA::IndexValue<TYPE>() {}                           \
+    RAJA_HOST_DEVICE explicit TYPE(::RAJA::Index_type v) : ::RAJA::IndexValue<TYPE>(v) {} \
+    static inline std::string getName() { return NAME; }                             \
+  }
+#define RAJA_INDEX_VALUE_T(TYPE, IDXT, NAME)                                          \
+  class TYPE : public ::RAJA::IndexValue<TYPE, IDXT> {                                \
+   public:                                                                            \
+    using IndexValueType = TYPE;                                                      \
+    RAJA_HOST_DEVICE TYPE() : ::RAJA::IndexValue<TYPE, IDXT>() {}                     \
+    RAJA_HOST_DEVICE explicit TYPE(IDXT v) : ::RAJA::IndexValue<TYPE, IDXT>(v) {}    \
+    static inline std::string getName() { return NAME; }                             \
+  }
+
+namespace RAJA {
+
 // ------------------------------------------------------------- segments
 // Random-access iterator over the values start, start + step, ... (the role
 // of Iterators::numeric_iterator / strided_numeric_iterator,
@@ -153,7 +256,7 @@ struct NumericIterator {
   RAJA_HOST_DEVICE NumericIterator operator+(difference_type k) const { return {T(v + T(k) * step), step}; }
   RAJA_HOST_DEVICE NumericIterator operator-(difference_type k) const { return {T(v - T(k) * step), step}; }
   RAJA_HOST_DEVICE difference_type operator-(const NumericIterator& o) const {
-    return difference_type((v - o.v) / step);
+    return difference_type(stripIndexType((v - o.v) / step));
   }
   RAJA_HOST_DEVICE bool operator==(const NumericIterator& o) const { return v == o.v; }
   RAJA_HOST_DEVICE bool operator!=(const NumericIterator& o) const { return v != o.v; }
@@ -236,14 +339,15 @@ class TypedIndexSet {
   // total number of indices
   size_t getLength() const {
     size_t n = 0;
-    for (const auto& v : segs_) n += size_t(std::visit([](const auto& g) { return Index_type(g.size()); }, v));
+    for (const auto& v : segs_)
+      n += size_t(std::visit([](const auto& g) { return Index_type(stripIndexType(g.size())); }, v));
     return n;
   }
   // position of segment i's first index in the whole traversal
   Index_type getStartingIcount(size_t i) const {
     Index_type n = 0;
     for (size_t k = 0; k < i && k < segs_.size(); ++k)
-      n += std::visit([](const auto& g) { return Index_type(g.size()); }, segs_[k]);
+      n += std::visit([](const auto& g) { return Index_type(stripIndexType(g.size())); }, segs_[k]);
     return n;
   }
   template <typename S>
@@ -260,11 +364,11 @@ using IndexSet = TypedIndexSet<RangeSegment, ListSegment, RangeStrideSegment>;
 // Element k of a segment, and its length (loop executors, forall params).
 namespace detail {
 template <typename T>
-RAJA_HOST_DEVICE Index_type seg_len(const TypedRangeSegment<T>& s) { return Index_type(s.e - s.b); }
+RAJA_HOST_DEVICE Index_type seg_len(const TypedRangeSegment<T>& s) { return Index_type(stripIndexType(s.e - s.b)); }
 template <typename T>
 RAJA_HOST_DEVICE T seg_at(const TypedRangeSegment<T>& s, Index_type k) { return T(s.b + T(k)); }
 template <typename T>
-RAJA_HOST_DEVICE Index_type seg_len(const TypedRangeStrideSegment<T>& s) { return Index_type(s.size()); }
+RAJA_HOST_DEVICE Index_type seg_len(const TypedRangeStrideSegment<T>& s) { return Index_type(stripIndexType(s.size())); }
 template <typename T>
 RAJA_HOST_DEVICE T seg_at(const TypedRangeStrideSegment<T>& s, Index_type k) { return T(s.b + T(k) * s.s); }
 template <typename T>
@@ -963,8 +1067,9 @@ void forall_impl(omp_parallel_for_exec, const TypedRangeSegment<T>& r, Body&& bo
 #pragma omp parallel
   {
     auto b = body;
+    const Index_type n = detail::seg_len(r);  // an integer loop: T may be a strongly typed index
 #pragma omp for schedule(static)
-    for (T i = r.b; i < r.e; ++i) b(i);
+    for (Index_type k = 0; k < n; ++k) b(detail::seg_at(r, k));
   }
 #else
   forall_impl(seq_exec{}, r, body);

@@ -120,6 +120,39 @@ static void plugin_hooks() {
   CHECK("plugin_workgroup_hooks", ok);
 }
 
+// Strongly typed indices (test/include/RAJA_test-index-types.hpp)
+RAJA_INDEX_VALUE(StrongIndexType, "StrongIndexType");
+RAJA_INDEX_VALUE_T(StrongInt, int, "StrongIntType");
+
+// forall over segments of strongly typed indices (the StrongIdxTypeList
+// cases of test/functional/forall/segment)
+template <typename IDX>
+static bool strong_forall_case() {
+  const Index_type first = 3, last = 1030;
+  std::vector<Index_type> w(last - first, 0), w2(last - first, 0);
+  Index_type* wp = w.data();
+  Index_type* wp2 = w2.data();
+  RAJA::TypedRangeSegment<IDX> r{IDX(first), IDX(last)};
+  RAJA::forall<RAJA::seq_exec>(r, [=](IDX i) { wp[RAJA::stripIndexType(i) - first] += RAJA::stripIndexType(i); });
+  RAJA::forall<RAJA::omp_parallel_for_exec>(r, [=](IDX i) { wp2[RAJA::stripIndexType(i - IDX(first))] += 1; });
+  std::vector<IDX> lst;
+  for (Index_type i = first; i < last; i += 7) lst.push_back(IDX(i));
+  RAJA::TypedListSegment<IDX> ls(lst.data(), Index_type(lst.size()));
+  RAJA::forall<RAJA::seq_exec>(ls, [=](IDX i) { wp2[RAJA::stripIndexType(i) - first] += 10; });
+  RAJA::TypedIndexSet<RAJA::TypedRangeSegment<IDX>> is;
+  is.push_back(RAJA::TypedRangeSegment<IDX>(IDX(first), IDX(first + 5)));
+  is.push_back(RAJA::TypedRangeSegment<IDX>(IDX(first + 5), IDX(last)));
+  Index_type count = 0;
+  Index_type* cp = &count;
+  RAJA::forall<RAJA::seq_exec>(is, [=](IDX) { ++*cp; });
+  bool ok = Index_type(RAJA::stripIndexType(r.size())) == last - first && count == last - first &&
+            is.getLength() == size_t(last - first);
+  for (Index_type i = first; i < last; ++i) {
+    ok = ok && w[i - first] == i && w2[i - first] == 1 + ((i - first) % 7 == 0 ? 10 : 0);
+  }
+  return ok;
+}
+
 // buildIndexSetAligned (test/functional/indexset-build/test-aligned-indexset.cpp)
 static void indexset_builders() {
   std::vector<Index_type> idx(16);
@@ -690,6 +723,12 @@ int main() {
   forall_adapters_and_regions();
   plugin_hooks();
   indexset_builders();
+  CHECK("strong_index_forall", strong_forall_case<StrongIndexType>() && strong_forall_case<StrongInt>());
+  {
+    StrongIndexType a(5), b(7);
+    CHECK("strong_index_ops", *(a + b) == 12 && (b - a) == 2 && a < b && RAJA::convertIndex<StrongInt>(b) == 7 &&
+                                  StrongIndexType::getName() == "StrongIndexType");
+  }
   printf("%d failures\n", g_fail);
   return g_fail;
 }
