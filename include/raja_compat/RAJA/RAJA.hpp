@@ -1876,6 +1876,18 @@ struct View {
   RAJA_HOST_DEVICE void set_data(T* p) { data = p; }
 };
 
+// TypedView<T, Layout, IndexTypes...> (util/View.hpp:55-57,
+// util/TypedViewBase.hpp): a view whose operator() takes exactly one index of
+// each listed type, so strongly typed indices of different spaces cannot be
+// swapped; the layout sees their raw values.
+template <typename T, typename LayoutT, typename... IndexTypes>
+struct TypedView : View<T, LayoutT> {
+  using View<T, LayoutT>::View;
+  RAJA_HOST_DEVICE T& operator()(IndexTypes... is) const {
+    return this->data[this->layout(stripIndexType(is)...)];
+  }
+};
+
 // Views whose elements are AtomicRefs (util/View.hpp:272-326):
 // make_atomic_view<Policy>(view)(i, j) += v is an atomic update.  With
 // seq_atomic the element reference is returned as it is.

@@ -123,6 +123,8 @@ static void plugin_hooks() {
 // Strongly typed indices (test/include/RAJA_test-index-types.hpp)
 RAJA_INDEX_VALUE(StrongIndexType, "StrongIndexType");
 RAJA_INDEX_VALUE_T(StrongInt, int, "StrongIntType");
+RAJA_INDEX_VALUE_T(RowIdx, int, "RowIdx");
+RAJA_INDEX_VALUE_T(ColIdx, int, "ColIdx");
 
 // forall over segments of strongly typed indices (the StrongIdxTypeList
 // cases of test/functional/forall/segment)
@@ -726,6 +728,15 @@ int main() {
   CHECK("strong_index_forall", strong_forall_case<StrongIndexType>() && strong_forall_case<StrongInt>());
   {
     StrongIndexType a(5), b(7);
+    std::vector<double> m(6 * 9, 0.0);
+    RAJA::TypedView<double, RAJA::Layout<2>, RowIdx, ColIdx> tv(m.data(), 6, 9);
+    RAJA::forall<RAJA::seq_exec>(RAJA::TypedRangeSegment<RowIdx>{RowIdx(0), RowIdx(6)}, [=](RowIdx r) {
+      for (ColIdx c(0); c < 9; ++c) tv(r, c) = 10.0 * *r + *c;
+    });
+    bool tv_ok = true;
+    for (int r = 0; r < 6; ++r)
+      for (int c = 0; c < 9; ++c) tv_ok = tv_ok && m[r * 9 + c] == 10.0 * r + c;
+    CHECK("typed_view_strong_indices", tv_ok);
     CHECK("strong_index_ops", *(a + b) == 12 && (b - a) == 2 && a < b && RAJA::convertIndex<StrongInt>(b) == 7 &&
                                   StrongIndexType::getName() == "StrongIndexType");
   }
