@@ -155,6 +155,44 @@ static bool strong_forall_case() {
   return ok;
 }
 
+// Several reducers in one loop body, with staggered initial values and
+// two accumulating loops (forall/reduce-multiple-segment).
+template <typename EXEC, typename RED>
+static bool multiple_reducers_case() {
+  const Index_type first = 5, last = 1357;
+  std::vector<double> a(last, 2.0);
+  double* p = a.data();
+  RAJA::ReduceSum<RED, double> s0(0.0), s1(2.0), s2(0.0), s3(6.0);
+  RAJA::ReduceMin<RED, double> mn0(1e9), mn1(-5.0);
+  RAJA::ReduceMax<RED, double> mx0(-1e9), mx1(50.0);
+  RAJA::ReduceMinLoc<RED, double, Index_type> ml(1e9, -1);
+  RAJA::ReduceMaxLoc<RED, double, Index_type> xl(-1e9, -1);
+  bool ok = true;
+  const double len = double(last - first);
+  for (int j = 0; j < 2; ++j) {
+    a[700] = -3.0 - j;       // the minimum moves on the second loop
+    a[900] = 40.0 + j;       // and so does the maximum
+    RAJA::forall<EXEC>(RAJA::TypedRangeSegment<Index_type>(first, last), [=](Index_type i) {
+      s0 += p[i];
+      s1 += p[i] * 2;
+      s2 += p[i] * 3;
+      s3 += p[i] * 4;
+      mn0.min(p[i]);
+      mn1.min(p[i]);
+      mx0.max(p[i]);
+      mx1.max(p[i]);
+      ml.minloc(p[i], i);
+      xl.maxloc(p[i], i);
+    });
+    double acc = 0.0;
+    for (int k = 0; k <= j; ++k) acc += 2.0 * (len - 2) + (-3.0 - k) + (40.0 + k);
+    ok = ok && s0.get() == acc && s1.get() == 2 * acc + 2.0 && s2.get() == 3 * acc && s3.get() == 4 * acc + 6.0;
+    ok = ok && mn0.get() == -3.0 - j && mn1.get() == -5.0 && mx0.get() == 40.0 + j && mx1.get() == 50.0;
+    ok = ok && ml.get() == -3.0 - j && ml.getLoc() == 700 && xl.get() == 40.0 + j && xl.getLoc() == 900;
+  }
+  return ok;
+}
+
 // buildIndexSetAligned (test/functional/indexset-build/test-aligned-indexset.cpp)
 static void indexset_builders() {
   std::vector<Index_type> idx(16);
@@ -725,6 +763,8 @@ int main() {
   forall_adapters_and_regions();
   plugin_hooks();
   indexset_builders();
+  CHECK("multiple_reducers_seq", (multiple_reducers_case<RAJA::seq_exec, RAJA::seq_reduce>()));
+  CHECK("multiple_reducers_omp", (multiple_reducers_case<RAJA::omp_parallel_for_exec, RAJA::omp_reduce>()));
   CHECK("strong_index_forall", strong_forall_case<StrongIndexType>() && strong_forall_case<StrongInt>());
   {
     StrongIndexType a(5), b(7);
