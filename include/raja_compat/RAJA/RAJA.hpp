@@ -414,6 +414,17 @@ struct seq_reduce {};
 struct omp_reduce {};
 struct seq_multi_reduce {};
 struct seq_atomic {};
+// IndexSet execution (policy/sequential/policy.hpp, policy/openmp/policy.hpp,
+// index/IndexSet.hpp): ExecPolicy<SegIt, SegExec> walks an IndexSet's
+// segments with SegIt (in order: seq_segit; spread over OpenMP threads:
+// omp_parallel_segit) and runs each segment with SegExec.
+struct seq_segit {};
+struct omp_parallel_segit {};
+template <typename SEG_IT, typename SEG_EXEC>
+struct ExecPolicy {
+  using seg_it = SEG_IT;
+  using seg_exec = SEG_EXEC;
+};
 struct omp_atomic {};
 
 // ------------------------------------------------------------ resources
@@ -607,6 +618,11 @@ struct is_resource<Resource> : std::true_type {};
 template <typename Pol>
 struct get_resource {
   using type = Host;
+};
+// an IndexSet policy runs on its segment policy's resource
+template <typename SEG_IT, typename SEG_EXEC>
+struct get_resource<ExecPolicy<SEG_IT, SEG_EXEC>> {
+  using type = typename get_resource<SEG_EXEC>::type;
 };
 template <typename Pol>
 typename get_resource<Pol>::type get_default_resource() {
@@ -1075,6 +1091,23 @@ void forall_impl(omp_parallel_for_exec, const TypedRangeSegment<T>& r, Body&& bo
   forall_impl(seq_exec{}, r, body);
 #endif
 }
+// omp_parallel_for_exec over list and strided segments (range segments
+// have their own overload above)
+template <typename Seg, typename Body, typename = decltype(detail::seg_len(std::declval<const Seg&>()))>
+void forall_impl(omp_parallel_for_exec, const Seg& seg, Body&& body) {
+  const Index_type n = detail::seg_len(seg);
+#if defined(_OPENMP)
+#pragma omp parallel
+  {
+    auto b = body;
+#pragma omp for schedule(static)
+    for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+  }
+#else
+  auto b = body;
+  for (Index_type k = 0; k < n; ++k) b(detail::seg_at(seg, k));
+#endif
+}
 // simd_exec: the sequential loop (any segment kind)
 template <typename Seg, typename Body, typename = decltype(detail::seg_len(std::declval<const Seg&>()))>
 void forall_impl(simd_exec, const Seg& seg, Body&& body) {
@@ -1187,6 +1220,47 @@ void region(Body&& body) {
 template <typename Pol, typename Body, typename... Segs>
 void forall_impl(Pol p, const TypedIndexSet<Segs...>& is, Body&& body) {
   for (const auto& s : is.segments()) std::visit([&](const auto& seg) { forall_impl(p, seg, body); }, s);
+}
+// A single segment under an IndexSet policy runs with the segment policy.
+template <typename IT, typename E, typename Seg, typename Body,
+          typename = decltype(detail::seg_len(std::declval<const Seg&>()))>
+void forall_impl(ExecPolicy<IT, E>, const Seg& seg, Body&& body) {
+  forall_impl(E{}, seg, std::forward<Body>(body));
+}
+// ExecPolicy<seq_segit, E>: the segment policy's own IndexSet loop (a
+// back-end may fuse the segments into one launch).
+template <typename E, typename Body, typename... Segs>
+void forall_impl(ExecPolicy<seq_segit, E>, const TypedIndexSet<Segs...>& is, Body&& body) {
+  forall_impl(E{}, is, std::forward<Body>(body));
+}
+// ExecPolicy<omp_parallel_segit, E>: the segments are shared among OpenMP
+// threads, each run with E (host policies; the loop body must be safe to
+// run for several segments at once).
+template <typename E, typename Body, typename... Segs>
+void forall_impl(ExecPolicy<omp_parallel_segit, E>, const TypedIndexSet<Segs...>& is, Body&& body) {
+  const auto& segs = is.segments();
+  const Index_type n = Index_type(segs.size());
+#if defined(_OPENMP)
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (Index_type k = 0; k < n; ++k) std::visit([&](const auto& seg) { forall_impl(E{}, seg, body); }, segs[k]);
+}
+
+// getIndices / getIndicesConditional (index/IndexSetUtils.hpp:47-120): the
+// indices of a segment or IndexSet, in order, into a container with
+// push_back (only those for which `conditional(index)` holds).
+template <typename CONTAINER_T, typename SEGMENT_T, typename CONDITIONAL>
+void getIndicesConditional(CONTAINER_T& con, const SEGMENT_T& seg, CONDITIONAL conditional) {
+  CONTAINER_T tcon;
+  auto take = [&](typename CONTAINER_T::value_type idx) {
+    if (conditional(idx)) tcon.push_back(idx);
+  };
+  forall_impl(seq_exec{}, seg, take);
+  con = tcon;
+}
+template <typename CONTAINER_T, typename SEGMENT_T>
+void getIndices(CONTAINER_T& con, const SEGMENT_T& seg) {
+  getIndicesConditional(con, seg, [](const typename CONTAINER_T::value_type&) { return true; });
 }
 
 // forall with expt params on host: each param gets a ValOp local starting

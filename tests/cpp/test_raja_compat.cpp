@@ -193,6 +193,50 @@ static bool multiple_reducers_case() {
   return ok;
 }
 
+// IndexSets under ExecPolicy<seq_segit | omp_parallel_segit, ...>
+// (forall/indexset) and getIndices[Conditional] (index/IndexSetUtils.hpp)
+static void indexset_exec_policies() {
+  std::vector<Index_type> lst{40, 41, 45, 47, 60};
+  RAJA::TypedIndexSet<RAJA::RangeSegment, RAJA::ListSegment, RAJA::RangeStrideSegment> is;
+  is.push_back(RAJA::RangeSegment(0, 10));
+  is.push_back(RAJA::ListSegment(lst.data(), Index_type(lst.size())));
+  is.push_back(RAJA::RangeStrideSegment(100, 130, 3));
+  is.push_back(RAJA::RangeSegment(200, 1200));
+  std::vector<Index_type> expect;
+  for (Index_type i = 0; i < 10; ++i) expect.push_back(i);
+  for (Index_type v : lst) expect.push_back(v);
+  for (Index_type i = 100; i < 130; i += 3) expect.push_back(i);
+  for (Index_type i = 200; i < 1200; ++i) expect.push_back(i);
+  std::vector<Index_type> got;
+  RAJA::getIndices(got, is);
+  CHECK("get_indices_indexset", got == expect);
+  std::vector<Index_type> even;
+  RAJA::getIndicesConditional(even, is, [](Index_type i) { return i % 2 == 0; });
+  bool ok = true;
+  size_t k = 0;
+  for (Index_type v : expect)
+    if (v % 2 == 0) ok = ok && k < even.size() && even[k++] == v;
+  std::vector<Index_type> rseg;
+  RAJA::getIndices(rseg, RAJA::RangeSegment(3, 7));
+  CHECK("get_indices_conditional_and_segment", ok && k == even.size() && (rseg == std::vector<Index_type>{3, 4, 5, 6}));
+
+  std::vector<int> hit(1200, 0);
+  int* hp = hit.data();
+  RAJA::forall<RAJA::ExecPolicy<RAJA::seq_segit, RAJA::seq_exec>>(is, [=](Index_type i) { hp[i] += 1; });
+  RAJA::forall<RAJA::ExecPolicy<RAJA::seq_segit, RAJA::omp_parallel_for_exec>>(is, [=](Index_type i) { hp[i] += 2; });
+  RAJA::forall<RAJA::ExecPolicy<RAJA::omp_parallel_segit, RAJA::seq_exec>>(is, [=](Index_type i) { hp[i] += 4; });
+  ok = true;
+  std::vector<int> ref(1200, 0);
+  for (Index_type v : expect) ref[v] = 7;
+  for (int i = 0; i < 1200; ++i) ok = ok && hit[i] == ref[i];
+  std::vector<Index_type> ic(1200, -1);
+  Index_type* icp = ic.data();
+  RAJA::forall_Icount<RAJA::ExecPolicy<RAJA::seq_segit, RAJA::seq_exec>>(
+      is, [=](Index_type icount, Index_type i) { icp[i] = icount; });
+  for (size_t j = 0; j < expect.size(); ++j) ok = ok && ic[expect[j]] == Index_type(j);
+  CHECK("indexset_exec_policies", ok);
+}
+
 // buildIndexSetAligned (test/functional/indexset-build/test-aligned-indexset.cpp)
 static void indexset_builders() {
   std::vector<Index_type> idx(16);
@@ -763,6 +807,7 @@ int main() {
   forall_adapters_and_regions();
   plugin_hooks();
   indexset_builders();
+  indexset_exec_policies();
   CHECK("multiple_reducers_seq", (multiple_reducers_case<RAJA::seq_exec, RAJA::seq_reduce>()));
   CHECK("multiple_reducers_omp", (multiple_reducers_case<RAJA::omp_parallel_for_exec, RAJA::omp_reduce>()));
   CHECK("strong_index_forall", strong_forall_case<StrongIndexType>() && strong_forall_case<StrongInt>());
