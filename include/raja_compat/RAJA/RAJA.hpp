@@ -1950,6 +1950,77 @@ struct View {
   RAJA_HOST_DEVICE void set_data(T* p) { data = p; }
 };
 
+// Index layouts (util/IndexLayout.hpp:28-230, util/View.hpp:58-72): each
+// dimension maps its index through DirectIndex (as is), IndexList
+// (index_list[i]) or ConditionalIndexList (index_list[i], or i when the list
+// is null) before the row-major strides apply.
+template <typename IdxLin = Index_type>
+struct DirectIndex {
+  RAJA_HOST_DEVICE constexpr IdxLin operator()(IdxLin i) const { return i; }
+};
+template <typename IdxLin = Index_type>
+struct IndexList {
+  IdxLin* index_list = nullptr;
+  RAJA_HOST_DEVICE constexpr IdxLin operator()(IdxLin i) const { return index_list[i]; }
+};
+template <typename IdxLin = Index_type>
+struct ConditionalIndexList {
+  IdxLin* index_list = nullptr;
+  RAJA_HOST_DEVICE constexpr IdxLin operator()(IdxLin i) const { return index_list ? index_list[i] : i; }
+};
+template <size_t DIM = 1, typename IdxLin = Index_type, typename... IndexTypes>
+struct IndexLayout {
+  static_assert(sizeof...(IndexTypes) == DIM, "one index map per dimension");
+  Layout<DIM, IdxLin> base;
+  std::tuple<IndexTypes...> maps;
+  template <typename... Ns>
+  IndexLayout(const std::tuple<IndexTypes...>& m, Ns... ns) : base(ns...), maps(m) {}
+  template <typename... Is>
+  RAJA_HOST_DEVICE IdxLin operator()(Is... is) const {
+    static_assert(sizeof...(Is) == DIM, "one index per dimension");
+    return apply(std::index_sequence_for<IndexTypes...>{}, is...);
+  }
+  RAJA_HOST_DEVICE Index_type size() const { return base.size(); }
+  RAJA_HOST_DEVICE Index_type size_noproj() const { return base.size(); }
+
+ private:
+  template <size_t... D, typename... Is>
+  RAJA_HOST_DEVICE IdxLin apply(std::index_sequence<D...>, Is... is) const {
+    return IdxLin((Index_type(0) + ... + (base.strides[D] * Index_type(std::get<D>(maps)(IdxLin(is))))));
+  }
+};
+template <typename... IndexTypes>
+std::tuple<IndexTypes...> make_index_tuple(IndexTypes... it) {
+  return std::tuple<IndexTypes...>(it...);
+}
+template <typename IdxLin = Index_type, typename... IndexTypes, typename... Ns>
+IndexLayout<sizeof...(Ns), IdxLin, IndexTypes...> make_index_layout(const std::tuple<IndexTypes...>& maps, Ns... ns) {
+  return IndexLayout<sizeof...(Ns), IdxLin, IndexTypes...>(maps, ns...);
+}
+template <size_t DIM, typename IdxLin, typename T, typename... IndexTypes>
+View<T, IndexLayout<DIM, IdxLin, IndexTypes...>> make_index_view(T* ptr,
+                                                                 const IndexLayout<DIM, IdxLin, IndexTypes...>& layout) {
+  return View<T, IndexLayout<DIM, IdxLin, IndexTypes...>>(ptr, layout);
+}
+
+// for_each over a container's elements, a type list or a tuple
+// (util/for_each.hpp:36-125); each returns the function object.
+template <typename Container, typename UnaryFunc>
+UnaryFunc for_each(Container&& c, UnaryFunc func) {
+  for (auto&& x : c) func(x);
+  return func;
+}
+template <typename... Ts, typename UnaryFunc>
+UnaryFunc for_each_type(const camp::list<Ts...>&, UnaryFunc func) {
+  (func(Ts{}), ...);
+  return func;
+}
+template <typename Tuple, typename UnaryFunc>
+UnaryFunc for_each_tuple(Tuple&& t, UnaryFunc func) {
+  std::apply([&](auto&&... x) { (func(x), ...); }, std::forward<Tuple>(t));
+  return func;
+}
+
 // TypedView<T, Layout, IndexTypes...> (util/View.hpp:55-57,
 // util/TypedViewBase.hpp): a view whose operator() takes exactly one index of
 // each listed type, so strongly typed indices of different spaces cannot be

@@ -2,6 +2,7 @@
 // against the known answers of the reference's functional tests.
 #include <algorithm>
 #include <cstdio>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <memory>
@@ -235,6 +236,34 @@ static void indexset_exec_policies() {
       is, [=](Index_type icount, Index_type i) { icp[i] = icount; });
   for (size_t j = 0; j < expect.size(); ++j) ok = ok && ic[expect[j]] == Index_type(j);
   CHECK("indexset_exec_policies", ok);
+}
+
+// index views (util/IndexLayout.hpp) and the for_each utilities
+static void index_views_and_for_each() {
+  std::vector<double> a(4 * 5);
+  for (int k = 0; k < 20; ++k) a[k] = k;
+  std::vector<Index_type> rows{3, 0, 2};
+  auto lay = RAJA::make_index_layout(
+      RAJA::make_index_tuple(RAJA::IndexList<>{rows.data()}, RAJA::DirectIndex<>()), 4, 5);
+  auto v = RAJA::make_index_view(a.data(), lay);
+  RAJA::View<double, RAJA::IndexLayout<1, Index_type, RAJA::ConditionalIndexList<>>> c0(
+      a.data(), RAJA::make_index_layout(RAJA::make_index_tuple(RAJA::ConditionalIndexList<>{nullptr}), 20));
+  std::vector<Index_type> pick{19, 4};
+  RAJA::View<double, RAJA::IndexLayout<1, Index_type, RAJA::ConditionalIndexList<>>> c1(
+      a.data(), RAJA::make_index_layout(RAJA::make_index_tuple(RAJA::ConditionalIndexList<>{pick.data()}), 20));
+  CHECK("index_view", v(0, 1) == 16 && v(1, 4) == 4 && v(2, 0) == 10 && c0(7) == 7 && c1(0) == 19 && c1(1) == 4);
+  int sum = 0;
+  std::vector<int> xs{1, 2, 3, 4};
+  RAJA::for_each(xs, [&](int x) { sum += x; });
+  int types = 0;
+  RAJA::for_each_type(camp::list<int, double, char>{}, [&](auto t) { types += int(sizeof(t)); });
+  std::string cat;
+  RAJA::for_each_tuple(std::make_tuple(1, std::string("b"), 'c'), [&](const auto& x) {
+    std::ostringstream o;
+    o << x;
+    cat += o.str();
+  });
+  CHECK("for_each_utilities", sum == 10 && types == int(sizeof(int) + sizeof(double) + sizeof(char)) && cat == "1bc");
 }
 
 // buildIndexSetAligned (test/functional/indexset-build/test-aligned-indexset.cpp)
@@ -808,6 +837,7 @@ int main() {
   plugin_hooks();
   indexset_builders();
   indexset_exec_policies();
+  index_views_and_for_each();
   CHECK("multiple_reducers_seq", (multiple_reducers_case<RAJA::seq_exec, RAJA::seq_reduce>()));
   CHECK("multiple_reducers_omp", (multiple_reducers_case<RAJA::omp_parallel_for_exec, RAJA::omp_reduce>()));
   CHECK("strong_index_forall", strong_forall_case<StrongIndexType>() && strong_forall_case<StrongInt>());
