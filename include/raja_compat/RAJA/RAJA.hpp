@@ -1246,6 +1246,20 @@ void forall_impl(ExecPolicy<omp_parallel_segit, E>, const TypedIndexSet<Segs...>
   for (Index_type k = 0; k < n; ++k) std::visit([&](const auto& seg) { forall_impl(E{}, seg, body); }, segs[k]);
 }
 
+// expt params under an IndexSet policy: each segment runs the segment
+// policy's params loop, which folds its result into the targets, so the
+// targets end up reduced over every segment.
+template <typename IT, typename E, typename Seg, typename Body, typename... Red,
+          typename = decltype(detail::seg_len(std::declval<const Seg&>()))>
+void forall_params_impl(ExecPolicy<IT, E>, const Seg& seg, Body&& body, Red&... reds) {
+  forall_params_impl(E{}, seg, body, reds...);
+}
+template <typename IT, typename E, typename Body, typename... Segs, typename... Red>
+void forall_params_impl(ExecPolicy<IT, E>, const TypedIndexSet<Segs...>& is, Body&& body, Red&... reds) {
+  for (const auto& s : is.segments())
+    std::visit([&](const auto& seg) { forall_params_impl(E{}, seg, body, reds...); }, s);
+}
+
 // getIndices / getIndicesConditional (index/IndexSetUtils.hpp:47-120): the
 // indices of a segment or IndexSet, in order, into a container with
 // push_back (only those for which `conditional(index)` holds).

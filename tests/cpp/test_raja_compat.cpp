@@ -236,6 +236,23 @@ static void indexset_exec_policies() {
       is, [=](Index_type icount, Index_type i) { icp[i] = icount; });
   for (size_t j = 0; j < expect.size(); ++j) ok = ok && ic[expect[j]] == Index_type(j);
   CHECK("indexset_exec_policies", ok);
+  double total = 1.0, vmin = 1e9;
+  Index_type imin = -1;
+  RAJA::forall<RAJA::ExecPolicy<RAJA::seq_segit, RAJA::seq_exec>>(
+      is, RAJA::expt::Reduce<RAJA::operators::plus>(&total), RAJA::expt::ReduceLoc<RAJA::operators::minimum>(&vmin, &imin),
+      [=](Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& s,
+          RAJA::expt::ValOp<RAJA::expt::ValLoc<double, Index_type>, RAJA::operators::minimum>& m) {
+        s += double(i);
+        m.minloc(double((i * 37) % 101), i);
+      });
+  double ref_total = 1.0, ref_min = 1e9;
+  Index_type ref_loc = -1;
+  for (Index_type v : expect) {
+    ref_total += double(v);
+    const double x = double((v * 37) % 101);
+    if (x < ref_min) { ref_min = x; ref_loc = v; }
+  }
+  CHECK("indexset_exec_policy_params", total == ref_total && vmin == ref_min && imin == ref_loc);
 }
 
 // index views (util/IndexLayout.hpp) and the for_each utilities
