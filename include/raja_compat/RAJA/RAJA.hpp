@@ -2017,6 +2017,61 @@ View<T, IndexLayout<DIM, IdxLin, IndexTypes...>> make_index_view(T* ptr,
   return View<T, IndexLayout<DIM, IdxLin, IndexTypes...>>(ptr, layout);
 }
 
+// make_permuted_view<meta_layout>(ptr, extents...) (util/View.hpp:328-417):
+// layout_right is row-major (the last index has stride one), layout_left
+// column-major (the first index has stride one), and an index sequence
+// gives the stride order (its last entry has stride one).
+struct layout_left {};
+struct layout_right {};
+template <typename meta_layout, typename IndexType = Index_type, typename T, typename... Extents>
+View<T, Layout<sizeof...(Extents), IndexType>> make_permuted_view(T* ptr, Extents... extents) {
+  constexpr size_t N = sizeof...(Extents);
+  const std::array<Index_type, N> sizes{{Index_type(extents)...}};
+  std::array<Index_type, N> order{};
+  for (size_t d = 0; d < N; ++d) order[d] = Index_type(d);
+  if constexpr (std::is_same<meta_layout, layout_left>::value) {
+    for (size_t d = 0; d < N; ++d) order[d] = Index_type(N - 1 - d);
+  } else if constexpr (!std::is_same<meta_layout, layout_right>::value) {
+    order = as_array<meta_layout>::get();
+  }
+  return View<T, Layout<N, IndexType>>(ptr, Layout<N, IndexType>(sizes, order));
+}
+
+// Integer helpers (util/math.hpp:36-105): floor(log2(n)) (0 for n <= 0),
+// the smallest power of two >= n and the largest <= n (0 for n <= 0), and
+// lhs mod rhs for a power-of-two rhs.
+template <typename T, std::enable_if_t<std::is_integral<T>::value, int> = 0>
+RAJA_HOST_DEVICE constexpr T log2(T n) noexcept {
+  T r = 0;
+  while (n > 1) {
+    n = T(n >> 1);
+    ++r;
+  }
+  return r;
+}
+template <typename T, std::enable_if_t<std::is_integral<T>::value, int> = 0>
+RAJA_HOST_DEVICE constexpr T next_pow2(T n) noexcept {
+  if (n <= 0) return 0;
+  T p = 1;
+  while (p < n) {
+    if (p > std::numeric_limits<T>::max() / 2) return 0;  // no larger power fits in T
+    p = T(p << 1);
+  }
+  return p;
+}
+template <typename T, std::enable_if_t<std::is_integral<T>::value, int> = 0>
+RAJA_HOST_DEVICE constexpr T prev_pow2(T n) noexcept {
+  if (n <= 0) return 0;
+  T p = 1;
+  while (p <= n / 2) p = T(p << 1);
+  return p;
+}
+template <typename L, typename R,
+          std::enable_if_t<std::is_integral<L>::value && std::is_integral<R>::value, int> = 0>
+RAJA_HOST_DEVICE constexpr auto power_of_2_mod(L lhs, R rhs) noexcept {
+  return lhs & (rhs - R(1));
+}
+
 // for_each over a container's elements, a type list or a tuple
 // (util/for_each.hpp:36-125); each returns the function object.
 template <typename Container, typename UnaryFunc>

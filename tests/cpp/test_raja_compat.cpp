@@ -280,6 +280,17 @@ static void index_views_and_for_each() {
     o << x;
     cat += o.str();
   });
+  std::vector<int> g(2 * 3 * 4);
+  for (int k = 0; k < 24; ++k) g[k] = k;
+  auto vr = RAJA::make_permuted_view<RAJA::layout_right>(g.data(), 2, 3, 4);
+  auto vl = RAJA::make_permuted_view<RAJA::layout_left>(g.data(), 2, 3, 4);
+  auto vp = RAJA::make_permuted_view<RAJA::PERM_JIK>(g.data(), 2, 3, 4);   // k fastest, then i, then j
+  CHECK("permuted_views", vr(1, 0, 2) == 14 && vl(1, 0, 2) == 13 && vp(1, 0, 2) == 6 && vr(1, 2, 3) == 23);
+  CHECK("math_helpers", RAJA::log2(1) == 0 && RAJA::log2(1023) == 9 && RAJA::log2(1024) == 10 && RAJA::log2(-5) == 0 &&
+                            RAJA::next_pow2(0) == 0 && RAJA::next_pow2(5) == 8 && RAJA::next_pow2(64) == 64 &&
+                            RAJA::next_pow2(-3) == 0 && RAJA::prev_pow2(5) == 4 && RAJA::prev_pow2(64) == 64 &&
+                            RAJA::prev_pow2(-1) == 0 && RAJA::power_of_2_mod(37, 16) == 5 &&
+                            RAJA::next_pow2(uint8_t(200)) == 0 && RAJA::prev_pow2(uint8_t(200)) == 128);
   CHECK("for_each_utilities", sum == 10 && types == int(sizeof(int) + sizeof(double) + sizeof(char)) && cat == "1bc");
 }
 
