@@ -198,49 +198,120 @@ class ClockSampler:
 
 
 # -------------------------------------------------------------- cpu legs
-def cpu_suite(n: int, seed: int = 0):
-    """Time the oracle's OpenMP restatement over the suite at n elements.
+class CpuSuite:
+    """The oracle's OpenMP restatement of RAJA's omp_parallel_for_exec path
+    over the bandwidth-sweep primitives at n elements per primitive.
 
-    Returns (total algorithmic bytes, seconds, cores, per-primitive times)."""
-    import numpy as np
+    Inputs are generated once (seeded numpy, the same distributions as the
+    device inputs) on first use of each primitive; output and sort work
+    buffers are allocated and touched up front, so a timed call pays for the
+    primitive only: sorts are timed in place on a fresh copy of the input
+    (RAJA's sort is in place), made outside the timer."""
 
-    import oracle
-    rng = np.random.default_rng(seed)
-    f32 = rng.uniform(-1, 1, n).astype(np.float32)
-    f64 = rng.uniform(-1, 1, n)
-    si = rng.integers(0, 1024, n).astype(np.int64)
-    u32 = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
-    u64 = rng.integers(0, 2 ** 64, n, dtype=np.uint64)
-    pk = rng.normal(0, 1, n).astype(np.float32)
-    pv = np.arange(n, dtype=np.int32)
-    zs = {nb: np.searchsorted(zipf_cdf(nb), rng.random(n), side="right").clip(0, nb - 1)
-          .astype(np.int32) for nb in (256, 65536)}
-    out = np.empty_like(si)
-    calls = [
-        ("reduce_sum_f32", lambda: oracle.reduce_sum(f32, parallel=True)),
-        ("reduce_sum_f64", lambda: oracle.reduce_sum(f64, parallel=True)),
-        ("minloc_f32", lambda: oracle.reduce_minloc(f32, parallel=True)),
-        ("maxloc_f32", lambda: oracle.reduce_maxloc(f32, parallel=True)),
-        ("minloc_f64", lambda: oracle.reduce_minloc(f64, parallel=True)),
-        ("maxloc_f64", lambda: oracle.reduce_maxloc(f64, parallel=True)),
-        ("exclusive_scan_i64", lambda: oracle.scan(si, "plus", exclusive=True, init=0,
-                                                   parallel=True, out=out)),
-        ("sort_u32", lambda: oracle.sort(u32, parallel=True, stable=False)),
-        ("sort_u64", lambda: oracle.sort(u64, parallel=True, stable=False)),
-        ("sort_pairs_f32_i32", lambda: oracle.sort_pairs(pk, pv, parallel=True, stable=False)),
-        ("histogram_256", lambda: oracle.histogram(zs[256], 256, parallel=True)),
-        ("histogram_65536", lambda: oracle.histogram(zs[65536], 65536, parallel=True)),
-    ]
-    table = dict(primitive_table(n))
-    per = {}
-    total = 0.0
-    for name, fn in calls:
+    def __init__(self, n: int, seed: int = 0):
+        import numpy as np
+        import oracle
+        self.np, self.orc, self.n, self.seed = np, oracle, n, seed
+        self.arrays: dict = {}
+        self.table = dict(primitive_table(n))
+        self.names = [p for p, _ in primitive_table(n)]
+
+    def _get(self, key):
+        np = self.np
+        if key in self.arrays:
+            return self.arrays[key]
+        n = self.n
+        rng = np.random.default_rng([self.seed, sorted(self._KEYS).index(key)])
+        if key == "f32":
+            a = rng.uniform(-1, 1, n).astype(np.float32)
+        elif key == "f64":
+            a = rng.uniform(-1, 1, n)
+        elif key == "scan_in":
+            a = rng.integers(0, 1024, n).astype(np.int64)
+        elif key == "u32":
+            a = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+        elif key == "u64":
+            a = rng.integers(0, 2 ** 64, n, dtype=np.uint64)
+        elif key == "pk":
+            a = rng.normal(0, 1, n).astype(np.float32)
+        elif key == "pv":
+            a = np.arange(n, dtype=np.int32)
+        else:  # z256, z65536
+            nb = int(key[1:])
+            a = np.searchsorted(zipf_cdf(nb), rng.random(n), side="right").clip(0, nb - 1) \
+                .astype(np.int32)
+        self.arrays[key] = a
+        return a
+
+    _KEYS = ("f32", "f64", "scan_in", "u32", "u64", "pk", "pv", "z256", "z65536")
+
+    def _work(self, key, like):
+        w = self.arrays.get("w_" + key)
+        if w is None:
+            w = self.np.ones_like(like)       # touched: no page faults in the timed call
+            self.arrays["w_" + key] = w
+        return w
+
+    def call(self, name: str):
+        """(prepare, timed): inputs are generated here, outside the timed
+        call; prepare() copies sort inputs into their work buffers."""
+        o, g, w, np = self.orc, self._get, self._work, self.np
+        if name == "reduce_sum_f32" or name == "reduce_sum_f64":
+            x = g(name[-3:])
+            return None, lambda: o.reduce_sum(x, parallel=True)
+        if name in ("minloc_f32", "maxloc_f32", "minloc_f64", "maxloc_f64"):
+            fn = o.reduce_minloc if name.startswith("min") else o.reduce_maxloc
+            x = g(name[-3:])
+            return None, lambda: fn(x, parallel=True)
+        if name == "exclusive_scan_i64":
+            x = g("scan_in")
+            out = w("scan", x)
+            return None, lambda: o.scan(x, "plus", exclusive=True, init=0, parallel=True, out=out)
+        if name in ("sort_u32", "sort_u64"):
+            src = g(name[-3:])
+            buf = w(name, src)
+            return (lambda: np.copyto(buf, src)), \
+                (lambda: o.sort_inplace(buf, parallel=True, stable=False))
+        if name == "sort_pairs_f32_i32":
+            ks, vs = g("pk"), g("pv")
+            kb, vb = w("pk", ks), w("pv", vs)
+            return (lambda: (np.copyto(kb, ks), np.copyto(vb, vs))), \
+                (lambda: o.sort_pairs_inplace(kb, vb, parallel=True, stable=False))
+        if name.startswith("histogram_"):
+            nb = int(name.split("_")[1])
+            x = g(f"z{nb}")
+            return None, lambda: o.histogram(x, nb, parallel=True)
+        raise KeyError(name)
+
+    def time(self, name: str) -> float:
+        prep, fn = self.call(name)
+        if prep:
+            prep()
         t0 = time.perf_counter()
         fn()
-        dt = time.perf_counter() - t0
-        per[name] = dt
-        total += dt
-    return sum(table.values()), total, oracle.max_threads(), per
+        return time.perf_counter() - t0
+
+
+def cpu_suite_rotation(suite: "CpuSuite", steps: int, warmup: int):
+    """Time `steps` rotation steps after `warmup` untimed ones: step k runs
+    primitive k mod 12 of the suite at the full n (a bounded sample of one
+    step of the workload).  Primitives the rotation did not reach run once
+    more, so every primitive has a time.  Returns per-primitive mean
+    seconds and the seconds the timed steps took."""
+    names = suite.names
+    for k in range(warmup):
+        suite.time(names[k % len(names)])
+    acc: dict[str, list] = {}
+    timed = 0.0
+    for k in range(steps):
+        nm = names[k % len(names)]
+        dt = suite.time(nm)
+        timed += dt
+        acc.setdefault(nm, []).append(dt)
+    for nm in names:
+        if nm not in acc:
+            acc[nm] = [suite.time(nm)]
+    return {nm: sum(v) / len(v) for nm, v in acc.items()}, timed
 
 
 def cpu_model() -> str:
@@ -279,33 +350,29 @@ def run_reference(args, rank: int, world: int):
     oracle.build()
     os.environ.setdefault("OMP_PROC_BIND", "close")
     n = 1 << args.cpu_log2n
-    for _ in range(args.warmup):
-        cpu_suite(n)
-    tot_bytes, tot_s = 0, 0.0
-    per_acc: dict[str, float] = {}
-    cores = 1
-    for k in range(args.steps):
-        b, s, cores, per = cpu_suite(n, seed=k)
-        tot_bytes += b
-        tot_s += s
-        for nm, v in per.items():
-            per_acc[nm] = per_acc.get(nm, 0.0) + v
-    value = tot_bytes / tot_s / 1e9
-    table = dict(primitive_table(n))
+    suite = CpuSuite(n)
+    per, _ = cpu_suite_rotation(suite, args.steps, args.warmup)
+    table = suite.table
+    step_s = sum(per.values())            # one full step: every primitive once
+    value = sum(table.values()) / step_s / 1e9
+    cores = oracle.max_threads()
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1000 * tot_s / args.steps, 3), "higher_is_better": True,
+        "ms_per_step": round(1000 * step_s, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "mixed (f32,f64,i32,i64,u32,u64)",
         "data": "synthetic (seeded, bandwidth-sweep shapes)",
         "config": config_block(args, n_override=n),
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"every primitive at N=2^{args.cpu_log2n} per step "
+                         "sample": f"each timed step runs one primitive of the suite at "
+                                   f"N=2^{args.cpu_log2n} in rotation (all 12 covered); "
+                                   f"ms_per_step = the sum of the per-primitive means "
                                    f"(oracle OpenMP restatement of omp_parallel_for_exec; "
                                    f"RAJA cannot be compiled here), CPU {cpu_model()}"},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "primitives": {nm: round(table[nm] * args.steps / per_acc[nm] / 1e9, 3) for nm in per_acc},
+        "primitives": {nm: {"ms": round(1000 * per[nm], 2),
+                            "gbs": round(table[nm] / per[nm] / 1e9, 3)} for nm in suite.names},
     }
     print(json.dumps(line), flush=True)
 
@@ -328,10 +395,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--log2n", type=int, default=28)
-    ap.add_argument("--cpu-log2n", type=int, default=22)
+    ap.add_argument("--cpu-log2n", type=int, default=28)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-cub", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -415,8 +483,20 @@ def main():
     peaks = load_peaks()
     hbm_peak = peaks.get("hbm_gbs") or 6800.0
     peak_src = "measured" if peaks.get("hbm_gbs") else "fallback"
-    for v in per_prim.values():
+    for name, v in per_prim.items():
         v["frac_of_" + peak_src + "_hbm"] = round(v["gbs"] / hbm_peak, 3)
+        if name.startswith("sort"):
+            v["gkeys_per_s"] = round(n / v["ms"] / 1e6, 2)
+    # the library's own run of each primitive left its outputs in `outs`:
+    # CUB runs on the same inputs and its results are compared bit for bit
+    if not args.no_cub:
+        try:
+            for name, c in bench_cub(inputs, outs, n, stream, reps).items():
+                per_prim[name]["cub_ms"] = c["ms"]
+                per_prim[name]["vs_cub"] = round(c["ms"] / per_prim[name]["ms"], 3)
+                per_prim[name]["equal_to_cub"] = c["equal"]
+        except Exception as e:  # report, do not lose the headline line
+            per_prim["cub_error"] = f"{type(e).__name__}: {e}"
     roof = roofline(kernels, n, hbm_peak, peak_src)
 
     # ---- e2e through the public API with host buffers
@@ -448,12 +528,14 @@ def main():
             "config": config_block(args),
             "frac_of_hbm_peak": round(value / world / hbm_peak, 3),
             "hbm_peak_gbs": hbm_peak, "hbm_peak_source": peak_src,
-            "primitives": per_prim, "kernels": kernels,
             "roofline": roof, "e2e": e2e, "cpu_baseline": cpu,
             "gpu_launches": launches_per_step * args.steps if launches_per_step else None,
             "gpu_launches_per_step": launches_per_step,
             "clocks": clk,
-            "extras": extras,
+            "extras": extras, "kernels": kernels,
+            # last, so that a record that keeps only the tail of the line
+            # still carries every primitive's time, GB/s, fraction and CUB ratio
+            "primitives": per_prim,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -609,27 +691,36 @@ def bench_accuracy(lib, seed=3):
         v = out[0].item()
         res[f"dot_rel_err_{nm}"] = abs((v - dx) - dlo) / abs(dx)
     del x64, y64
-    # inclusive scan of the first 2^26 elements: max error over prefixes,
-    # relative to sum|x| so far
-    m = 1 << 26
-    xs = x[:m].contiguous()
-    ref = exact_prefix_f64(xs)
-    absp = torch.cumsum(xs.double().abs(), 0)
-    o = torch.empty_like(xs)
+    # inclusive scan of all 2^28 elements: max error over prefixes, relative
+    # to sum|x| so far.  An FP32 output cannot be closer to the exact prefix
+    # than its own rounding, so the floor for any FP32-output scan (the
+    # exact prefixes rounded to FP32) is reported beside the modes.
+    ref = exact_prefix_f64(x)
+    absp = torch.cumsum(x.double().abs(), 0)
+    o = torch.empty_like(x)
     for nm, mode in (("naive_f32", 0), ("comp_f32", 1)):
-        assert lib.b200_scan_inclusive_f32(xs.data_ptr(), o.data_ptr(), m, 0, mode, s) == 0
+        assert lib.b200_scan_inclusive_f32(x.data_ptr(), o.data_ptr(), n, 0, mode, s) == 0
         torch.cuda.synchronize()
         res[f"scan_maxerr_over_abs_{nm}"] = float(((o.double() - ref).abs() / absp).max())
-    o64 = torch.empty(m, dtype=torch.float64, device="cuda")
-    xs64 = xs.double()
-    assert lib.b200_scan_inclusive_f64(xs64.data_ptr(), o64.data_ptr(), m, 0, 0, s) == 0
+    del o
+    res["scan_maxerr_over_abs_f32_rounding_floor"] = float(
+        ((ref.float().double() - ref).abs() / absp).max())
+    o64 = torch.empty(n, dtype=torch.float64, device="cuda")
+    x64 = x.double()
+    assert lib.b200_scan_inclusive_f64(x64.data_ptr(), o64.data_ptr(), n, 0, 0, s) == 0
     torch.cuda.synchronize()
     res["scan_maxerr_over_abs_naive_f64"] = float(((o64 - ref).abs() / absp).max())
-    res["scan_n"] = m
+    del o64, x64, ref, absp
+    res["scan_n"] = n
     res["exact_reference"] = "int64 limb sums on the device (bench.py exact_sum / exact_prefix_f64)"
-    res["comp_f32_no_worse_than_naive_f64"] = bool(
+    # The FP32-compensated sum and dot return a double and can beat naive
+    # FP64; the FP32 scan returns FP32 prefixes, so it is held to the FP32
+    # rounding floor instead of to the FP64 scan.
+    res["comp_f32_sum_and_dot_no_worse_than_naive_f64"] = bool(
         res["sum_rel_err_comp_f32"] <= res["sum_rel_err_naive_f64"] * 1.0000001 + 1e-300
         and res["dot_rel_err_comp_f32"] <= res["dot_rel_err_naive_f64"] * 1.0000001 + 1e-300)
+    res["scan_comp_f32_err_over_f32_rounding_floor"] = round(
+        res["scan_maxerr_over_abs_comp_f32"] / max(res["scan_maxerr_over_abs_f32_rounding_floor"], 1e-300), 3)
     return res
 
 
@@ -845,6 +936,61 @@ def bench_jacobi(lib, sweeps=20, seed=5):
     return out
 
 
+def load_cub_arm():
+    """baseline/libcubarm.so (built here if missing): CUB's DeviceScan and
+    DeviceRadixSort, the calls RAJA's CUDA scan and sort make."""
+    import ctypes as C
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "build_cub_arm", os.path.join(ROOT, "baseline", "build_cub_arm.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    lib = C.CDLL(mod.build())
+    lib.cub_arm_error.restype = C.c_char_p
+    lib.cub_arm_setup.argtypes = [C.c_size_t]
+    for nm in ("cub_exclusive_scan_i64", "cub_sort_keys_u32", "cub_sort_keys_u64"):
+        getattr(lib, nm).argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.cub_sort_pairs_f32_i32.argtypes = [C.c_void_p] * 4 + [C.c_size_t, C.c_void_p]
+    return lib
+
+
+def bench_cub(inputs, outs, n, stream, reps):
+    """CUB on the same inputs as the library's scan and sorts, CUDA events
+    over `reps` calls after one warm-up; each result is compared with the
+    library's (already in `outs`).  Returns {primitive: {ms, equal}}."""
+    import torch
+    cub = load_cub_arm()
+    if cub.cub_arm_setup(n) != 0:
+        raise RuntimeError(cub.cub_arm_error().decode())
+    s = stream.cuda_stream
+    P = lambda x: x.data_ptr()  # noqa: E731
+    o = {k: torch.empty_like(outs[k]) for k in ("scan_out", "u32_out", "u64_out", "pk_out", "pv_out")}
+    calls = {
+        "exclusive_scan_i64": (lambda: cub.cub_exclusive_scan_i64(P(inputs["scan_in"]), P(o["scan_out"]), n, s),
+                               ["scan_out"]),
+        "sort_u32": (lambda: cub.cub_sort_keys_u32(P(inputs["u32"]), P(o["u32_out"]), n, s), ["u32_out"]),
+        "sort_u64": (lambda: cub.cub_sort_keys_u64(P(inputs["u64"]), P(o["u64_out"]), n, s), ["u64_out"]),
+        "sort_pairs_f32_i32": (lambda: cub.cub_sort_pairs_f32_i32(P(inputs["pk"]), P(o["pk_out"]), P(inputs["pv"]),
+                                                                  P(o["pv_out"]), n, s), ["pk_out", "pv_out"]),
+    }
+    res = {}
+    for name, (fn, keys) in calls.items():
+        if fn() != 0:
+            raise RuntimeError(cub.cub_arm_error().decode())
+        a, b = _events()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        eq = all(torch.equal(o[k].view(torch.uint8), outs[k].view(torch.uint8)) for k in keys)
+        res[name] = {"ms": round(a.elapsed_time(b) / reps, 4), "equal": bool(eq)}
+    cub.cub_arm_teardown()
+    del o
+    torch.cuda.empty_cache()
+    return res
+
+
 def load_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -1001,22 +1147,22 @@ def run_e2e(args, lib, inputs, outs, n, stream, table, dist):
 
 
 def run_cpu_baseline(args):
+    """One pass over every primitive at N=2^cpu_log2n (the same N as the
+    device step by default) on all host cores, after one untimed pass."""
     import oracle
     oracle.build()
     n = 1 << args.cpu_log2n
-    cpu_suite(n)                      # warm-up (page faults, thread pool)
-    b, s, cores, _ = cpu_suite(n, seed=1)
-    reps = max(1, int(10.0 / max(s, 1e-3)))
-    reps = min(reps, 8)
-    tb, ts = 0, 0.0
-    for r in range(reps):
-        b, s, cores, _ = cpu_suite(n, seed=2 + r)
-        tb += b
-        ts += s
-    return {"value": round(tb / ts / 1e9, 3), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{reps} passes of every primitive at N=2^{args.cpu_log2n} "
-                      f"(oracle OpenMP restatement of omp_parallel_for_exec), CPU {cpu_model()}",
-            "seconds": round(ts, 2)}
+    suite = CpuSuite(n, seed=1)
+    t_gen = time.perf_counter()
+    per, _ = cpu_suite_rotation(suite, len(suite.names), len(suite.names))
+    ts = sum(per.values())
+    value = sum(suite.table.values()) / ts / 1e9
+    return {"value": round(value, 3), "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
+            "sample": f"one timed pass of every primitive at N=2^{args.cpu_log2n} after one "
+                      f"untimed pass (oracle OpenMP restatement of omp_parallel_for_exec), "
+                      f"CPU {cpu_model()}",
+            "seconds": round(ts, 2), "wall_s_with_setup": round(time.perf_counter() - t_gen, 1),
+            "primitives_gbs": {nm: round(suite.table[nm] / per[nm] / 1e9, 3) for nm in suite.names}}
 
 
 if __name__ == "__main__":

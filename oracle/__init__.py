@@ -182,6 +182,24 @@ def sort(keys: np.ndarray, descending: bool = False, parallel: bool = False,
     return k
 
 
+def sort_inplace(k: np.ndarray, descending: bool = False, parallel: bool = False,
+                 stable: bool = True) -> np.ndarray:
+    """Sort a contiguous array in place (RAJA's sorts are in place)."""
+    assert k.flags.c_contiguous
+    _fn(f"orc_sort_{_SFX[k.dtype]}", None, [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int])(
+        _p(k), k.size, int(descending), int(parallel), int(stable))
+    return k
+
+
+def sort_pairs_inplace(k: np.ndarray, v: np.ndarray, descending: bool = False,
+                       parallel: bool = False, stable: bool = True):
+    assert k.flags.c_contiguous and v.flags.c_contiguous and k.size == v.size
+    name = f"orc_sort_pairs_{_SFX[k.dtype]}_{_SFX[v.dtype]}"
+    _fn(name, None, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int])(
+        _p(k), _p(v), k.size, int(descending), int(parallel), int(stable))
+    return k, v
+
+
 def sort_pairs(keys: np.ndarray, vals: np.ndarray, descending: bool = False,
                parallel: bool = False, stable: bool = True):
     k = np.array(keys, copy=True)

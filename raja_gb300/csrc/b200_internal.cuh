@@ -319,6 +319,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+// Drain wait after a bounded wait gave up: a bulk copy from valid global
+// memory always completes, so this waits for it to land before the block
+// reuses or releases its shared memory.  Its bound is fixed and large,
+// independent of b200_set_spin_limit, so lowering that limit cannot let a
+// block exit with a copy still writing into shared memory.
+constexpr uint32_t kDrainPolls = 1u << 28;
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kDrainPolls; ++i)
+    if (mbar_try_wait(bar, parity)) return;
+}
 
 // Error-free transformations (Knuth TwoSum, FMA-based TwoProd).
 template <class F>

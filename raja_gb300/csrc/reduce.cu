@@ -708,6 +708,8 @@ B200_BIT(bitand_u64, uint64_t, false)
 // completion ticket) taken from the file-scope device array below instead
 // of the per-stream arena.  The caller still passes the input and the
 // output.  It calls no cudaMalloc, cudaFree or other allocating routine.
+// It runs the same kernel, grid and chunk mapping as b200_reduce_sum_f64,
+// so the two return identical bits for the same input and mode.
 //
 // Limits: the array holds kNoAllocParts partials of up to 16 bytes.  The
 // naive and compensated modes use one partial per block and fit on any
@@ -754,6 +756,8 @@ int run_reduce_noalloc(const char* name, const double* x, size_t n, bool det, do
                        b200_stream_t stream) {
   if (!out) return fail(B200_ERR_ARG, "%s: null output pointer", name);
   if (n > 0 && !x) return fail(B200_ERR_ARG, "%s: null input pointer", name);
+  if (n >= (size_t(1) << 40)) return fail(B200_ERR_ARG, "%s: n=%zu too large", name, n);
+  static_assert(sizeof(typename Op::Part) <= 16, "partials fit the 16-byte slots");
   const size_t chunk = Chunk<double>::SIZE;
   const size_t nchunks = (n + chunk - 1) / chunk;
   if (det && nchunks > kNoAllocParts)
@@ -785,5 +789,7 @@ extern "C" int b200_reduce_sum_f64_noalloc(const double* x, size_t n, int mode, 
     return fail(B200_ERR_ARG, "%s: unknown mode %d", name, mode);
   const bool det = (mode & B200_MODE_DETERMINISTIC) != 0;
   if (mode & B200_MODE_COMPENSATED) return run_reduce_noalloc<SumCompF64>(name, x, n, det, out, stream);
-  return run_reduce_noalloc<SumNaive<double>>(name, x, n, det, out, stream);
+  // the same Op as b200_reduce_sum_f64 (exponent-aligned int64 chunk sums),
+  // so both entry points give the same bits for the same input and mode
+  return run_reduce_noalloc<SumF64Aligned<F64_DADD>>(name, x, n, det, out, stream);
 }

@@ -294,7 +294,7 @@ scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op
   if (tma_ok && full) {
     if (!mbar_wait(&sm.bar, 0, spin_limit)) {
       if (tid == 0) atomicOr_system(status, kStatusTmaTimeout);
-      mbar_wait(&sm.bar, 0, spin_limit);  // let the copy land before the block exits
+      mbar_drain(&sm.bar, 0);  // let the copy land before the block goes on
     }
   } else {
     for (int e = tid; e < TS; e += SBLOCK) st[e] = (base + e < n) ? in[base + e] : T(0);

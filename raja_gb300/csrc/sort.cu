@@ -284,7 +284,7 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   if (tma_ok && lim == TILE) {
     if (!mbar_wait(&sm.bar, 0, spin_limit)) {
       if (tid == 0) atomicOr_system(err, kStatusTmaTimeout);
-      mbar_wait(&sm.bar, 0, spin_limit);  // let the copy land before the block exits
+      mbar_drain(&sm.bar, 0);  // let the copy land before the block goes on
     }
   } else {
     // partial (last) tile: padding keys sort after every real key

@@ -176,12 +176,12 @@ def test_sort_2m_skewed_keys(prims, orc, case):
         np.testing.assert_array_equal(to_host(d), orc.sort(x, descending=desc), err_msg=case)
 
 
-# 2^26 and 2^27 keys (2^28 is covered by the full-size tests): uniform
+# 2^26, 2^27 and 2^28 keys (2^28 is the bandwidth-sweep size): uniform
 # keys, keys with few distinct top bits, and stable f32/i32 pairs with many
 # equal keys, +-0.0 and infinities, ascending and descending, in place and
 # out of place.  The reference is a stable torch sort of an
-# order-preserving int64 key.
-NL = [(1 << 26) + 777, (1 << 27) + 5]
+# order-preserving int64 key, so every key and value is compared exactly.
+NL = [(1 << 26) + 777, (1 << 27) + 5, 1 << 28]
 
 
 def _ord64(t):

@@ -8,14 +8,10 @@ calls that reuse its static scratch.  This file is collected last so that a
 run stopping at the first failure has already run every other test; it also
 passes on its own in a fresh process.
 """
-import ctypes as C
-
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
-
-U64 = 2.0 ** -53
 
 
 def _sum(lib, name, x, mode, out):
@@ -26,22 +22,25 @@ def _sum(lib, name, x, mode, out):
 
 
 def test_noalloc_sum_matches_arena_sum_twice_in_a_row(prims):
+    """Both entry points run the same kernel, grid and chunk mapping, so the
+    sums must agree bit for bit in every mode, on aligned inputs (16-byte
+    vector loads) and on a view one element in (scalar loads)."""
     import torch
     from raja_gb300 import _lib
     lib = _lib.load()
     rng = np.random.default_rng(42)
     for n in (0, 1, 4097, (1 << 20) + 3, 1 << 24):
-        x = torch.from_numpy(rng.uniform(-1, 1, n)).cuda()
-        a = float(x.abs().sum().item()) if n else 0.0
-        for mode in (0, 1, 2, 3):
-            ref = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
-            _sum(lib, "b200_reduce_sum_f64", x, mode, ref)
-            for _ in range(2):  # two calls in a row share the static scratch
-                got = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
-                _sum(lib, "b200_reduce_sum_f64_noalloc", x, mode, got)
-                torch.cuda.synchronize()
-                bound = max(n - 1, 1) * U64 * a
-                assert abs(got.item() - ref.item()) <= bound, (n, mode)
+        base = torch.from_numpy(rng.uniform(-1, 1, n + 1)).cuda()
+        for x in (base[:n], base[1:]):
+            for mode in (0, 1, 2, 3):
+                ref = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+                _sum(lib, "b200_reduce_sum_f64", x, mode, ref)
+                for _ in range(2):  # two calls in a row share the static scratch
+                    got = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+                    _sum(lib, "b200_reduce_sum_f64_noalloc", x, mode, got)
+                    torch.cuda.synchronize()
+                    g, r = got.cpu().view(torch.int64).item(), ref.cpu().view(torch.int64).item()
+                    assert g == r, (n, mode, x.data_ptr() % 16, got.item(), ref.item())
     prims.synchronize()
 
 
