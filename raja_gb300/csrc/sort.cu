@@ -212,6 +212,52 @@ __global__ void __launch_bounds__(RADIX) bins_kernel(const uint32_t* __restrict_
   }
 }
 
+// Decoupled look-back for digit d of tile `tile`: the global start of the
+// tile's run of digit d.  LBW predecessors per poll: the loads of one window
+// are independent, then consumed in order until an inclusive count is
+// found.  A not-yet-published tile stops the consumption; the wait is
+// bounded (the status word records a give-up).  Publishes the tile's
+// inclusive count (start + cnt) before returning.
+template <class ST>
+__device__ __forceinline__ ST digit_lookback(const ST* __restrict__ status,
+                                             const uint32_t* __restrict__ bins, size_t tile, int d,
+                                             uint32_t cnt, ST* my_status, uint32_t* err,
+                                             uint32_t spin_limit) {
+  using S = Status<ST>;
+  if (tile == 0) return ST(bins[d]);
+  constexpr int LBW = 8;
+  ST acc = 0;
+  long long t = (long long)tile - 1;
+  uint32_t spins = 0;
+  bool done = false;
+  while (!done) {
+    ST w[LBW];
+#pragma unroll
+    for (int j = 0; j < LBW; ++j)
+      w[j] = (t - j >= 0) ? ld_relaxed(status + size_t(t - j) * RADIX + d) : ST(S::INCL);
+    int used = LBW;
+#pragma unroll
+    for (int j = 0; j < LBW; ++j) {
+      if (j >= used) break;
+      const ST flag = w[j] & ~S::MASK;
+      if (flag == 0) { used = j; break; }
+      acc += w[j] & S::MASK;
+      if (flag == S::INCL) { done = true; break; }
+    }
+    if (done) break;
+    t -= used;
+    if (used < LBW) {
+      if (++spins > spin_limit) {
+        atomicOr_system(err, kStatusSortTimeout);
+        break;
+      }
+      __nanosleep(100);
+    }
+  }
+  st_relaxed(my_status, ST(S::INCL | (acc + cnt)));
+  return acc;
+}
+
 // ------------------------------------------------------------- onesweep
 // One tile per block.  Tiles take their id from an atomic counter in launch
 // order, so every predecessor of a tile has started and publishes its
@@ -383,47 +429,9 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
     sm.idx[p] = uint16_t(e);
   }
 
-  // ---- decoupled look-back for digit d, LBW predecessors per poll: the
-  // loads of one window are independent, then consumed in order until an
-  // inclusive count is found.  A not-yet-published tile stops the
-  // consumption; the wait is bounded.
+  // ---- decoupled look-back for digit d (global start of this tile's run)
   ST gstart = 0;
-  if (!downer) {
-  } else if (tile == 0) {
-    gstart = ST(bins[d]);
-  } else {
-    constexpr int LBW = 8;
-    ST acc = 0;
-    long long t = (long long)tile - 1;
-    uint32_t spins = 0;
-    bool done = false;
-    while (!done) {
-      ST w[LBW];
-#pragma unroll
-      for (int j = 0; j < LBW; ++j)
-        w[j] = (t - j >= 0) ? ld_relaxed(status + size_t(t - j) * RADIX + d) : ST(S::INCL);
-      int used = LBW;
-#pragma unroll
-      for (int j = 0; j < LBW; ++j) {
-        if (j >= used) break;
-        const ST flag = w[j] & ~S::MASK;
-        if (flag == 0) { used = j; break; }
-        acc += w[j] & S::MASK;
-        if (flag == S::INCL) { done = true; break; }
-      }
-      if (done) break;
-      t -= used;
-      if (used < LBW) {
-        if (++spins > spin_limit) {
-          atomicOr_system(err, kStatusSortTimeout);
-          break;
-        }
-        __nanosleep(100);
-      }
-    }
-    gstart = acc;
-    st_relaxed(my_status, ST(S::INCL | (acc + cnt)));
-  }
+  if (downer) gstart = digit_lookback<ST>(status, bins, tile, d, cnt, my_status, err, spin_limit);
   if (downer) sm.gdst[d] = gstart - ST(lstart);
   __syncthreads();
 
