@@ -685,6 +685,11 @@ struct ValOp<ValLoc<T, I>, Op> {
   RAJA_HOST_DEVICE I getLoc() const { return val.loc; }
 };
 
+// ValLocOp<T, I, Op>: the lambda argument type of a ReduceLoc param
+// (pattern/params/params_base.hpp:253)
+template <typename T, typename I, template <typename, typename, typename> class Op>
+using ValLocOp = ValOp<ValLoc<T, I>, Op>;
+
 // A kernel name param (pattern/params/kernel_name.hpp:11-22: RAJA::Name
 // returns one); expt::Name is kept as a second spelling.
 struct KernelName {
@@ -2464,6 +2469,11 @@ RAJA_COMPAT_RES_T(Pol) stable_sort_pairs(Span<K> k, Span<V> v, C c = C{}) {
 // ------------------------------------------------------------- WorkGroup
 // pattern/WorkGroup.hpp:117-530.  Host runners execute the loops in
 // enqueue order (ordered) like the reference's WorkRunnerForallOrdered.
+// WorkGroup execution policies (policy/sequential/policy.hpp:86,
+// policy/openmp/policy.hpp:295): the host runners execute the loops with
+// the matching forall policy
+using seq_work = seq_exec;
+using omp_work = omp_parallel_for_exec;
 struct ordered {};
 struct reverse_ordered {};
 struct unordered {};

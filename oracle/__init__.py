@@ -1,7 +1,9 @@
 """ORACLE -- test infrastructure only (see oracle/oracle.cpp).
 
 numpy-facing ctypes wrappers over liboracle.so, the CPU restatement of
-RAJA's seq_exec / omp_parallel_for_exec semantics for the primitive path.
+RAJA's seq_exec / omp_parallel_for_exec semantics for the primitive path,
+pinned bit for bit against outputs of RAJA's own host policies
+(tests/golden/ref_fixtures.npz, tests/test_ref_fixtures.py).
 Only tests/, __graft_entry__.smoke() and the CPU-baseline legs of bench.py
 use it, always as the checker or the timed CPU reference, never as the
 product.

@@ -7,11 +7,16 @@
 // and the CPU-baseline legs of bench.py load it; nothing in the product
 // links or calls it.
 //
-// RAJA itself cannot be compiled here: every header needs camp (an empty
-// git submodule in the reference tree) and a CMake-generated config.hpp, so
-// the restatement is pinned instead against the known answers of RAJA's own
-// test suite (tests/test_oracle_pins.py) and against independent numpy /
-// math.fsum computations.
+// Pinned against RAJA itself: oracle/refbuild/ compiles RAJA's own host
+// policies from the unmodified reference headers (with a hand-written
+// config.hpp and a clean-room subset of the camp library, whose submodule
+// is empty in the reference tree), and tests/golden/make_ref_fixtures.py
+// records their outputs.  tests/test_ref_fixtures.py requires this file to
+// reproduce them bit for bit: reducers (MinLoc/MaxLoc ties included), every
+// scan kind and op under seq and OpenMP (four threads), stable sorts under
+// both policies, histograms and the daxpy body; unstable sorts follow
+// RAJA's own rule (same keys, same values per key).  The known answers of
+// RAJA's test suite (tests/test_oracle_pins.py) are checked as well.
 //
 // Build: oracle/build_oracle.py (g++ -O2 -fopenmp -ffp-contract=off).
 // -ffp-contract=off keeps a*b+c as two rounded operations, as written in
@@ -556,6 +561,7 @@ ORC_PAIRS(u32_u32, uint32_t, uint32_t)
 ORC_PAIRS(i32_i32, int32_t, int32_t)
 ORC_PAIRS(f32_i32, float, int32_t)
 ORC_PAIRS(u64_i32, uint64_t, int32_t)
+ORC_PAIRS(i64_i32, int64_t, int32_t)
 ORC_PAIRS(u64_i64, uint64_t, int64_t)
 ORC_PAIRS(i64_i64, int64_t, int64_t)
 ORC_PAIRS(f64_i64, double, int64_t)
