@@ -42,18 +42,59 @@
 
 #include "../b200prims.h"
 
+#if !defined(RAJA_COMPAT_FRONTEND)
+// An installed RAJA.  RAJA's scan and sort front-ends call impl::scan:: and
+// impl::sort:: by qualified name, which finds only the overloads declared
+// before those front-ends, so this header comes before RAJA/RAJA.hpp: it
+// includes the parts of RAJA its declarations need, declares the b200
+// overloads, and then includes RAJA/RAJA.hpp itself (RAJA's own back-ends
+// sit at the same place inside RAJA/RAJA.hpp).
+#if defined(RAJA_scan_HPP) || defined(RAJA_sort_HPP)
+#error "include raja_b200/RAJA_b200.hpp before RAJA/RAJA.hpp (it adds impl::scan / impl::sort overloads)"
+#endif
+#include "RAJA/config.hpp"
+#include "RAJA/policy/PolicyBase.hpp"
+#include "RAJA/util/Operators.hpp"
+#include "RAJA/util/resource.hpp"
+#include "RAJA/pattern/reduce.hpp"
+#include "RAJA/pattern/multi_reduce.hpp"
+#include "RAJA/pattern/atomic.hpp"
+#endif
+
 #if defined(RAJA_ENABLE_NVTX)
 #include <nvtx3/nvToolsExt.h>
+#endif
+
+// Host-and-device functions of this header.  RAJA's own RAJA_HOST_DEVICE
+// is empty in an installed RAJA configured without its CUDA back-end, which
+// the b200 policies do not need.
+#if defined(__CUDACC__)
+#define B200_HOST_DEVICE __host__ __device__
+#else
+#define B200_HOST_DEVICE
 #endif
 
 namespace RAJA {
 
 // ------------------------------------------------------------ policies
+// On an installed RAJA the exec policy carries RAJA's policy traits (a
+// CUDA-platform forall policy, as the reference's cuda_exec does), so that
+// RAJA's front-ends accept it; raja_compat needs none.
+#if defined(RAJA_COMPAT_FRONTEND)
 template <int BLOCK = 256, bool Async = false>
 struct b200_exec {
   static constexpr int block_size = BLOCK;
   static constexpr bool async = Async;
 };
+#else
+template <int BLOCK = 256, bool Async = false>
+struct b200_exec : make_policy_pattern_launch_platform_t<Policy::cuda, Pattern::forall,
+                                                         (Async ? Launch::async : Launch::sync),
+                                                         Platform::cuda> {
+  static constexpr int block_size = BLOCK;
+  static constexpr bool async = Async;
+};
+#endif
 template <int BLOCK = 256>
 using b200_exec_async = b200_exec<BLOCK, true>;
 struct b200_reduce {};
@@ -353,47 +394,47 @@ struct VLoc {
 template <class T>
 struct SumK {
   using V = T;
-  RAJA_HOST_DEVICE static V ident() { return T(0); }
-  RAJA_HOST_DEVICE static V merge(V a, V b) { return a + b; }
+  B200_HOST_DEVICE static V ident() { return T(0); }
+  B200_HOST_DEVICE static V merge(V a, V b) { return a + b; }
   static V fold_init(V a, V b) { return a + b; }
 };
 template <class T>
 struct MinK {
   using V = T;
-  RAJA_HOST_DEVICE static V ident() { return operators::limits<T>::max(); }
-  RAJA_HOST_DEVICE static V merge(V a, V b) { return (b < a) ? b : a; }
+  B200_HOST_DEVICE static V ident() { return operators::limits<T>::max(); }
+  B200_HOST_DEVICE static V merge(V a, V b) { return (b < a) ? b : a; }
   static V fold_init(V a, V b) { return (b < a) ? b : a; }
 };
 template <class T>
 struct MaxK {
   using V = T;
-  RAJA_HOST_DEVICE static V ident() { return operators::limits<T>::min(); }
-  RAJA_HOST_DEVICE static V merge(V a, V b) { return (a < b) ? b : a; }
+  B200_HOST_DEVICE static V ident() { return operators::limits<T>::min(); }
+  B200_HOST_DEVICE static V merge(V a, V b) { return (a < b) ? b : a; }
   static V fold_init(V a, V b) { return (a < b) ? b : a; }
 };
 template <class T>
 struct OrK {
   using V = T;
-  RAJA_HOST_DEVICE static V ident() { return T(0); }
-  RAJA_HOST_DEVICE static V merge(V a, V b) { return a | b; }
+  B200_HOST_DEVICE static V ident() { return T(0); }
+  B200_HOST_DEVICE static V merge(V a, V b) { return a | b; }
   static V fold_init(V a, V b) { return a | b; }
 };
 template <class T>
 struct AndK {
   using V = T;
-  RAJA_HOST_DEVICE static V ident() { return T(~T(0)); }
-  RAJA_HOST_DEVICE static V merge(V a, V b) { return a & b; }
+  B200_HOST_DEVICE static V ident() { return T(~T(0)); }
+  B200_HOST_DEVICE static V merge(V a, V b) { return a & b; }
   static V fold_init(V a, V b) { return a & b; }
 };
 template <class T, class I, bool MIN>
 struct LocK {
   using V = VLoc<T, I>;
-  RAJA_HOST_DEVICE static V ident() {
+  B200_HOST_DEVICE static V ident() {
     return V{MIN ? operators::limits<T>::max() : operators::limits<T>::min(), I(-1)};
   }
   // device merges: strictly better value wins, equal values keep the
   // lowest location -- the order a sequential loop would have produced
-  RAJA_HOST_DEVICE static V merge(V a, V b) {
+  B200_HOST_DEVICE static V merge(V a, V b) {
     const bool better = MIN ? (b.val < a.val) : (a.val < b.val);
     if (better || (b.val == a.val && b.loc < a.loc && !(a.loc == I(-1)))) return b;
     return a;
@@ -437,7 +478,7 @@ class DevReducer {
  public:
   explicit DevReducer(V init) : shared_(new Shared{init, {}}), original_(true), val_(K::ident()) {}
 
-  RAJA_HOST_DEVICE DevReducer(const DevReducer& o) : val_(K::ident()) {
+  B200_HOST_DEVICE DevReducer(const DevReducer& o) : val_(K::ident()) {
 #if defined(__CUDA_ARCH__)
     // per-thread copy of the launch copy: owns the combine
     slot_ = o.slot_;
@@ -462,7 +503,7 @@ class DevReducer {
   }
   DevReducer& operator=(const DevReducer&) = delete;
 
-  RAJA_HOST_DEVICE ~DevReducer() {
+  B200_HOST_DEVICE ~DevReducer() {
 #if defined(__CUDA_ARCH__)
     if (owner_) grid_combine(slot_, val_, [](V a, V b) { return K::merge(a, b); });
 #else
@@ -476,7 +517,7 @@ class DevReducer {
 #endif
   }
 
-  RAJA_HOST_DEVICE void combine(const V& v) const { val_ = K::merge(val_, v); }
+  B200_HOST_DEVICE void combine(const V& v) const { val_ = K::merge(val_, v); }
 
   // Fold the pending launch results into init, in launch order.
   // One synchronisation per stream with pending launches (other streams are
@@ -514,8 +555,8 @@ class ReduceSum<b200_reduce, T> : public b200::detail::DevReducer<b200::detail::
 
  public:
   explicit ReduceSum(T init = T(0)) : B(init) {}
-  RAJA_HOST_DEVICE ReduceSum(const ReduceSum& o) : B(o) {}
-  RAJA_HOST_DEVICE const ReduceSum& operator+=(T v) const { this->val_ += v; return *this; }
+  B200_HOST_DEVICE ReduceSum(const ReduceSum& o) : B(o) {}
+  B200_HOST_DEVICE const ReduceSum& operator+=(T v) const { this->val_ += v; return *this; }
   T get() const { return this->fold(); }
   operator T() const { return get(); }
   void reset(T v) { this->reset_value(v); }
@@ -526,8 +567,8 @@ class ReduceMin<b200_reduce, T> : public b200::detail::DevReducer<b200::detail::
 
  public:
   explicit ReduceMin(T init = operators::limits<T>::max()) : B(init) {}
-  RAJA_HOST_DEVICE ReduceMin(const ReduceMin& o) : B(o) {}
-  RAJA_HOST_DEVICE const ReduceMin& min(T v) const { this->combine(v); return *this; }
+  B200_HOST_DEVICE ReduceMin(const ReduceMin& o) : B(o) {}
+  B200_HOST_DEVICE const ReduceMin& min(T v) const { this->combine(v); return *this; }
   T get() const { return this->fold(); }
   operator T() const { return get(); }
   void reset(T v) { this->reset_value(v); }
@@ -538,8 +579,8 @@ class ReduceMax<b200_reduce, T> : public b200::detail::DevReducer<b200::detail::
 
  public:
   explicit ReduceMax(T init = operators::limits<T>::min()) : B(init) {}
-  RAJA_HOST_DEVICE ReduceMax(const ReduceMax& o) : B(o) {}
-  RAJA_HOST_DEVICE const ReduceMax& max(T v) const { this->combine(v); return *this; }
+  B200_HOST_DEVICE ReduceMax(const ReduceMax& o) : B(o) {}
+  B200_HOST_DEVICE const ReduceMax& max(T v) const { this->combine(v); return *this; }
   T get() const { return this->fold(); }
   operator T() const { return get(); }
   void reset(T v) { this->reset_value(v); }
@@ -550,8 +591,8 @@ class ReduceBitOr<b200_reduce, T> : public b200::detail::DevReducer<b200::detail
 
  public:
   explicit ReduceBitOr(T init = T(0)) : B(init) {}
-  RAJA_HOST_DEVICE ReduceBitOr(const ReduceBitOr& o) : B(o) {}
-  RAJA_HOST_DEVICE const ReduceBitOr& operator|=(T v) const { this->val_ |= v; return *this; }
+  B200_HOST_DEVICE ReduceBitOr(const ReduceBitOr& o) : B(o) {}
+  B200_HOST_DEVICE const ReduceBitOr& operator|=(T v) const { this->val_ |= v; return *this; }
   T get() const { return this->fold(); }
   operator T() const { return get(); }
   void reset(T v) { this->reset_value(v); }
@@ -562,8 +603,8 @@ class ReduceBitAnd<b200_reduce, T> : public b200::detail::DevReducer<b200::detai
 
  public:
   explicit ReduceBitAnd(T init = T(~T(0))) : B(init) {}
-  RAJA_HOST_DEVICE ReduceBitAnd(const ReduceBitAnd& o) : B(o) {}
-  RAJA_HOST_DEVICE const ReduceBitAnd& operator&=(T v) const { this->val_ &= v; return *this; }
+  B200_HOST_DEVICE ReduceBitAnd(const ReduceBitAnd& o) : B(o) {}
+  B200_HOST_DEVICE const ReduceBitAnd& operator&=(T v) const { this->val_ &= v; return *this; }
   T get() const { return this->fold(); }
   operator T() const { return get(); }
   void reset(T v) { this->reset_value(v); }
@@ -578,8 +619,8 @@ class ReduceMinLoc<b200_reduce, T, I>
 
  public:
   ReduceMinLoc(T init, I idx) : B(typename K::V{init, idx}) {}
-  RAJA_HOST_DEVICE ReduceMinLoc(const ReduceMinLoc& o) : B(o) {}
-  RAJA_HOST_DEVICE const ReduceMinLoc& minloc(T v, I l) const {
+  B200_HOST_DEVICE ReduceMinLoc(const ReduceMinLoc& o) : B(o) {}
+  B200_HOST_DEVICE const ReduceMinLoc& minloc(T v, I l) const {
     if (v < this->val_.val || (v == this->val_.val && l < this->val_.loc)) this->val_ = {v, l};
     return *this;
   }
@@ -596,8 +637,8 @@ class ReduceMaxLoc<b200_reduce, T, I>
 
  public:
   ReduceMaxLoc(T init, I idx) : B(typename K::V{init, idx}) {}
-  RAJA_HOST_DEVICE ReduceMaxLoc(const ReduceMaxLoc& o) : B(o) {}
-  RAJA_HOST_DEVICE const ReduceMaxLoc& maxloc(T v, I l) const {
+  B200_HOST_DEVICE ReduceMaxLoc(const ReduceMaxLoc& o) : B(o) {}
+  B200_HOST_DEVICE const ReduceMaxLoc& maxloc(T v, I l) const {
     if (this->val_.val < v || (v == this->val_.val && l < this->val_.loc)) this->val_ = {v, l};
     return *this;
   }
@@ -649,6 +690,27 @@ forall_indexset_kernel(Body body_in, const T* begins, const long long* prefix, i
     }
     body(T(begins[lo] + T(k - prefix[lo])));
   }
+}
+
+// Minimal tuple usable in device code.
+template <class... Ts>
+struct DTuple;
+template <>
+struct DTuple<> {};
+template <class T, class... Ts>
+struct DTuple<T, Ts...> {
+  T head;
+  DTuple<Ts...> tail;
+};
+template <size_t I, class T, class... Ts>
+B200_HOST_DEVICE auto& dget(DTuple<T, Ts...>& t) {
+  if constexpr (I == 0) return t.head;
+  else return dget<I - 1>(t.tail);
+}
+template <size_t I, class T, class... Ts>
+B200_HOST_DEVICE const auto& dget(const DTuple<T, Ts...>& t) {
+  if constexpr (I == 0) return t.head;
+  else return dget<I - 1>(t.tail);
 }
 
 // Make the launch copy of the body with the context active, so captured
@@ -719,6 +781,7 @@ b200::NameScope kernel_name_scope(const b200_exec<BLOCK, Async>&, const char* n)
   return b200::NameScope(n);
 }
 
+#if defined(RAJA_COMPAT_FRONTEND)
 // ------------------------------------------------------------ resources
 // resources::Cuda for the b200 policies: a CUDA stream on one device, with
 // the interface of camp's Cuda resource as RAJA uses it (allocate /
@@ -979,7 +1042,7 @@ struct ParamKind<expt::detail::Reducer<Op<T, T, T>, T, VOp>> {
               typename std::conditional<std::is_same<Op<T, T, T>, operators::bit_or<T, T, T>>::value,
                                         OrK<T>, AndK<T>>::type>::type>::type>::type;
   static T to_target(typename type::V v) { return v; }
-  static RAJA_HOST_DEVICE typename type::V from_valop(const VOp& v) { return v.val; }
+  static B200_HOST_DEVICE typename type::V from_valop(const VOp& v) { return v.val; }
 };
 template <class T, class I, class Op, class VOp>
 struct ParamKind<expt::detail::ReducerLoc<T, I, Op, VOp>> {
@@ -987,29 +1050,8 @@ struct ParamKind<expt::detail::ReducerLoc<T, I, Op, VOp>> {
       std::is_same<Op, operators::minimum<expt::ValLoc<T, I>, expt::ValLoc<T, I>, expt::ValLoc<T, I>>>::value;
   using type = LocK<T, I, is_min>;
   static expt::ValLoc<T, I> to_target(typename type::V v) { return expt::ValLoc<T, I>(v.val, v.loc); }
-  static RAJA_HOST_DEVICE typename type::V from_valop(const VOp& v) { return {v.val.val, v.val.loc}; }
+  static B200_HOST_DEVICE typename type::V from_valop(const VOp& v) { return {v.val.val, v.val.loc}; }
 };
-
-// Minimal tuple usable in device code.
-template <class... Ts>
-struct DTuple;
-template <>
-struct DTuple<> {};
-template <class T, class... Ts>
-struct DTuple<T, Ts...> {
-  T head;
-  DTuple<Ts...> tail;
-};
-template <size_t I, class T, class... Ts>
-RAJA_HOST_DEVICE auto& dget(DTuple<T, Ts...>& t) {
-  if constexpr (I == 0) return t.head;
-  else return dget<I - 1>(t.tail);
-}
-template <size_t I, class T, class... Ts>
-RAJA_HOST_DEVICE const auto& dget(const DTuple<T, Ts...>& t) {
-  if constexpr (I == 0) return t.head;
-  else return dget<I - 1>(t.tail);
-}
 
 template <class R, class VOp>
 __device__ inline void combine_param(const DevSlot<typename ParamKind<R>::type::V>& slot, const VOp& v) {
@@ -1165,7 +1207,7 @@ using b200_global_thread_z = b200_global_z_direct;
 template <int KIND, int D, bool LOOP, typename SEGMENT>
 struct LoopExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
   template <typename BODY>
-  RAJA_HOST_DEVICE static void exec(const LaunchContext& ctx, const SEGMENT& seg, const BODY& body) {
+  B200_HOST_DEVICE static void exec(const LaunchContext& ctx, const SEGMENT& seg, const BODY& body) {
 #if defined(__CUDA_ARCH__)
     (void)ctx;
     const b200::launch::Pos p = b200::launch::pos<KIND, D>();
@@ -1183,7 +1225,7 @@ struct LoopExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
 template <int KIND, int D, bool LOOP, typename SEGMENT>
 struct LoopICountExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
   template <typename BODY>
-  RAJA_HOST_DEVICE static void exec(const LaunchContext& ctx, const SEGMENT& seg, const BODY& body) {
+  B200_HOST_DEVICE static void exec(const LaunchContext& ctx, const SEGMENT& seg, const BODY& body) {
 #if defined(__CUDA_ARCH__)
     (void)ctx;
     using I = std::decay_t<decltype(detail::seg_at(seg, 0))>;
@@ -1202,7 +1244,7 @@ struct LoopICountExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
 template <int KIND, int D, bool LOOP, typename SEGMENT>
 struct TileExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
   template <typename TILE_T, typename BODY>
-  RAJA_HOST_DEVICE static void exec(const LaunchContext& ctx, TILE_T ts, const SEGMENT& seg, const BODY& body) {
+  B200_HOST_DEVICE static void exec(const LaunchContext& ctx, TILE_T ts, const SEGMENT& seg, const BODY& body) {
 #if defined(__CUDA_ARCH__)
     (void)ctx;
     const b200::launch::Pos p = b200::launch::pos<KIND, D>();
@@ -1220,7 +1262,7 @@ struct TileExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
 template <int KIND, int D, bool LOOP, typename SEGMENT>
 struct TileTCountExecute<b200_loop_pol<KIND, D, LOOP>, SEGMENT> {
   template <typename TILE_T, typename BODY>
-  RAJA_HOST_DEVICE static void exec(const LaunchContext& ctx, TILE_T ts, const SEGMENT& seg, const BODY& body) {
+  B200_HOST_DEVICE static void exec(const LaunchContext& ctx, TILE_T ts, const SEGMENT& seg, const BODY& body) {
 #if defined(__CUDA_ARCH__)
     (void)ctx;
     using I = std::decay_t<decltype(detail::seg_at(seg, 0))>;
@@ -1346,6 +1388,8 @@ struct get_resource<b200_launch_t<Async, NT>> {
 };
 }  // namespace resources
 
+#endif  // RAJA_COMPAT_FRONTEND
+
 // ----------------------------------------------------------------- scans
 namespace b200 {
 namespace detail {
@@ -1375,6 +1419,24 @@ B200_SCAN_BIND(i64, int64_t)
 B200_SCAN_BIND(u32, uint32_t)
 B200_SCAN_BIND(u64, uint64_t)
 #undef B200_SCAN_BIND
+// long long / unsigned long long: the 64-bit entry points (a distinct type
+// from int64_t / uint64_t on LP64 hosts)
+#define B200_SCAN_BIND_LL(SUF, T, C)                                                         \
+  template <>                                                                                \
+  inline int scan_incl<T>(const T* in, T* out, size_t n, int op, cudaStream_t s) {           \
+    return b200_scan_inclusive_##SUF(reinterpret_cast<const C*>(in), reinterpret_cast<C*>(out), n, op, s); \
+  }                                                                                          \
+  template <>                                                                                \
+  inline int scan_excl<T>(const T* in, T* out, size_t n, int op, T init, cudaStream_t s) {   \
+    return b200_scan_exclusive_##SUF(reinterpret_cast<const C*>(in), reinterpret_cast<C*>(out), n, op, \
+                                     C(init), s);                                            \
+  }
+static_assert(sizeof(long long) == 8, "64-bit long long");
+#if !defined(_WIN32)
+B200_SCAN_BIND_LL(i64, long long, int64_t)
+B200_SCAN_BIND_LL(u64, unsigned long long, uint64_t)
+#endif
+#undef B200_SCAN_BIND_LL
 template <>
 inline int scan_incl<float>(const float* in, float* out, size_t n, int op, cudaStream_t s) {
   return b200_scan_inclusive_f32(in, out, n, op, B200_MODE_NAIVE, s);
@@ -1395,6 +1457,7 @@ inline int scan_excl<double>(const double* in, double* out, size_t n, int op, do
 }  // namespace detail
 }  // namespace b200
 
+#if defined(RAJA_COMPAT_FRONTEND)
 // policy/cuda/scan.hpp:141-235 (CUB DeviceScan) replaced by libb200prims.
 template <int BLOCK, bool Async, typename T, typename F>
 void scan_inclusive(b200_exec<BLOCK, Async>, const T* b, const T* e, T* out, F) {
@@ -1411,6 +1474,8 @@ void scan_exclusive(b200_exec<BLOCK, Async>, const T* b, const T* e, T* out, F, 
               "b200 exclusive_scan");
   if (!Async) b200::wait();
 }
+
+#endif  // RAJA_COMPAT_FRONTEND
 
 // ----------------------------------------------------------------- sorts
 // policy/cuda/sort.hpp:92-653 (CUB DeviceRadixSort) replaced by the
@@ -1432,6 +1497,14 @@ B200_SORT_BIND(i64, int64_t)
 B200_SORT_BIND(f32, float)
 B200_SORT_BIND(f64, double)
 #undef B200_SORT_BIND
+template <>
+inline int keys<long long>(long long* k, size_t n, int desc, cudaStream_t s) {
+  return b200_sort_keys_i64(reinterpret_cast<int64_t*>(k), n, desc, s);
+}
+template <>
+inline int keys<unsigned long long>(unsigned long long* k, size_t n, int desc, cudaStream_t s) {
+  return b200_sort_keys_u64(reinterpret_cast<uint64_t*>(k), n, desc, s);
+}
 #define B200_PAIRS_BIND(SUF, K, V)                                                   \
   template <>                                                                        \
   inline int pairs<K, V>(K * k, V * v, size_t n, int desc, cudaStream_t s) {         \
@@ -1455,6 +1528,7 @@ constexpr int desc_of() {
 }
 }  // namespace b200d
 
+#if defined(RAJA_COMPAT_FRONTEND)
 template <int BLOCK, bool Async, typename T, typename C>
 void sort_stable(b200_exec<BLOCK, Async>, T* b, T* e, C) {
   b200::check(b200d::keys<T>(b, size_t(e - b), b200d::desc_of<C, T>(), b200::stream()), "b200 sort");
@@ -1691,6 +1765,8 @@ inline void synchronize<b200_synchronize>() {
   b200::wait();
 }
 
+#endif  // RAJA_COMPAT_FRONTEND
+
 // --------------------------------------------------------------- atomics
 // b200_atomic: CUDA atomics in device code (min / max of floating types by
 // compare-and-swap with the `<` rule), GCC __atomic builtins on the host.
@@ -1701,20 +1777,20 @@ namespace atom {
 template <typename T>
 using Word = std::conditional_t<sizeof(T) == 4, unsigned int, unsigned long long>;
 template <typename T>
-RAJA_HOST_DEVICE inline Word<T> bits(T v) {
+B200_HOST_DEVICE inline Word<T> bits(T v) {
   Word<T> w;
   memcpy(&w, &v, sizeof(T));
   return w;
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T from_bits(Word<T> w) {
+B200_HOST_DEVICE inline T from_bits(Word<T> w) {
   T v;
   memcpy(&v, &w, sizeof(T));
   return v;
 }
 // generic read-modify-write by compare-and-swap: new value = f(old)
 template <typename T, typename F>
-RAJA_HOST_DEVICE inline T rmw(T* acc, F f) {
+B200_HOST_DEVICE inline T rmw(T* acc, F f) {
   static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte atomics");
   Word<T>* p = reinterpret_cast<Word<T>*>(acc);
 #ifdef __CUDA_ARCH__
@@ -1738,15 +1814,15 @@ RAJA_HOST_DEVICE inline T rmw(T* acc, F f) {
 }  // namespace b200
 
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicLoad(b200_atomic, T* acc) {
+B200_HOST_DEVICE inline T atomicLoad(b200_atomic, T* acc) {
   return b200::atom::rmw(acc, [](T o) { return o; });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline void atomicStore(b200_atomic, T* acc, T v) {
+B200_HOST_DEVICE inline void atomicStore(b200_atomic, T* acc, T v) {
   b200::atom::rmw(acc, [v](T) { return v; });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicAdd(b200_atomic, T* acc, T v) {
+B200_HOST_DEVICE inline T atomicAdd(b200_atomic, T* acc, T v) {
 #ifdef __CUDA_ARCH__
   if constexpr (std::is_same<T, int>::value || std::is_same<T, unsigned>::value ||
                 std::is_same<T, unsigned long long>::value || std::is_same<T, float>::value ||
@@ -1756,11 +1832,11 @@ RAJA_HOST_DEVICE inline T atomicAdd(b200_atomic, T* acc, T v) {
   return b200::atom::rmw(acc, [v](T o) { return T(o + v); });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicSub(b200_atomic, T* acc, T v) {
+B200_HOST_DEVICE inline T atomicSub(b200_atomic, T* acc, T v) {
   return b200::atom::rmw(acc, [v](T o) { return T(o - v); });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicMin(b200_atomic, T* acc, T v) {
+B200_HOST_DEVICE inline T atomicMin(b200_atomic, T* acc, T v) {
 #ifdef __CUDA_ARCH__
   if constexpr (std::is_same<T, int>::value || std::is_same<T, unsigned>::value ||
                 std::is_same<T, long long>::value || std::is_same<T, unsigned long long>::value)
@@ -1769,7 +1845,7 @@ RAJA_HOST_DEVICE inline T atomicMin(b200_atomic, T* acc, T v) {
   return b200::atom::rmw(acc, [v](T o) { return v < o ? v : o; });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicMax(b200_atomic, T* acc, T v) {
+B200_HOST_DEVICE inline T atomicMax(b200_atomic, T* acc, T v) {
 #ifdef __CUDA_ARCH__
   if constexpr (std::is_same<T, int>::value || std::is_same<T, unsigned>::value ||
                 std::is_same<T, long long>::value || std::is_same<T, unsigned long long>::value)
@@ -1778,39 +1854,39 @@ RAJA_HOST_DEVICE inline T atomicMax(b200_atomic, T* acc, T v) {
   return b200::atom::rmw(acc, [v](T o) { return o < v ? v : o; });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicInc(b200_atomic, T* acc) {
+B200_HOST_DEVICE inline T atomicInc(b200_atomic, T* acc) {
   return atomicAdd(b200_atomic{}, acc, T(1));
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicInc(b200_atomic, T* acc, T val) {
+B200_HOST_DEVICE inline T atomicInc(b200_atomic, T* acc, T val) {
   return b200::atom::rmw(acc, [val](T o) { return val <= o ? T(0) : T(o + T(1)); });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicDec(b200_atomic, T* acc) {
+B200_HOST_DEVICE inline T atomicDec(b200_atomic, T* acc) {
   return atomicSub(b200_atomic{}, acc, T(1));
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicDec(b200_atomic, T* acc, T val) {
+B200_HOST_DEVICE inline T atomicDec(b200_atomic, T* acc, T val) {
   return b200::atom::rmw(acc, [val](T o) { return (o == T(0) || val < o) ? val : T(o - T(1)); });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicAnd(b200_atomic, T* acc, T v) {
+B200_HOST_DEVICE inline T atomicAnd(b200_atomic, T* acc, T v) {
   return b200::atom::rmw(acc, [v](T o) { return T(o & v); });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicOr(b200_atomic, T* acc, T v) {
+B200_HOST_DEVICE inline T atomicOr(b200_atomic, T* acc, T v) {
   return b200::atom::rmw(acc, [v](T o) { return T(o | v); });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicXor(b200_atomic, T* acc, T v) {
+B200_HOST_DEVICE inline T atomicXor(b200_atomic, T* acc, T v) {
   return b200::atom::rmw(acc, [v](T o) { return T(o ^ v); });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicExchange(b200_atomic, T* acc, T v) {
+B200_HOST_DEVICE inline T atomicExchange(b200_atomic, T* acc, T v) {
   return b200::atom::rmw(acc, [v](T) { return v; });
 }
 template <typename T>
-RAJA_HOST_DEVICE inline T atomicCAS(b200_atomic, T* acc, T compare, T v) {
+B200_HOST_DEVICE inline T atomicCAS(b200_atomic, T* acc, T compare, T v) {
 #ifdef __CUDA_ARCH__
   using W = b200::atom::Word<T>;
   return b200::atom::from_bits<T>(::atomicCAS(reinterpret_cast<W*>(acc), b200::atom::bits(compare),
@@ -1846,10 +1922,10 @@ class DevMultiReduce {
   }
   // copies (the loop body's capture, on the host and on the device) share
   // the bins and own nothing
-  RAJA_HOST_DEVICE DevMultiReduce(const DevMultiReduce& o)
+  B200_HOST_DEVICE DevMultiReduce(const DevMultiReduce& o)
       : st_(o.st_), dev_(o.dev_), n_(o.n_), owner_(false) {}
   DevMultiReduce& operator=(const DevMultiReduce&) = delete;
-  RAJA_HOST_DEVICE ~DevMultiReduce() {
+  B200_HOST_DEVICE ~DevMultiReduce() {
 #if !defined(__CUDA_ARCH__)
     release();
 #endif
@@ -1870,7 +1946,7 @@ class DevMultiReduce {
     release();
     setup(std::vector<T>(num_bins, init));
   }
-  RAJA_HOST_DEVICE void combine(size_t bin, T v) const { Op::atomic(dev_ + bin, v); }
+  B200_HOST_DEVICE void combine(size_t bin, T v) const { Op::atomic(dev_ + bin, v); }
 
  private:
   struct State {
@@ -1914,27 +1990,27 @@ class DevMultiReduce {
 
 template <typename T> struct DMrSum {
   static T ident() { return T(0); }
-  RAJA_HOST_DEVICE static void atomic(T* p, T v) { atomicAdd(b200_atomic{}, p, v); }
+  B200_HOST_DEVICE static void atomic(T* p, T v) { atomicAdd(b200_atomic{}, p, v); }
   static void fold(T& a, T v) { a += v; }
 };
 template <typename T> struct DMrMin {
   static T ident() { return operators::limits<T>::max(); }
-  RAJA_HOST_DEVICE static void atomic(T* p, T v) { atomicMin(b200_atomic{}, p, v); }
+  B200_HOST_DEVICE static void atomic(T* p, T v) { atomicMin(b200_atomic{}, p, v); }
   static void fold(T& a, T v) { if (v < a) a = v; }
 };
 template <typename T> struct DMrMax {
   static T ident() { return operators::limits<T>::min(); }
-  RAJA_HOST_DEVICE static void atomic(T* p, T v) { atomicMax(b200_atomic{}, p, v); }
+  B200_HOST_DEVICE static void atomic(T* p, T v) { atomicMax(b200_atomic{}, p, v); }
   static void fold(T& a, T v) { if (a < v) a = v; }
 };
 template <typename T> struct DMrOr {
   static T ident() { return T(0); }
-  RAJA_HOST_DEVICE static void atomic(T* p, T v) { atomicOr(b200_atomic{}, p, v); }
+  B200_HOST_DEVICE static void atomic(T* p, T v) { atomicOr(b200_atomic{}, p, v); }
   static void fold(T& a, T v) { a |= v; }
 };
 template <typename T> struct DMrAnd {
   static T ident() { return T(~T(0)); }
-  RAJA_HOST_DEVICE static void atomic(T* p, T v) { atomicAnd(b200_atomic{}, p, v); }
+  B200_HOST_DEVICE static void atomic(T* p, T v) { atomicAnd(b200_atomic{}, p, v); }
   static void fold(T& a, T v) { a &= v; }
 };
 }  // namespace detail
@@ -1950,13 +2026,13 @@ template <typename T> struct DMrAnd {
     struct reference {                                                                          \
       const B* mr;                                                                              \
       size_t bin;                                                                               \
-      RAJA_HOST_DEVICE const reference& METHOD(T v) const {                                     \
+      B200_HOST_DEVICE const reference& METHOD(T v) const {                                     \
         mr->combine(bin, v);                                                                    \
         return *this;                                                                           \
       }                                                                                         \
       T get() const { return mr->get(bin); }                                                    \
     };                                                                                          \
-    RAJA_HOST_DEVICE reference operator[](size_t bin) const { return reference{this, bin}; }    \
+    B200_HOST_DEVICE reference operator[](size_t bin) const { return reference{this, bin}; }    \
   };
 RAJA_B200_MULTI_REDUCER(MultiReduceSum, DMrSum, operator+=)
 RAJA_B200_MULTI_REDUCER(MultiReduceMin, DMrMin, min)
@@ -1966,3 +2042,8 @@ RAJA_B200_MULTI_REDUCER(MultiReduceBitAnd, DMrAnd, operator&=)
 #undef RAJA_B200_MULTI_REDUCER
 
 }  // namespace RAJA
+
+#if !defined(RAJA_COMPAT_FRONTEND)
+// an installed RAJA: the reference's own extension points
+#include "RAJA_b200_extension_points.hpp"
+#endif

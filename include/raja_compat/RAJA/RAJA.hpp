@@ -26,6 +26,10 @@
 // omp_reduce; include/raja_b200/RAJA_b200.hpp adds the b200 family.
 #pragma once
 
+// Marks this front-end for back-end headers that also build against an
+// installed RAJA (include/raja_b200/RAJA_b200.hpp).
+#define RAJA_COMPAT_FRONTEND 1
+
 #include <algorithm>
 #include <array>
 #include <cstddef>

@@ -9,6 +9,9 @@
 #include <memory>
 #include <stdexcept>
 #include <type_traits>
+#if defined(__CUDACC__)
+#include <cuda_runtime.h>
+#endif
 
 #include "camp/helpers.hpp"
 
@@ -129,7 +132,7 @@ public:
 template <typename Res>
 struct EventProxy {
   using native_event = decltype(val<Res&>().get_event());
-  explicit EventProxy(Res r) : res(r) {}
+  EventProxy(Res r) : res(r) {}
   EventProxy(EventProxy&&) = default;
   EventProxy& operator=(EventProxy&&) = default;
   native_event get() { return res.get_event(); }
@@ -142,6 +145,43 @@ struct EventProxy {
   }
   Res res;
 };
+
+#if defined(__CUDACC__)
+// A CUDA stream on the current device, with the part of camp's Cuda
+// resource interface the b200 policies use (get_stream, get_default,
+// get_platform, wait, stream-ordered memory helpers).
+class Cuda
+{
+public:
+  Cuda() : s(nullptr) {}
+  explicit Cuda(cudaStream_t st) : s(st) {}
+  static Cuda get_default() { return Cuda(); }
+  static Cuda CudaFromStream(cudaStream_t st, int = 0) { return Cuda(st); }
+  Platform get_platform() const { return Platform::cuda; }
+  cudaStream_t get_stream() const { return s; }
+  Event get_event() { return Event(); }
+  Event get_event_erased() { return Event(); }
+  void wait() { cudaStreamSynchronize(s); }
+  void wait_for(Event*) {}
+  template <typename T>
+  T* allocate(size_t n, MemoryAccess = MemoryAccess::Device)
+  {
+    void* p = nullptr;
+    cudaMallocAsync(&p, sizeof(T) * n, s);
+    return static_cast<T*>(p);
+  }
+  void deallocate(void* p, MemoryAccess = MemoryAccess::Device) { cudaFreeAsync(p, s); }
+  void memcpy(void* dst, const void* src, size_t bytes)
+  {
+    cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s);
+  }
+  void memset(void* p, int v, size_t bytes) { cudaMemsetAsync(p, v, bytes, s); }
+  bool operator==(Cuda const& o) const { return s == o.s; }
+
+private:
+  cudaStream_t s;
+};
+#endif
 
 template <typename Res>
 struct is_resource : std::false_type {

@@ -1,0 +1,156 @@
+// A RAJA application that switches one policy alias from seq_exec to
+// b200_exec, built against an installed RAJA (the reference's own headers)
+// plus raja_b200/RAJA_b200.hpp.  Every b200 result is checked against the
+// seq_exec result of the same code.  Without a CUDA device only the
+// sequential half runs (the program still proves that each RAJA front-end
+// binds to a b200 overload: forall over ranges and IndexSets, ReduceSum /
+// ReduceMinLoc on b200_reduce, expt::Reduce params, scans and sorts).
+#include "raja_b200/RAJA_b200.hpp"  // before RAJA/RAJA.hpp, which it includes
+
+// Loop bodies run on the host (seq_exec) and the device (b200_exec).  RAJA
+// spells this RAJA_HOST_DEVICE, which is empty in a RAJA configured without
+// its own CUDA back-end (as here), so the bodies say it directly.
+#define APP_HOST_DEVICE __host__ __device__
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+namespace {
+int failures = 0;
+void check(bool ok, const char* what)
+{
+  std::printf("%s %s\n", ok ? "PASS" : "FAIL", what);
+  if (!ok) ++failures;
+}
+
+template <typename ExecPol, typename RedPol>
+struct Results {
+  std::vector<double> y;
+  double sum = 0, psum = 0;
+  double minv = 0;
+  RAJA::Index_type minloc = -1;
+  RAJA::expt::ValLoc<double> pmin;
+  std::vector<long long> incl, excl;
+  std::vector<int> keys, vals;
+  std::vector<double> iset;
+};
+
+// The application code: one alias decides where it runs.
+template <typename ExecPol, typename RedPol>
+Results<ExecPol, RedPol> run(const std::vector<double>& x0, const std::vector<int>& k0, double* x,
+                             double* y, long long* a, long long* b, int* k, int* v, double* z)
+{
+  const RAJA::Index_type n = RAJA::Index_type(x0.size());
+  for (RAJA::Index_type i = 0; i < n; ++i) {
+    x[i] = x0[i];
+    y[i] = 1.0;
+    a[i] = (long long)(i % 7);
+    k[i] = k0[i];
+    v[i] = int(i);
+    z[i] = 0.0;
+  }
+  Results<ExecPol, RedPol> r;
+  // forall: daxpy
+  RAJA::forall<ExecPol>(RAJA::TypedRangeSegment<RAJA::Index_type>(0, n),
+                        [=] APP_HOST_DEVICE(RAJA::Index_type i) { y[i] += 2.5 * x[i]; });
+  // classic reducers captured by the body
+  RAJA::ReduceSum<RedPol, double> sum(0.0);
+  RAJA::ReduceMinLoc<RedPol, double, RAJA::Index_type> mnl(1e300, -1);
+  RAJA::forall<ExecPol>(RAJA::TypedRangeSegment<RAJA::Index_type>(0, n),
+                        [=] APP_HOST_DEVICE(RAJA::Index_type i) {
+                          sum += y[i];
+                          mnl.minloc(x[i], i);
+                        });
+  r.sum = sum.get();
+  r.minv = mnl.get();
+  r.minloc = mnl.getLoc();
+  // expt params
+  double ps = 0.0;
+  RAJA::expt::ValLoc<double> pm(1e300, -1);
+  using SUM = RAJA::expt::ValOp<double, RAJA::operators::plus>;
+  using MINL = RAJA::expt::ValLocOp<double, RAJA::Index_type, RAJA::operators::minimum>;
+  RAJA::forall<ExecPol>(RAJA::TypedRangeSegment<RAJA::Index_type>(0, n),
+                        RAJA::expt::Reduce<RAJA::operators::plus>(&ps),
+                        RAJA::expt::Reduce<RAJA::operators::minimum>(&pm), RAJA::Name("binding params"),
+                        [=] APP_HOST_DEVICE(RAJA::Index_type i, SUM & s, MINL & m) {
+                          s += y[i];
+                          m.minloc(x[i], i);
+                        });
+  r.psum = ps;
+  r.pmin = pm;
+  // scans
+  RAJA::inclusive_scan<ExecPol>(RAJA::make_span(a, n), RAJA::make_span(b, n));
+  r.incl.assign(b, b + n);
+  RAJA::exclusive_scan_inplace<ExecPol>(RAJA::make_span(a, n), RAJA::operators::maximum<long long>{});
+  r.excl.assign(a, a + n);
+  // sorts
+  RAJA::stable_sort_pairs<ExecPol>(RAJA::make_span(k, n), RAJA::make_span(v, n),
+                                   RAJA::operators::greater<int>{});
+  r.keys.assign(k, k + n);
+  r.vals.assign(v, v + n);
+  // IndexSet: a range and a list segment
+  RAJA::TypedIndexSet<RAJA::TypedRangeSegment<RAJA::Index_type>, RAJA::TypedListSegment<RAJA::Index_type>> is;
+  is.push_back(RAJA::TypedRangeSegment<RAJA::Index_type>(0, n / 2));
+  std::vector<RAJA::Index_type> odd;
+  for (RAJA::Index_type i = n / 2 + 1; i < n; i += 2) odd.push_back(i);
+  camp::resources::Resource res = RAJA::resources::get_resource<ExecPol>::type::get_default();
+  is.push_back(RAJA::TypedListSegment<RAJA::Index_type>(odd.data(), odd.size(), res));
+  RAJA::forall<RAJA::ExecPolicy<RAJA::seq_segit, ExecPol>>(
+      is, [=] APP_HOST_DEVICE(RAJA::Index_type i) { z[i] = y[i] * 2.0; });
+  r.iset.assign(z, z + n);
+  return r;
+}
+}  // namespace
+
+int main()
+{
+  const RAJA::Index_type n = 100003;
+  std::vector<double> x0(n);
+  std::vector<int> k0(n);
+  unsigned s = 12345u;
+  for (RAJA::Index_type i = 0; i < n; ++i) {
+    s = s * 1664525u + 1013904223u;
+    x0[i] = double(s >> 8) / double(1u << 24) - 0.5;
+    k0[i] = int(s % 1000u);
+  }
+  std::vector<double> hx(n), hy(n), hz(n);
+  std::vector<long long> ha(n), hb(n);
+  std::vector<int> hk(n), hv(n);
+  auto seq = run<RAJA::seq_exec, RAJA::seq_reduce>(x0, k0, hx.data(), hy.data(), ha.data(), hb.data(),
+                                                    hk.data(), hv.data(), hz.data());
+  std::printf("seq_exec: sum %.17g, minloc %.17g at %ld\n", seq.sum, seq.minv, (long)seq.minloc);
+
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    std::printf("no CUDA device: b200 half not run (the program compiled and linked)\n");
+    return failures ? 1 : 0;
+  }
+  double *x, *y, *z;
+  long long *a, *b;
+  int *k, *v;
+  cudaMallocManaged(&x, n * sizeof(double));
+  cudaMallocManaged(&y, n * sizeof(double));
+  cudaMallocManaged(&z, n * sizeof(double));
+  cudaMallocManaged(&a, n * sizeof(long long));
+  cudaMallocManaged(&b, n * sizeof(long long));
+  cudaMallocManaged(&k, n * sizeof(int));
+  cudaMallocManaged(&v, n * sizeof(int));
+  auto dev = run<RAJA::b200_exec<256>, RAJA::b200_reduce>(x0, k0, x, y, a, b, k, v, z);
+  cudaDeviceSynchronize();
+  double tol = 4.0 * n * 1.1102230246251565e-16 * 4.0 * n;
+  bool y_ok = true;
+  for (RAJA::Index_type i = 0; i < n; ++i)
+    y_ok = y_ok && std::fabs(dev.iset[i] - seq.iset[i]) <= 4e-16 * std::fabs(seq.iset[i]) + 1e-300;
+  check(std::fabs(dev.sum - seq.sum) <= tol, "ReduceSum<b200_reduce>");
+  check(dev.minv == seq.minv && dev.minloc == seq.minloc, "ReduceMinLoc<b200_reduce> (value, first index)");
+  check(std::fabs(dev.psum - seq.psum) <= tol, "expt::Reduce<plus> on b200_exec");
+  check(dev.pmin.getVal() == seq.pmin.getVal() && dev.pmin.getLoc() == seq.pmin.getLoc(),
+        "expt::Reduce<minimum> over ValLoc on b200_exec");
+  check(dev.incl == seq.incl, "inclusive_scan<b200_exec>");
+  check(dev.excl == seq.excl, "exclusive_scan_inplace<b200_exec>(maximum)");
+  check(dev.keys == seq.keys && dev.vals == seq.vals, "stable_sort_pairs<b200_exec>(greater)");
+  check(y_ok, "forall over an IndexSet (range + list) on ExecPolicy<seq_segit, b200_exec>");
+  return failures ? 1 : 0;
+}

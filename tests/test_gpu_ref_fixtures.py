@@ -15,8 +15,8 @@ policies compiled from the unmodified reference headers
   * unstable sorts: RAJA's own rule (equal keys, same values per key);
   * floating-point sums: within 2 (n-1) u sum|x| of RAJA's seq result
     (both lie within (n-1) u sum|x| of the exact sum); floating-point scans:
-    every prefix within 2 n u sum|x[:i]|; daxpy within 2 u |y| (the GPU
-    fuses a*x+y into one rounding).
+    every prefix within 2 n u sum|x[:i]|; daxpy within 2 u (|y| + |2.5 x|)
+    (the GPU fuses a*x+y into one rounding).
 """
 import os
 import struct
@@ -168,4 +168,6 @@ def test_histogram_and_daxpy_match_raja(prims, fx):
     got = to_host(dy)
     for pol in ("seq", "omp"):
         ref = fx[f"daxpy/{pol}/out"]
-        assert np.all(np.abs(got - ref) <= 2 * EPS["f64"] * np.abs(ref) + 1e-300), pol
+        # one rounding (fused) against two (product, then sum)
+        tol = 2 * EPS["f64"] * (np.abs(y) + 2.5 * np.abs(x))
+        assert np.all(np.abs(got - ref) <= tol), pol
