@@ -431,6 +431,13 @@ int b200_batch_autotune_axpy_sum_f32(b200_batch_plan plan, float a, const float*
  * what the ordered WorkGroup runner does). */
 int b200_loop_axpy_sum_f32(float a, const float* x, float* y, size_t n, double* sum, int mode,
                            b200_stream_t stream);
+/* The ordered WorkGroup runner's schedule for the same work: loop i runs
+ * as its own launch (b200_loop_axpy_sum_f32), in order, all issued from
+ * this call (policy/cuda/WorkGroup/WorkRunner.hpp:38-162 launches one forall
+ * per enqueued loop).  lens_host, xs_host, ys_host: host arrays of nloops
+ * lengths and device pointers; sums: device array of nloops doubles. */
+int b200_loops_axpy_sum_f32(int nloops, const int64_t* lens_host, float a, const float* const* xs_host,
+                            float* const* ys_host, double* sums, int mode, b200_stream_t stream);
 
 /* Segmented sum scans of int32 over the plan's segments (restart at each
  * segment; exclusive writes 0 at each head). */

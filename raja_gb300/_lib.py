@@ -90,6 +90,7 @@ def _signatures() -> dict[str, tuple]:
         "b200_batched_axpy_sum_f32": (_I, [_P, C.c_float, _P, _P, _P, _I, _P]),
         "b200_batch_autotune_axpy_sum_f32": (_I, [_P, C.c_float, _P, _P, _P, _I, _P]),
         "b200_loop_axpy_sum_f32": (_I, [C.c_float, _P, _P, _SZ, _P, _I, _P]),
+        "b200_loops_axpy_sum_f32": (_I, [_I, _P, C.c_float, _P, _P, _P, _I, _P]),
         "b200_segmented_scan_inclusive_i32": (_I, [_P, _P, _P, _P]),
         "b200_segmented_scan_exclusive_i32": (_I, [_P, _P, _P, _P]),
         "b200_segmented_sort_keys_u32": (_I, [_P, _P, _I, _P]),

@@ -91,58 +91,77 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 }
 
 // Body of one tile: y += a*x over [lo, hi) of one loop; returns the
-// thread's compensated partial of the updated y.
+// thread's compensated partial of the updated y.  When x and y share their
+// offset from a 16-byte boundary (the loops of one flat array do), the tile
+// runs as a scalar head of 0-3 elements up to that boundary, 16-byte
+// vectors, and a scalar tail of 0-3 elements, so loops that start at any
+// element offset, and each loop's short last tile, stay on the vector
+// path.  Otherwise the tile runs scalar.
 template <int BLOCK, int ITEMS>
 __device__ __forceinline__ double tile_axpy_sum(float a, const float* __restrict__ x,
                                                 float* __restrict__ y, int64_t lo, int64_t hi,
                                                 bool comp) {
   float s = 0.f, c = 0.f;
+  auto add = [&](float r) {
+    if (comp) {
+      float t, e2;
+      two_sum(s, r, t, e2);
+      s = t;
+      c += e2;
+    } else {
+      s += r;
+    }
+  };
   const int tid = threadIdx.x;
   constexpr int VN = 4;
-  const bool vec = (hi - lo == int64_t(BLOCK) * ITEMS) &&
-                   ((reinterpret_cast<uintptr_t>(x + lo) | reinterpret_cast<uintptr_t>(y + lo)) % 16 == 0);
-  if (vec) {
+  const uintptr_t ax = reinterpret_cast<uintptr_t>(x + lo), ay = reinterpret_cast<uintptr_t>(y + lo);
+  if ((((ax ^ ay) & 15) == 0) && ((ax & 3) == 0)) {
+    const int64_t n = hi - lo;
+    const int64_t h0 = int64_t(((16 - (ax & 15)) & 15) >> 2);  // elements before the boundary
+    const int64_t nh = h0 < n ? h0 : n;
+    const int64_t vb = lo + nh;                 // first vector element
+    const int64_t nv = (hi - vb) / VN;          // whole vectors in the tile
+    const int64_t tb = vb + nv * VN;            // first tail element
     float4 vx[ITEMS / VN], vy[ITEMS / VN];
 #pragma unroll
     for (int j = 0; j < ITEMS / VN; ++j) {
-      const int64_t e = lo + (int64_t(j) * BLOCK + tid) * VN;
-      vx[j] = __ldcs(reinterpret_cast<const float4*>(x + e));
-      vy[j] = __ldcs(reinterpret_cast<const float4*>(y + e));
+      const int64_t v = int64_t(j) * BLOCK + tid;
+      if (v < nv) {
+        vx[j] = __ldcs(reinterpret_cast<const float4*>(x + vb + v * VN));
+        vy[j] = __ldcs(reinterpret_cast<const float4*>(y + vb + v * VN));
+      }
+    }
+    if (tid < nh) {
+      const float r = y[lo + tid] + a * x[lo + tid];
+      y[lo + tid] = r;
+      add(r);
     }
 #pragma unroll
     for (int j = 0; j < ITEMS / VN; ++j) {
-      const int64_t e = lo + (int64_t(j) * BLOCK + tid) * VN;
-      float4 r;
-      r.x = vy[j].x + a * vx[j].x;
-      r.y = vy[j].y + a * vx[j].y;
-      r.z = vy[j].z + a * vx[j].z;
-      r.w = vy[j].w + a * vx[j].w;
-      __stcs(reinterpret_cast<float4*>(y + e), r);
-      const float rv[4] = {r.x, r.y, r.z, r.w};
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (comp) {
-          float t, e2;
-          two_sum(s, rv[k], t, e2);
-          s = t;
-          c += e2;
-        } else {
-          s += rv[k];
-        }
+      const int64_t v = int64_t(j) * BLOCK + tid;
+      if (v < nv) {
+        float4 r;
+        r.x = vy[j].x + a * vx[j].x;
+        r.y = vy[j].y + a * vx[j].y;
+        r.z = vy[j].z + a * vx[j].z;
+        r.w = vy[j].w + a * vx[j].w;
+        __stcs(reinterpret_cast<float4*>(y + vb + v * VN), r);
+        add(r.x);
+        add(r.y);
+        add(r.z);
+        add(r.w);
       }
+    }
+    if (tid < hi - tb) {
+      const float r = y[tb + tid] + a * x[tb + tid];
+      y[tb + tid] = r;
+      add(r);
     }
   } else {
     for (int64_t i = lo + tid; i < hi; i += BLOCK) {
       const float r = y[i] + a * x[i];
       y[i] = r;
-      if (comp) {
-        float t, e2;
-        two_sum(s, r, t, e2);
-        s = t;
-        c += e2;
-      } else {
-        s += r;
-      }
+      add(r);
     }
   }
   return double(s) + double(c);
@@ -708,6 +727,20 @@ int b200_loop_axpy_sum_f32(float a, const float* x, float* y, size_t n, double* 
   B200_LAUNCH(name, (loop_axpy_sum_kernel<BLOCK, ITEMS>), unsigned(grid), BLOCK, 0, s, a, x, y,
               int64_t(n), sum, static_cast<double*>(scr), counters + 1,
               (mode & B200_MODE_COMPENSATED) ? 1 : 0);
+  clear_error();
+  return B200_OK;
+}
+
+int b200_loops_axpy_sum_f32(int nloops, const int64_t* lens_host, float a, const float* const* xs_host,
+                            float* const* ys_host, double* sums, int mode, b200_stream_t stream) {
+  const char* name = "b200_loops_axpy_sum_f32";
+  if (nloops < 0) return fail(B200_ERR_ARG, "%s: nloops=%d", name, nloops);
+  if (nloops > 0 && (!lens_host || !xs_host || !ys_host || !sums))
+    return fail(B200_ERR_ARG, "%s: null pointer", name);
+  for (int i = 0; i < nloops; ++i) {
+    if (lens_host[i] < 0) return fail(B200_ERR_ARG, "%s: loop %d has length %lld", name, i, (long long)lens_host[i]);
+    B200_TRY(b200_loop_axpy_sum_f32(a, xs_host[i], ys_host[i], size_t(lens_host[i]), sums + i, mode, stream));
+  }
   clear_error();
   return B200_OK;
 }

@@ -55,6 +55,53 @@ def test_batched_axpy_sum_matches_per_loop_oracle(prims, orc, autotune):
     assert info["total"] == int(lens.sum()) and info["tiles"] > 0
 
 
+def test_batched_full_workgroup_shape_loop_by_loop(prims, orc):
+    """The batched-loops configuration at full size: 4096 loops with
+    lognormal(median 2000, sigma 1.5) lengths clipped to [32, 2^20], carved
+    from one flat array (so most loops start off a 16-byte boundary), fp32
+    axpy plus a compensated per-loop sum.  Every loop is checked against the
+    oracle, and the one-launch-per-loop schedule (the ordered WorkGroup
+    runner's) gives the same results within the same bounds."""
+    import ctypes as C
+
+    import torch
+    from raja_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(4)
+    lens = lognormal_lengths(rng, 4096, 2000, 1.5, 32, 1 << 20)
+    offs = np.concatenate([[0], np.cumsum(lens)])
+    total = int(offs[-1])
+    x = rng.uniform(-1, 1, total).astype(np.float32)
+    y = rng.uniform(-1, 1, total).astype(np.float32)
+    dx, dy, dy2 = to_dev(x), to_dev(y), to_dev(y)
+    px = torch.tensor([dx.data_ptr() + 4 * int(o) for o in offs[:-1]], dtype=torch.int64, device="cuda")
+    py = torch.tensor([dy.data_ptr() + 4 * int(o) for o in offs[:-1]], dtype=torch.int64, device="cuda")
+    plan = prims.BatchPlan(lens)
+    sums = torch.full((len(lens),), np.nan, dtype=torch.float64, device="cuda")
+    prims.batched_axpy_sum(plan, 0.75, px, py, sums)
+    # the same work as one launch per loop, issued from C++
+    sums2 = torch.full((len(lens),), np.nan, dtype=torch.float64, device="cuda")
+    hx = (C.c_void_p * len(lens))(*[dx.data_ptr() + 4 * int(o) for o in offs[:-1]])
+    hy = (C.c_void_p * len(lens))(*[dy2.data_ptr() + 4 * int(o) for o in offs[:-1]])
+    hl = (C.c_int64 * len(lens))(*[int(n) for n in lens])
+    rc = lib.b200_loops_axpy_sum_f32(len(lens), hl, C.c_float(0.75), hx, hy, sums2.data_ptr(), 1,
+                                     torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, lib.b200_last_error_string()
+    prims.synchronize()
+    yr = orc.axpy(np.float32(0.75), x, y.copy())
+    gy, gy2 = to_host(dy), to_host(dy2)
+    np.testing.assert_allclose(gy, yr, rtol=4 * U32, atol=4 * U32)
+    assert np.array_equal(gy, gy2)                 # the same per-element arithmetic
+    s1, s2 = to_host(sums), to_host(sums2)
+    for i in range(len(lens)):
+        seg = gy[offs[i]:offs[i + 1]]
+        exact, lo = orc.exact_sum(seg)
+        bound = 1e-6 * float(np.abs(seg).sum()) + 1e-300
+        assert abs((s1[i] - exact) - lo) <= bound, (i, int(lens[i]))
+        assert abs((s2[i] - exact) - lo) <= bound, (i, int(lens[i]))
+    plan.close()
+
+
 def test_loop_axpy_sum_single(prims, orc):
     import torch
     rng = np.random.default_rng(2)
