@@ -32,6 +32,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
@@ -161,6 +162,40 @@ inline LaunchCtx& ctx() {
   return c;
 }
 
+// WorkGroup capture (host): while a b200 WorkPool copies an enqueued loop
+// body, each captured b200 reducer gets a slot for that loop -- one
+// partial per tile of the loop, a ticket, and an index into the results
+// of a run -- recorded in the pool's registry.  The registry also delivers
+// each run's results to the reducers (pending reads, folded by get()).
+struct WgRegistry {
+  std::vector<void*> blocks;  // device memory of the slots (freed with the group)
+  std::vector<std::function<void(const unsigned char* results_host, const std::shared_ptr<void>& keep,
+                                 cudaStream_t s)>>
+      deliver;  // one per reducer, in slot index order
+  ~WgRegistry() {
+    for (void* b : blocks) cudaFree(b);
+  }
+};
+constexpr size_t kWgResultBytes = 32;  // one result of a run per reducer
+struct WgCaptureCtx {
+  bool active = false;
+  WgRegistry* reg = nullptr;
+  long long ntiles = 0;               // tiles of the loop being captured
+  unsigned long long capture_id = 0;  // new for every enqueue
+};
+inline WgCaptureCtx& wg_capture() {
+  static thread_local WgCaptureCtx c;
+  return c;
+}
+
+// Device side of a WorkGroup run: the tile of the loop a block is running
+// and where the run's per-reducer results go.  Set by the runner kernels
+// before each loop body runs.
+struct WgDevCtx {
+  long long tile;
+  unsigned char* results;
+};
+
 // Grid for a kernel that always runs `block` threads: one block per `block`
 // elements, capped at the resident blocks of the whole GPU (the loop
 // grid-strides beyond that).  The occupancy query runs once per (kernel,
@@ -287,6 +322,41 @@ __device__ inline void grid_combine(const DevSlot<T>& s, T v, Merge merge) {
     *s.result = acc;
     *s.ticket = 0u;
   }
+}
+
+// The device context of a WorkGroup run, one per block (set by the runner
+// kernels, read by the loop reducers' combine).
+__device__ __forceinline__ WgDevCtx& wg_dev_ctx() {
+  __shared__ WgDevCtx c;
+  return c;
+}
+
+// Fold count partials in index order with every thread of the block
+// (thread t takes t, t + nthreads, ...; then a fixed tree): the result,
+// valid in thread 0, depends only on the partials and the block shape.
+template <class T, class Merge>
+__device__ inline T fold_partials(const T* parts, unsigned count, Merge merge) {
+  const unsigned tid = lin_tid(), nt = lin_nthreads();
+  T r{};
+  for (unsigned b = tid; b < count; b += nt) {
+    const T p = ld_cg(parts + b);
+    r = b == tid ? p : merge(r, p);
+  }
+  __shared__ __align__(16) unsigned char fold_raw[32 * sizeof(T) + 16];
+  T* fin = reinterpret_cast<T*>(fold_raw);
+  const int lane = int(tid & 31), warp = int(tid >> 5);
+  const int holders = int(count < nt ? count : nt);
+  const int present = int(nt) - warp * 32 < 32 ? int(nt) - warp * 32 : 32;
+  int valid = holders - warp * 32;
+  valid = valid < 0 ? 0 : (valid > 32 ? 32 : valid);
+  r = warp_fold(r, lane, valid, present, merge);
+  if (lane == 0 && valid > 0) fin[warp] = r;
+  __syncthreads();
+  T acc = fin[0];
+  if (tid == 0)
+    for (int w = 1; w * 32 < holders; ++w) acc = merge(acc, fin[w]);
+  __syncthreads();
+  return acc;
 }
 
 // Stream-ordered pool of the current device for the C++ layer's per-launch
@@ -458,6 +528,7 @@ class DevReducer {
   struct Pending {
     SlotMem mem;
     cudaStream_t stream;
+    std::shared_ptr<void> keep;  // a WorkGroup run's results (cell not pooled)
   };
   struct Shared {
     V init;
@@ -467,13 +538,26 @@ class DevReducer {
     // every such copy of one launch must share one slot.
     unsigned long long slot_launch = 0;
     DevSlot<V> slot{nullptr, nullptr, nullptr};
+    // likewise for the WorkGroup capture of one enqueued loop
+    unsigned long long slot_capture = 0;
+    DevSlot<V> wg_slot{nullptr, nullptr, nullptr};
+    long long wg_id = -1, wg_ntiles = 0;
   };
   Shared* shared_ = nullptr;
   bool original_ = false;
   bool launch_copy_ = false;
   bool owner_ = false;
+  bool wg_ = false;          // a WorkGroup loop's copy: tile-ordered combine
+  long long wg_id_ = -1;     // index of this reducer in a run's results
+  long long wg_ntiles_ = 0;  // tiles of its loop
   DevSlot<V> slot_{nullptr, nullptr, nullptr};
   mutable V val_;
+
+  // The tile-ordered combine of a WorkGroup loop's reducer: every tile
+  // publishes its block's partial; the block that completes the loop's tile
+  // count folds the partials in tile order (deterministic) and writes the
+  // run's result.
+  __device__ void wg_combine(V v) const;
 
  public:
   explicit DevReducer(V init) : shared_(new Shared{init, {}}), original_(true), val_(K::ident()) {}
@@ -483,10 +567,46 @@ class DevReducer {
     // per-thread copy of the launch copy: owns the combine
     slot_ = o.slot_;
     owner_ = o.launch_copy_;
+    wg_ = o.wg_;
+    wg_id_ = o.wg_id_;
+    wg_ntiles_ = o.wg_ntiles_;
 #else
     shared_ = o.shared_;
     LaunchCtx& c = ctx();
-    if (c.active && !o.launch_copy_) {
+    WgCaptureCtx& w = wg_capture();
+    if (w.active && !o.launch_copy_ && w.ntiles == 0) {
+      // an empty loop never runs: no slot, the reducer keeps its value
+      slot_ = o.slot_;
+      launch_copy_ = false;
+    } else if (w.active && !o.launch_copy_) {
+      if (shared_->slot_capture != w.capture_id) {
+        const size_t pbytes = ((size_t(w.ntiles > 0 ? w.ntiles : 1) * sizeof(V) + 255) / 256) * 256;
+        void* blk = nullptr;
+        check_cuda(cudaMalloc(&blk, pbytes + 256), "WorkGroup reducer slot");
+        check_cuda(cudaMemset(static_cast<char*>(blk) + pbytes, 0, sizeof(unsigned)), "WorkGroup reducer ticket");
+        w.reg->blocks.push_back(blk);
+        shared_->wg_slot = DevSlot<V>{static_cast<V*>(blk),
+                                      reinterpret_cast<unsigned*>(static_cast<char*>(blk) + pbytes), nullptr};
+        shared_->wg_id = (long long)w.reg->deliver.size();
+        shared_->wg_ntiles = w.ntiles;
+        shared_->slot_capture = w.capture_id;
+        Shared* sh = shared_;
+        const long long id = shared_->wg_id;
+        w.reg->deliver.push_back([sh, id](const unsigned char* res, const std::shared_ptr<void>& keep,
+                                          cudaStream_t s) {
+          Pending p;
+          p.mem.cell.host = const_cast<unsigned char*>(res + id * kWgResultBytes);
+          p.stream = s;
+          p.keep = keep;
+          sh->pending.push_back(p);
+        });
+      }
+      slot_ = shared_->wg_slot;
+      wg_id_ = shared_->wg_id;
+      wg_ntiles_ = shared_->wg_ntiles;
+      wg_ = true;
+      launch_copy_ = true;
+    } else if (c.active && !o.launch_copy_) {
       if (shared_->slot_launch != c.launch_id) {
         SlotMem mem;
         shared_->slot = alloc_slot<V>(c.grid, c.stream, &mem);
@@ -498,6 +618,9 @@ class DevReducer {
     } else {
       slot_ = o.slot_;
       launch_copy_ = o.launch_copy_;
+      wg_ = o.wg_;
+      wg_id_ = o.wg_id_;
+      wg_ntiles_ = o.wg_ntiles_;
     }
 #endif
   }
@@ -505,7 +628,10 @@ class DevReducer {
 
   B200_HOST_DEVICE ~DevReducer() {
 #if defined(__CUDA_ARCH__)
-    if (owner_) grid_combine(slot_, val_, [](V a, V b) { return K::merge(a, b); });
+    if (owner_) {
+      if (wg_) wg_combine(val_);
+      else grid_combine(slot_, val_, [](V a, V b) { return K::merge(a, b); });
+    }
 #else
     if (original_) {
       try {
@@ -533,8 +659,8 @@ class DevReducer {
     }
     for (const Pending& p : pend) {
       shared_->init = K::fold_init(shared_->init, read_cell<V>(p.mem.cell));
-      release_cell(p.mem.cell);
-      cudaFreeAsync(p.mem.block, p.stream);
+      if (!p.keep) release_cell(p.mem.cell);
+      if (p.mem.block) cudaFreeAsync(p.mem.block, p.stream);
     }
     pend.clear();
     return shared_->init;
@@ -544,6 +670,28 @@ class DevReducer {
     shared_->init = v;
   }
 };
+
+template <class K>
+__device__ void DevReducer<K>::wg_combine(V v) const {
+  __shared__ bool last;
+  const WgDevCtx& c = wg_dev_ctx();
+  auto merge = [](V a, V b) { return K::merge(a, b); };
+  v = block_reduce(v, merge);
+  if (lin_tid() == 0) {
+    slot_.partials[c.tile] = v;
+    __threadfence();
+    last = ::atomicAdd(slot_.ticket, 1u) == unsigned(wg_ntiles_ - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const V r = fold_partials(slot_.partials, unsigned(wg_ntiles_), merge);
+  if (lin_tid() == 0) {
+    static_assert(sizeof(V) <= kWgResultBytes, "reducer value larger than a result slot");
+    memcpy(c.results + wg_id_ * kWgResultBytes, &r, sizeof(V));
+    *slot_.ticket = 0u;  // ready for the next run
+  }
+}
 
 }  // namespace detail
 }  // namespace b200
@@ -673,11 +821,20 @@ __global__ void __launch_bounds__(BLOCK) forall_list_kernel(Body body_in, const 
   const long long stride = (long long)gridDim.x * BLOCK;
   for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < len; i += stride) body(idx[i]);
 }
-// All range segments of an IndexSet in one launch: a prefix of segment
-// lengths maps the flat iteration k to (segment, offset) by binary search.
+// Every segment of an IndexSet in one launch, whatever the mix of range,
+// strided and list segments: a table holds each segment's kind and
+// parameters, and a prefix of segment lengths maps the flat iteration k to
+// (segment, offset) by binary search.
+template <class T>
+struct SegDesc {
+  int kind;       // 0 range, 1 strided range, 2 list
+  T begin;        // range / strided: first index
+  T step;         // strided: stride
+  const T* list;  // list: the indices (device-accessible)
+};
 template <int BLOCK, class Body, class T>
 __global__ void __launch_bounds__(BLOCK)
-forall_indexset_kernel(Body body_in, const T* begins, const long long* prefix, int nseg,
+forall_indexset_kernel(Body body_in, const SegDesc<T>* segs, const long long* prefix, int nseg,
                        long long total) {
   Body body(body_in);
   const long long stride = (long long)gridDim.x * BLOCK;
@@ -688,7 +845,11 @@ forall_indexset_kernel(Body body_in, const T* begins, const long long* prefix, i
       if (prefix[mid] <= k) lo = mid;
       else hi = mid;
     }
-    body(T(begins[lo] + T(k - prefix[lo])));
+    const SegDesc<T> d = segs[lo];
+    const long long off = k - prefix[lo];
+    const T idx = d.kind == 0 ? T(d.begin + T(off))
+                              : (d.kind == 1 ? T(d.begin + T(off) * d.step) : d.list[off]);
+    body(idx);
   }
 }
 
@@ -972,56 +1133,74 @@ void forall_impl(b200_exec<BLOCK, Async>, const TypedListSegment<T>& l, Body&& b
   k<<<g, BLOCK, 0, s>>>(lb, l.data, len);
   b200::detail::finish<Async>("b200 forall");
 }
-// IndexSet: when every segment is a range, one launch covers them all (the
-// reference launches each segment separately, policy/cuda/forall.hpp:675-706);
-// otherwise the segments run one after another, each with its own launch.
+// IndexSet: one launch covers every segment, whatever the mix of range,
+// strided and list segments (the reference launches each segment
+// separately, policy/cuda/forall.hpp:675-706).  Segments with zero length
+// take no iterations; the segment table lives in launch-pool memory for the
+// duration of the launch.
+namespace b200 {
+namespace detail {
+template <class T, class Seg>
+inline bool seg_desc(const Seg& g, SegDesc<T>* d, long long* len) {
+  using G = std::decay_t<Seg>;
+  if constexpr (std::is_same<G, TypedRangeSegment<T>>::value) {
+    *d = SegDesc<T>{0, g.b, T(1), nullptr};
+    *len = (long long)stripIndexType(g.size());
+    return true;
+  } else if constexpr (std::is_same<G, TypedRangeStrideSegment<T>>::value) {
+    *d = SegDesc<T>{1, g.b, g.s, nullptr};
+    *len = (long long)stripIndexType(g.size());
+    return true;
+  } else if constexpr (std::is_same<G, TypedListSegment<T>>::value) {
+    *d = SegDesc<T>{2, T(0), T(0), g.data};
+    *len = (long long)g.size();
+    return true;
+  } else {
+    return false;  // another segment type: run per segment
+  }
+}
+}  // namespace detail
+}  // namespace b200
+
 template <int BLOCK, bool Async, class Body, class... Segs>
 void forall_impl(b200_exec<BLOCK, Async> pol, const TypedIndexSet<Segs...>& is, Body&& body) {
   using T = typename TypedIndexSet<Segs...>::value_type;
-  using Range = TypedRangeSegment<T>;
   using B = std::decay_t<Body>;
   const auto& segs = is.segments();
   const int nseg = int(segs.size());
   if (nseg == 0) return;
-  bool all_range = true;
-  for (const auto& v : segs)
-    all_range = all_range && std::visit([](const auto& g) { return std::is_same<std::decay_t<decltype(g)>, Range>::value; }, v);
-  if constexpr (!one_of<Range, Segs...>::value) {
-    all_range = false;
+  std::vector<b200::detail::SegDesc<T>> desc(nseg);
+  std::vector<long long> prefix(nseg + 1, 0);
+  bool table_ok = true;
+  for (int i = 0; i < nseg; ++i) {
+    long long len = 0;
+    table_ok = table_ok && std::visit([&](const auto& g) { return b200::detail::seg_desc<T>(g, &desc[i], &len); },
+                                      segs[i]);
+    prefix[i + 1] = prefix[i] + len;
   }
-  if (!all_range) {
+  if (!table_ok) {
     for (const auto& v : segs) std::visit([&](const auto& g) { forall_impl(pol, g, body); }, v);
     return;
   }
-  if constexpr (one_of<Range, Segs...>::value) {
-    std::vector<T> begins(nseg);
-    std::vector<long long> prefix(nseg + 1, 0);
-    for (int i = 0; i < nseg; ++i) {
-      const Range& r = std::get<Range>(segs[i]);
-      begins[i] = r.b;
-      prefix[i + 1] = prefix[i] + (long long)stripIndexType(r.size());
-    }
-    const long long total = prefix[nseg];
-    if (total == 0) return;
-    cudaStream_t s = b200::stream();
-    void* tbl = nullptr;
-    const size_t bb = ((nseg * sizeof(T) + 255) / 256) * 256;
-    tbl = b200::detail::launch_alloc(bb + (nseg + 1) * sizeof(long long), s, "indexset table");
-    T* d_begins = static_cast<T*>(tbl);
-    long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + bb);
-    b200::check_cuda(cudaMemcpyAsync(d_begins, begins.data(), nseg * sizeof(T), cudaMemcpyHostToDevice, s),
-                     "indexset table");
-    b200::check_cuda(cudaMemcpyAsync(d_prefix, prefix.data(), (nseg + 1) * sizeof(long long),
-                                     cudaMemcpyHostToDevice, s),
-                     "indexset table");
-    auto k = b200::detail::forall_indexset_kernel<BLOCK, B, T>;
-    const unsigned g = b200::detail::grid_for<b200::detail::forall_indexset_kernel<BLOCK, B, T>>(BLOCK, total);
-    B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
-    k<<<g, BLOCK, 0, s>>>(lb, d_begins, d_prefix, nseg, total);
-    b200::check_cuda(cudaGetLastError(), "b200 forall indexset");
-    b200::check_cuda(cudaFreeAsync(tbl, s), "indexset table");
-    if (!Async) b200::wait();
-  }
+  const long long total = prefix[nseg];
+  if (total == 0) return;
+  cudaStream_t s = b200::stream();
+  const size_t db = ((nseg * sizeof(b200::detail::SegDesc<T>) + 255) / 256) * 256;
+  void* tbl = b200::detail::launch_alloc(db + (nseg + 1) * sizeof(long long), s, "indexset table");
+  auto* d_desc = static_cast<b200::detail::SegDesc<T>*>(tbl);
+  long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + db);
+  b200::check_cuda(cudaMemcpyAsync(d_desc, desc.data(), nseg * sizeof(desc[0]), cudaMemcpyHostToDevice, s),
+                   "indexset table");
+  b200::check_cuda(cudaMemcpyAsync(d_prefix, prefix.data(), (nseg + 1) * sizeof(long long),
+                                   cudaMemcpyHostToDevice, s),
+                   "indexset table");
+  auto k = b200::detail::forall_indexset_kernel<BLOCK, B, T>;
+  const unsigned g = b200::detail::grid_for<b200::detail::forall_indexset_kernel<BLOCK, B, T>>(BLOCK, total);
+  B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
+  k<<<g, BLOCK, 0, s>>>(lb, d_desc, d_prefix, nseg, total);
+  b200::check_cuda(cudaGetLastError(), "b200 forall indexset");
+  b200::check_cuda(cudaFreeAsync(tbl, s), "indexset table");
+  if (!Async) b200::wait();
 }
 
 // ------------------------------------------------------ forall with params
@@ -1558,9 +1737,12 @@ namespace b200 {
 namespace detail {
 using wg_fn = void (*)(const void* body, long long begin, long long lo, long long hi);
 
+// One tile of one loop.  Every thread runs with its own copy of the body,
+// so captured b200 reducers accumulate privately; the copies' destructors
+// (all threads of the block, at the end of the tile) combine them.
 template <class Body>
 __device__ void wg_run(const void* body, long long begin, long long lo, long long hi) {
-  const Body& b = *static_cast<const Body*>(body);
+  const Body b(*static_cast<const Body*>(body));
   for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) b(Index_type(begin + i));
 }
 // Device address of wg_run<Body>, read once per loop-body type by a
@@ -1598,23 +1780,42 @@ struct WgTile {
   int loop;
   long long lo, hi;
 };
+constexpr int kWgItems = 8;  // elements per thread of one WorkGroup tile
+
+// All loops in one launch: block b runs tiles b, b + grid, ...
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
-wg_kernel(const WgTile* tiles, long long ntiles, const WgLoop* loops, const unsigned char* bodies) {
+wg_kernel(const WgTile* tiles, long long ntiles, const WgLoop* loops, const unsigned char* bodies,
+          unsigned char* results) {
+  constexpr long long TILE = (long long)BLOCK * kWgItems;
+  WgDevCtx& c = wg_dev_ctx();
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const WgTile tl = tiles[t];
     const WgLoop lp = loops[tl.loop];
+    if (threadIdx.x == 0) {
+      c.tile = tl.lo / TILE;
+      c.results = results;
+    }
+    __syncthreads();
     lp.fn(bodies + lp.body_off, lp.begin, tl.lo, tl.hi);
+    __syncthreads();
   }
 }
+// One loop per launch (the ordered runners): block b runs tile b.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
-wg_one_kernel(const WgLoop* loops, int which, const unsigned char* bodies) {
+wg_one_kernel(const WgLoop* loops, int which, const unsigned char* bodies, unsigned char* results) {
+  constexpr long long TILE = (long long)BLOCK * kWgItems;
   const WgLoop lp = loops[which];
-  const long long chunk = (lp.len + gridDim.x - 1) / gridDim.x;
-  const long long lo = (long long)blockIdx.x * chunk;
-  const long long hi = lo + chunk < lp.len ? lo + chunk : lp.len;
-  if (lo < hi) lp.fn(bodies + lp.body_off, lp.begin, lo, hi);
+  WgDevCtx& c = wg_dev_ctx();
+  if (threadIdx.x == 0) {
+    c.tile = blockIdx.x;
+    c.results = results;
+  }
+  __syncthreads();
+  const long long lo = (long long)blockIdx.x * TILE;
+  const long long hi = lo + TILE < lp.len ? lo + TILE : lp.len;
+  lp.fn(bodies + lp.body_off, lp.begin, lo, hi);
 }
 }  // namespace detail
 }  // namespace b200
@@ -1630,20 +1831,38 @@ class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH
   WorkPool() = default;
   template <typename A>
   explicit WorkPool(const A&) {}  // the allocator: device storage comes from cudaMalloc
+  // Loop bodies are device lambdas whose captures are plain data or b200
+  // reducers: the body is copied once here (captured b200 reducers take a
+  // slot of this loop in the pool, so their per-loop combine runs inside
+  // the group's launch) and its bytes move to device memory.
   template <typename T, typename Body>
   void enqueue(TypedRangeSegment<T> seg, Body body) {
-    static_assert(std::is_trivially_copyable<Body>::value,
-                  "b200_work loop bodies must be trivially copyable device lambdas");
+    static_assert(std::is_copy_constructible<Body>::value, "b200_work loop bodies are copied");
     // with plugins registered, the capture hooks bracket the body copy
     // (pattern/WorkGroup.hpp:287-296)
     const bool hooks = !util::PluginRegistry::empty();
     const util::PluginContext ctx(Platform::cuda, std::string());
     if (hooks) util::callPreCapturePlugins(ctx);
     const b200::detail::wg_fn fp = b200::detail::wg_fn_of<Body>();
+    const long long len = (long long)seg.size();
+    constexpr long long TILE = (long long)(BLOCK > 0 ? BLOCK : 256) * b200::detail::kWgItems;
+    b200::detail::WgCaptureCtx& w = b200::detail::wg_capture();
+    w.active = true;
+    w.reg = m_reg.get();
+    w.ntiles = (len + TILE - 1) / TILE;
+    ++w.capture_id;
+    alignas(Body) unsigned char raw[sizeof(Body)];
+    try {
+      ::new (raw) Body(body);  // the capture copy: stays as bytes, never destroyed
+    } catch (...) {
+      w.active = false;
+      throw;
+    }
+    w.active = false;
     const size_t off = (m_bytes.size() + 15) / 16 * 16;
     m_bytes.resize(off + sizeof(Body));
-    std::memcpy(m_bytes.data() + off, &body, sizeof(Body));
-    m_loops.push_back(b200::detail::WgLoop{fp, (long long)seg.b, (long long)seg.size(), off});
+    std::memcpy(m_bytes.data() + off, raw, sizeof(Body));
+    m_loops.push_back(b200::detail::WgLoop{fp, (long long)seg.b, len, off});
     if (hooks) util::callPostCapturePlugins(ctx);
   }
   void reserve(size_t n, size_t bytes) {
@@ -1656,6 +1875,7 @@ class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH
  private:
   std::vector<b200::detail::WgLoop> m_loops;
   std::vector<unsigned char> m_bytes;
+  std::shared_ptr<b200::detail::WgRegistry> m_reg = std::make_shared<b200::detail::WgRegistry>();
 };
 
 template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
@@ -1672,19 +1892,25 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
     std::swap(m_loops_off, o.m_loops_off);
     std::swap(m_tiles_off, o.m_tiles_off);
     std::swap(m_bodies_off, o.m_bodies_off);
+    std::swap(m_reg, o.m_reg);
     return *this;
   }
   ~WorkGroup() {
     if (m_dev) cudaFree(m_dev);
   }
-  // Upload loops, bodies and the tile table once (instantiate).
-  void setup(const std::vector<b200::detail::WgLoop>& loops, const std::vector<unsigned char>& bytes) {
-    constexpr long long TILE = (long long)BLOCK * 8;
+  // Upload loops, bodies and the tile table once (instantiate); the
+  // registry holds the slots of the reducers the bodies captured.
+  void setup(const std::vector<b200::detail::WgLoop>& loops, const std::vector<unsigned char>& bytes,
+             std::shared_ptr<b200::detail::WgRegistry> reg) {
+    m_reg = std::move(reg);
+    constexpr long long TILE = (long long)(BLOCK > 0 ? BLOCK : 256) * b200::detail::kWgItems;
     std::vector<b200::detail::WgTile> tiles;
     for (size_t i = 0; i < loops.size(); ++i)
       for (long long lo = 0; lo < loops[i].len; lo += TILE)
         tiles.push_back(b200::detail::WgTile{int(i), lo, lo + TILE < loops[i].len ? lo + TILE : loops[i].len});
     m_nloops = int(loops.size());
+    m_loop_len.clear();
+    for (const auto& l : loops) m_loop_len.push_back(l.len);
     m_ntiles = (long long)tiles.size();
     m_loops_off = 0;
     m_tiles_off = (loops.size() * sizeof(b200::detail::WgLoop) + 255) / 256 * 256;
@@ -1719,22 +1945,39 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
     auto* loops = reinterpret_cast<const b200::detail::WgLoop*>(d + m_loops_off);
     auto* tiles = reinterpret_cast<const b200::detail::WgTile*>(d + m_tiles_off);
     auto* bodies = reinterpret_cast<const unsigned char*>(d + m_bodies_off);
+    // this run's reducer results: mapped host memory that the last tile of
+    // each loop writes and the reducers read at get()
+    std::shared_ptr<void> results;
+    unsigned char* results_dev = nullptr;
+    const size_t nred = m_reg ? m_reg->deliver.size() : 0;
+    if (nred > 0) {
+      void* h = nullptr;
+      b200::check_cuda(cudaHostAlloc(&h, nred * b200::detail::kWgResultBytes, cudaHostAllocMapped),
+                       "WorkGroup results");
+      results = std::shared_ptr<void>(h, [](void* q) { cudaFreeHost(q); });
+      void* dp = nullptr;
+      b200::check_cuda(cudaHostGetDevicePointer(&dp, h, 0), "WorkGroup results");
+      results_dev = static_cast<unsigned char*>(dp);
+    }
+    constexpr int B = BLOCK > 0 ? BLOCK : 256;
+    constexpr long long TILE = (long long)B * b200::detail::kWgItems;
     if (std::is_same<ORDER, unordered>::value) {
       if (m_ntiles > 0) {
-        auto k = b200::detail::wg_kernel<BLOCK>;
-        const unsigned g = b200::detail::grid_for<b200::detail::wg_kernel<BLOCK>>(BLOCK, m_ntiles * BLOCK);
-        k<<<g, BLOCK, 0, s>>>(tiles, m_ntiles, loops, bodies);
+        auto k = b200::detail::wg_kernel<B>;
+        const unsigned g = b200::detail::grid_for<b200::detail::wg_kernel<B>>(B, m_ntiles * B);
+        k<<<g, B, 0, s>>>(tiles, m_ntiles, loops, bodies, results_dev);
       }
     } else {
-      // one launch per loop, in (reverse) enqueue order
-      auto k = b200::detail::wg_one_kernel<BLOCK>;
+      // one launch per loop, in (reverse) enqueue order: block b runs tile b
+      auto k = b200::detail::wg_one_kernel<B>;
       for (int i = 0; i < m_nloops; ++i) {
         const int which = std::is_same<ORDER, reverse_ordered>::value ? m_nloops - 1 - i : i;
-        const unsigned g = b200::detail::grid_for<b200::detail::wg_one_kernel<BLOCK>>(BLOCK, 1ll << 22);
-        k<<<g, BLOCK, 0, s>>>(loops, which, bodies);
+        const long long nt = (m_loop_len[which] + TILE - 1) / TILE;
+        if (nt > 0) k<<<unsigned(nt), B, 0, s>>>(loops, which, bodies, results_dev);
       }
     }
     b200::check_cuda(cudaGetLastError(), "WorkGroup run");
+    for (size_t r = 0; r < nred; ++r) m_reg->deliver[r](static_cast<const unsigned char*>(results.get()), results, s);
     if (!Async) b200::wait();
     if (hooks) util::callPostLaunchPlugins(ctx);
     return site;
@@ -1746,15 +1989,18 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
   int m_nloops = 0;
   long long m_ntiles = 0;
   size_t m_loops_off = 0, m_tiles_off = 0, m_bodies_off = 0;
+  std::vector<long long> m_loop_len;
+  std::shared_ptr<b200::detail::WgRegistry> m_reg;
 };
 
 template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
 typename WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc>::group_type
 WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc>::instantiate() {
   group_type g;
-  g.setup(m_loops, m_bytes);
+  g.setup(m_loops, m_bytes, m_reg);
   m_loops.clear();
   m_bytes.clear();
+  m_reg = std::make_shared<b200::detail::WgRegistry>();
   return g;
 }
 

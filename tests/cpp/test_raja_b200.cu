@@ -8,6 +8,7 @@
 // Prints one PASS/FAIL line per case; the exit status is the failure count.
 #include <chrono>
 #include <cstdio>
+#include <cmath>
 #include <cstdlib>
 #include <memory>
 #include <random>
@@ -392,6 +393,95 @@ void test_workgroup_reuse() {
   for (int i = 0; i < 2 * n; ++i) ok = ok && a[i] == (i < n ? 4 : 40);
   CHECK("workgroup_b200_dispatch_allocator_reuse", ok);
   cudaFree(a);
+}
+
+// Loops whose bodies capture ReduceSum / ReduceMinLoc on b200_reduce: the
+// batched-loops configuration (4096 loops, lognormal lengths with median
+// 2000 and sigma 1.5 clipped to [32, 2^20]), fp64 axpy plus one sum and one
+// MinLoc per loop, run twice.  The unordered runner combines each loop's
+// reducers inside its single launch (the reference's unordered CUDA runner
+// leaves reducers unsupported, policy/cuda/WorkGroup/WorkRunner.hpp:323-329);
+// the ordered runner launches the loops one by one.  Values are multiples of
+// 1/8 so sums are exact in any order: both must equal seq_exec loop by loop.
+template <class ORDER>
+void workgroup_reducers_case(const char* tag) {
+  std::mt19937 rng(41);
+  std::lognormal_distribution<double> ln(std::log(2000.0), 1.5);
+  const int nloops = 4096;
+  std::vector<Index_type> lens(nloops), offs(nloops + 1, 0);
+  for (int l = 0; l < nloops; ++l) {
+    double v = std::round(ln(rng));
+    v = v < 32 ? 32 : (v > double(1 << 20) ? double(1 << 20) : v);
+    lens[l] = Index_type(v);
+    offs[l + 1] = offs[l] + lens[l];
+  }
+  lens[7] = 0;  // an empty loop keeps its reducers' values
+  for (int l = 7; l < nloops; ++l) offs[l + 1] = offs[l] + lens[l];
+  const Index_type total = offs[nloops];
+  double* x = managed<double>(total);
+  double* y = managed<double>(total);
+  double* hy = managed<double>(total);
+  for (Index_type i = 0; i < total; ++i) {
+    x[i] = double(int(rng() % 257) - 128) / 8.0;
+    y[i] = hy[i] = double(int(rng() % 257) - 128) / 8.0;
+  }
+  using pool_t = RAJA::WorkPool<RAJA::WorkGroupPolicy<RAJA::b200_work<256>, ORDER>, Index_type>;
+  using hpool_t = RAJA::WorkPool<RAJA::WorkGroupPolicy<RAJA::seq_exec, RAJA::ordered>, Index_type>;
+  using dsum_t = RAJA::ReduceSum<RAJA::b200_reduce, double>;
+  using dloc_t = RAJA::ReduceMinLoc<RAJA::b200_reduce, double, Index_type>;
+  using hsum_t = RAJA::ReduceSum<RAJA::seq_reduce, double>;
+  using hloc_t = RAJA::ReduceMinLoc<RAJA::seq_reduce, double, Index_type>;
+  std::vector<std::unique_ptr<dsum_t>> ds;
+  std::vector<std::unique_ptr<dloc_t>> dl;
+  std::vector<std::unique_ptr<hsum_t>> hs;
+  std::vector<std::unique_ptr<hloc_t>> hl;
+  pool_t pool;
+  hpool_t hpool;
+  const double a = 0.5;
+  for (int l = 0; l < nloops; ++l) {
+    ds.emplace_back(new dsum_t(1.0));
+    dl.emplace_back(new dloc_t(1e300, -1));
+    hs.emplace_back(new hsum_t(1.0));
+    hl.emplace_back(new hloc_t(1e300, -1));
+    const dsum_t& s = *ds.back();
+    const dloc_t& m = *dl.back();
+    const hsum_t& hsr = *hs.back();
+    const hloc_t& hm = *hl.back();
+    pool.enqueue(RAJA::RangeSegment(offs[l], offs[l + 1]), [=] RAJA_DEVICE(Index_type i) {
+      y[i] += a * x[i];
+      s += y[i];
+      m.minloc(y[i], i);
+    });
+    hpool.enqueue(RAJA::RangeSegment(offs[l], offs[l + 1]), [=](Index_type i) {
+      hy[i] += a * x[i];
+      hsr += hy[i];
+      hm.minloc(hy[i], i);
+    });
+  }
+  auto g = pool.instantiate();
+  auto hg = hpool.instantiate();
+  g.run();
+  g.run();  // the reducers accumulate over both runs
+  hg.run();
+  hg.run();
+  bool ok = true;
+  int bad = -1;
+  for (int l = 0; l < nloops && ok; ++l) {
+    ok = ds[l]->get() == hs[l]->get() && dl[l]->get() == hl[l]->get() && dl[l]->getLoc() == hl[l]->getLoc();
+    if (!ok) bad = l;
+  }
+  for (Index_type i = 0; i < total && ok; ++i) ok = y[i] == hy[i];
+  char nm[128];
+  snprintf(nm, sizeof nm, "workgroup_%s_fused_reducers_%d_loops_%lld_elems%s", tag, nloops, (long long)total,
+           ok ? "" : " (first mismatch logged)");
+  if (bad >= 0)
+    printf("  loop %d: sum %.17g vs %.17g, minloc %.17g@%lld vs %.17g@%lld\n", bad, ds[bad]->get(),
+           hs[bad]->get(), dl[bad]->get(), (long long)dl[bad]->getLoc(), hl[bad]->get(),
+           (long long)hl[bad]->getLoc());
+  CHECK(nm, ok);
+  cudaFree(x);
+  cudaFree(y);
+  cudaFree(hy);
 }
 
 void test_multi_reduce_and_atomics() {
@@ -1383,6 +1473,8 @@ void perf_lambda_paths() {
 int main() {
   setvbuf(stdout, nullptr, _IONBF, 0);  // every PASS line reaches the log even if the run aborts
   test_workgroup_reuse();
+  workgroup_reducers_case<RAJA::unordered>("unordered");
+  workgroup_reducers_case<RAJA::ordered>("ordered");
   test_multi_reduce_and_atomics();
   test_reducers();
   test_forall_and_params();
