@@ -33,6 +33,7 @@
 #include <atomic>
 #include <cstring>
 #include <functional>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
@@ -180,7 +181,7 @@ constexpr size_t kWgResultBytes = 32;  // one result of a run per reducer
 struct WgCaptureCtx {
   bool active = false;
   WgRegistry* reg = nullptr;
-  long long ntiles = 0;               // tiles of the loop being captured
+  long long ntiles = 0;               // tiles of the loop being captured, at the smallest tile size
   unsigned long long capture_id = 0;  // new for every enqueue
 };
 inline WgCaptureCtx& wg_capture() {
@@ -188,20 +189,22 @@ inline WgCaptureCtx& wg_capture() {
   return c;
 }
 
-// Device side of a WorkGroup run: the tile of the loop a block is running
-// and where the run's per-reducer results go.  Set by the runner kernels
-// before each loop body runs.
+// Device side of a WorkGroup run: the tile of the loop a block is running,
+// the loop's tile count at this run's tile size, and where the run's
+// per-reducer results go.  Set by the runner kernels before each loop body
+// runs.
 struct WgDevCtx {
   long long tile;
+  long long ntiles;
   unsigned char* results;
 };
 
-// Grid for a kernel that always runs `block` threads: one block per `block`
-// elements, capped at the resident blocks of the whole GPU (the loop
-// grid-strides beyond that).  The occupancy query runs once per (kernel,
+// Grid for a kernel that always runs `block` threads: one block per
+// `block` x `items` elements, capped at the resident blocks of the whole
+// GPU (the loop grid-strides beyond that).  The occupancy query runs once per (kernel,
 // device), as RAJA's CUDA back-end caches it after the first launch.
 template <auto Kernel>
-inline unsigned grid_for(int block, long long len) {
+inline unsigned grid_for(int block, long long len, int items = 1) {
   static std::atomic<long long> resident[kMaxDevices] = {};
   const int dev = current_device_index();
   long long cap = resident[dev].load(std::memory_order_acquire);
@@ -211,7 +214,8 @@ inline unsigned grid_for(int block, long long len) {
     cap = (long long)sm_count() * (bps > 0 ? bps : 1);
     resident[dev].store(cap, std::memory_order_release);
   }
-  long long g = (len + block - 1) / block;
+  const long long per = (long long)block * (items > 0 ? items : 1);
+  long long g = (len + per - 1) / per;
   if (g > cap) g = cap;
   if (g < 1) g = 1;
   return unsigned(g);
@@ -541,7 +545,7 @@ class DevReducer {
     // likewise for the WorkGroup capture of one enqueued loop
     unsigned long long slot_capture = 0;
     DevSlot<V> wg_slot{nullptr, nullptr, nullptr};
-    long long wg_id = -1, wg_ntiles = 0;
+    long long wg_id = -1;
   };
   Shared* shared_ = nullptr;
   bool original_ = false;
@@ -549,7 +553,6 @@ class DevReducer {
   bool owner_ = false;
   bool wg_ = false;          // a WorkGroup loop's copy: tile-ordered combine
   long long wg_id_ = -1;     // index of this reducer in a run's results
-  long long wg_ntiles_ = 0;  // tiles of its loop
   DevSlot<V> slot_{nullptr, nullptr, nullptr};
   mutable V val_;
 
@@ -569,7 +572,6 @@ class DevReducer {
     owner_ = o.launch_copy_;
     wg_ = o.wg_;
     wg_id_ = o.wg_id_;
-    wg_ntiles_ = o.wg_ntiles_;
 #else
     shared_ = o.shared_;
     LaunchCtx& c = ctx();
@@ -588,7 +590,6 @@ class DevReducer {
         shared_->wg_slot = DevSlot<V>{static_cast<V*>(blk),
                                       reinterpret_cast<unsigned*>(static_cast<char*>(blk) + pbytes), nullptr};
         shared_->wg_id = (long long)w.reg->deliver.size();
-        shared_->wg_ntiles = w.ntiles;
         shared_->slot_capture = w.capture_id;
         Shared* sh = shared_;
         const long long id = shared_->wg_id;
@@ -603,7 +604,6 @@ class DevReducer {
       }
       slot_ = shared_->wg_slot;
       wg_id_ = shared_->wg_id;
-      wg_ntiles_ = shared_->wg_ntiles;
       wg_ = true;
       launch_copy_ = true;
     } else if (c.active && !o.launch_copy_) {
@@ -620,7 +620,6 @@ class DevReducer {
       launch_copy_ = o.launch_copy_;
       wg_ = o.wg_;
       wg_id_ = o.wg_id_;
-      wg_ntiles_ = o.wg_ntiles_;
     }
 #endif
   }
@@ -680,12 +679,12 @@ __device__ void DevReducer<K>::wg_combine(V v) const {
   if (lin_tid() == 0) {
     slot_.partials[c.tile] = v;
     __threadfence();
-    last = ::atomicAdd(slot_.ticket, 1u) == unsigned(wg_ntiles_ - 1);
+    last = ::atomicAdd(slot_.ticket, 1u) == unsigned(c.ntiles - 1);
   }
   __syncthreads();
   if (!last) return;
   __threadfence();
-  const V r = fold_partials(slot_.partials, unsigned(wg_ntiles_), merge);
+  const V r = fold_partials(slot_.partials, unsigned(c.ntiles), merge);
   if (lin_tid() == 0) {
     static_assert(sizeof(V) <= kWgResultBytes, "reducer value larger than a result slot");
     memcpy(c.results + wg_id_ * kWgResultBytes, &r, sizeof(V));
@@ -796,6 +795,284 @@ class ReduceMaxLoc<b200_reduce, T, I>
   void reset(T v, I l) { this->reset_value(typename K::V{v, l}); }
 };
 
+// ------------------------------------------------------------- autotuner
+// b200_exec<0> and b200_work<0> choose their launch shape (threads per
+// block, elements per thread) on line.  The first calls of a kernel -- per
+// device and per power-of-two size class for forall, per instantiated group
+// for WorkGroup -- cycle through the candidate shapes, each call bracketed
+// by a pair of CUDA events on its stream; once every candidate has
+// kSamples timings, the shape with the least time per element serves every
+// later call.  Every call does its whole work with the shape it is given,
+// so tuning never repeats or skips a loop body; floating-point reductions
+// may round differently from one shape to another until the choice is
+// made.  Calls made while their stream is being captured into a graph are
+// not timed (they take the best shape so far).  A fixed BLOCK > 0 is never
+// tuned.
+namespace b200 {
+namespace tune {
+
+struct Shape {
+  int block;
+  int items;
+};
+constexpr int kSamples = 3;
+// forall: the 256-thread, one-element-per-thread shape first (the default
+// until timings arrive)
+constexpr Shape kForallShapes[] = {{256, 1}, {128, 1}, {128, 4}, {256, 4}, {256, 16},
+                                   {512, 1}, {512, 4}, {1024, 1}, {1024, 4}};
+// WorkGroup tiles of block x items elements
+constexpr Shape kWorkShapes[] = {{256, 8}, {128, 2}, {128, 4}, {128, 8}, {128, 16}, {256, 2},
+                                 {256, 4}, {256, 16}, {512, 2}, {512, 4}, {512, 8}, {512, 16}};
+
+struct Report {
+  std::string name;
+  int device;
+  int size_class;  // floor(log2(elements)) for forall, -1 for a WorkGroup
+  bool settled;
+  Shape best;
+  int candidates;
+  int timed_calls;
+};
+
+class Tuner {
+ public:
+  struct Ticket {
+    int cand = 0;
+    cudaEvent_t start = nullptr, stop = nullptr;
+  };
+  Tuner(std::string name, int device, int size_class, const Shape* shapes, int n)
+      : name_(std::move(name)), device_(device), class_(size_class), shapes_(shapes, shapes + n),
+        samples_(n), inflight_(n, 0) {}
+  ~Tuner() {
+    for (auto& p : pending_) {
+      cudaEventDestroy(p.t.start);
+      cudaEventDestroy(p.t.stop);
+    }
+    for (cudaEvent_t e : free_) cudaEventDestroy(e);
+  }
+  Tuner(const Tuner&) = delete;
+  Tuner& operator=(const Tuner&) = delete;
+
+  Shape shape(int cand) const { return shapes_[size_t(cand)]; }
+
+  // The candidate for the next call, with its start event recorded when the
+  // call is to be timed.
+  Ticket begin(cudaStream_t s) {
+    std::lock_guard<std::mutex> g(m_);
+    harvest();
+    Ticket t;
+    if (best_ >= 0) {
+      t.cand = best_;
+      return t;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+      t.cand = best_so_far();
+      return t;
+    }
+    const int n = int(shapes_.size());
+    for (int k = 0; k < n; ++k) {
+      const int c = (next_ + k) % n;
+      if (int(samples_[size_t(c)].size()) + inflight_[size_t(c)] < kSamples) {
+        next_ = (c + 1) % n;
+        t.cand = c;
+        t.start = event();
+        t.stop = event();
+        check_cuda(cudaEventRecord(t.start, s), "b200 tuner event");
+        ++inflight_[size_t(c)];
+        return t;
+      }
+    }
+    t.cand = best_so_far();  // every candidate issued; timings still in flight
+    return t;
+  }
+  // After the call's launches: record the stop event of a timed call.
+  void end(Ticket& t, cudaStream_t s, long long work) {
+    if (!t.start) return;
+    std::lock_guard<std::mutex> g(m_);
+    const cudaError_t e = cudaEventRecord(t.stop, s);
+    if (e != cudaSuccess) {
+      --inflight_[size_t(t.cand)];
+      free_.push_back(t.start);
+      free_.push_back(t.stop);
+      check_cuda(e, "b200 tuner event");
+    }
+    pending_.push_back(Pending{t, work > 0 ? work : 1});
+    ++timed_;
+  }
+  // A call that threw between begin and end.
+  void abandon(Ticket& t) {
+    if (!t.start) return;
+    std::lock_guard<std::mutex> g(m_);
+    --inflight_[size_t(t.cand)];
+    free_.push_back(t.start);
+    free_.push_back(t.stop);
+  }
+  Report report() {
+    std::lock_guard<std::mutex> g(m_);
+    harvest();
+    const int b = best_ >= 0 ? best_ : best_so_far();
+    return Report{name_, device_, class_, best_ >= 0, shapes_[size_t(b)], int(shapes_.size()), timed_};
+  }
+
+ private:
+  struct Pending {
+    Ticket t;
+    long long work;
+  };
+  cudaEvent_t event() {
+    if (!free_.empty()) {
+      cudaEvent_t e = free_.back();
+      free_.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    check_cuda(cudaEventCreate(&e), "b200 tuner event");
+    return e;
+  }
+  // Collect the timings whose stop event has completed (never waits).
+  void harvest() {
+    for (size_t i = 0; i < pending_.size();) {
+      Pending& p = pending_[i];
+      const cudaError_t q = cudaEventQuery(p.t.stop);
+      if (q == cudaErrorNotReady) {
+        ++i;
+        continue;
+      }
+      float ms = 0.f;
+      if (q == cudaSuccess && cudaEventElapsedTime(&ms, p.t.start, p.t.stop) == cudaSuccess)
+        samples_[size_t(p.t.cand)].push_back(double(ms) / double(p.work));
+      else
+        (void)cudaGetLastError();  // a failed timing is dropped; the call reported its own errors
+      --inflight_[size_t(p.t.cand)];
+      free_.push_back(p.t.start);
+      free_.push_back(p.t.stop);
+      pending_[i] = pending_.back();
+      pending_.pop_back();
+    }
+    if (best_ >= 0) return;
+    for (const auto& v : samples_)
+      if (int(v.size()) < kSamples) return;
+    best_ = best_so_far();
+  }
+  // The candidate with the least time per element among those timed (the
+  // fastest of each candidate's samples), else the first.
+  int best_so_far() const {
+    int b = -1;
+    double bt = 0.0;
+    for (size_t c = 0; c < samples_.size(); ++c) {
+      if (samples_[c].empty()) continue;
+      const double t = *std::min_element(samples_[c].begin(), samples_[c].end());
+      if (b < 0 || t < bt) {
+        b = int(c);
+        bt = t;
+      }
+    }
+    return b < 0 ? 0 : b;
+  }
+
+  std::mutex m_;
+  std::string name_;
+  int device_, class_;
+  std::vector<Shape> shapes_;
+  std::vector<std::vector<double>> samples_;
+  std::vector<int> inflight_;
+  std::vector<Pending> pending_;
+  std::vector<cudaEvent_t> free_;
+  int best_ = -1, next_ = 0, timed_ = 0;
+};
+
+// Every tuner made so far, for reports.
+struct Registry {
+  std::mutex m;
+  std::vector<std::weak_ptr<Tuner>> all;
+};
+inline Registry& registry() {
+  static Registry* r = new Registry;  // outlives static tuners at exit
+  return *r;
+}
+inline std::shared_ptr<Tuner> make_tuner(std::string name, int device, int size_class, const Shape* shapes,
+                                         int n) {
+  auto t = std::make_shared<Tuner>(std::move(name), device, size_class, shapes, n);
+  Registry& r = registry();
+  std::lock_guard<std::mutex> g(r.m);
+  r.all.push_back(t);
+  return t;
+}
+// The state of every live tuner: its candidates, timed calls and the shape
+// it uses now (the chosen one once settled).
+inline std::vector<Report> reports() {
+  std::vector<std::shared_ptr<Tuner>> live;
+  {
+    Registry& r = registry();
+    std::lock_guard<std::mutex> g(r.m);
+    std::vector<std::weak_ptr<Tuner>> keep;
+    for (auto& w : r.all)
+      if (auto t = w.lock()) {
+        live.push_back(t);
+        keep.push_back(w);
+      }
+    r.all.swap(keep);
+  }
+  std::vector<Report> out;
+  for (auto& t : live) out.push_back(t->report());
+  return out;
+}
+
+inline int size_class(long long n) {
+  int c = 0;
+  while (c < 62 && (n >> (c + 1)) > 0) ++c;
+  return c;
+}
+// The tuner of one forall kernel family (Tag) for this device and size.
+template <class Tag>
+inline Tuner& forall_tuner(const char* name, long long len) {
+  static std::mutex m;
+  static std::map<std::pair<int, int>, std::shared_ptr<Tuner>>* tab =
+      new std::map<std::pair<int, int>, std::shared_ptr<Tuner>>;  // kept to exit
+  const int dev = current_device_index(), cls = size_class(len);
+  std::lock_guard<std::mutex> g(m);
+  auto& t = (*tab)[{dev, cls}];
+  if (!t) t = make_tuner(name, dev, cls, kForallShapes, int(sizeof(kForallShapes) / sizeof(kForallShapes[0])));
+  return *t;
+}
+
+template <class F>
+inline void with_block(int block, F&& f) {
+  switch (block) {
+    case 128: f(std::integral_constant<int, 128>{}); break;
+    case 512: f(std::integral_constant<int, 512>{}); break;
+    case 1024: f(std::integral_constant<int, 1024>{}); break;
+    default: f(std::integral_constant<int, 256>{}); break;
+  }
+}
+
+// Run launch(integral_constant<int, block>, items) with BLOCK's fixed shape
+// (one element per thread up to the resident grid), or, for BLOCK == 0,
+// with the shape that Tag's tuner gives this call.
+template <int BLOCK, class Tag, class F>
+inline void shaped_launch(const char* name, long long len, cudaStream_t s, F&& launch) {
+  if constexpr (BLOCK > 0) {
+    launch(std::integral_constant<int, BLOCK>{}, 1);
+  } else {
+    Tuner& t = forall_tuner<Tag>(name, len);
+    Tuner::Ticket tk = t.begin(s);
+    const Shape sh = t.shape(tk.cand);
+    try {
+      with_block(sh.block, [&](auto B) { launch(B, sh.items); });
+    } catch (...) {
+      t.abandon(tk);
+      throw;
+    }
+    t.end(tk, s, len);
+  }
+}
+template <int Family, class... Ts>
+struct Tag {};
+
+}  // namespace tune
+}  // namespace b200
+
 // ---------------------------------------------------------------- forall
 namespace b200 {
 namespace detail {
@@ -899,6 +1176,36 @@ struct LaunchCopy {
 template <bool Async>
 inline void finish(const char* what) {
   check_cuda(cudaGetLastError(), what);
+  if (!Async) wait();
+}
+
+// One launch over the segments of an IndexSet described by `desc` (kind
+// and parameters per segment) and `prefix` (their running lengths, nseg+1
+// entries): the table goes to launch-pool memory on the b200 stream and is
+// freed behind the launch.
+template <int BLOCK, bool Async, class Body, class T>
+void indexset_launch(const std::vector<SegDesc<T>>& desc, const std::vector<long long>& prefix, Body&& body) {
+  using B = std::decay_t<Body>;
+  const int nseg = int(desc.size());
+  const long long total = prefix[size_t(nseg)];
+  if (total == 0) return;
+  cudaStream_t s = stream();
+  const size_t db = ((nseg * sizeof(SegDesc<T>) + 255) / 256) * 256;
+  void* tbl = launch_alloc(db + (nseg + 1) * sizeof(long long), s, "indexset table");
+  auto* d_desc = static_cast<SegDesc<T>*>(tbl);
+  long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + db);
+  check_cuda(cudaMemcpyAsync(d_desc, desc.data(), nseg * sizeof(desc[0]), cudaMemcpyHostToDevice, s),
+             "indexset table");
+  check_cuda(cudaMemcpyAsync(d_prefix, prefix.data(), (nseg + 1) * sizeof(long long), cudaMemcpyHostToDevice, s),
+             "indexset table");
+  tune::shaped_launch<BLOCK, tune::Tag<3, B, T>>("forall indexset", total, s, [&](auto NB, int items) {
+    auto k = forall_indexset_kernel<NB(), B, T>;
+    const unsigned g = grid_for<forall_indexset_kernel<NB(), B, T>>(NB(), total, items);
+    B lb = LaunchCopy<B>::make(body, g, s);
+    k<<<g, NB(), 0, s>>>(lb, d_desc, d_prefix, nseg, total);
+  });
+  check_cuda(cudaGetLastError(), "b200 forall indexset");
+  check_cuda(cudaFreeAsync(tbl, s), "indexset table");
   if (!Async) wait();
 }
 
@@ -1102,11 +1409,13 @@ void forall_impl(b200_exec<BLOCK, Async>, const TypedRangeSegment<T>& r, Body&& 
   using B = std::decay_t<Body>;
   const long long len = (long long)stripIndexType(r.size());
   if (len <= 0) return;
-  auto k = b200::detail::forall_range_kernel<BLOCK, B, T>;
-  const unsigned g = b200::detail::grid_for<b200::detail::forall_range_kernel<BLOCK, B, T>>(BLOCK, len);
   cudaStream_t s = b200::stream();
-  B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
-  k<<<g, BLOCK, 0, s>>>(lb, r.b, len);
+  b200::tune::shaped_launch<BLOCK, b200::tune::Tag<0, B, T>>("forall range", len, s, [&](auto NB, int items) {
+    auto k = b200::detail::forall_range_kernel<NB(), B, T>;
+    const unsigned g = b200::detail::grid_for<b200::detail::forall_range_kernel<NB(), B, T>>(NB(), len, items);
+    B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
+    k<<<g, NB(), 0, s>>>(lb, r.b, len);
+  });
   b200::detail::finish<Async>("b200 forall");
 }
 template <int BLOCK, bool Async, class Body, class T>
@@ -1114,11 +1423,13 @@ void forall_impl(b200_exec<BLOCK, Async>, const TypedRangeStrideSegment<T>& r, B
   using B = std::decay_t<Body>;
   const long long len = (long long)stripIndexType(r.size());
   if (len <= 0) return;
-  auto k = b200::detail::forall_stride_kernel<BLOCK, B, T>;
-  const unsigned g = b200::detail::grid_for<b200::detail::forall_stride_kernel<BLOCK, B, T>>(BLOCK, len);
   cudaStream_t s = b200::stream();
-  B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
-  k<<<g, BLOCK, 0, s>>>(lb, r.b, r.s, len);
+  b200::tune::shaped_launch<BLOCK, b200::tune::Tag<1, B, T>>("forall strided", len, s, [&](auto NB, int items) {
+    auto k = b200::detail::forall_stride_kernel<NB(), B, T>;
+    const unsigned g = b200::detail::grid_for<b200::detail::forall_stride_kernel<NB(), B, T>>(NB(), len, items);
+    B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
+    k<<<g, NB(), 0, s>>>(lb, r.b, r.s, len);
+  });
   b200::detail::finish<Async>("b200 forall");
 }
 template <int BLOCK, bool Async, class Body, class T>
@@ -1126,11 +1437,13 @@ void forall_impl(b200_exec<BLOCK, Async>, const TypedListSegment<T>& l, Body&& b
   using B = std::decay_t<Body>;
   const long long len = (long long)l.size();
   if (len <= 0) return;
-  auto k = b200::detail::forall_list_kernel<BLOCK, B, T>;
-  const unsigned g = b200::detail::grid_for<b200::detail::forall_list_kernel<BLOCK, B, T>>(BLOCK, len);
   cudaStream_t s = b200::stream();
-  B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
-  k<<<g, BLOCK, 0, s>>>(lb, l.data, len);
+  b200::tune::shaped_launch<BLOCK, b200::tune::Tag<2, B, T>>("forall list", len, s, [&](auto NB, int items) {
+    auto k = b200::detail::forall_list_kernel<NB(), B, T>;
+    const unsigned g = b200::detail::grid_for<b200::detail::forall_list_kernel<NB(), B, T>>(NB(), len, items);
+    B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
+    k<<<g, NB(), 0, s>>>(lb, l.data, len);
+  });
   b200::detail::finish<Async>("b200 forall");
 }
 // IndexSet: one launch covers every segment, whatever the mix of range,
@@ -1165,7 +1478,6 @@ inline bool seg_desc(const Seg& g, SegDesc<T>* d, long long* len) {
 template <int BLOCK, bool Async, class Body, class... Segs>
 void forall_impl(b200_exec<BLOCK, Async> pol, const TypedIndexSet<Segs...>& is, Body&& body) {
   using T = typename TypedIndexSet<Segs...>::value_type;
-  using B = std::decay_t<Body>;
   const auto& segs = is.segments();
   const int nseg = int(segs.size());
   if (nseg == 0) return;
@@ -1182,25 +1494,7 @@ void forall_impl(b200_exec<BLOCK, Async> pol, const TypedIndexSet<Segs...>& is, 
     for (const auto& v : segs) std::visit([&](const auto& g) { forall_impl(pol, g, body); }, v);
     return;
   }
-  const long long total = prefix[nseg];
-  if (total == 0) return;
-  cudaStream_t s = b200::stream();
-  const size_t db = ((nseg * sizeof(b200::detail::SegDesc<T>) + 255) / 256) * 256;
-  void* tbl = b200::detail::launch_alloc(db + (nseg + 1) * sizeof(long long), s, "indexset table");
-  auto* d_desc = static_cast<b200::detail::SegDesc<T>*>(tbl);
-  long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + db);
-  b200::check_cuda(cudaMemcpyAsync(d_desc, desc.data(), nseg * sizeof(desc[0]), cudaMemcpyHostToDevice, s),
-                   "indexset table");
-  b200::check_cuda(cudaMemcpyAsync(d_prefix, prefix.data(), (nseg + 1) * sizeof(long long),
-                                   cudaMemcpyHostToDevice, s),
-                   "indexset table");
-  auto k = b200::detail::forall_indexset_kernel<BLOCK, B, T>;
-  const unsigned g = b200::detail::grid_for<b200::detail::forall_indexset_kernel<BLOCK, B, T>>(BLOCK, total);
-  B lb = b200::detail::LaunchCopy<B>::make(body, g, s);
-  k<<<g, BLOCK, 0, s>>>(lb, d_desc, d_prefix, nseg, total);
-  b200::check_cuda(cudaGetLastError(), "b200 forall indexset");
-  b200::check_cuda(cudaFreeAsync(tbl, s), "indexset table");
-  if (!Async) b200::wait();
+  b200::detail::indexset_launch<BLOCK, Async>(desc, prefix, std::forward<Body>(body));
 }
 
 // ------------------------------------------------------ forall with params
@@ -1295,14 +1589,17 @@ void forall_params_impl(b200_exec<BLOCK, Async>, const Seg& r, Body&& body, Red&
   using B = std::decay_t<Body>;
   using Slots = b200::detail::DTuple<b200::detail::DevSlot<typename b200::detail::ParamKind<Red>::type::V>...>;
   const long long len = (long long)::RAJA::detail::seg_len(r);
-  auto k = b200::detail::forall_params_kernel<BLOCK, B, Seg, Red...>;
-  const unsigned g =
-      b200::detail::grid_for<b200::detail::forall_params_kernel<BLOCK, B, Seg, Red...>>(BLOCK, len > 0 ? len : 1);
   cudaStream_t s = b200::stream();
   b200::detail::SlotMem mem[sizeof...(Red) + 1];
-  size_t bi = 0;
-  Slots slots{b200::detail::alloc_slot<typename b200::detail::ParamKind<Red>::type::V>(g, s, &mem[bi++])...};
-  k<<<g, BLOCK, 0, s>>>(body, r, len, slots);
+  b200::tune::shaped_launch<BLOCK, b200::tune::Tag<4, B, Seg, Red...>>(
+      "forall params", len > 0 ? len : 1, s, [&](auto NB, int items) {
+        auto k = b200::detail::forall_params_kernel<NB(), B, Seg, Red...>;
+        const unsigned g = b200::detail::grid_for<b200::detail::forall_params_kernel<NB(), B, Seg, Red...>>(
+            NB(), len > 0 ? len : 1, items);
+        size_t bi = 0;
+        Slots slots{b200::detail::alloc_slot<typename b200::detail::ParamKind<Red>::type::V>(g, s, &mem[bi++])...};
+        k<<<g, NB(), 0, s>>>(body, r, len, slots);
+      });
   b200::check_cuda(cudaGetLastError(), "b200 forall params");
   // param_resolve waits for the kernel, as the reference does
   const bool ok = resolve_params(mem, s, reds...);
@@ -1776,46 +2073,72 @@ struct WgLoop {
   long long len;
   size_t body_off;
 };
-struct WgTile {
-  int loop;
-  long long lo, hi;
-};
-constexpr int kWgItems = 8;  // elements per thread of one WorkGroup tile
+constexpr int kWgItems = 8;  // elements per thread of a fixed-BLOCK WorkGroup tile
 
-// All loops in one launch: block b runs tiles b, b + grid, ...
+// All loops in one launch over tiles of `tile` elements: prefix[l] is the
+// first tile of loop l (prefix[nloops] the tile count), and block b runs
+// tiles b, b + grid, ...; a tile finds its loop by binary search.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
-wg_kernel(const WgTile* tiles, long long ntiles, const WgLoop* loops, const unsigned char* bodies,
-          unsigned char* results) {
-  constexpr long long TILE = (long long)BLOCK * kWgItems;
+wg_kernel(const long long* prefix, int nloops, long long tile, const WgLoop* loops,
+          const unsigned char* bodies, unsigned char* results) {
   WgDevCtx& c = wg_dev_ctx();
+  const long long ntiles = prefix[nloops];
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const WgTile tl = tiles[t];
-    const WgLoop lp = loops[tl.loop];
+    int lo = 0, hi = nloops;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (prefix[mid] <= t) lo = mid;
+      else hi = mid;
+    }
+    const WgLoop lp = loops[lo];
+    const long long k = t - prefix[lo];
     if (threadIdx.x == 0) {
-      c.tile = tl.lo / TILE;
+      c.tile = k;
+      c.ntiles = prefix[lo + 1] - prefix[lo];
       c.results = results;
     }
     __syncthreads();
-    lp.fn(bodies + lp.body_off, lp.begin, tl.lo, tl.hi);
+    const long long a = k * tile;
+    lp.fn(bodies + lp.body_off, lp.begin, a, a + tile < lp.len ? a + tile : lp.len);
     __syncthreads();
   }
 }
 // One loop per launch (the ordered runners): block b runs tile b.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
-wg_one_kernel(const WgLoop* loops, int which, const unsigned char* bodies, unsigned char* results) {
-  constexpr long long TILE = (long long)BLOCK * kWgItems;
+wg_one_kernel(const WgLoop* loops, int which, long long tile, const unsigned char* bodies,
+              unsigned char* results) {
   const WgLoop lp = loops[which];
   WgDevCtx& c = wg_dev_ctx();
   if (threadIdx.x == 0) {
     c.tile = blockIdx.x;
+    c.ntiles = (lp.len + tile - 1) / tile;
     c.results = results;
   }
   __syncthreads();
-  const long long lo = (long long)blockIdx.x * TILE;
-  const long long hi = lo + TILE < lp.len ? lo + TILE : lp.len;
+  const long long lo = (long long)blockIdx.x * tile;
+  const long long hi = lo + tile < lp.len ? lo + tile : lp.len;
   lp.fn(bodies + lp.body_off, lp.begin, lo, hi);
+}
+// The tile shapes a b200_work<BLOCK> group runs with: BLOCK x kWgItems, or
+// for BLOCK == 0 the tuner's candidates.
+template <int BLOCK>
+inline std::vector<tune::Shape> wg_shapes() {
+  if constexpr (BLOCK > 0) {
+    return {tune::Shape{BLOCK, kWgItems}};
+  } else {
+    return std::vector<tune::Shape>(std::begin(tune::kWorkShapes), std::end(tune::kWorkShapes));
+  }
+}
+template <int BLOCK>
+inline long long wg_min_tile() {
+  long long m = 0;
+  for (const tune::Shape& sh : wg_shapes<BLOCK>()) {
+    const long long t = (long long)sh.block * sh.items;
+    if (m == 0 || t < m) m = t;
+  }
+  return m;
 }
 }  // namespace detail
 }  // namespace b200
@@ -1845,11 +2168,13 @@ class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH
     if (hooks) util::callPreCapturePlugins(ctx);
     const b200::detail::wg_fn fp = b200::detail::wg_fn_of<Body>();
     const long long len = (long long)seg.size();
-    constexpr long long TILE = (long long)(BLOCK > 0 ? BLOCK : 256) * b200::detail::kWgItems;
+    // reducer partials for the largest tile count any shape of this group
+    // can run with
+    const long long tile = b200::detail::wg_min_tile<BLOCK>();
     b200::detail::WgCaptureCtx& w = b200::detail::wg_capture();
     w.active = true;
     w.reg = m_reg.get();
-    w.ntiles = (len + TILE - 1) / TILE;
+    w.ntiles = (len + tile - 1) / tile;
     ++w.capture_id;
     alignas(Body) unsigned char raw[sizeof(Body)];
     try {
@@ -1888,45 +2213,64 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
   WorkGroup& operator=(WorkGroup&& o) noexcept {
     std::swap(m_dev, o.m_dev);
     std::swap(m_nloops, o.m_nloops);
-    std::swap(m_ntiles, o.m_ntiles);
     std::swap(m_loops_off, o.m_loops_off);
-    std::swap(m_tiles_off, o.m_tiles_off);
     std::swap(m_bodies_off, o.m_bodies_off);
+    std::swap(m_loop_len, o.m_loop_len);
+    std::swap(m_shapes, o.m_shapes);
+    std::swap(m_prefix_off, o.m_prefix_off);
+    std::swap(m_ntiles, o.m_ntiles);
+    std::swap(m_tuner, o.m_tuner);
     std::swap(m_reg, o.m_reg);
     return *this;
   }
   ~WorkGroup() {
     if (m_dev) cudaFree(m_dev);
   }
-  // Upload loops, bodies and the tile table once (instantiate); the
-  // registry holds the slots of the reducers the bodies captured.
+  // Upload loops, bodies and, per tile shape, the loops' first tiles once
+  // (instantiate); the registry holds the slots of the reducers the bodies
+  // captured.
   void setup(const std::vector<b200::detail::WgLoop>& loops, const std::vector<unsigned char>& bytes,
              std::shared_ptr<b200::detail::WgRegistry> reg) {
     m_reg = std::move(reg);
-    constexpr long long TILE = (long long)(BLOCK > 0 ? BLOCK : 256) * b200::detail::kWgItems;
-    std::vector<b200::detail::WgTile> tiles;
-    for (size_t i = 0; i < loops.size(); ++i)
-      for (long long lo = 0; lo < loops[i].len; lo += TILE)
-        tiles.push_back(b200::detail::WgTile{int(i), lo, lo + TILE < loops[i].len ? lo + TILE : loops[i].len});
     m_nloops = int(loops.size());
     m_loop_len.clear();
     for (const auto& l : loops) m_loop_len.push_back(l.len);
-    m_ntiles = (long long)tiles.size();
+    m_shapes = b200::detail::wg_shapes<BLOCK>();
+    auto round = [](size_t b) { return (b + 255) / 256 * 256; };
+    // one prefix table per shape: loop l's first tile, then the tile count
+    std::vector<long long> prefix;
+    m_prefix_off.clear();
+    m_ntiles.clear();
+    size_t off = round(loops.size() * sizeof(b200::detail::WgLoop));
+    for (const b200::tune::Shape& sh : m_shapes) {
+      const long long tile = (long long)sh.block * sh.items;
+      const size_t first = prefix.size();
+      long long acc = 0;
+      for (const auto& l : loops) {
+        prefix.push_back(acc);
+        acc += (l.len + tile - 1) / tile;
+      }
+      prefix.push_back(acc);
+      m_prefix_off.push_back(off + first * sizeof(long long));
+      m_ntiles.push_back(acc);
+    }
     m_loops_off = 0;
-    m_tiles_off = (loops.size() * sizeof(b200::detail::WgLoop) + 255) / 256 * 256;
-    m_bodies_off = m_tiles_off + (tiles.size() * sizeof(b200::detail::WgTile) + 255) / 256 * 256;
+    m_bodies_off = round(off + prefix.size() * sizeof(long long));
     const size_t total = m_bodies_off + bytes.size() + 16;
     b200::check_cuda(cudaMalloc(&m_dev, total), "WorkGroup storage");
     char* d = static_cast<char*>(m_dev);
     if (!loops.empty())
       b200::check_cuda(cudaMemcpy(d + m_loops_off, loops.data(), loops.size() * sizeof(loops[0]),
                                   cudaMemcpyHostToDevice), "WorkGroup loops");
-    if (!tiles.empty())
-      b200::check_cuda(cudaMemcpy(d + m_tiles_off, tiles.data(), tiles.size() * sizeof(tiles[0]),
-                                  cudaMemcpyHostToDevice), "WorkGroup tiles");
+    if (!prefix.empty())
+      b200::check_cuda(cudaMemcpy(d + off, prefix.data(), prefix.size() * sizeof(long long), cudaMemcpyHostToDevice),
+                       "WorkGroup tiles");
     if (!bytes.empty())
       b200::check_cuda(cudaMemcpy(d + m_bodies_off, bytes.data(), bytes.size(), cudaMemcpyHostToDevice),
                        "WorkGroup bodies");
+    if (m_shapes.size() > 1)
+      m_tuner = b200::tune::make_tuner("WorkGroup", b200::current_device_index(), -1, m_shapes.data(),
+                                       int(m_shapes.size()));
   }
   using resource_type = resources::Cuda;
   WorkSite<policy, Index, xargs<>, Alloc> run() { return run(resource_type::get_default()); }
@@ -1943,7 +2287,6 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
     cudaStream_t s = b200::stream();
     char* d = static_cast<char*>(m_dev);
     auto* loops = reinterpret_cast<const b200::detail::WgLoop*>(d + m_loops_off);
-    auto* tiles = reinterpret_cast<const b200::detail::WgTile*>(d + m_tiles_off);
     auto* bodies = reinterpret_cast<const unsigned char*>(d + m_bodies_off);
     // this run's reducer results: mapped host memory that the last tile of
     // each loop writes and the reducers read at get()
@@ -1959,37 +2302,64 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
       b200::check_cuda(cudaHostGetDevicePointer(&dp, h, 0), "WorkGroup results");
       results_dev = static_cast<unsigned char*>(dp);
     }
-    constexpr int B = BLOCK > 0 ? BLOCK : 256;
-    constexpr long long TILE = (long long)B * b200::detail::kWgItems;
-    if (std::is_same<ORDER, unordered>::value) {
-      if (m_ntiles > 0) {
-        auto k = b200::detail::wg_kernel<B>;
-        const unsigned g = b200::detail::grid_for<b200::detail::wg_kernel<B>>(B, m_ntiles * B);
-        k<<<g, B, 0, s>>>(tiles, m_ntiles, loops, bodies, results_dev);
-      }
-    } else {
-      // one launch per loop, in (reverse) enqueue order: block b runs tile b
-      auto k = b200::detail::wg_one_kernel<B>;
-      for (int i = 0; i < m_nloops; ++i) {
-        const int which = std::is_same<ORDER, reverse_ordered>::value ? m_nloops - 1 - i : i;
-        const long long nt = (m_loop_len[which] + TILE - 1) / TILE;
-        if (nt > 0) k<<<unsigned(nt), B, 0, s>>>(loops, which, bodies, results_dev);
-      }
+    // the tile shape of this run: the fixed one, or the tuner's
+    b200::tune::Tuner::Ticket tk;
+    if (m_tuner) tk = m_tuner->begin(s);
+    const size_t si = size_t(tk.cand);
+    const b200::tune::Shape sh = m_shapes[si];
+    const long long tile = (long long)sh.block * sh.items;
+    auto* prefix = reinterpret_cast<const long long*>(d + m_prefix_off[si]);
+    try {
+      b200::tune::with_block(sh.block, [&](auto NB) {
+        if (std::is_same<ORDER, unordered>::value) {
+          if (m_ntiles[si] > 0) {
+            auto k = b200::detail::wg_kernel<NB()>;
+            const unsigned g = b200::detail::grid_for<b200::detail::wg_kernel<NB()>>(NB(), m_ntiles[si] * NB());
+            k<<<g, NB(), 0, s>>>(prefix, m_nloops, tile, loops, bodies, results_dev);
+          }
+        } else {
+          // one launch per loop, in (reverse) enqueue order: block b runs tile b
+          auto k = b200::detail::wg_one_kernel<NB()>;
+          for (int i = 0; i < m_nloops; ++i) {
+            const int which = std::is_same<ORDER, reverse_ordered>::value ? m_nloops - 1 - i : i;
+            const long long nt = (m_loop_len[which] + tile - 1) / tile;
+            if (nt > 0) k<<<unsigned(nt), NB(), 0, s>>>(loops, which, tile, bodies, results_dev);
+          }
+        }
+      });
+      b200::check_cuda(cudaGetLastError(), "WorkGroup run");
+    } catch (...) {
+      if (m_tuner) m_tuner->abandon(tk);
+      throw;
     }
-    b200::check_cuda(cudaGetLastError(), "WorkGroup run");
-    for (size_t r = 0; r < nred; ++r) m_reg->deliver[r](static_cast<const unsigned char*>(results.get()), results, s);
+    if (m_tuner) {
+      long long elems = 0;
+      for (long long l : m_loop_len) elems += l;
+      m_tuner->end(tk, s, elems);
+    }
+    for (size_t q = 0; q < nred; ++q) m_reg->deliver[q](static_cast<const unsigned char*>(results.get()), results, s);
     if (!Async) b200::wait();
     if (hooks) util::callPostLaunchPlugins(ctx);
     return site;
   }
   void clear() {}
+  // The tuner's state for a b200_work<0> group (candidates, timed runs, the
+  // shape in use); a fixed BLOCK reports its one shape as settled.
+  b200::tune::Report tuning() const {
+    if (m_tuner) return m_tuner->report();
+    const b200::tune::Shape sh = m_shapes.empty() ? b200::tune::Shape{BLOCK, b200::detail::kWgItems} : m_shapes[0];
+    return b200::tune::Report{"WorkGroup", -1, -1, true, sh, 1, 0};
+  }
 
  private:
   void* m_dev = nullptr;
   int m_nloops = 0;
-  long long m_ntiles = 0;
-  size_t m_loops_off = 0, m_tiles_off = 0, m_bodies_off = 0;
+  size_t m_loops_off = 0, m_bodies_off = 0;
   std::vector<long long> m_loop_len;
+  std::vector<b200::tune::Shape> m_shapes;
+  std::vector<size_t> m_prefix_off;  // per shape
+  std::vector<long long> m_ntiles;   // per shape
+  std::shared_ptr<b200::tune::Tuner> m_tuner;
   std::shared_ptr<b200::detail::WgRegistry> m_reg;
 };
 

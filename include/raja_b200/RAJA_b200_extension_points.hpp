@@ -12,6 +12,10 @@
 //   forall_impl(resources::Cuda, ExecPolicy<seq_segit, b200_exec<B, A>>,
 //               const TypedIndexSet<...>&, LoopBody&&)
 //                                    policy/cuda/forall.hpp:675-692
+//   wrap::forall(Res, ExecPolicy<seq_segit, b200_exec<B, A>>,
+//               const TypedIndexSet<...>&, LoopBody, ForallParams)
+//               (the front-end's IndexSet dispatch, pattern/forall.hpp:
+//               279-299): one launch over every segment
 //   impl::scan::{inclusive_inplace, exclusive_inplace, inclusive, exclusive}
 //               (resources::Cuda, b200_exec<B, A>, ...)
 //                                    policy/cuda/scan.hpp:45-235
@@ -189,6 +193,25 @@ RAJA_INLINE resources::EventProxy<resources::Cuda> unstable_pairs(resources::Cud
 
 }  // namespace RAJA
 
+// ---- forall over an IndexSet.  RAJA's front-end hands IndexSet policies
+// to wrap::forall by qualified name (pattern/forall.hpp:383-417), whose
+// generic form runs one forall per segment (pattern/forall.hpp:279-299), as
+// the CUDA back-end's IndexSet forall_impl does (policy/cuda/forall.hpp:
+// 675-706).  This more specialised overload, declared before RAJA's
+// front-end, runs every range, strided and list segment in one launch; it
+// is defined at the end of this header.
+#include "RAJA/index/IndexSet.hpp"
+#include "RAJA/policy/sequential/policy.hpp"
+
+namespace RAJA {
+namespace wrap {
+template <typename Res, int BLOCK, bool Async, typename... SegmentTypes, typename LoopBody, typename ForallParams>
+resources::EventProxy<Res> forall(Res r, ExecPolicy<seq_segit, b200_exec<BLOCK, Async>>,
+                                  const TypedIndexSet<SegmentTypes...>& iset, LoopBody loop_body,
+                                  ForallParams f_params);
+}  // namespace wrap
+}  // namespace RAJA
+
 // ---------------------------------------------------------------------------
 // RAJA itself, then the overloads that need its front-end types.
 #include "RAJA/RAJA.hpp"
@@ -309,12 +332,15 @@ template <int BLOCK, bool Async, class Iter, class Body, class... R, size_t... I
 void forall_ref_params(const b200_exec<BLOCK, Async>& pol, Iter begin, long long len, Body&& body,
                        std::index_sequence<I...>, R&... reds) {
   using B = std::decay_t<Body>;
-  auto k = forall_ref_params_kernel<BLOCK, B, Iter, R...>;
   ParamLaunchInfo<sizeof...(R)> info;
-  info.grid = grid_for<forall_ref_params_kernel<BLOCK, B, Iter, R...>>(BLOCK, len > 0 ? len : 1);
   info.stream = stream();
-  DTuple<RefSlot<R>...> slots{param_init(pol, reds, info)...};
-  k<<<info.grid, BLOCK, 0, info.stream>>>(body, begin, len, slots);
+  tune::shaped_launch<BLOCK, tune::Tag<5, B, Iter, R...>>(
+      "forall params", len > 0 ? len : 1, info.stream, [&](auto NB, int items) {
+        auto k = forall_ref_params_kernel<NB(), B, Iter, R...>;
+        info.grid = grid_for<forall_ref_params_kernel<NB(), B, Iter, R...>>(NB(), len > 0 ? len : 1, items);
+        DTuple<RefSlot<R>...> slots{param_init(pol, reds, info)...};
+        k<<<info.grid, NB(), 0, info.stream>>>(body, begin, len, slots);
+      });
   check_cuda(cudaGetLastError(), "b200 forall params");
   // param_resolve waits for the launch, as the reference's does
   const uint32_t* status = nullptr;
@@ -367,11 +393,14 @@ forall_impl(resources::Cuda cuda_res, b200_exec<BLOCK, Async> const& pol, Iterab
   b200::detail::ResourceStream bound(cuda_res.get_stream());
   if (len > 0) {
     if constexpr (expt::type_traits::is_ForallParamPack_empty<ForallParam>::value) {
-      auto k = b200::detail::forall_iter_kernel<BLOCK, B, Iterator>;
-      const unsigned g = b200::detail::grid_for<b200::detail::forall_iter_kernel<BLOCK, B, Iterator>>(BLOCK, len);
       cudaStream_t s = b200::stream();
-      B lb = b200::detail::LaunchCopy<B>::make(loop_body, g, s);
-      k<<<g, BLOCK, 0, s>>>(lb, begin, len);
+      b200::tune::shaped_launch<BLOCK, b200::tune::Tag<6, B, Iterator>>("forall", len, s, [&](auto NB, int items) {
+        auto k = b200::detail::forall_iter_kernel<NB(), B, Iterator>;
+        const unsigned g =
+            b200::detail::grid_for<b200::detail::forall_iter_kernel<NB(), B, Iterator>>(NB(), len, items);
+        B lb = b200::detail::LaunchCopy<B>::make(loop_body, g, s);
+        k<<<g, NB(), 0, s>>>(lb, begin, len);
+      });
       b200::detail::finish<Async>("b200 forall");
     } else {
       b200::detail::forall_ref_dispatch_params(pol, begin, len, std::forward<LoopBody>(loop_body),
@@ -382,19 +411,95 @@ forall_impl(resources::Cuda cuda_res, b200_exec<BLOCK, Async> const& pol, Iterab
   return resources::EventProxy<resources::Cuda>(cuda_res);
 }
 
-// ---- IndexSet segments, one after another (policy/cuda/forall.hpp:675-692)
+// ---- IndexSet segments in one launch
+namespace b200 {
+namespace detail {
+
+// Kind and parameters of one segment of RAJA's (range, strided, list);
+// false for another segment type.
+template <class T>
+struct RefSegDesc {
+  template <class Seg>
+  void operator()(const Seg& g, SegDesc<T>* d, long long* len, bool* ok) const {
+    using G = std::decay_t<Seg>;
+    *len = (long long)g.size();
+    if constexpr (std::is_same<G, TypedRangeSegment<T>>::value) {
+      *d = SegDesc<T>{0, *g.begin(), T(1), nullptr};
+    } else if constexpr (std::is_same<G, TypedRangeStrideSegment<T>>::value) {
+      const T step = *len > 1 ? T(*(g.begin() + 1) - *g.begin()) : T(1);
+      *d = SegDesc<T>{1, *g.begin(), step, nullptr};
+    } else if constexpr (std::is_same<G, TypedListSegment<T>>::value) {
+      *d = SegDesc<T>{2, T(0), T(0), g.begin()};
+    } else {
+      *ok = false;
+    }
+  }
+};
+
+// Whether a ForallParamPack holds reducers (a kernel name alone does not).
+template <class FP>
+constexpr bool has_reducer_params() {
+  if constexpr (expt::type_traits::is_ForallParamPack_empty<FP>::value) {
+    return false;
+  } else {
+    using R = decltype(::RAJA::expt::detail::filter_reducers(std::declval<FP&>().param_tup));
+    return camp::tuple_size<std::decay_t<R>>::value > 0;
+  }
+}
+
+template <class Res>
+inline cudaStream_t res_stream(Res& r) {
+  if constexpr (std::is_same<std::decay_t<Res>, camp::resources::Cuda>::value) return r.get_stream();
+  else return stream();
+}
+
+// Every segment in one launch on the resource's stream; IndexSets with
+// another segment type, or with reducer params, run per segment.
+template <int BLOCK, bool Async, class Res, class LoopBody, class ForallParams, class... SegmentTypes>
+void ref_indexset_forall(Res& r, const TypedIndexSet<SegmentTypes...>& iset, LoopBody&& loop_body,
+                         ForallParams f_params) {
+  using T = typename TypedIndexSet<SegmentTypes...>::value_type;
+  const int nseg = int(iset.getNumSegments());
+  std::vector<SegDesc<T>> desc(size_t(nseg > 0 ? nseg : 0));
+  std::vector<long long> prefix(size_t(nseg) + 1, 0);
+  bool ok = !has_reducer_params<ForallParams>();
+  for (int i = 0; i < nseg && ok; ++i) {
+    long long len = 0;
+    iset.segmentCall(size_t(i), RefSegDesc<T>{}, &desc[size_t(i)], &len, &ok);
+    prefix[size_t(i) + 1] = prefix[size_t(i)] + len;
+  }
+  ResourceStream bound(res_stream(r));
+  if (ok) {
+    if (nseg > 0) indexset_launch<BLOCK, Async>(desc, prefix, std::forward<LoopBody>(loop_body));
+    return;
+  }
+  for (int i = 0; i < nseg; ++i)
+    iset.segmentCall(size_t(i), ::RAJA::detail::CallForall{}, b200_exec<BLOCK, true>(), loop_body, r, f_params);
+  if (!Async) wait();
+}
+
+}  // namespace detail
+}  // namespace b200
+
+// the CUDA back-end's extension point (policy/cuda/forall.hpp:675-692)
 template <typename LoopBody, int BLOCK, bool Async, typename... SegmentTypes>
 RAJA_INLINE resources::EventProxy<resources::Cuda> forall_impl(
     resources::Cuda r, ExecPolicy<seq_segit, b200_exec<BLOCK, Async>>,
     const TypedIndexSet<SegmentTypes...>& iset, LoopBody&& loop_body) {
-  const int num_seg = iset.getNumSegments();
-  for (int isi = 0; isi < num_seg; ++isi)
-    iset.segmentCall(r, isi, detail::CallForall(), b200_exec<BLOCK, true>(), loop_body);
-  if (!Async) {
-    b200::detail::ResourceStream bound(r.get_stream());
-    b200::wait();
-  }
+  b200::detail::ref_indexset_forall<BLOCK, Async>(r, iset, std::forward<LoopBody>(loop_body),
+                                                  expt::ForallParamPack<>());
   return resources::EventProxy<resources::Cuda>(r);
 }
+
+// the front-end's IndexSet dispatch (declared before RAJA/RAJA.hpp)
+namespace wrap {
+template <typename Res, int BLOCK, bool Async, typename... SegmentTypes, typename LoopBody, typename ForallParams>
+resources::EventProxy<Res> forall(Res r, ExecPolicy<seq_segit, b200_exec<BLOCK, Async>>,
+                                  const TypedIndexSet<SegmentTypes...>& iset, LoopBody loop_body,
+                                  ForallParams f_params) {
+  b200::detail::ref_indexset_forall<BLOCK, Async>(r, iset, std::move(loop_body), f_params);
+  return resources::EventProxy<Res>(r);
+}
+}  // namespace wrap
 
 }  // namespace RAJA

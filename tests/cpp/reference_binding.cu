@@ -90,13 +90,16 @@ Results<ExecPol, RedPol> run(const std::vector<double>& x0, const std::vector<in
                                    RAJA::operators::greater<int>{});
   r.keys.assign(k, k + n);
   r.vals.assign(v, v + n);
-  // IndexSet: a range and a list segment
-  RAJA::TypedIndexSet<RAJA::TypedRangeSegment<RAJA::Index_type>, RAJA::TypedListSegment<RAJA::Index_type>> is;
-  is.push_back(RAJA::TypedRangeSegment<RAJA::Index_type>(0, n / 2));
+  // IndexSet: a range, a list and a strided segment
+  RAJA::TypedIndexSet<RAJA::TypedRangeSegment<RAJA::Index_type>, RAJA::TypedListSegment<RAJA::Index_type>,
+                      RAJA::TypedRangeStrideSegment<RAJA::Index_type>>
+      is;
+  is.push_back(RAJA::TypedRangeSegment<RAJA::Index_type>(0, n / 4));
   std::vector<RAJA::Index_type> odd;
   for (RAJA::Index_type i = n / 2 + 1; i < n; i += 2) odd.push_back(i);
   camp::resources::Resource res = RAJA::resources::get_resource<ExecPol>::type::get_default();
   is.push_back(RAJA::TypedListSegment<RAJA::Index_type>(odd.data(), odd.size(), res));
+  is.push_back(RAJA::TypedRangeStrideSegment<RAJA::Index_type>(n / 4, n / 2, 3));
   RAJA::forall<RAJA::ExecPolicy<RAJA::seq_segit, ExecPol>>(
       is, [=] APP_HOST_DEVICE(RAJA::Index_type i) { z[i] = y[i] * 2.0; });
   r.iset.assign(z, z + n);
@@ -139,6 +142,15 @@ int main()
   cudaMallocManaged(&v, n * sizeof(int));
   auto dev = run<RAJA::b200_exec<256>, RAJA::b200_reduce>(x0, k0, x, y, a, b, k, v, z);
   cudaDeviceSynchronize();
+  // the same application with its launch shape tuned on line (BLOCK 0),
+  // run enough times for the tuners to cycle through their shapes
+  bool tuned_ok = true;
+  for (int rep = 0; rep < 30; ++rep) {
+    auto t = run<RAJA::b200_exec<0>, RAJA::b200_reduce>(x0, k0, x, y, a, b, k, v, z);
+    cudaDeviceSynchronize();
+    tuned_ok = tuned_ok && t.incl == dev.incl && t.excl == dev.excl && t.keys == dev.keys && t.vals == dev.vals &&
+               t.iset == dev.iset && t.minv == dev.minv && t.minloc == dev.minloc;
+  }
   double tol = 4.0 * n * 1.1102230246251565e-16 * 4.0 * n;
   bool y_ok = true;
   for (RAJA::Index_type i = 0; i < n; ++i)
@@ -151,6 +163,7 @@ int main()
   check(dev.incl == seq.incl, "inclusive_scan<b200_exec>");
   check(dev.excl == seq.excl, "exclusive_scan_inplace<b200_exec>(maximum)");
   check(dev.keys == seq.keys && dev.vals == seq.vals, "stable_sort_pairs<b200_exec>(greater)");
-  check(y_ok, "forall over an IndexSet (range + list) on ExecPolicy<seq_segit, b200_exec>");
+  check(y_ok, "forall over an IndexSet (range + list + strided) on ExecPolicy<seq_segit, b200_exec>");
+  check(tuned_ok, "the same application on b200_exec<0> (launch shape tuned on line)");
   return failures ? 1 : 0;
 }

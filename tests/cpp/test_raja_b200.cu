@@ -484,6 +484,90 @@ void workgroup_reducers_case(const char* tag) {
   cudaFree(hy);
 }
 
+// b200_exec<0> / b200_work<0>: the launch shape is tuned on line.  Every
+// call must be right whatever shape it runs with, and the tuners settle
+// once each candidate has been timed.
+void test_autotune() {
+  const Index_type n = (Index_type(1) << 20) + 3;
+  double* x = managed<double>(n);
+  double* y = managed<double>(n);
+  long long hx = 0;
+  for (Index_type i = 0; i < n; ++i) {
+    x[i] = double(i % 17);
+    y[i] = 0.0;
+    hx += (long long)(i % 17);
+  }
+  using tuned = RAJA::b200_exec<0>;
+  const int calls = 40;
+  bool sums_ok = true, params_ok = true;
+  for (int c = 0; c < calls; ++c) {
+    RAJA::forall<tuned>(RAJA::RangeSegment(0, n), [=] RAJA_DEVICE(Index_type i) { y[i] += x[i]; });
+    RAJA::ReduceSum<red, long long> s(5);
+    RAJA::forall<tuned>(RAJA::RangeSegment(0, n), [=] RAJA_DEVICE(Index_type i) { s += (long long)x[i]; });
+    sums_ok = sums_ok && s.get() == hx + 5;
+    double ps = 1.0;
+    RAJA::forall<tuned>(RAJA::RangeSegment(0, n), RAJA::expt::Reduce<RAJA::operators::plus>(&ps),
+                        [=] RAJA_DEVICE(Index_type i, RAJA::expt::ValOp<double, RAJA::operators::plus>& v) {
+                          v += x[i];
+                        });
+    params_ok = params_ok && ps == double(hx) + 1.0;
+  }
+  bool y_ok = true;
+  for (Index_type i = 0; i < n && y_ok; ++i) y_ok = y[i] == double(calls) * x[i];
+  CHECK("autotuned_forall_every_call_exact", y_ok);
+  CHECK("autotuned_forall_reducer_every_call_exact", sums_ok);
+  CHECK("autotuned_forall_params_every_call_exact", params_ok);
+  int settled = 0, seen = 0;
+  for (const auto& r : RAJA::b200::tune::reports()) {
+    if (r.size_class != 20) continue;
+    ++seen;
+    printf("  tuner %s class 2^%d: %s, %d candidates, %d timed, shape %d x %d\n", r.name.c_str(), r.size_class,
+           r.settled ? "settled" : "tuning", r.candidates, r.timed_calls, r.best.block, r.best.items);
+    settled += r.settled ? 1 : 0;
+  }
+  CHECK("autotuned_forall_tuners_settle", seen >= 3 && settled == seen);
+
+  // WorkGroup: 600 uneven loops with fused reducers, the tile shape tuned
+  // over the runs; integer-valued data keeps every sum exact
+  std::mt19937 rng(5);
+  std::lognormal_distribution<double> ln(std::log(2000.0), 1.5);
+  const int nloops = 600;
+  std::vector<Index_type> offs(nloops + 1, 0);
+  for (int l = 0; l < nloops; ++l) {
+    double v = std::round(ln(rng));
+    v = v < 32 ? 32 : (v > double(1 << 18) ? double(1 << 18) : v);
+    offs[l + 1] = offs[l] + Index_type(v);
+  }
+  const Index_type total = offs[nloops];
+  double* w = managed<double>(total);
+  for (Index_type i = 0; i < total; ++i) w[i] = double(int(rng() % 33) - 16);
+  using pool_t = RAJA::WorkPool<RAJA::WorkGroupPolicy<RAJA::b200_work<0>, RAJA::unordered>, Index_type>;
+  std::vector<std::unique_ptr<RAJA::ReduceSum<red, double>>> ds;
+  std::vector<double> expect(nloops, 0.0);
+  pool_t pool;
+  for (int l = 0; l < nloops; ++l) {
+    ds.emplace_back(new RAJA::ReduceSum<red, double>(0.0));
+    const RAJA::ReduceSum<red, double>& s = *ds.back();
+    for (Index_type i = offs[l]; i < offs[l + 1]; ++i) expect[l] += w[i];
+    pool.enqueue(RAJA::RangeSegment(offs[l], offs[l + 1]), [=] RAJA_DEVICE(Index_type i) { s += w[i]; });
+  }
+  auto g = pool.instantiate();
+  const int runs = 12 * 3 + 4;
+  bool wg_ok = true;
+  for (int r = 0; r < runs; ++r) {
+    g.run();
+    for (int l = 0; l < nloops && wg_ok; ++l) wg_ok = ds[l]->get() == double(r + 1) * expect[l];
+  }
+  const RAJA::b200::tune::Report rep = g.tuning();
+  printf("  WorkGroup tuner: %s, %d candidates, %d timed, tile %d x %d\n", rep.settled ? "settled" : "tuning",
+         rep.candidates, rep.timed_calls, rep.best.block, rep.best.items);
+  CHECK("autotuned_workgroup_reducers_every_run_exact", wg_ok);
+  CHECK("autotuned_workgroup_settles", rep.settled && rep.candidates == 12);
+  cudaFree(x);
+  cudaFree(y);
+  cudaFree(w);
+}
+
 void test_multi_reduce_and_atomics() {
   const Index_type n = 200003;
   const int nb = 37;
@@ -1475,6 +1559,7 @@ int main() {
   test_workgroup_reuse();
   workgroup_reducers_case<RAJA::unordered>("unordered");
   workgroup_reducers_case<RAJA::ordered>("ordered");
+  test_autotune();
   test_multi_reduce_and_atomics();
   test_reducers();
   test_forall_and_params();
