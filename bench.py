@@ -511,7 +511,7 @@ def main():
         torch.cuda.empty_cache()
         for nm, fn in (("forall_daxpy_dot", bench_forall_dot),
                        ("batched_workgroup_4096_loops", bench_batched), ("jacobi_256_meshes", bench_jacobi),
-                       ("indexset_10000_segments", bench_indexset),
+                       ("raja_api_indexset_workgroup", bench_raja_api),
                        ("accuracy_ill_conditioned", bench_accuracy)):
             try:
                 extras[nm] = fn(lib)
@@ -1003,18 +1003,21 @@ def bench_cub(inputs, outs, n, stream, reps):
     return res
 
 
-def bench_indexset(lib):
-    """forall over an IndexSet of 10,000 Pareto(1.5) segments on the b200
-    policies: one launch for the whole set against one launch per segment
-    (all-range sets and sets mixing range, strided and list segments).  The
-    lambda bodies are C++ (tests/cpp/bench_indexset.cu), built here with
-    nvcc against the library."""
+def bench_raja_api(lib):
+    """The batched forms through the RAJA API on the b200 policies: forall
+    over an IndexSet of 10,000 Pareto(1.5) segments (one launch for the
+    whole set against one launch per segment; all-range sets and sets mixing
+    range, strided and list segments), and a WorkGroup of 4096 lognormal
+    loops with per-loop ReduceSum<b200_reduce, float> (one unordered run,
+    fixed and tuned shape, against the ordered one-launch-per-loop run).
+    The lambda bodies are C++ (tests/cpp/bench_raja_api.cu), built here
+    with nvcc against the library."""
     import raja_gb300.build as b
     lib_path = b.build()
     out_dir = os.path.join(b.BUILD)
     os.makedirs(out_dir, exist_ok=True)
-    exe = os.path.join(out_dir, "bench_indexset")
-    src = os.path.join(ROOT, "tests", "cpp", "bench_indexset.cu")
+    exe = os.path.join(out_dir, "bench_raja_api")
+    src = os.path.join(ROOT, "tests", "cpp", "bench_raja_api.cu")
     if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(src), os.path.getmtime(lib_path)):
         cmd = [b.nvcc(), "-std=c++17", "--extended-lambda", "--expt-relaxed-constexpr", "-O2", *b.ARCH,
                f"-I{ROOT}/include/raja_compat", f"-I{ROOT}/include", src, "-o", exe,
@@ -1022,10 +1025,10 @@ def bench_indexset(lib):
                f"-rpath={os.path.dirname(lib_path)}"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError("bench_indexset build failed: " + r.stderr[-500:])
+            raise RuntimeError("bench_raja_api build failed: " + r.stderr[-500:])
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     if r.returncode != 0:
-        raise RuntimeError("bench_indexset failed: " + (r.stdout + r.stderr)[-500:])
+        raise RuntimeError("bench_raja_api failed: " + (r.stdout + r.stderr)[-500:])
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 

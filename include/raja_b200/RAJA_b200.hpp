@@ -165,22 +165,66 @@ inline LaunchCtx& ctx() {
 
 // WorkGroup capture (host): while a b200 WorkPool copies an enqueued loop
 // body, each captured b200 reducer gets a slot for that loop -- one
-// partial per tile of the loop, a ticket, and an index into the results
-// of a run -- recorded in the pool's registry.  The registry also delivers
-// each run's results to the reducers (pending reads, folded by get()).
+// partial per tile of the loop and a ticket, in device memory -- and an
+// accumulator cell in mapped pinned memory, into which the last tile of
+// every run folds the loop's result (runs fold in stream order, so no host
+// work is needed per run).  The pool's registry owns both and records the
+// streams that runs went to; a reducer's get() waits for those streams and
+// reads its cell.
+constexpr size_t kWgCellBytes = 32;  // value (at most 24 bytes), then a "has a value" word at byte 28
 struct WgRegistry {
-  std::vector<void*> blocks;  // device memory of the slots (freed with the group)
-  std::vector<std::function<void(const unsigned char* results_host, const std::shared_ptr<void>& keep,
-                                 cudaStream_t s)>>
-      deliver;  // one per reducer, in slot index order
+  std::vector<void*> blocks;       // device memory of the slots
+  std::vector<void*> host_blocks;  // mapped pinned memory of the cells
+  unsigned char* cell_host = nullptr;
+  unsigned char* cell_dev = nullptr;
+  size_t cells_left = 0;
+  std::mutex m;
+  std::vector<cudaStream_t> streams;  // streams with runs not yet waited for
+  WgRegistry() = default;
+  WgRegistry(const WgRegistry&) = delete;
+  WgRegistry& operator=(const WgRegistry&) = delete;
   ~WgRegistry() {
     for (void* b : blocks) cudaFree(b);
+    for (void* b : host_blocks) cudaFreeHost(b);
+  }
+  // A zeroed cell (host and device addresses), from 64 KB pinned chunks.
+  void new_cell(unsigned char** host, unsigned char** dev) {
+    std::lock_guard<std::mutex> g(m);
+    if (cells_left == 0) {
+      constexpr size_t chunk = 65536;
+      void* h = nullptr;
+      check_cuda(cudaHostAlloc(&h, chunk, cudaHostAllocMapped), "WorkGroup reducer cells");
+      host_blocks.push_back(h);
+      void* d = nullptr;
+      check_cuda(cudaHostGetDevicePointer(&d, h, 0), "WorkGroup reducer cells");
+      std::memset(h, 0, chunk);
+      cell_host = static_cast<unsigned char*>(h);
+      cell_dev = static_cast<unsigned char*>(d);
+      cells_left = chunk / kWgCellBytes;
+    }
+    *host = cell_host;
+    *dev = cell_dev;
+    cell_host += kWgCellBytes;
+    cell_dev += kWgCellBytes;
+    --cells_left;
+  }
+  void ran_on(cudaStream_t s) {
+    std::lock_guard<std::mutex> g(m);
+    if (std::find(streams.begin(), streams.end(), s) == streams.end()) streams.push_back(s);
+  }
+  // Wait for every run issued so far.
+  void wait_runs() {
+    std::vector<cudaStream_t> ss;
+    {
+      std::lock_guard<std::mutex> g(m);
+      ss.swap(streams);
+    }
+    for (cudaStream_t s : ss) check_cuda(cudaStreamSynchronize(s), "WorkGroup reducer wait");
   }
 };
-constexpr size_t kWgResultBytes = 32;  // one result of a run per reducer
 struct WgCaptureCtx {
   bool active = false;
-  WgRegistry* reg = nullptr;
+  std::shared_ptr<WgRegistry> reg;
   long long ntiles = 0;               // tiles of the loop being captured, at the smallest tile size
   unsigned long long capture_id = 0;  // new for every enqueue
 };
@@ -189,14 +233,12 @@ inline WgCaptureCtx& wg_capture() {
   return c;
 }
 
-// Device side of a WorkGroup run: the tile of the loop a block is running,
-// the loop's tile count at this run's tile size, and where the run's
-// per-reducer results go.  Set by the runner kernels before each loop body
-// runs.
+// Device side of a WorkGroup run: the tile of the loop a block is running
+// and the loop's tile count at this run's tile size.  Set by the runner
+// kernels before each loop body runs.
 struct WgDevCtx {
   long long tile;
   long long ntiles;
-  unsigned char* results;
 };
 
 // Grid for a kernel that always runs `block` threads: one block per
@@ -532,7 +574,6 @@ class DevReducer {
   struct Pending {
     SlotMem mem;
     cudaStream_t stream;
-    std::shared_ptr<void> keep;  // a WorkGroup run's results (cell not pooled)
   };
   struct Shared {
     V init;
@@ -545,21 +586,22 @@ class DevReducer {
     // likewise for the WorkGroup capture of one enqueued loop
     unsigned long long slot_capture = 0;
     DevSlot<V> wg_slot{nullptr, nullptr, nullptr};
-    long long wg_id = -1;
+    // the WorkGroup accumulator cells this reducer folds at get()
+    std::vector<unsigned char*> wg_cells;
+    std::vector<std::shared_ptr<WgRegistry>> wg_regs;
   };
   Shared* shared_ = nullptr;
   bool original_ = false;
   bool launch_copy_ = false;
   bool owner_ = false;
-  bool wg_ = false;          // a WorkGroup loop's copy: tile-ordered combine
-  long long wg_id_ = -1;     // index of this reducer in a run's results
+  bool wg_ = false;  // a WorkGroup loop's copy: tile-ordered combine
   DevSlot<V> slot_{nullptr, nullptr, nullptr};
   mutable V val_;
 
   // The tile-ordered combine of a WorkGroup loop's reducer: every tile
   // publishes its block's partial; the block that completes the loop's tile
-  // count folds the partials in tile order (deterministic) and writes the
-  // run's result.
+  // count folds the partials in tile order (deterministic) and folds the
+  // run's result into the reducer's accumulator cell.
   __device__ void wg_combine(V v) const;
 
  public:
@@ -571,7 +613,6 @@ class DevReducer {
     slot_ = o.slot_;
     owner_ = o.launch_copy_;
     wg_ = o.wg_;
-    wg_id_ = o.wg_id_;
 #else
     shared_ = o.shared_;
     LaunchCtx& c = ctx();
@@ -586,24 +627,21 @@ class DevReducer {
         void* blk = nullptr;
         check_cuda(cudaMalloc(&blk, pbytes + 256), "WorkGroup reducer slot");
         check_cuda(cudaMemset(static_cast<char*>(blk) + pbytes, 0, sizeof(unsigned)), "WorkGroup reducer ticket");
-        w.reg->blocks.push_back(blk);
+        {
+          std::lock_guard<std::mutex> g(w.reg->m);
+          w.reg->blocks.push_back(blk);
+        }
+        unsigned char *cell_host = nullptr, *cell_dev = nullptr;
+        w.reg->new_cell(&cell_host, &cell_dev);
         shared_->wg_slot = DevSlot<V>{static_cast<V*>(blk),
-                                      reinterpret_cast<unsigned*>(static_cast<char*>(blk) + pbytes), nullptr};
-        shared_->wg_id = (long long)w.reg->deliver.size();
+                                      reinterpret_cast<unsigned*>(static_cast<char*>(blk) + pbytes),
+                                      reinterpret_cast<V*>(cell_dev)};
+        shared_->wg_cells.push_back(cell_host);
+        if (std::find(shared_->wg_regs.begin(), shared_->wg_regs.end(), w.reg) == shared_->wg_regs.end())
+          shared_->wg_regs.push_back(w.reg);
         shared_->slot_capture = w.capture_id;
-        Shared* sh = shared_;
-        const long long id = shared_->wg_id;
-        w.reg->deliver.push_back([sh, id](const unsigned char* res, const std::shared_ptr<void>& keep,
-                                          cudaStream_t s) {
-          Pending p;
-          p.mem.cell.host = const_cast<unsigned char*>(res + id * kWgResultBytes);
-          p.stream = s;
-          p.keep = keep;
-          sh->pending.push_back(p);
-        });
       }
       slot_ = shared_->wg_slot;
-      wg_id_ = shared_->wg_id;
       wg_ = true;
       launch_copy_ = true;
     } else if (c.active && !o.launch_copy_) {
@@ -619,7 +657,6 @@ class DevReducer {
       slot_ = o.slot_;
       launch_copy_ = o.launch_copy_;
       wg_ = o.wg_;
-      wg_id_ = o.wg_id_;
     }
 #endif
   }
@@ -644,9 +681,11 @@ class DevReducer {
 
   B200_HOST_DEVICE void combine(const V& v) const { val_ = K::merge(val_, v); }
 
-  // Fold the pending launch results into init, in launch order.
-  // One synchronisation per stream with pending launches (other streams are
-  // not waited for); the results are then read from their host cells.
+  // Fold the pending launch results into init, in launch order, then the
+  // accumulator cells of WorkGroup loops that captured this reducer.  One
+  // synchronisation per stream with pending launches or runs (other
+  // streams are not waited for); the results are then read from their host
+  // cells.
   V fold() const {
     if (!shared_) return V{};
     std::vector<Pending>& pend = shared_->pending;
@@ -658,10 +697,19 @@ class DevReducer {
     }
     for (const Pending& p : pend) {
       shared_->init = K::fold_init(shared_->init, read_cell<V>(p.mem.cell));
-      if (!p.keep) release_cell(p.mem.cell);
+      release_cell(p.mem.cell);
       if (p.mem.block) cudaFreeAsync(p.mem.block, p.stream);
     }
     pend.clear();
+    for (const auto& r : shared_->wg_regs) r->wait_runs();
+    for (unsigned char* c : shared_->wg_cells) {
+      volatile unsigned* has = reinterpret_cast<volatile unsigned*>(c + 28);
+      if (*has == 0u) continue;
+      V v;
+      std::memcpy(&v, c, sizeof(V));
+      shared_->init = K::fold_init(shared_->init, v);
+      *has = 0u;  // folded: the next run starts the cell afresh
+    }
     return shared_->init;
   }
   void reset_value(V v) {
@@ -686,8 +734,19 @@ __device__ void DevReducer<K>::wg_combine(V v) const {
   __threadfence();
   const V r = fold_partials(slot_.partials, unsigned(c.ntiles), merge);
   if (lin_tid() == 0) {
-    static_assert(sizeof(V) <= kWgResultBytes, "reducer value larger than a result slot");
-    memcpy(c.results + wg_id_ * kWgResultBytes, &r, sizeof(V));
+    static_assert(sizeof(V) <= 24, "reducer value larger than a WorkGroup cell");
+    // the cell is mapped host memory; runs of one group fold in stream order
+    unsigned char* cell = reinterpret_cast<unsigned char*>(slot_.result);
+    volatile unsigned* has = reinterpret_cast<volatile unsigned*>(cell + 28);
+    V acc = r;
+    if (*has != 0u) {
+      V prev;
+      memcpy(&prev, cell, sizeof(V));
+      acc = merge(prev, r);
+    }
+    memcpy(cell, &acc, sizeof(V));
+    __threadfence_system();
+    *has = 1u;
     *slot_.ticket = 0u;  // ready for the next run
   }
 }
@@ -2081,7 +2140,7 @@ constexpr int kWgItems = 8;  // elements per thread of a fixed-BLOCK WorkGroup t
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
 wg_kernel(const long long* prefix, int nloops, long long tile, const WgLoop* loops,
-          const unsigned char* bodies, unsigned char* results) {
+          const unsigned char* bodies) {
   WgDevCtx& c = wg_dev_ctx();
   const long long ntiles = prefix[nloops];
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -2096,7 +2155,6 @@ wg_kernel(const long long* prefix, int nloops, long long tile, const WgLoop* loo
     if (threadIdx.x == 0) {
       c.tile = k;
       c.ntiles = prefix[lo + 1] - prefix[lo];
-      c.results = results;
     }
     __syncthreads();
     const long long a = k * tile;
@@ -2107,14 +2165,12 @@ wg_kernel(const long long* prefix, int nloops, long long tile, const WgLoop* loo
 // One loop per launch (the ordered runners): block b runs tile b.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
-wg_one_kernel(const WgLoop* loops, int which, long long tile, const unsigned char* bodies,
-              unsigned char* results) {
+wg_one_kernel(const WgLoop* loops, int which, long long tile, const unsigned char* bodies) {
   const WgLoop lp = loops[which];
   WgDevCtx& c = wg_dev_ctx();
   if (threadIdx.x == 0) {
     c.tile = blockIdx.x;
     c.ntiles = (lp.len + tile - 1) / tile;
-    c.results = results;
   }
   __syncthreads();
   const long long lo = (long long)blockIdx.x * tile;
@@ -2173,7 +2229,7 @@ class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH
     const long long tile = b200::detail::wg_min_tile<BLOCK>();
     b200::detail::WgCaptureCtx& w = b200::detail::wg_capture();
     w.active = true;
-    w.reg = m_reg.get();
+    w.reg = m_reg;
     w.ntiles = (len + tile - 1) / tile;
     ++w.capture_id;
     alignas(Body) unsigned char raw[sizeof(Body)];
@@ -2181,9 +2237,11 @@ class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH
       ::new (raw) Body(body);  // the capture copy: stays as bytes, never destroyed
     } catch (...) {
       w.active = false;
+      w.reg.reset();
       throw;
     }
     w.active = false;
+    w.reg.reset();
     const size_t off = (m_bytes.size() + 15) / 16 * 16;
     m_bytes.resize(off + sizeof(Body));
     std::memcpy(m_bytes.data() + off, raw, sizeof(Body));
@@ -2288,20 +2346,6 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
     char* d = static_cast<char*>(m_dev);
     auto* loops = reinterpret_cast<const b200::detail::WgLoop*>(d + m_loops_off);
     auto* bodies = reinterpret_cast<const unsigned char*>(d + m_bodies_off);
-    // this run's reducer results: mapped host memory that the last tile of
-    // each loop writes and the reducers read at get()
-    std::shared_ptr<void> results;
-    unsigned char* results_dev = nullptr;
-    const size_t nred = m_reg ? m_reg->deliver.size() : 0;
-    if (nred > 0) {
-      void* h = nullptr;
-      b200::check_cuda(cudaHostAlloc(&h, nred * b200::detail::kWgResultBytes, cudaHostAllocMapped),
-                       "WorkGroup results");
-      results = std::shared_ptr<void>(h, [](void* q) { cudaFreeHost(q); });
-      void* dp = nullptr;
-      b200::check_cuda(cudaHostGetDevicePointer(&dp, h, 0), "WorkGroup results");
-      results_dev = static_cast<unsigned char*>(dp);
-    }
     // the tile shape of this run: the fixed one, or the tuner's
     b200::tune::Tuner::Ticket tk;
     if (m_tuner) tk = m_tuner->begin(s);
@@ -2315,7 +2359,7 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
           if (m_ntiles[si] > 0) {
             auto k = b200::detail::wg_kernel<NB()>;
             const unsigned g = b200::detail::grid_for<b200::detail::wg_kernel<NB()>>(NB(), m_ntiles[si] * NB());
-            k<<<g, NB(), 0, s>>>(prefix, m_nloops, tile, loops, bodies, results_dev);
+            k<<<g, NB(), 0, s>>>(prefix, m_nloops, tile, loops, bodies);
           }
         } else {
           // one launch per loop, in (reverse) enqueue order: block b runs tile b
@@ -2323,7 +2367,7 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
           for (int i = 0; i < m_nloops; ++i) {
             const int which = std::is_same<ORDER, reverse_ordered>::value ? m_nloops - 1 - i : i;
             const long long nt = (m_loop_len[which] + tile - 1) / tile;
-            if (nt > 0) k<<<unsigned(nt), NB(), 0, s>>>(loops, which, tile, bodies, results_dev);
+            if (nt > 0) k<<<unsigned(nt), NB(), 0, s>>>(loops, which, tile, bodies);
           }
         }
       });
@@ -2337,7 +2381,8 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
       for (long long l : m_loop_len) elems += l;
       m_tuner->end(tk, s, elems);
     }
-    for (size_t q = 0; q < nred; ++q) m_reg->deliver[q](static_cast<const unsigned char*>(results.get()), results, s);
+    // reducers captured by the loops read their cells after this stream
+    if (m_reg) m_reg->ran_on(s);
     if (!Async) b200::wait();
     if (hooks) util::callPostLaunchPlugins(ctx);
     return site;
