@@ -1,10 +1,11 @@
 // raja_compat -- a minimal RAJA-API front-end (namespace RAJA) for builds
 // where RAJA itself is not available.
 //
-// The reference's own headers cannot be compiled without its camp and BLT
-// submodules, so this header restates the small part of RAJA's front-end
-// that the data-parallel primitive path uses, with the reference's
-// semantics:
+// RAJA's own headers need its camp library and a CMake-generated config,
+// which an application may not have.  This header restates the small part
+// of RAJA's front-end that the data-parallel primitive path uses, with the
+// reference's semantics (its host policies reproduce RAJA's own seq / omp
+// results bit for bit on the shared fixtures):
 //
 //   forall / forall with expt params       pattern/forall.hpp:323-652
 //   Reduce{Sum,Min,Max,MinLoc,MaxLoc,
