@@ -398,7 +398,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--log2n", type=int, default=28)
     ap.add_argument("--cpu-log2n", type=int, default=28)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cub", action="store_true")
@@ -1106,7 +1106,11 @@ def run_e2e(args, lib, inputs, outs, n, stream, table, dist):
     The copies run on two copy streams and overlap the primitives: each
     primitive waits for its own inputs only, its outputs are copied back as
     soon as it finishes, and events keep a buffer from being overwritten
-    while the previous step still reads it or copies it back."""
+    while an earlier step still reads it or copies it back.  Steps alternate
+    between two sets of device buffers, so one step's inputs stream in while
+    the step before it still computes and copies its results out (the host
+    link carries both directions at once: 343 GB/s together, against 211
+    GB/s in and 194 GB/s out alone)."""
     import torch
     keys_in = ["f32", "f64", "scan_in", "u32", "u64", "pk", "pv", "z256", "z65536"]
     host = {k: torch.empty(inputs[k].shape, dtype=inputs[k].dtype, pin_memory=True)
@@ -1119,20 +1123,25 @@ def run_e2e(args, lib, inputs, outs, n, stream, table, dist):
                 for k in out_keys}
     h2d = sum(host[k].numel() * host[k].element_size() for k in keys_in)
     d2h = sum(host_out[k].numel() * host_out[k].element_size() for k in out_keys)
-    calls = dict(step_calls(lib, inputs, outs, n, stream.cuda_stream))
+    inputs2 = {k: torch.empty_like(inputs[k]) for k in keys_in}
+    outs2 = {k: torch.empty_like(outs[k]) for k in out_keys}
+    sets = [(inputs, outs, dict(step_calls(lib, inputs, outs, n, stream.cuda_stream))),
+            (inputs2, outs2, dict(step_calls(lib, inputs2, outs2, n, stream.cuda_stream)))]
     last_out = {}                       # output key -> index of its last writer
     for i, (_, _, os_) in enumerate(E2E_PLAN):
         for k in os_:
             last_out[k] = i
     h2d_s, d2h_s = torch.cuda.Stream(), torch.cuda.Stream()
-    state = {"in_free": {}, "out_free": {}}
+    states = [{"in_free": {}, "out_free": {}}, {"in_free": {}, "out_free": {}}]
 
     def ev(s):
         e = torch.cuda.Event()
         e.record(s)
         return e
 
-    def one(start=None):
+    def one(step, start=None):
+        inputs, outs, calls = sets[step % 2]
+        state = states[step % 2]
         in_free, out_free = state["in_free"], state["out_free"]
         ready = {}
         if start is not None:
@@ -1167,14 +1176,15 @@ def run_e2e(args, lib, inputs, outs, n, stream, table, dist):
                     nxt_out[k] = ev(d2h_s)
         state["in_free"], state["out_free"] = nxt_in, nxt_out
 
-    one()
+    one(0)
+    one(1)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)
     for i in range(args.e2e_steps):
-        one(start=a if i == 0 else None)
+        one(i, start=a if i == 0 else None)
     stream.wait_stream(d2h_s)
     stream.wait_stream(h2d_s)
     b.record(stream)
@@ -1186,7 +1196,8 @@ def run_e2e(args, lib, inputs, outs, n, stream, table, dist):
             "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
             "ms_per_step": round(ms / args.e2e_steps, 3),
             "path": "pinned host -> device copies (copy stream), C-ABI calls, device -> pinned "
-                    "host copies (second copy stream), overlapped per primitive"}
+                    "host copies (second copy stream), overlapped per primitive; steps alternate "
+                    "between two sets of device buffers"}
 
 
 def run_cpu_baseline(args):
