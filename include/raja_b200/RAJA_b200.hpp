@@ -168,9 +168,9 @@ inline LaunchCtx& ctx() {
 // partial per tile of the loop and a ticket, in device memory -- and an
 // accumulator cell in mapped pinned memory, into which the last tile of
 // every run folds the loop's result (runs fold in stream order, so no host
-// work is needed per run).  The pool's registry owns both and records the
-// streams that runs went to; a reducer's get() waits for those streams and
-// reads its cell.
+// work is needed per run).  The pool's registry owns both and records an
+// event behind the last run on each stream; a reducer's get() waits for
+// those events and reads its cell.
 constexpr size_t kWgCellBytes = 32;  // value (at most 24 bytes), then a "has a value" word at byte 28
 struct WgRegistry {
   std::vector<void*> blocks;       // device memory of the slots
@@ -179,13 +179,21 @@ struct WgRegistry {
   unsigned char* cell_dev = nullptr;
   size_t cells_left = 0;
   std::mutex m;
-  std::vector<cudaStream_t> streams;  // streams with runs not yet waited for
+  // per stream a run went to: an event recorded behind its last run, and
+  // whether that run has been waited for
+  struct RunMark {
+    cudaStream_t stream;
+    cudaEvent_t event;
+    bool pending;
+  };
+  std::vector<RunMark> marks;
   WgRegistry() = default;
   WgRegistry(const WgRegistry&) = delete;
   WgRegistry& operator=(const WgRegistry&) = delete;
   ~WgRegistry() {
     for (void* b : blocks) cudaFree(b);
     for (void* b : host_blocks) cudaFreeHost(b);
+    for (const RunMark& r : marks) cudaEventDestroy(r.event);
   }
   // A zeroed cell (host and device addresses), from 64 KB pinned chunks.
   void new_cell(unsigned char** host, unsigned char** dev) {
@@ -208,18 +216,27 @@ struct WgRegistry {
     cell_dev += kWgCellBytes;
     --cells_left;
   }
+  // After a run's launches on stream s (the events outlive the stream).
   void ran_on(cudaStream_t s) {
     std::lock_guard<std::mutex> g(m);
-    if (std::find(streams.begin(), streams.end(), s) == streams.end()) streams.push_back(s);
+    auto it = std::find_if(marks.begin(), marks.end(), [s](const RunMark& r) { return r.stream == s; });
+    if (it == marks.end()) {
+      cudaEvent_t e = nullptr;
+      check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "WorkGroup run event");
+      marks.push_back(RunMark{s, e, false});
+      it = marks.end() - 1;
+    }
+    check_cuda(cudaEventRecord(it->event, s), "WorkGroup run event");
+    it->pending = true;
   }
   // Wait for every run issued so far.
   void wait_runs() {
-    std::vector<cudaStream_t> ss;
-    {
-      std::lock_guard<std::mutex> g(m);
-      ss.swap(streams);
+    std::lock_guard<std::mutex> g(m);
+    for (RunMark& r : marks) {
+      if (!r.pending) continue;
+      check_cuda(cudaEventSynchronize(r.event), "WorkGroup reducer wait");
+      r.pending = false;
     }
-    for (cudaStream_t s : ss) check_cuda(cudaStreamSynchronize(s), "WorkGroup reducer wait");
   }
 };
 struct WgCaptureCtx {

@@ -851,6 +851,37 @@ void test_resources() {
     CHECK("resource_workgroup_run", ok);
     dev.deallocate(a);
   }
+  // WorkGroup reducers across runs on two streams, read after the group and
+  // one of the resources are gone: get() waits for both streams' runs
+  {
+    const int n = 3000;
+    int* a = nullptr;
+    cudaMallocManaged(&a, n * sizeof(int));
+    for (int i = 0; i < n; ++i) a[i] = i % 11;
+    long long expect = 0;
+    for (int i = 0; i < n; ++i) expect += a[i];
+    RAJA::ReduceSum<red, long long> s(3);
+    RAJA::ReduceMax<red, int> mx(-1);
+    {
+      using wpol = RAJA::WorkGroupPolicy<RAJA::b200_work<256, true>, RAJA::unordered>;
+      RAJA::WorkPool<wpol, Index_type> pool;
+      pool.enqueue(RAJA::RangeSegment(0, n / 3), [=] __device__(Index_type i) { s += a[i]; });
+      pool.enqueue(RAJA::RangeSegment(n / 3, n), [=] __device__(Index_type i) {
+        s += a[i];
+        mx.max(a[i]);
+      });
+      auto group = pool.instantiate();
+      res::Cuda keep;
+      {
+        res::Cuda gone;
+        group.run(keep);
+        group.run(gone);
+        group.run(keep);
+      }
+    }
+    CHECK("workgroup_reducers_two_streams_after_group_destroyed", s.get() == 3 + 3 * expect && mx.get() == 10);
+    cudaFree(a);
+  }
 }
 
 // RAJA::launch on the b200 policies (test/functional/launch): nested
