@@ -216,6 +216,15 @@ struct WgRegistry {
     cell_dev += kWgCellBytes;
     --cells_left;
   }
+  // Before a run's launches on stream s: when loops captured reducers, the
+  // run follows every earlier run on other streams (runs of one group share
+  // the reducers' partials and tickets, and fold into the cells in order).
+  void order_after_runs(cudaStream_t s) {
+    std::lock_guard<std::mutex> g(m);
+    if (blocks.empty()) return;
+    for (const RunMark& r : marks)
+      if (r.stream != s) check_cuda(cudaStreamWaitEvent(s, r.event, 0), "WorkGroup run order");
+  }
   // After a run's launches on stream s (the events outlive the stream).
   void ran_on(cudaStream_t s) {
     std::lock_guard<std::mutex> g(m);
@@ -2363,6 +2372,7 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
     char* d = static_cast<char*>(m_dev);
     auto* loops = reinterpret_cast<const b200::detail::WgLoop*>(d + m_loops_off);
     auto* bodies = reinterpret_cast<const unsigned char*>(d + m_bodies_off);
+    if (m_reg) m_reg->order_after_runs(s);
     // the tile shape of this run: the fixed one, or the tuner's
     b200::tune::Tuner::Ticket tk;
     if (m_tuner) tk = m_tuner->begin(s);
