@@ -404,6 +404,9 @@ int b200_multi_reduce_bitand_u64(const int32_t* bins, const uint64_t* vals, size
  * indices [0, lens[i]); for the segmented primitives, segment i covers
  * [offsets[i], offsets[i+1]) of one flattened array, offsets being the
  * prefix sums of lens.  A plan belongs to the device current at creation.
+ * A plan holds the per-loop tickets and tile partials of its runs, so calls
+ * with one plan must not overlap on the GPU: issue them on one stream, or
+ * order the streams.
  * ====================================================================== */
 typedef struct b200_batch_plan_s* b200_batch_plan;
 
