@@ -88,6 +88,11 @@ struct b200_exec {
   static constexpr int block_size = BLOCK;
   static constexpr bool async = Async;
 };
+template <int BLOCK = 256, bool Async = false>
+struct b200_work {};
+// order policy of the one-launch WorkGroup runner (the compat front-end's
+// own unordered)
+using b200_unordered = unordered;
 #else
 template <int BLOCK = 256, bool Async = false>
 struct b200_exec : make_policy_pattern_launch_platform_t<Policy::cuda, Pattern::forall,
@@ -96,14 +101,22 @@ struct b200_exec : make_policy_pattern_launch_platform_t<Policy::cuda, Pattern::
   static constexpr int block_size = BLOCK;
   static constexpr bool async = Async;
 };
+// WorkGroup exec policy (as cuda_work, policy/cuda/policy.hpp:384-389)
+template <int BLOCK = 256, bool Async = false>
+struct b200_work : make_policy_pattern_launch_platform_t<Policy::cuda, Pattern::workgroup_exec,
+                                                         (Async ? Launch::async : Launch::sync),
+                                                         Platform::cuda> {};
+// Order policy of the one-launch WorkGroup runner: every loop in one
+// persistent launch (RAJA's own unordered CUDA order policy is
+// unordered_cuda_loop_y_block_iter_x_threadblock_average,
+// policy/cuda/policy.hpp:395-400).
+struct b200_unordered : make_policy_pattern_platform_t<Policy::cuda, Pattern::workgroup_order, Platform::cuda> {};
 #endif
 template <int BLOCK = 256>
 using b200_exec_async = b200_exec<BLOCK, true>;
 struct b200_reduce {};
 struct b200_multi_reduce {};
 struct b200_atomic {};
-template <int BLOCK = 256, bool Async = false>
-struct b200_work {};
 struct b200_synchronize {};
 
 namespace b200 {
@@ -2108,6 +2121,8 @@ void sort_unstable_pairs(b200_exec<BLOCK, Async> p, K* kb, K* ke, V* vb, C c) {
   sort_stable_pairs(p, kb, ke, vb, c);
 }
 
+#endif  // RAJA_COMPAT_FRONTEND
+
 // ------------------------------------------------------------- WorkGroup
 // b200_work: enqueued loops (range segment + trivially copyable device
 // lambda) are kept as (function pointer, body bytes, range).  The unordered
@@ -2222,40 +2237,40 @@ inline long long wg_min_tile() {
   }
   return m;
 }
-}  // namespace detail
-}  // namespace b200
 
-template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
-class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc>;
+// The loops of one b200 WorkGroup: capture at enqueue, upload on the first
+// run, one persistent launch per unordered run (or one launch per loop for
+// the ordered runners).  Shared by RAJA's WorkGroup (through a
+// detail::WorkRunner specialisation) and the compat front-end's.
+enum WgOrder { kWgUnordered = 0, kWgOrdered = 1, kWgReverse = 2 };
 
-template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
-class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc> {
+template <int BLOCK>
+class WgCore {
  public:
-  using policy = WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>;
-  using group_type = WorkGroup<policy, Index, xargs<>, Alloc>;
-  WorkPool() = default;
-  template <typename A>
-  explicit WorkPool(const A&) {}  // the allocator: device storage comes from cudaMalloc
-  // Loop bodies are device lambdas whose captures are plain data or b200
-  // reducers: the body is copied once here (captured b200 reducers take a
-  // slot of this loop in the pool, so their per-loop combine runs inside
-  // the group's launch) and its bytes move to device memory.
-  template <typename T, typename Body>
-  void enqueue(TypedRangeSegment<T> seg, Body body) {
+  WgCore() = default;
+  WgCore(const WgCore&) = delete;
+  WgCore& operator=(const WgCore&) = delete;
+  // A moved-from core is empty with a fresh registry, ready for new loops.
+  WgCore(WgCore&& o) noexcept { swap(o); }
+  WgCore& operator=(WgCore&& o) noexcept {
+    swap(o);
+    return *this;
+  }
+  ~WgCore() { free_device(); }
+
+  // Capture loop [begin, begin + len): the body is copied once here, with
+  // the capture context active so that captured b200 reducers take a slot
+  // of this loop in the registry, and its bytes move to device memory at
+  // the first run.
+  template <typename Body>
+  void enqueue(long long begin, long long len, const Body& body) {
     static_assert(std::is_copy_constructible<Body>::value, "b200_work loop bodies are copied");
-    // with plugins registered, the capture hooks bracket the body copy
-    // (pattern/WorkGroup.hpp:287-296)
-    const bool hooks = !util::PluginRegistry::empty();
-    const util::PluginContext ctx(Platform::cuda, std::string());
-    if (hooks) util::callPreCapturePlugins(ctx);
-    const b200::detail::wg_fn fp = b200::detail::wg_fn_of<Body>();
-    const long long len = (long long)seg.size();
-    // reducer partials for the largest tile count any shape of this group
-    // can run with
-    const long long tile = b200::detail::wg_min_tile<BLOCK>();
-    b200::detail::WgCaptureCtx& w = b200::detail::wg_capture();
+    const wg_fn fp = wg_fn_of<Body>();
+    // reducer partials for the largest tile count any shape can run with
+    const long long tile = wg_min_tile<BLOCK>();
+    WgCaptureCtx& w = wg_capture();
     w.active = true;
-    w.reg = m_reg;
+    w.reg = reg_;
     w.ntiles = (len + tile - 1) / tile;
     ++w.capture_id;
     alignas(Body) unsigned char raw[sizeof(Body)];
@@ -2268,23 +2283,199 @@ class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH
     }
     w.active = false;
     w.reg.reset();
-    const size_t off = (m_bytes.size() + 15) / 16 * 16;
-    m_bytes.resize(off + sizeof(Body));
-    std::memcpy(m_bytes.data() + off, raw, sizeof(Body));
-    m_loops.push_back(b200::detail::WgLoop{fp, (long long)seg.b, len, off});
-    if (hooks) util::callPostCapturePlugins(ctx);
+    const size_t off = (bytes_.size() + 15) / 16 * 16;
+    bytes_.resize(off + sizeof(Body));
+    std::memcpy(bytes_.data() + off, raw, sizeof(Body));
+    loops_.push_back(WgLoop{fp, begin, len, off});
+    uploaded_ = false;
   }
   void reserve(size_t n, size_t bytes) {
-    m_loops.reserve(n);
-    m_bytes.reserve(bytes);
+    loops_.reserve(n);
+    bytes_.reserve(bytes);
   }
-  size_t num_loops() const { return m_loops.size(); }
-  group_type instantiate();
+  size_t num_loops() const { return loops_.size(); }
+
+  // Launch every loop on stream s (uploading the loops the first time).
+  void run(cudaStream_t s, WgOrder order) {
+    if (loops_.empty()) return;
+    if (!uploaded_) upload();
+    reg_->order_after_runs(s);
+    char* d = static_cast<char*>(dev_);
+    auto* loops = reinterpret_cast<const WgLoop*>(d + loops_off_);
+    auto* bodies = reinterpret_cast<const unsigned char*>(d + bodies_off_);
+    // the tile shape of this run: the fixed one, or the tuner's
+    tune::Tuner::Ticket tk;
+    if (tuner_) tk = tuner_->begin(s);
+    const size_t si = size_t(tk.cand);
+    const tune::Shape sh = shapes_[si];
+    const long long tile = (long long)sh.block * sh.items;
+    auto* prefix = reinterpret_cast<const long long*>(d + prefix_off_[si]);
+    const int nloops = int(loops_.size());
+    try {
+      tune::with_block(sh.block, [&](auto NB) {
+        if (order == kWgUnordered) {
+          if (ntiles_[si] > 0) {
+            auto k = wg_kernel<NB()>;
+            const unsigned g = grid_for<wg_kernel<NB()>>(NB(), ntiles_[si] * NB());
+            k<<<g, NB(), 0, s>>>(prefix, nloops, tile, loops, bodies);
+          }
+        } else {
+          // one launch per loop, in (reverse) enqueue order: block b runs tile b
+          auto k = wg_one_kernel<NB()>;
+          for (int i = 0; i < nloops; ++i) {
+            const int which = order == kWgReverse ? nloops - 1 - i : i;
+            const long long nt = (loops_[size_t(which)].len + tile - 1) / tile;
+            if (nt > 0) k<<<unsigned(nt), NB(), 0, s>>>(loops, which, tile, bodies);
+          }
+        }
+      });
+      check_cuda(cudaGetLastError(), "WorkGroup run");
+    } catch (...) {
+      if (tuner_) tuner_->abandon(tk);
+      throw;
+    }
+    if (tuner_) tuner_->end(tk, s, elements_);
+    // reducers captured by the loops read their cells after this run
+    reg_->ran_on(s);
+  }
+
+  // The tuner's state for b200_work<0> (candidates, timed runs, the shape
+  // in use); a fixed BLOCK reports its one shape as settled.
+  tune::Report tuning() const {
+    if (tuner_) return tuner_->report();
+    const std::vector<tune::Shape> sh = wg_shapes<BLOCK>();
+    return tune::Report{"WorkGroup", -1, -1, true, sh[0], 1, 0};
+  }
+
+  // Forget the loops and free their device storage (reducers keep the
+  // registry, and with it their cells, alive).
+  void clear() {
+    free_device();
+    loops_.clear();
+    bytes_.clear();
+    uploaded_ = false;
+    tuner_.reset();
+  }
 
  private:
-  std::vector<b200::detail::WgLoop> m_loops;
-  std::vector<unsigned char> m_bytes;
-  std::shared_ptr<b200::detail::WgRegistry> m_reg = std::make_shared<b200::detail::WgRegistry>();
+  void swap(WgCore& o) noexcept {
+    std::swap(loops_, o.loops_);
+    std::swap(bytes_, o.bytes_);
+    std::swap(reg_, o.reg_);
+    std::swap(dev_, o.dev_);
+    std::swap(uploaded_, o.uploaded_);
+    std::swap(loops_off_, o.loops_off_);
+    std::swap(bodies_off_, o.bodies_off_);
+    std::swap(elements_, o.elements_);
+    std::swap(shapes_, o.shapes_);
+    std::swap(prefix_off_, o.prefix_off_);
+    std::swap(ntiles_, o.ntiles_);
+    std::swap(tuner_, o.tuner_);
+  }
+  void free_device() {
+    if (dev_) cudaFree(dev_);
+    dev_ = nullptr;
+  }
+  // Loops, bodies and, per tile shape, the loops' first tiles, in one
+  // device allocation.
+  void upload() {
+    free_device();
+    shapes_ = wg_shapes<BLOCK>();
+    auto round = [](size_t b) { return (b + 255) / 256 * 256; };
+    std::vector<long long> prefix;
+    prefix_off_.clear();
+    ntiles_.clear();
+    elements_ = 0;
+    for (const auto& l : loops_) elements_ += l.len;
+    const size_t off = round(loops_.size() * sizeof(WgLoop));
+    for (const tune::Shape& sh : shapes_) {
+      const long long tile = (long long)sh.block * sh.items;
+      const size_t first = prefix.size();
+      long long acc = 0;
+      for (const auto& l : loops_) {
+        prefix.push_back(acc);
+        acc += (l.len + tile - 1) / tile;
+      }
+      prefix.push_back(acc);
+      prefix_off_.push_back(off + first * sizeof(long long));
+      ntiles_.push_back(acc);
+    }
+    loops_off_ = 0;
+    bodies_off_ = round(off + prefix.size() * sizeof(long long));
+    check_cuda(cudaMalloc(&dev_, bodies_off_ + bytes_.size() + 16), "WorkGroup storage");
+    char* d = static_cast<char*>(dev_);
+    check_cuda(cudaMemcpy(d + loops_off_, loops_.data(), loops_.size() * sizeof(WgLoop), cudaMemcpyHostToDevice),
+               "WorkGroup loops");
+    check_cuda(cudaMemcpy(d + off, prefix.data(), prefix.size() * sizeof(long long), cudaMemcpyHostToDevice),
+               "WorkGroup tiles");
+    if (!bytes_.empty())
+      check_cuda(cudaMemcpy(d + bodies_off_, bytes_.data(), bytes_.size(), cudaMemcpyHostToDevice),
+                 "WorkGroup bodies");
+    tuner_.reset();
+    if (shapes_.size() > 1)
+      tuner_ = tune::make_tuner("WorkGroup", current_device_index(), -1, shapes_.data(), int(shapes_.size()));
+    uploaded_ = true;
+  }
+
+  std::vector<WgLoop> loops_;
+  std::vector<unsigned char> bytes_;
+  std::shared_ptr<WgRegistry> reg_ = std::make_shared<WgRegistry>();
+  void* dev_ = nullptr;
+  bool uploaded_ = false;
+  size_t loops_off_ = 0, bodies_off_ = 0;
+  long long elements_ = 0;
+  std::vector<tune::Shape> shapes_;
+  std::vector<size_t> prefix_off_;  // per shape
+  std::vector<long long> ntiles_;   // per shape
+  std::shared_ptr<tune::Tuner> tuner_;
+};
+
+}  // namespace detail
+}  // namespace b200
+
+#if defined(RAJA_COMPAT_FRONTEND)
+template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
+class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc>;
+
+// The compat front-end's WorkPool / WorkGroup on b200_work: plugin hooks
+// and resources around the shared core.
+namespace b200 {
+namespace detail {
+template <class ORDER>
+constexpr WgOrder wg_order() {
+  return std::is_same<ORDER, unordered>::value ? kWgUnordered
+                                               : (std::is_same<ORDER, reverse_ordered>::value ? kWgReverse : kWgOrdered);
+}
+}  // namespace detail
+}  // namespace b200
+
+template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
+class WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc> {
+ public:
+  using policy = WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>;
+  using group_type = WorkGroup<policy, Index, xargs<>, Alloc>;
+  WorkPool() = default;
+  template <typename A>
+  explicit WorkPool(const A&) {}  // the allocator: device storage comes from cudaMalloc
+  // Loop bodies are device lambdas whose captures are plain data or b200
+  // reducers (captured reducers take a slot of this loop, so their per-loop
+  // combine runs inside the group's launch).
+  template <typename T, typename Body>
+  void enqueue(TypedRangeSegment<T> seg, Body body) {
+    // with plugins registered, the capture hooks bracket the body copy
+    // (pattern/WorkGroup.hpp:287-296)
+    const bool hooks = !util::PluginRegistry::empty();
+    const util::PluginContext ctx(Platform::cuda, std::string());
+    if (hooks) util::callPreCapturePlugins(ctx);
+    m_core.enqueue((long long)seg.b, (long long)seg.size(), body);
+    if (hooks) util::callPostCapturePlugins(ctx);
+  }
+  void reserve(size_t n, size_t bytes) { m_core.reserve(n, bytes); }
+  size_t num_loops() const { return m_core.num_loops(); }
+  group_type instantiate() { return group_type(std::move(m_core)); }
+
+ private:
+  b200::detail::WgCore<BLOCK> m_core;
 };
 
 template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
@@ -2292,159 +2483,33 @@ class WorkGroup<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATC
  public:
   using policy = WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>;
   WorkGroup() = default;
+  explicit WorkGroup(b200::detail::WgCore<BLOCK>&& core) : m_core(std::move(core)) {}
   WorkGroup(const WorkGroup&) = delete;
-  WorkGroup(WorkGroup&& o) noexcept { *this = std::move(o); }
-  WorkGroup& operator=(WorkGroup&& o) noexcept {
-    std::swap(m_dev, o.m_dev);
-    std::swap(m_nloops, o.m_nloops);
-    std::swap(m_loops_off, o.m_loops_off);
-    std::swap(m_bodies_off, o.m_bodies_off);
-    std::swap(m_loop_len, o.m_loop_len);
-    std::swap(m_shapes, o.m_shapes);
-    std::swap(m_prefix_off, o.m_prefix_off);
-    std::swap(m_ntiles, o.m_ntiles);
-    std::swap(m_tuner, o.m_tuner);
-    std::swap(m_reg, o.m_reg);
-    return *this;
-  }
-  ~WorkGroup() {
-    if (m_dev) cudaFree(m_dev);
-  }
-  // Upload loops, bodies and, per tile shape, the loops' first tiles once
-  // (instantiate); the registry holds the slots of the reducers the bodies
-  // captured.
-  void setup(const std::vector<b200::detail::WgLoop>& loops, const std::vector<unsigned char>& bytes,
-             std::shared_ptr<b200::detail::WgRegistry> reg) {
-    m_reg = std::move(reg);
-    m_nloops = int(loops.size());
-    m_loop_len.clear();
-    for (const auto& l : loops) m_loop_len.push_back(l.len);
-    m_shapes = b200::detail::wg_shapes<BLOCK>();
-    auto round = [](size_t b) { return (b + 255) / 256 * 256; };
-    // one prefix table per shape: loop l's first tile, then the tile count
-    std::vector<long long> prefix;
-    m_prefix_off.clear();
-    m_ntiles.clear();
-    size_t off = round(loops.size() * sizeof(b200::detail::WgLoop));
-    for (const b200::tune::Shape& sh : m_shapes) {
-      const long long tile = (long long)sh.block * sh.items;
-      const size_t first = prefix.size();
-      long long acc = 0;
-      for (const auto& l : loops) {
-        prefix.push_back(acc);
-        acc += (l.len + tile - 1) / tile;
-      }
-      prefix.push_back(acc);
-      m_prefix_off.push_back(off + first * sizeof(long long));
-      m_ntiles.push_back(acc);
-    }
-    m_loops_off = 0;
-    m_bodies_off = round(off + prefix.size() * sizeof(long long));
-    const size_t total = m_bodies_off + bytes.size() + 16;
-    b200::check_cuda(cudaMalloc(&m_dev, total), "WorkGroup storage");
-    char* d = static_cast<char*>(m_dev);
-    if (!loops.empty())
-      b200::check_cuda(cudaMemcpy(d + m_loops_off, loops.data(), loops.size() * sizeof(loops[0]),
-                                  cudaMemcpyHostToDevice), "WorkGroup loops");
-    if (!prefix.empty())
-      b200::check_cuda(cudaMemcpy(d + off, prefix.data(), prefix.size() * sizeof(long long), cudaMemcpyHostToDevice),
-                       "WorkGroup tiles");
-    if (!bytes.empty())
-      b200::check_cuda(cudaMemcpy(d + m_bodies_off, bytes.data(), bytes.size(), cudaMemcpyHostToDevice),
-                       "WorkGroup bodies");
-    if (m_shapes.size() > 1)
-      m_tuner = b200::tune::make_tuner("WorkGroup", b200::current_device_index(), -1, m_shapes.data(),
-                                       int(m_shapes.size()));
-  }
+  WorkGroup(WorkGroup&&) noexcept = default;
+  WorkGroup& operator=(WorkGroup&&) noexcept = default;
   using resource_type = resources::Cuda;
   WorkSite<policy, Index, xargs<>, Alloc> run() { return run(resource_type::get_default()); }
   // The loops run on the resource's stream (pattern/WorkGroup.hpp:357-370).
   WorkSite<policy, Index, xargs<>, Alloc> run(resource_type r) {
     WorkSite<policy, Index, xargs<>, Alloc> site(r);
-    if (m_nloops == 0) return site;
+    if (m_core.num_loops() == 0) return site;
     auto bound = bind_resource(r);
     // with plugins registered, the launch hooks bracket the run
     // (pattern/WorkGroup.hpp:515-528)
     const bool hooks = !util::PluginRegistry::empty();
     const util::PluginContext ctx(Platform::cuda, std::string());
     if (hooks) util::callPreLaunchPlugins(ctx);
-    cudaStream_t s = b200::stream();
-    char* d = static_cast<char*>(m_dev);
-    auto* loops = reinterpret_cast<const b200::detail::WgLoop*>(d + m_loops_off);
-    auto* bodies = reinterpret_cast<const unsigned char*>(d + m_bodies_off);
-    if (m_reg) m_reg->order_after_runs(s);
-    // the tile shape of this run: the fixed one, or the tuner's
-    b200::tune::Tuner::Ticket tk;
-    if (m_tuner) tk = m_tuner->begin(s);
-    const size_t si = size_t(tk.cand);
-    const b200::tune::Shape sh = m_shapes[si];
-    const long long tile = (long long)sh.block * sh.items;
-    auto* prefix = reinterpret_cast<const long long*>(d + m_prefix_off[si]);
-    try {
-      b200::tune::with_block(sh.block, [&](auto NB) {
-        if (std::is_same<ORDER, unordered>::value) {
-          if (m_ntiles[si] > 0) {
-            auto k = b200::detail::wg_kernel<NB()>;
-            const unsigned g = b200::detail::grid_for<b200::detail::wg_kernel<NB()>>(NB(), m_ntiles[si] * NB());
-            k<<<g, NB(), 0, s>>>(prefix, m_nloops, tile, loops, bodies);
-          }
-        } else {
-          // one launch per loop, in (reverse) enqueue order: block b runs tile b
-          auto k = b200::detail::wg_one_kernel<NB()>;
-          for (int i = 0; i < m_nloops; ++i) {
-            const int which = std::is_same<ORDER, reverse_ordered>::value ? m_nloops - 1 - i : i;
-            const long long nt = (m_loop_len[which] + tile - 1) / tile;
-            if (nt > 0) k<<<unsigned(nt), NB(), 0, s>>>(loops, which, tile, bodies);
-          }
-        }
-      });
-      b200::check_cuda(cudaGetLastError(), "WorkGroup run");
-    } catch (...) {
-      if (m_tuner) m_tuner->abandon(tk);
-      throw;
-    }
-    if (m_tuner) {
-      long long elems = 0;
-      for (long long l : m_loop_len) elems += l;
-      m_tuner->end(tk, s, elems);
-    }
-    // reducers captured by the loops read their cells after this stream
-    if (m_reg) m_reg->ran_on(s);
+    m_core.run(b200::stream(), b200::detail::wg_order<ORDER>());
     if (!Async) b200::wait();
     if (hooks) util::callPostLaunchPlugins(ctx);
     return site;
   }
   void clear() {}
-  // The tuner's state for a b200_work<0> group (candidates, timed runs, the
-  // shape in use); a fixed BLOCK reports its one shape as settled.
-  b200::tune::Report tuning() const {
-    if (m_tuner) return m_tuner->report();
-    const b200::tune::Shape sh = m_shapes.empty() ? b200::tune::Shape{BLOCK, b200::detail::kWgItems} : m_shapes[0];
-    return b200::tune::Report{"WorkGroup", -1, -1, true, sh, 1, 0};
-  }
+  b200::tune::Report tuning() const { return m_core.tuning(); }
 
  private:
-  void* m_dev = nullptr;
-  int m_nloops = 0;
-  size_t m_loops_off = 0, m_bodies_off = 0;
-  std::vector<long long> m_loop_len;
-  std::vector<b200::tune::Shape> m_shapes;
-  std::vector<size_t> m_prefix_off;  // per shape
-  std::vector<long long> m_ntiles;   // per shape
-  std::shared_ptr<b200::tune::Tuner> m_tuner;
-  std::shared_ptr<b200::detail::WgRegistry> m_reg;
+  b200::detail::WgCore<BLOCK> m_core;
 };
-
-template <int BLOCK, bool Async, typename ORDER, typename STORAGE, typename DISPATCH, typename Index, typename Alloc>
-typename WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc>::group_type
-WorkPool<WorkGroupPolicy<b200_work<BLOCK, Async>, ORDER, STORAGE, DISPATCH>, Index, xargs<>, Alloc>::instantiate() {
-  group_type g;
-  g.setup(m_loops, m_bytes, m_reg);
-  m_loops.clear();
-  m_bytes.clear();
-  m_reg = std::make_shared<b200::detail::WgRegistry>();
-  return g;
-}
 
 // ----------------------------------------------------------- synchronize
 template <>

@@ -25,6 +25,10 @@
 //   param_init / param_combine / param_resolve for expt::Reduce and
 //               expt::ReduceLoc params on b200_exec
 //                                    policy/cuda/params/reduce.hpp:21-62
+//   detail::WorkRunner<b200_work<B, A>, order, dispatch, allocator, index>
+//               (enqueue / run / clear, behind RAJA's unchanged WorkPool,
+//               WorkGroup and WorkSite)
+//                                    policy/cuda/WorkGroup/WorkRunner.hpp:38-407
 //
 // The resource is camp's CUDA resource (camp::resources::Cuda, present in
 // a RAJA installed with CUDA).  The reducer classes ReduceSum<b200_reduce,
@@ -490,6 +494,71 @@ RAJA_INLINE resources::EventProxy<resources::Cuda> forall_impl(
                                                   expt::ForallParamPack<>());
   return resources::EventProxy<resources::Cuda>(r);
 }
+
+// ---- WorkGroup (pattern/WorkGroup.hpp:207-530): RAJA's WorkPool /
+// WorkGroup / WorkSite stay unchanged and call their runner,
+// detail::WorkRunner<exec, order, dispatch, allocator, index, args...>
+// (policy/cuda/WorkGroup/WorkRunner.hpp:38-407 for cuda_work).  The b200
+// runner keeps the loops itself (RAJA's work storage stays empty): its
+// enqueue captures the range and the body, its run launches every loop
+// in one persistent launch (b200_unordered) or one launch per loop
+// (ordered, reverse_ordered), with captured b200_reduce reducers combined
+// inside the launch.
+namespace detail {
+template <int BLOCK, bool Async, typename ORDER, typename DISPATCH, typename ALLOC, typename INDEX>
+struct WorkRunner<b200_work<BLOCK, Async>, ORDER, DISPATCH, ALLOC, INDEX> {
+  static_assert(std::is_same<ORDER, b200_unordered>::value || std::is_same<ORDER, ordered>::value ||
+                    std::is_same<ORDER, reverse_ordered>::value,
+                "b200_work runs b200_unordered, ordered or reverse_ordered WorkGroups");
+  using exec_policy = b200_work<BLOCK, Async>;
+  using order_policy = ORDER;
+  using dispatch_policy = DISPATCH;
+  using Allocator = ALLOC;
+  using index_type = INDEX;
+  using resource_type = resources::Cuda;
+  // RAJA's WorkStorage is typed by a dispatcher; the b200 runner stores
+  // nothing there, so the sequential runner's dispatcher serves.
+  using dispatcher_type = typename WorkRunner<seq_work, ordered, DISPATCH, ALLOC, INDEX>::dispatcher_type;
+
+  WorkRunner() = default;
+  WorkRunner(const WorkRunner&) = delete;
+  WorkRunner& operator=(const WorkRunner&) = delete;
+  WorkRunner(WorkRunner&&) noexcept = default;
+  WorkRunner& operator=(WorkRunner&&) noexcept = default;
+
+  template <typename WorkContainer, typename Iterable, typename LoopBody>
+  void enqueue(WorkContainer&, Iterable&& iter, LoopBody&& loop_body) {
+    using Seg = camp::decay<Iterable>;
+    static_assert(std::is_same<Seg, TypedRangeSegment<typename Seg::value_type>>::value,
+                  "b200_work loops take range segments");
+    const long long begin = (long long)*std::begin(iter);
+    const long long len = (long long)std::distance(std::begin(iter), std::end(iter));
+    if (len > 0) core_.enqueue(begin, len, loop_body);
+  }
+
+  using per_run_storage = int;
+
+  template <typename WorkContainer>
+  per_run_storage run(WorkContainer const&, resource_type r) {
+    b200::detail::ResourceStream bound(r.get_stream());
+    constexpr b200::detail::WgOrder o =
+        std::is_same<ORDER, b200_unordered>::value
+            ? b200::detail::kWgUnordered
+            : (std::is_same<ORDER, reverse_ordered>::value ? b200::detail::kWgReverse : b200::detail::kWgOrdered);
+    core_.run(b200::stream(), o);
+    if (!Async) b200::wait();
+    return 0;
+  }
+
+  void clear() { core_.clear(); }
+
+  // the tuner's state for b200_work<0>
+  b200::tune::Report tuning() const { return core_.tuning(); }
+
+ private:
+  b200::detail::WgCore<BLOCK> core_;
+};
+}  // namespace detail
 
 // the front-end's IndexSet dispatch (declared before RAJA/RAJA.hpp)
 namespace wrap {

@@ -4,7 +4,8 @@
 // seq_exec result of the same code.  Without a CUDA device only the
 // sequential half runs (the program still proves that each RAJA front-end
 // binds to a b200 overload: forall over ranges and IndexSets, ReduceSum /
-// ReduceMinLoc on b200_reduce, expt::Reduce params, scans and sorts).
+// ReduceMinLoc on b200_reduce, expt::Reduce params, scans, sorts, and
+// WorkPool / WorkGroup through the b200_work WorkRunner).
 #include "raja_b200/RAJA_b200.hpp"  // before RAJA/RAJA.hpp, which it includes
 
 // Loop bodies run on the host (seq_exec) and the device (b200_exec).  RAJA
@@ -15,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <memory>
 #include <vector>
 
 namespace {
@@ -105,6 +107,41 @@ Results<ExecPol, RedPol> run(const std::vector<double>& x0, const std::vector<in
   r.iset.assign(z, z + n);
   return r;
 }
+// A WorkGroup of uneven loops, each w[i] += i + 5 and a per-loop ReduceSum
+// of w[i], run `runs` times; the sums are read after the group is gone (RAJA's
+// host reducers fold their loop copies into the parent when the group's
+// storage is destroyed).
+struct WgResults {
+  std::vector<long long> w, sums;
+};
+template <typename WorkPol, typename OrderPol, typename RedPol>
+WgResults run_workgroup(long long* w, const std::vector<RAJA::Index_type>& offs, int runs)
+{
+  const int nloops = int(offs.size()) - 1;
+  const RAJA::Index_type total = offs.back();
+  for (RAJA::Index_type i = 0; i < total; ++i) w[i] = i % 13;
+  using policy = RAJA::WorkGroupPolicy<WorkPol, OrderPol, RAJA::ragged_array_of_objects>;
+  using pool_t = RAJA::WorkPool<policy, RAJA::Index_type, RAJA::xargs<>, std::allocator<char>>;
+  std::vector<std::unique_ptr<RAJA::ReduceSum<RedPol, long long>>> sums;
+  {
+    pool_t pool(std::allocator<char>{});
+    for (int l = 0; l < nloops; ++l) {
+      sums.emplace_back(new RAJA::ReduceSum<RedPol, long long>(l));
+      const RAJA::ReduceSum<RedPol, long long>& s = *sums.back();
+      pool.enqueue(RAJA::TypedRangeSegment<RAJA::Index_type>(offs[l], offs[l + 1]),
+                   [=] APP_HOST_DEVICE(RAJA::Index_type i) {
+                     w[i] += i + 5;
+                     s += w[i];
+                   });
+    }
+    auto group = pool.instantiate();
+    for (int r = 0; r < runs; ++r) group.run();
+  }
+  WgResults out;
+  out.w.assign(w, w + total);
+  for (auto& s : sums) out.sums.push_back(s->get());
+  return out;
+}
 }  // namespace
 
 int main()
@@ -124,6 +161,10 @@ int main()
   auto seq = run<RAJA::seq_exec, RAJA::seq_reduce>(x0, k0, hx.data(), hy.data(), ha.data(), hb.data(),
                                                     hk.data(), hv.data(), hz.data());
   std::printf("seq_exec: sum %.17g, minloc %.17g at %ld\n", seq.sum, seq.minv, (long)seq.minloc);
+  std::vector<RAJA::Index_type> offs(1, 0);
+  for (int l = 0; l < 37; ++l) offs.push_back(offs.back() + 17 + (l * 7919) % 4000);
+  std::vector<long long> hw(offs.back());
+  auto wseq = run_workgroup<RAJA::seq_work, RAJA::ordered, RAJA::seq_reduce>(hw.data(), offs, 3);
 
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -144,6 +185,16 @@ int main()
   cudaDeviceSynchronize();
   // the same application with its launch shape tuned on line (BLOCK 0),
   // run enough times for the tuners to cycle through their shapes
+  long long* w = nullptr;
+  cudaMallocManaged(&w, offs.back() * sizeof(long long));
+  auto wdev = run_workgroup<RAJA::b200_work<256>, RAJA::b200_unordered, RAJA::b200_reduce>(w, offs, 3);
+  auto word = run_workgroup<RAJA::b200_work<256>, RAJA::ordered, RAJA::b200_reduce>(w, offs, 3);
+  auto wtun = run_workgroup<RAJA::b200_work<0>, RAJA::b200_unordered, RAJA::b200_reduce>(w, offs, 3);
+  check(wdev.w == wseq.w && wdev.sums == wseq.sums,
+        "WorkGroup<b200_work<256>, b200_unordered> with ReduceSum<b200_reduce> per loop");
+  check(word.w == wseq.w && word.sums == wseq.sums, "WorkGroup<b200_work<256>, ordered>");
+  check(wtun.w == wseq.w && wtun.sums == wseq.sums, "WorkGroup<b200_work<0>, b200_unordered> (tuned tiles)");
+  cudaFree(w);
   bool tuned_ok = true;
   for (int rep = 0; rep < 30; ++rep) {
     auto t = run<RAJA::b200_exec<0>, RAJA::b200_reduce>(x0, k0, x, y, a, b, k, v, z);

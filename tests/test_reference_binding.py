@@ -6,8 +6,9 @@ an installed RAJA -- the reference's unmodified headers, with the
 hand-written config and the clean-room camp subset of oracle/refbuild/ --
 plus include/raja_b200/RAJA_b200.hpp, and linked with libb200prims and the
 reference's src/PluginStrategy.cpp.  RAJA's forall (ranges and IndexSets),
-ReduceSum / ReduceMinLoc on b200_reduce, expt::Reduce params, scans and
-sorts must all resolve to b200 overloads for it to build.  The program then
+ReduceSum / ReduceMinLoc on b200_reduce, expt::Reduce params, scans, sorts
+and WorkPool / WorkGroup (b200_work, through detail::WorkRunner) must all
+resolve to b200 overloads for it to build.  The program then
 runs: its seq_exec half always, and its b200 half, checked against seq_exec,
 where a CUDA device is present.  The test needs the reference tree (not
 present on the GPU host) and skips without it.
