@@ -44,6 +44,15 @@
 
 #include "../b200prims.h"
 
+// Host-and-device functions of this header.  RAJA's own RAJA_HOST_DEVICE
+// is empty in an installed RAJA configured without its CUDA back-end, which
+// the b200 policies do not need.
+#if defined(__CUDACC__)
+#define B200_HOST_DEVICE __host__ __device__
+#else
+#define B200_HOST_DEVICE
+#endif
+
 #if !defined(RAJA_COMPAT_FRONTEND)
 // An installed RAJA.  RAJA's scan and sort front-ends call impl::scan:: and
 // impl::sort:: by qualified name, which finds only the overloads declared
@@ -51,9 +60,31 @@
 // includes the parts of RAJA its declarations need, declares the b200
 // overloads, and then includes RAJA/RAJA.hpp itself (RAJA's own back-ends
 // sit at the same place inside RAJA/RAJA.hpp).
-#if defined(RAJA_scan_HPP) || defined(RAJA_sort_HPP)
-#error "include raja_b200/RAJA_b200.hpp before RAJA/RAJA.hpp (it adds impl::scan / impl::sort overloads)"
+#if defined(RAJA_scan_HPP) || defined(RAJA_sort_HPP) || defined(RAJA_pattern_atomic_HPP)
+#error "include raja_b200/RAJA_b200.hpp before RAJA/RAJA.hpp (it adds impl::scan / impl::sort / atomic overloads)"
 #endif
+// RAJA's policy-generic atomics (atomicAdd<Policy>(acc, v) and the rest)
+// call RAJA::atomicAdd(Policy{}, acc, v) by qualified name
+// (pattern/atomic.hpp:113-118), so the b200_atomic forms are declared here,
+// ahead of every RAJA header; they are defined with the other atomics below.
+namespace RAJA {
+struct b200_atomic;
+template <typename T> B200_HOST_DEVICE inline T atomicLoad(b200_atomic, T* acc);
+template <typename T> B200_HOST_DEVICE inline void atomicStore(b200_atomic, T* acc, T v);
+template <typename T> B200_HOST_DEVICE inline T atomicAdd(b200_atomic, T* acc, T v);
+template <typename T> B200_HOST_DEVICE inline T atomicSub(b200_atomic, T* acc, T v);
+template <typename T> B200_HOST_DEVICE inline T atomicMin(b200_atomic, T* acc, T v);
+template <typename T> B200_HOST_DEVICE inline T atomicMax(b200_atomic, T* acc, T v);
+template <typename T> B200_HOST_DEVICE inline T atomicInc(b200_atomic, T* acc);
+template <typename T> B200_HOST_DEVICE inline T atomicInc(b200_atomic, T* acc, T val);
+template <typename T> B200_HOST_DEVICE inline T atomicDec(b200_atomic, T* acc);
+template <typename T> B200_HOST_DEVICE inline T atomicDec(b200_atomic, T* acc, T val);
+template <typename T> B200_HOST_DEVICE inline T atomicAnd(b200_atomic, T* acc, T v);
+template <typename T> B200_HOST_DEVICE inline T atomicOr(b200_atomic, T* acc, T v);
+template <typename T> B200_HOST_DEVICE inline T atomicXor(b200_atomic, T* acc, T v);
+template <typename T> B200_HOST_DEVICE inline T atomicExchange(b200_atomic, T* acc, T v);
+template <typename T> B200_HOST_DEVICE inline T atomicCAS(b200_atomic, T* acc, T compare, T v);
+}  // namespace RAJA
 #include "RAJA/config.hpp"
 #include "RAJA/policy/PolicyBase.hpp"
 #include "RAJA/util/Operators.hpp"
@@ -65,15 +96,6 @@
 
 #if defined(RAJA_ENABLE_NVTX)
 #include <nvtx3/nvToolsExt.h>
-#endif
-
-// Host-and-device functions of this header.  RAJA's own RAJA_HOST_DEVICE
-// is empty in an installed RAJA configured without its CUDA back-end, which
-// the b200 policies do not need.
-#if defined(__CUDACC__)
-#define B200_HOST_DEVICE __host__ __device__
-#else
-#define B200_HOST_DEVICE
 #endif
 
 namespace RAJA {

@@ -4,7 +4,8 @@
 // seq_exec result of the same code.  Without a CUDA device only the
 // sequential half runs (the program still proves that each RAJA front-end
 // binds to a b200 overload: forall over ranges and IndexSets, ReduceSum /
-// ReduceMinLoc on b200_reduce, expt::Reduce params, scans, sorts, and
+// ReduceMinLoc on b200_reduce, expt::Reduce params, scans, sorts,
+// MultiReduceSum on b200_multi_reduce, atomicAdd on b200_atomic, and
 // WorkPool / WorkGroup through the b200_work WorkRunner).
 #include "raja_b200/RAJA_b200.hpp"  // before RAJA/RAJA.hpp, which it includes
 
@@ -13,6 +14,7 @@
 // its own CUDA back-end (as here), so the bodies say it directly.
 #define APP_HOST_DEVICE __host__ __device__
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -142,6 +144,27 @@ WgResults run_workgroup(long long* w, const std::vector<RAJA::Index_type>& offs,
   for (auto& s : sums) out.sums.push_back(s->get());
   return out;
 }
+// MultiReduceSum over bins and per-bin counts by atomicAdd (integer-valued
+// data: every order gives the same sums).
+struct MultiResults {
+  std::vector<double> sums;
+  std::vector<int> counts;
+};
+template <typename ExecPol, typename MRPol, typename AtomPol>
+MultiResults run_multi(const int* bins, const double* vals, int* cnt, RAJA::Index_type n, int nb)
+{
+  for (int b = 0; b < nb; ++b) cnt[b] = 0;
+  RAJA::MultiReduceSum<MRPol, double> mr(nb, 0.5);
+  RAJA::forall<ExecPol>(RAJA::TypedRangeSegment<RAJA::Index_type>(0, n),
+                        [=] APP_HOST_DEVICE(RAJA::Index_type i) {
+                          mr[bins[i]] += vals[i];
+                          RAJA::atomicAdd<AtomPol>(cnt + bins[i], 1);
+                        });
+  MultiResults r;
+  for (int b = 0; b < nb; ++b) r.sums.push_back(mr.get(b));
+  r.counts.assign(cnt, cnt + nb);
+  return r;
+}
 }  // namespace
 
 int main()
@@ -165,6 +188,15 @@ int main()
   for (int l = 0; l < 37; ++l) offs.push_back(offs.back() + 17 + (l * 7919) % 4000);
   std::vector<long long> hw(offs.back());
   auto wseq = run_workgroup<RAJA::seq_work, RAJA::ordered, RAJA::seq_reduce>(hw.data(), offs, 3);
+  const int nb = 37;
+  std::vector<int> hbins(n), hcnt(nb);
+  std::vector<double> hvals(n);
+  for (RAJA::Index_type i = 0; i < n; ++i) {
+    hbins[i] = int((i * 2654435761u) % nb);
+    hvals[i] = double(int(i % 9) - 4);
+  }
+  auto mseq = run_multi<RAJA::seq_exec, RAJA::seq_multi_reduce, RAJA::seq_atomic>(hbins.data(), hvals.data(),
+                                                                                  hcnt.data(), n, nb);
 
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -185,6 +217,19 @@ int main()
   cudaDeviceSynchronize();
   // the same application with its launch shape tuned on line (BLOCK 0),
   // run enough times for the tuners to cycle through their shapes
+  int *mbins = nullptr, *mcnt = nullptr;
+  double* mvals = nullptr;
+  cudaMallocManaged(&mbins, n * sizeof(int));
+  cudaMallocManaged(&mvals, n * sizeof(double));
+  cudaMallocManaged(&mcnt, nb * sizeof(int));
+  std::copy(hbins.begin(), hbins.end(), mbins);
+  std::copy(hvals.begin(), hvals.end(), mvals);
+  auto mdev = run_multi<RAJA::b200_exec<256>, RAJA::b200_multi_reduce, RAJA::b200_atomic>(mbins, mvals, mcnt, n, nb);
+  check(mdev.sums == mseq.sums && mdev.counts == mseq.counts,
+        "MultiReduceSum<b200_multi_reduce> and atomicAdd<b200_atomic>");
+  cudaFree(mbins);
+  cudaFree(mvals);
+  cudaFree(mcnt);
   long long* w = nullptr;
   cudaMallocManaged(&w, offs.back() * sizeof(long long));
   auto wdev = run_workgroup<RAJA::b200_work<256>, RAJA::b200_unordered, RAJA::b200_reduce>(w, offs, 3);
