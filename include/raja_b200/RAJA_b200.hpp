@@ -254,15 +254,19 @@ struct WgRegistry {
   // Before a run's launches on stream s: when loops captured reducers, the
   // run follows every earlier run on other streams (runs of one group share
   // the reducers' partials and tickets, and fold into the cells in order).
+  // Runs issued while s is being captured into a graph are left out: the
+  // graph's launches are ordered by the caller, and the reducers' cells are
+  // read after the caller has synchronised the graph's stream.
   void order_after_runs(cudaStream_t s) {
     std::lock_guard<std::mutex> g(m);
-    if (blocks.empty()) return;
+    if (blocks.empty() || capturing(s)) return;
     for (const RunMark& r : marks)
       if (r.stream != s) check_cuda(cudaStreamWaitEvent(s, r.event, 0), "WorkGroup run order");
   }
   // After a run's launches on stream s (the events outlive the stream).
   void ran_on(cudaStream_t s) {
     std::lock_guard<std::mutex> g(m);
+    if (blocks.empty() || capturing(s)) return;
     auto it = std::find_if(marks.begin(), marks.end(), [s](const RunMark& r) { return r.stream == s; });
     if (it == marks.end()) {
       cudaEvent_t e = nullptr;
@@ -272,6 +276,10 @@ struct WgRegistry {
     }
     check_cuda(cudaEventRecord(it->event, s), "WorkGroup run event");
     it->pending = true;
+  }
+  static bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
   }
   // Wait for every run issued so far.
   void wait_runs() {

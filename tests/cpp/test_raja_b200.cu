@@ -568,6 +568,52 @@ void test_autotune() {
   cudaFree(w);
 }
 
+// Stream capture of RAJA-API loops into a CUDA graph, then replays: a
+// repeated sweep of forall loops and a WorkGroup run costs one graph launch.
+void test_graph_capture() {
+  namespace res = RAJA::resources;
+  const Index_type n = (Index_type(1) << 20) + 5;
+  double* x = managed<double>(n);
+  double* y = managed<double>(n);
+  int* a = managed<int>(n);
+  for (Index_type i = 0; i < n; ++i) {
+    x[i] = double(i % 7);
+    y[i] = 0.0;
+    a[i] = 0;
+  }
+  cudaStream_t cs = nullptr;
+  cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  res::Cuda r = res::Cuda::CudaFromStream(cs);
+  using aexec = RAJA::b200_exec_async<256>;
+  // first calls outside the capture: per-kernel launch setup, WorkGroup upload
+  RAJA::forall<aexec>(r, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) { y[i] += x[i]; });
+  using wpol = RAJA::WorkGroupPolicy<RAJA::b200_work<256, true>, RAJA::unordered>;
+  RAJA::WorkPool<wpol, Index_type> pool;
+  pool.enqueue(RAJA::RangeSegment(0, n / 2), [=] __device__(Index_type i) { a[i] += 1; });
+  pool.enqueue(RAJA::RangeSegment(n / 2, n), [=] __device__(Index_type i) { a[i] += 2; });
+  auto group = pool.instantiate();
+  group.run(r);
+  cudaStreamSynchronize(cs);
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  bool ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  for (int k = 0; k < 4; ++k)
+    RAJA::forall<aexec>(r, RAJA::RangeSegment(0, n), [=] __device__(Index_type i) { y[i] += x[i]; });
+  group.run(r);
+  ok = ok && cudaStreamEndCapture(cs, &g) == cudaSuccess;
+  ok = ok && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+  for (int rep = 0; ok && rep < 10; ++rep) ok = cudaGraphLaunch(ge, cs) == cudaSuccess;
+  ok = ok && cudaStreamSynchronize(cs) == cudaSuccess;
+  for (Index_type i = 0; i < n && ok; ++i) ok = y[i] == 41.0 * x[i] && a[i] == (i < n / 2 ? 11 : 22);
+  CHECK("graph_capture_forall_and_workgroup_replayed", ok);
+  if (ge) cudaGraphExecDestroy(ge);
+  if (g) cudaGraphDestroy(g);
+  cudaStreamDestroy(cs);
+  cudaFree(x);
+  cudaFree(y);
+  cudaFree(a);
+}
+
 void test_multi_reduce_and_atomics() {
   const Index_type n = 200003;
   const int nb = 37;
@@ -1591,6 +1637,7 @@ int main() {
   workgroup_reducers_case<RAJA::unordered>("unordered");
   workgroup_reducers_case<RAJA::ordered>("ordered");
   test_autotune();
+  test_graph_capture();
   test_multi_reduce_and_atomics();
   test_reducers();
   test_forall_and_params();
