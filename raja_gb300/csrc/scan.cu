@@ -238,15 +238,21 @@ struct StatusWords {
   }
 };
 
+// Per-tile working set of a block besides the tile itself.
 template <class Op>
-struct ScanSmem {
-  using T = typename Op::T;
+struct ScanWork {
   using Local = typename Op::Local;
-  alignas(128) T stage[Tile<Op>::SIZE];      // the tile, filled by one TMA bulk copy
   Local wsum[SWARPS];                        // warp totals over the whole tile
   Local wtot[Tile<Op>::G * SWARPS];          // warp totals, sub-tile major
   Local pref[Tile<Op>::G * SWARPS];          // their exclusive prefix in the tile
   typename Op::Carry prefix;                 // the tile's carry-in
+};
+
+template <class Op>
+struct ScanSmem {
+  using T = typename Op::T;
+  alignas(128) T stage[Tile<Op>::SIZE];      // the tile, filled by one TMA bulk copy
+  ScanWork<Op> work;
   uint64_t bar;
   uint32_t tile;
 };
@@ -263,43 +269,22 @@ struct ScanSmem {
 template <class Op>
 constexpr int scan_min_blocks() { return Tile<Op>::G == 16 ? 3 : 4; }
 
+// Scan one tile held in shared memory (st) and write its outputs: thread
+// totals and the tile aggregate, published at once; the decoupled
+// look-back (warp 0) beside the sub-tile scans and the prefix table (warp
+// 1); then carry-in + prefixes applied as the outputs are stored.
 template <class Op, bool EXCL>
-__global__ void __launch_bounds__(SBLOCK, scan_min_blocks<Op>())
-scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op::T init,
-            int tma_ok, int vec_out, uint64_t* words, uint32_t* tile_counter,
-            uint32_t* status, uint32_t spin_limit) {
+__device__ __forceinline__ void scan_tile(ScanWork<Op>& sm, const typename Op::T* st, size_t tile, size_t n,
+                                          typename Op::T init, int vec_out, typename Op::T* out,
+                                          uint64_t* words, uint32_t* status, uint32_t spin_limit) {
   using T = typename Op::T;
   using Local = typename Op::Local;
   using Carry = typename Op::Carry;
   constexpr int VN = Tile<Op>::VN, G = Tile<Op>::G, TS = Tile<Op>::SIZE, PT = Tile<Op>::PT;
   static_assert(G * SWARPS == 32 * PT, "prefix table: PT entries per lane of warp 1");
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  ScanSmem<Op>& sm = *reinterpret_cast<ScanSmem<Op>*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  T* st = sm.stage;
-  if (tid == 0) {
-    sm.tile = atomicAdd(tile_counter, 1u);
-    mbar_init(&sm.bar, 1);
-    fence_mbar_init();
-    const size_t b0 = size_t(sm.tile) * TS;
-    if (tma_ok && b0 + TS <= n) {
-      mbar_arrive_expect_tx(&sm.bar, TS * sizeof(T));
-      tma_load_1d(st, in + b0, TS * sizeof(T), &sm.bar);
-    }
-  }
-  __syncthreads();
-  const size_t tile = sm.tile;
   const size_t base = tile * TS;
   const bool full = base + TS <= n;
-  if (tma_ok && full) {
-    if (!mbar_wait(&sm.bar, 0, spin_limit)) {
-      if (tid == 0) atomicOr_system(status, kStatusTmaTimeout);
-      mbar_drain(&sm.bar, 0);  // let the copy land before the block goes on
-    }
-  } else {
-    for (int e = tid; e < TS; e += SBLOCK) st[e] = (base + e < n) ? in[base + e] : T(0);
-    __syncthreads();
-  }
   {
     using SW = StatusWords<Carry>;
     // ---- granule totals (registers) and the tile aggregate: thread
@@ -514,6 +499,42 @@ scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op
       }
     }
   }
+}
+
+template <class Op, bool EXCL>
+__global__ void __launch_bounds__(SBLOCK, scan_min_blocks<Op>())
+scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op::T init,
+            int tma_ok, int vec_out, uint64_t* words, uint32_t* tile_counter,
+            uint32_t* status, uint32_t spin_limit) {
+  using T = typename Op::T;
+  constexpr int TS = Tile<Op>::SIZE;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  ScanSmem<Op>& sm = *reinterpret_cast<ScanSmem<Op>*>(smem_raw);
+  const int tid = threadIdx.x;
+  T* st = sm.stage;
+  if (tid == 0) {
+    sm.tile = atomicAdd(tile_counter, 1u);
+    mbar_init(&sm.bar, 1);
+    fence_mbar_init();
+    const size_t b0 = size_t(sm.tile) * TS;
+    if (tma_ok && b0 + TS <= n) {
+      mbar_arrive_expect_tx(&sm.bar, TS * sizeof(T));
+      tma_load_1d(st, in + b0, TS * sizeof(T), &sm.bar);
+    }
+  }
+  __syncthreads();
+  const size_t tile = sm.tile;
+  const size_t base = tile * TS;
+  if (tma_ok && base + TS <= n) {
+    if (!mbar_wait(&sm.bar, 0, spin_limit)) {
+      if (tid == 0) atomicOr_system(status, kStatusTmaTimeout);
+      mbar_drain(&sm.bar, 0);  // let the copy land before the block goes on
+    }
+  } else {
+    for (int e = tid; e < TS; e += SBLOCK) st[e] = (base + e < n) ? in[base + e] : T(0);
+    __syncthreads();
+  }
+  scan_tile<Op, EXCL>(sm.work, st, tile, n, init, vec_out, out, words, status, spin_limit);
 }
 
 template <class Op, bool EXCL>
