@@ -1192,12 +1192,52 @@ def run_e2e(args, lib, inputs, outs, n, stream, table, dist):
     ms = max_over_ranks(a.elapsed_time(b), dist, "cuda")
     world = dist.get_world_size() if dist else 1
     value = aggregate_gbs(world, sum(table.values()), args.e2e_steps, ms)
+    link = link_probe([(host[k], inputs[k]) for k in keys_in], [(host_out[k], outs[k]) for k in out_keys],
+                      h2d_s, d2h_s)
+    # the step's copies alone, both directions at once, bound the step
+    bound_ms = link["all_copies_ms"]
+    link["copy_bound_ms_per_step"] = round(bound_ms, 2)
+    link["e2e_frac_of_copy_bound"] = round(bound_ms / (ms / args.e2e_steps), 3)
     return {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
-            "ms_per_step": round(ms / args.e2e_steps, 3),
+            "ms_per_step": round(ms / args.e2e_steps, 3), "host_link": link,
             "path": "pinned host -> device copies (copy stream), C-ABI calls, device -> pinned "
                     "host copies (second copy stream), overlapped per primitive; steps alternate "
                     "between two sets of device buffers"}
+
+
+def link_probe(ins, outs, h2d_s, d2h_s):
+    """Host-link rates right after the end-to-end run, on the step's own
+    pinned buffers: every input host-to-device alone, every result
+    device-to-host alone, and both at once (the rates can differ between
+    host buffers, so the probe covers all of them)."""
+    import torch
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    torch.cuda.synchronize()
+    nb_in = sum(h.numel() * h.element_size() for h, _ in ins)
+    nb_out = sum(h.numel() * h.element_size() for h, _ in outs)
+
+    def timed(do_in, do_out):
+        a, b = ev(), ev()
+        a.record(h2d_s)
+        d2h_s.wait_event(a)
+        if do_in:
+            with torch.cuda.stream(h2d_s):
+                for h, d in ins:
+                    d.copy_(h, non_blocking=True)
+        if do_out:
+            with torch.cuda.stream(d2h_s):
+                for h, d in outs:
+                    h.copy_(d, non_blocking=True)
+        h2d_s.wait_stream(d2h_s)
+        b.record(h2d_s)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3
+
+    t_in, t_out, t_both = timed(True, False), timed(False, True), timed(True, True)
+    return {"h2d_gbs": round(nb_in / t_in / 1e9, 1), "d2h_gbs": round(nb_out / t_out / 1e9, 1),
+            "bidir_gbs": round((nb_in + nb_out) / t_both / 1e9, 1),
+            "all_copies_ms": round(1e3 * t_both, 2)}
 
 
 def run_cpu_baseline(args):
