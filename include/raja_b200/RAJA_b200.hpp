@@ -3,7 +3,9 @@
 //
 //   RAJA::b200_exec<BLOCK, Async>   forall over range / strided / list /
 //                                   IndexSet segments (replaces cuda_exec,
-//                                   policy/cuda/forall.hpp:554-706)
+//                                   policy/cuda/forall.hpp:554-706); BLOCK 0
+//                                   tunes block size and elements per thread
+//                                   on line (b200::tune)
 //   RAJA::b200_reduce               ReduceSum/Min/Max/MinLoc/MaxLoc/BitOr/
 //                                   BitAnd captured in device lambdas
 //                                   (replaces cuda_reduce,
@@ -12,19 +14,28 @@
 //   scans, sorts                    impl::scan / impl::sort overloads that
 //                                   forward to libb200prims (replace the CUB
 //                                   wrappers policy/cuda/scan.hpp, sort.hpp)
-//   RAJA::b200_work<BLOCK>          WorkGroup runner: unordered loops run in
-//                                   one persistent launch
-//                                   (policy/cuda/WorkGroup/WorkRunner.hpp)
+//   RAJA::b200_multi_reduce         MultiReduceSum/Min/Max/BitOr/BitAnd
+//                                   (policy/cuda/multi_reduce.hpp)
+//   RAJA::b200_atomic               RAJA's atomic family (policy/cuda/atomic.hpp)
+//   RAJA::b200_work<BLOCK>          WorkGroup runner: b200_unordered runs
+//                                   every loop in one persistent launch with
+//                                   captured reducers combined inside it;
+//                                   ordered / reverse_ordered launch per loop
+//                                   (policy/cuda/WorkGroup/WorkRunner.hpp);
+//                                   BLOCK 0 tunes the tile shape per group
 //   RAJA::b200_synchronize          RAJA::synchronize<> target
 //   RAJA::resources::Cuda           stream resource for the b200 policies:
 //                                   forall / scan / sort / WorkGroup::run
 //                                   take it first and return EventProxy
 //
-// Include after a RAJA front-end (the real RAJA or raja_compat).  Lambda
-// loop bodies stay templated and are compiled into the application with
-// nvcc --extended-lambda; fixed-type work goes through the C ABI in
-// b200prims.h.  Errors throw std::runtime_error, as RAJA's CUDA back-end
-// does (policy/cuda/raja_cudaerrchk.hpp:116-137).
+// With an installed RAJA, include this header before RAJA/RAJA.hpp (it
+// includes RAJA/RAJA.hpp itself): RAJA's front-ends reach the b200
+// overloads through qualified calls that see only earlier declarations.
+// With raja_compat, include it after RAJA/RAJA.hpp.  Lambda loop bodies
+// stay templated and are compiled into the application with nvcc
+// --extended-lambda; fixed-type work goes through the C ABI in b200prims.h.
+// Errors throw std::runtime_error, as RAJA's CUDA back-end does
+// (policy/cuda/raja_cudaerrchk.hpp:116-137).
 #pragma once
 
 #include <cuda_runtime.h>
