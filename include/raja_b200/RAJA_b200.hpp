@@ -960,8 +960,8 @@ constexpr int kSamples = 3;
 constexpr Shape kForallShapes[] = {{256, 1}, {128, 1}, {128, 4}, {256, 4}, {256, 16},
                                    {512, 1}, {512, 4}, {1024, 1}, {1024, 4}};
 // WorkGroup tiles of block x items elements
-constexpr Shape kWorkShapes[] = {{256, 8}, {128, 2}, {128, 4}, {128, 8}, {128, 16}, {256, 2},
-                                 {256, 4}, {256, 16}, {512, 2}, {512, 4}, {512, 8}, {512, 16}};
+constexpr Shape kWorkShapes[] = {{256, 8}, {128, 4}, {128, 8}, {128, 16}, {128, 32}, {256, 4},
+                                 {256, 16}, {256, 32}, {512, 2}, {512, 4}, {512, 8}, {512, 16}};
 
 struct Report {
   std::string name;
@@ -2219,8 +2219,12 @@ constexpr int kWgItems = 8;  // elements per thread of a fixed-BLOCK WorkGroup t
 // All loops in one launch over tiles of `tile` elements: prefix[l] is the
 // first tile of loop l (prefix[nloops] the tile count), and block b runs
 // tiles b, b + grid, ...; a tile finds its loop by binary search.
+// The loop bodies are reached through device function pointers, which
+// makes the kernels take a full register budget unless it is capped: at
+// 32 registers a thread, 2048 threads fit on an SM and twice as many
+// elements are in flight as at the default 64.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK)
+__global__ void __launch_bounds__(BLOCK, 2048 / BLOCK)
 wg_kernel(const long long* prefix, int nloops, long long tile, const WgLoop* loops,
           const unsigned char* bodies) {
   WgDevCtx& c = wg_dev_ctx();
@@ -2246,7 +2250,7 @@ wg_kernel(const long long* prefix, int nloops, long long tile, const WgLoop* loo
 }
 // One loop per launch (the ordered runners): block b runs tile b.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK)
+__global__ void __launch_bounds__(BLOCK, 2048 / BLOCK)
 wg_one_kernel(const WgLoop* loops, int which, long long tile, const unsigned char* bodies) {
   const WgLoop lp = loops[which];
   WgDevCtx& c = wg_dev_ctx();
