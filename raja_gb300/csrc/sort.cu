@@ -293,7 +293,10 @@ constexpr int sweep_min_blocks() {
   return b < 1 ? 1 : (b > cap ? cap : b);
 }
 
-template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST>
+// HI: which 32-bit half of a 64-bit key holds this pass's digit (0 or 1,
+// known at compile time so the half is selected without a branch; 0 for
+// 32-bit keys).
+template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST, int HI>
 __global__ void __launch_bounds__(SweepShape<K, HAS_V>::RB, (sweep_min_blocks<K, V, HAS_V, ST>()))
 onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __restrict__ vin,
                 V* __restrict__ vout, size_t n, int shift, int desc,
@@ -353,7 +356,7 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
     return KB::raw(sm.kin[e]);
   };
   const int wofs = warp * (32 * KPT) + lane;  // warp-striped positions
-  const bool dhi = shift >= 32;
+  constexpr bool dhi = HI == 1;
   const uint32_t dsel = 0x4440u | uint32_t((shift >> 3) & 3);
 
   // ---- early counts: per-warp digit histograms with shared atomics, so
@@ -364,7 +367,14 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
   for (int q = 0; q < KPT / 4; ++q) digs[q] = 0;
 #pragma unroll
   for (int k = 0; k < KPT; ++k) {
-    const uint32_t d = digit_of(ukey(wofs + k * 32), dhi, dsel);
+    uint32_t d;
+    if constexpr (sizeof(K) == 8 && !FIRST) {
+      // only the half that holds the digit is read (keys are already in
+      // order-preserving form after the first pass)
+      d = __byte_perm(reinterpret_cast<const uint32_t*>(&sm.kin[wofs + k * 32])[HI], 0u, dsel);
+    } else {
+      d = digit_of(ukey(wofs + k * 32), dhi, dsel);
+    }
     digs[k / 4] += d << (8 * (k % 4));
     atomicAdd(&sm.wcnt[warp][d], 1u);
   }
@@ -458,14 +468,14 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
 }
 
 // Launch one pass (one block per tile).
-template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST>
+template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST, int HI>
 int launch_sweep_t(const char* name, size_t tiles, cudaStream_t s, const K* src, K* dst,
                    const V* vsrc, V* vdst, size_t n, int shift, int desc, const uint32_t* bins,
                    ST* status, ST* status_next, uint32_t* counter, uint32_t* err, uint32_t lim) {
   const int tma_ok = (reinterpret_cast<uintptr_t>(src) % 16 == 0) &&
                      (!HAS_V || reinterpret_cast<uintptr_t>(vsrc) % 16 == 0);
   using SM = SweepSmem<K, V, HAS_V, ST>;
-  auto kern = onesweep_kernel<K, V, HAS_V, ST, FIRST, LAST>;
+  auto kern = onesweep_kernel<K, V, HAS_V, ST, FIRST, LAST, HI>;
   constexpr int threads = SweepShape<K, HAS_V>::RB;
   static KernelSetup ks;
   DeviceProps props;
@@ -482,17 +492,25 @@ int launch_sweep(const char* name, size_t tiles, cudaStream_t s, const K* src, K
                  const V* vsrc, V* vdst, size_t n, int shift, int first, int last, int desc,
                  const uint32_t* bins, ST* status, ST* status_next, uint32_t* counter,
                  uint32_t* err, uint32_t lim) {
+  // the first pass takes digit 0 (low half), the last the top digit
+  constexpr int TOP = sizeof(K) == 8 ? 1 : 0;
   if (first)
-    return launch_sweep_t<K, V, HAS_V, ST, true, false>(name, tiles, s, src, dst, vsrc, vdst, n,
-                                                        shift, desc, bins, status, status_next,
-                                                        counter, err, lim);
+    return launch_sweep_t<K, V, HAS_V, ST, true, false, 0>(name, tiles, s, src, dst, vsrc, vdst, n,
+                                                           shift, desc, bins, status, status_next,
+                                                           counter, err, lim);
   if (last)
-    return launch_sweep_t<K, V, HAS_V, ST, false, true>(name, tiles, s, src, dst, vsrc, vdst, n,
-                                                        shift, desc, bins, status, status_next,
-                                                        counter, err, lim);
-  return launch_sweep_t<K, V, HAS_V, ST, false, false>(name, tiles, s, src, dst, vsrc, vdst, n,
-                                                       shift, desc, bins, status, status_next,
-                                                       counter, err, lim);
+    return launch_sweep_t<K, V, HAS_V, ST, false, true, TOP>(name, tiles, s, src, dst, vsrc, vdst, n,
+                                                             shift, desc, bins, status, status_next,
+                                                             counter, err, lim);
+  if constexpr (sizeof(K) == 8) {
+    if (shift >= 32)
+      return launch_sweep_t<K, V, HAS_V, ST, false, false, 1>(name, tiles, s, src, dst, vsrc, vdst, n,
+                                                              shift, desc, bins, status, status_next,
+                                                              counter, err, lim);
+  }
+  return launch_sweep_t<K, V, HAS_V, ST, false, false, 0>(name, tiles, s, src, dst, vsrc, vdst, n,
+                                                          shift, desc, bins, status, status_next,
+                                                          counter, err, lim);
 }
 
 struct NoVal {};
