@@ -1318,25 +1318,86 @@ inline void finish(const char* what) {
   if (!Async) wait();
 }
 
-// One launch over the segments of an IndexSet described by `desc` (kind
-// and parameters per segment) and `prefix` (their running lengths, nseg+1
-// entries): the table goes to launch-pool memory on the b200 stream and is
-// freed behind the launch.
-template <int BLOCK, bool Async, class Body, class T>
-void indexset_launch(const std::vector<SegDesc<T>>& desc, const std::vector<long long>& prefix, Body&& body) {
+// Host staging of small per-launch tables (IndexSet segment tables) in
+// pinned memory, so that their copy to the device is a plain asynchronous
+// DMA (a copy from pageable memory first stages through the driver).  A
+// ring of four grow-only buffers per host thread; an event behind the last
+// copy out of a buffer says when it may be rewritten, so a thread blocks
+// only when four copies are still queued.
+class PinnedStage {
+ public:
+  static constexpr int kSlots = 4;
+  ~PinnedStage() {
+    for (Slot& sl : slots_) {
+      if (sl.done) cudaEventDestroy(sl.done);
+      if (sl.p) cudaFreeHost(sl.p);
+    }
+  }
+  // A buffer of at least `bytes` whose previous copy has completed.
+  unsigned char* get(size_t bytes) {
+    Slot& sl = slots_[next_];
+    if (sl.pending) {
+      check_cuda(cudaEventSynchronize(sl.done), "pinned staging");
+      sl.pending = false;
+    }
+    if (bytes > sl.cap) {
+      if (sl.p) cudaFreeHost(sl.p);
+      sl.p = nullptr;
+      sl.cap = 0;
+      check_cuda(cudaHostAlloc(reinterpret_cast<void**>(&sl.p), bytes, cudaHostAllocDefault), "pinned staging");
+      sl.cap = bytes;
+    }
+    return sl.p;
+  }
+  // After the copy out of the buffer get() returned was issued on stream s.
+  void copied(cudaStream_t s) {
+    Slot& sl = slots_[next_];
+    if (!sl.done) check_cuda(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming), "pinned staging");
+    check_cuda(cudaEventRecord(sl.done, s), "pinned staging");
+    sl.pending = true;
+    next_ = (next_ + 1) % kSlots;
+  }
+
+ private:
+  struct Slot {
+    unsigned char* p = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+  };
+  Slot slots_[kSlots];
+  int next_ = 0;
+};
+inline PinnedStage& pinned_stage() {
+  static thread_local PinnedStage st;
+  return st;
+}
+
+// Layout of an IndexSet's table, the same on the host and the device: the
+// segment descriptors (padded to 256 bytes), then the running lengths
+// (nseg + 1 entries).  Returns the total bytes; *desc_bytes is the padded
+// descriptor part.
+template <class T>
+inline size_t seg_table_bytes(int nseg, size_t* desc_bytes) {
+  *desc_bytes = ((size_t(nseg) * sizeof(SegDesc<T>) + 255) / 256) * 256;
+  return *desc_bytes + (size_t(nseg) + 1) * sizeof(long long);
+}
+
+// One launch over the segments of an IndexSet whose table (built by the
+// caller in the pinned stage buffer `host`) holds nseg descriptors and
+// their running lengths: one copy to launch-pool memory on the b200
+// stream, freed behind the launch.
+template <int BLOCK, bool Async, class T, class Body>
+void indexset_launch(const unsigned char* host, int nseg, size_t desc_bytes, size_t bytes, long long total,
+                     Body&& body) {
   using B = std::decay_t<Body>;
-  const int nseg = int(desc.size());
-  const long long total = prefix[size_t(nseg)];
   if (total == 0) return;
   cudaStream_t s = stream();
-  const size_t db = ((nseg * sizeof(SegDesc<T>) + 255) / 256) * 256;
-  void* tbl = launch_alloc(db + (nseg + 1) * sizeof(long long), s, "indexset table");
+  void* tbl = launch_alloc(bytes, s, "indexset table");
+  check_cuda(cudaMemcpyAsync(tbl, host, bytes, cudaMemcpyHostToDevice, s), "indexset table");
+  pinned_stage().copied(s);
   auto* d_desc = static_cast<SegDesc<T>*>(tbl);
-  long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + db);
-  check_cuda(cudaMemcpyAsync(d_desc, desc.data(), nseg * sizeof(desc[0]), cudaMemcpyHostToDevice, s),
-             "indexset table");
-  check_cuda(cudaMemcpyAsync(d_prefix, prefix.data(), (nseg + 1) * sizeof(long long), cudaMemcpyHostToDevice, s),
-             "indexset table");
+  long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + desc_bytes);
   tune::shaped_launch<BLOCK, tune::Tag<3, B, T>>("forall indexset", total, s, [&](auto NB, int items) {
     auto k = forall_indexset_kernel<NB(), B, T>;
     const unsigned g = grid_for<forall_indexset_kernel<NB(), B, T>>(NB(), total, items);
@@ -1620,20 +1681,23 @@ void forall_impl(b200_exec<BLOCK, Async> pol, const TypedIndexSet<Segs...>& is, 
   const auto& segs = is.segments();
   const int nseg = int(segs.size());
   if (nseg == 0) return;
-  std::vector<b200::detail::SegDesc<T>> desc(nseg);
-  std::vector<long long> prefix(nseg + 1, 0);
+  size_t db = 0;
+  const size_t bytes = b200::detail::seg_table_bytes<T>(nseg, &db);
+  unsigned char* h = b200::detail::pinned_stage().get(bytes);
+  auto* desc = reinterpret_cast<b200::detail::SegDesc<T>*>(h);
+  long long* prefix = reinterpret_cast<long long*>(h + db);
+  prefix[0] = 0;
   bool table_ok = true;
-  for (int i = 0; i < nseg; ++i) {
+  for (int i = 0; i < nseg && table_ok; ++i) {
     long long len = 0;
-    table_ok = table_ok && std::visit([&](const auto& g) { return b200::detail::seg_desc<T>(g, &desc[i], &len); },
-                                      segs[i]);
+    table_ok = std::visit([&](const auto& g) { return b200::detail::seg_desc<T>(g, &desc[i], &len); }, segs[i]);
     prefix[i + 1] = prefix[i] + len;
   }
   if (!table_ok) {
     for (const auto& v : segs) std::visit([&](const auto& g) { forall_impl(pol, g, body); }, v);
     return;
   }
-  b200::detail::indexset_launch<BLOCK, Async>(desc, prefix, std::forward<Body>(body));
+  b200::detail::indexset_launch<BLOCK, Async, T>(h, nseg, db, bytes, prefix[nseg], std::forward<Body>(body));
 }
 
 // ------------------------------------------------------ forall with params

@@ -464,18 +464,26 @@ void ref_indexset_forall(Res& r, const TypedIndexSet<SegmentTypes...>& iset, Loo
                          ForallParams f_params) {
   using T = typename TypedIndexSet<SegmentTypes...>::value_type;
   const int nseg = int(iset.getNumSegments());
-  std::vector<SegDesc<T>> desc(size_t(nseg > 0 ? nseg : 0));
-  std::vector<long long> prefix(size_t(nseg) + 1, 0);
-  bool ok = !has_reducer_params<ForallParams>();
-  for (int i = 0; i < nseg && ok; ++i) {
-    long long len = 0;
-    iset.segmentCall(size_t(i), RefSegDesc<T>{}, &desc[size_t(i)], &len, &ok);
-    prefix[size_t(i) + 1] = prefix[size_t(i)] + len;
-  }
   ResourceStream bound(res_stream(r));
-  if (ok) {
-    if (nseg > 0) indexset_launch<BLOCK, Async>(desc, prefix, std::forward<LoopBody>(loop_body));
-    return;
+  bool ok = !has_reducer_params<ForallParams>();
+  if (ok && nseg > 0) {
+    size_t db = 0;
+    const size_t bytes = seg_table_bytes<T>(nseg, &db);
+    unsigned char* h = pinned_stage().get(bytes);
+    auto* desc = reinterpret_cast<SegDesc<T>*>(h);
+    long long* prefix = reinterpret_cast<long long*>(h + db);
+    prefix[0] = 0;
+    for (int i = 0; i < nseg && ok; ++i) {
+      long long len = 0;
+      iset.segmentCall(size_t(i), RefSegDesc<T>{}, &desc[size_t(i)], &len, &ok);
+      prefix[size_t(i) + 1] = prefix[size_t(i)] + len;
+    }
+    if (ok) {
+      indexset_launch<BLOCK, Async, T>(h, nseg, db, bytes, prefix[nseg], std::forward<LoopBody>(loop_body));
+      return;
+    }
+  } else if (ok) {
+    return;  // no segments
   }
   for (int i = 0; i < nseg; ++i)
     iset.segmentCall(size_t(i), ::RAJA::detail::CallForall{}, b200_exec<BLOCK, true>(), loop_body, r, f_params);
