@@ -307,6 +307,17 @@ int b200_sort_pairs_f64_i64(double* keys, int64_t* vals, size_t n, int descendin
                             b200_stream_t stream);
 int b200_sort_pairs_f64_i32(double* keys, int32_t* vals, size_t n, int descending,
                             b200_stream_t stream);
+/* with the four above, every key type pairs with 32- and 64-bit values
+ * (the C++ layer sorts any 4- or 8-byte value type through these as bit
+ * patterns) */
+int b200_sort_pairs_i64_i32(int64_t* keys, int32_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_u32_i64(uint32_t* keys, int64_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_i32_i64(int32_t* keys, int64_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
+int b200_sort_pairs_f32_i64(float* keys, int64_t* vals, size_t n, int descending,
+                            b200_stream_t stream);
 int b200_sort_pairs_copy_f32_i32(const float* keys_in, const int32_t* vals_in,
                                  float* keys_out, int32_t* vals_out, size_t n,
                                  int descending, b200_stream_t stream);

@@ -2162,8 +2162,6 @@ void scan_exclusive(b200_exec<BLOCK, Async>, const T* b, const T* e, T* out, F, 
 namespace b200d {
 template <class K>
 inline int keys(K* k, size_t n, int desc, cudaStream_t s);
-template <class K, class V>
-inline int pairs(K* k, V* v, size_t n, int desc, cudaStream_t s);
 #define B200_SORT_BIND(SUF, K)                                                       \
   template <>                                                                        \
   inline int keys<K>(K * k, size_t n, int desc, cudaStream_t s) {                    \
@@ -2184,21 +2182,36 @@ template <>
 inline int keys<unsigned long long>(unsigned long long* k, size_t n, int desc, cudaStream_t s) {
   return b200_sort_keys_u64(reinterpret_cast<uint64_t*>(k), n, desc, s);
 }
-#define B200_PAIRS_BIND(SUF, K, V)                                                   \
-  template <>                                                                        \
-  inline int pairs<K, V>(K * k, V * v, size_t n, int desc, cudaStream_t s) {         \
-    return b200_sort_pairs_##SUF(k, v, n, desc, s);                                  \
+// Values travel with their keys as bit patterns, so every trivially
+// copyable 4- or 8-byte value type sorts through the 32- or 64-bit value
+// entry of its key type.
+template <class K, int VB>
+inline int pairs_bits(K* k, void* v, size_t n, int desc, cudaStream_t s);
+#define B200_PAIRS_BITS(K, SUF32, SUF64)                                                         \
+  template <>                                                                                   \
+  inline int pairs_bits<K, 4>(K * k, void* v, size_t n, int desc, cudaStream_t s) {             \
+    return b200_sort_pairs_##SUF32(k, static_cast<int32_t*>(v), n, desc, s);                    \
+  }                                                                                             \
+  template <>                                                                                   \
+  inline int pairs_bits<K, 8>(K * k, void* v, size_t n, int desc, cudaStream_t s) {             \
+    return b200_sort_pairs_##SUF64(k, static_cast<int64_t*>(v), n, desc, s);                    \
   }
-B200_PAIRS_BIND(u32_i32, uint32_t, int32_t)
-B200_PAIRS_BIND(u32_u32, uint32_t, uint32_t)
-B200_PAIRS_BIND(i32_i32, int32_t, int32_t)
-B200_PAIRS_BIND(f32_i32, float, int32_t)
-B200_PAIRS_BIND(u64_i32, uint64_t, int32_t)
-B200_PAIRS_BIND(u64_i64, uint64_t, int64_t)
-B200_PAIRS_BIND(i64_i64, int64_t, int64_t)
-B200_PAIRS_BIND(f64_i64, double, int64_t)
-B200_PAIRS_BIND(f64_i32, double, int32_t)
-#undef B200_PAIRS_BIND
+B200_PAIRS_BITS(uint32_t, u32_i32, u32_i64)
+B200_PAIRS_BITS(int32_t, i32_i32, i32_i64)
+B200_PAIRS_BITS(float, f32_i32, f32_i64)
+B200_PAIRS_BITS(uint64_t, u64_i32, u64_i64)
+B200_PAIRS_BITS(int64_t, i64_i32, i64_i64)
+B200_PAIRS_BITS(double, f64_i32, f64_i64)
+#undef B200_PAIRS_BITS
+template <class K, class V>
+inline int pairs(K* k, V* v, size_t n, int desc, cudaStream_t s) {
+  static_assert(std::is_trivially_copyable<V>::value && (sizeof(V) == 4 || sizeof(V) == 8),
+                "b200 sort_pairs takes trivially copyable 4- or 8-byte values");
+  using KK = typename std::conditional<
+      std::is_same<K, long long>::value, int64_t,
+      typename std::conditional<std::is_same<K, unsigned long long>::value, uint64_t, K>::type>::type;
+  return pairs_bits<KK, int(sizeof(V))>(reinterpret_cast<KK*>(k), static_cast<void*>(v), n, desc, s);
+}
 template <class C, class T>
 constexpr int desc_of() {
   static_assert(std::is_same<C, operators::less<T>>::value || std::is_same<C, operators::greater<T>>::value,

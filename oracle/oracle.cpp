@@ -566,6 +566,9 @@ ORC_PAIRS(u64_i64, uint64_t, int64_t)
 ORC_PAIRS(i64_i64, int64_t, int64_t)
 ORC_PAIRS(f64_i64, double, int64_t)
 ORC_PAIRS(f64_i32, double, int32_t)
+ORC_PAIRS(u32_i64, uint32_t, int64_t)
+ORC_PAIRS(i32_i64, int32_t, int64_t)
+ORC_PAIRS(f32_i64, float, int64_t)
 #undef ORC_PAIRS
 
 // ---- MultiReduceSum histogram (+1 per element); bins outside [0,nbins)

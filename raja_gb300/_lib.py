@@ -75,7 +75,7 @@ def _signatures() -> dict[str, tuple]:
     for t in ("u32", "u64", "f32"):
         sig[f"b200_sort_keys_copy_{t}"] = (_I, [_P, _P, _SZ, _I, _P])
     for kv in ("u32_i32", "u32_u32", "i32_i32", "f32_i32", "u64_i32", "u64_i64", "i64_i64",
-               "f64_i64", "f64_i32"):
+               "f64_i64", "f64_i32", "i64_i32", "u32_i64", "i32_i64", "f32_i64"):
         sig[f"b200_sort_pairs_{kv}"] = (_I, [_P, _P, _SZ, _I, _P])
     for kv in ("f32_i32", "u32_i32"):
         sig[f"b200_sort_pairs_copy_{kv}"] = (_I, [_P, _P, _P, _P, _SZ, _I, _P])

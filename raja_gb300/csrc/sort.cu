@@ -661,6 +661,10 @@ B200_SORT_PAIRS(u64_i64, uint64_t, int64_t)
 B200_SORT_PAIRS(i64_i64, int64_t, int64_t)
 B200_SORT_PAIRS(f64_i64, double, int64_t)
 B200_SORT_PAIRS(f64_i32, double, int32_t)
+B200_SORT_PAIRS(i64_i32, int64_t, int32_t)
+B200_SORT_PAIRS(u32_i64, uint32_t, int64_t)
+B200_SORT_PAIRS(i32_i64, int32_t, int64_t)
+B200_SORT_PAIRS(f32_i64, float, int64_t)
 #undef B200_SORT_PAIRS
 
 int b200_sort_pairs_copy_f32_i32(const float* kin, const int32_t* vin, float* kout,

@@ -327,6 +327,38 @@ void test_sorts() {
     for (Index_type i = 0; i < n; ++i) ok = ok && k[i] == kr[i] && v[i] == vr[i];
     snprintf(nm, sizeof nm, "sort_pairs_greater_%ld", (long)n);
     CHECK(nm, ok);
+    // any 4- or 8-byte value type: double and Index_type values, float keys
+    {
+      double* dv = managed<double>(n);
+      double* dvr = managed<double>(n);
+      Index_type* iv = managed<Index_type>(n);
+      Index_type* ivr = managed<Index_type>(n);
+      float* fk = managed<float>(n);
+      float* fkr = managed<float>(n);
+      fill();
+      for (Index_type i = 0; i < n; ++i) {
+        dv[i] = dvr[i] = 0.5 * double(i);
+        iv[i] = ivr[i] = n - i;
+        fk[i] = fkr[i] = float(k[i]) * 0.25f;
+      }
+      RAJA::stable_sort_pairs<exec>(RAJA::make_span(k, n), RAJA::make_span(dv, n));
+      RAJA::stable_sort_pairs<RAJA::seq_exec>(RAJA::make_span(kr, n), RAJA::make_span(dvr, n));
+      RAJA::stable_sort_pairs<exec>(RAJA::make_span(fk, n), RAJA::make_span(iv, n),
+                                    RAJA::operators::greater<float>{});
+      RAJA::stable_sort_pairs<RAJA::seq_exec>(RAJA::make_span(fkr, n), RAJA::make_span(ivr, n),
+                                              RAJA::operators::greater<float>{});
+      ok = true;
+      for (Index_type i = 0; i < n; ++i)
+        ok = ok && k[i] == kr[i] && dv[i] == dvr[i] && fk[i] == fkr[i] && iv[i] == ivr[i];
+      snprintf(nm, sizeof nm, "stable_sort_pairs_double_and_index_values_%ld", (long)n);
+      CHECK(nm, ok);
+      cudaFree(dv);
+      cudaFree(dvr);
+      cudaFree(iv);
+      cudaFree(ivr);
+      cudaFree(fk);
+      cudaFree(fkr);
+    }
     cudaFree(k);
     cudaFree(kr);
     cudaFree(v);

@@ -67,7 +67,8 @@ def test_sort_keys_bit_exact(prims, orc, kt):
 
 PAIRS = [(np.uint32, np.int32), (np.uint32, np.uint32), (np.int32, np.int32),
          (np.float32, np.int32), (np.uint64, np.int32), (np.uint64, np.int64),
-         (np.int64, np.int64), (np.float64, np.int64), (np.float64, np.int32)]
+         (np.int64, np.int64), (np.float64, np.int64), (np.float64, np.int32),
+         (np.int64, np.int32), (np.uint32, np.int64), (np.int32, np.int64), (np.float32, np.int64)]
 
 
 @pytest.mark.parametrize("kt,vt", PAIRS)
