@@ -89,6 +89,8 @@ struct KeyBits {
   }
 };
 
+__device__ __forceinline__ int pass_of_shift(int shift) { return shift >> 3; }
+
 // Status word: 2 flag bits on top, running count below.
 template <class ST>
 struct Status {
@@ -190,13 +192,18 @@ hist_kernel(const K* __restrict__ keys, size_t n, int desc, uint32_t* __restrict
 }
 
 // Exclusive scan of each pass's histogram -> digit bases.
+// A pass whose digit is the same for every key (one bin holds all n) keeps
+// the order: it is flagged in `same`, and runs as a plain copy.
 template <int P>
 __global__ void __launch_bounds__(RADIX) bins_kernel(const uint32_t* __restrict__ hist,
-                                                     uint32_t* __restrict__ bins) {
+                                                     uint32_t* __restrict__ bins, uint32_t n,
+                                                     int* __restrict__ same) {
   __shared__ uint32_t wsum[RADIX / 32];
   const int d = threadIdx.x, lane = d & 31, w = d >> 5;
   for (int p = 0; p < P; ++p) {
     const uint32_t c = hist[p * RADIX + d];
+    const int one_bin = __syncthreads_or(c == n);
+    if (d == 0) same[p] = one_bin;
     uint32_t inc = c;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -281,6 +288,7 @@ struct SweepSmem {
   uint32_t wtot[RADIX / 32];
   uint64_t bar;
   uint32_t tile;
+  int same;                                       // this pass's digit is one value
 };
 
 // Blocks per SM the shared memory allows (228 KB per SM, 1 KB reserved per
@@ -293,6 +301,64 @@ constexpr int sweep_min_blocks() {
   return b < 1 ? 1 : (b > cap ? cap : b);
 }
 
+// The tile of a pass whose digit is the same for every key keeps its
+// order: its keys (mapped to / from order-preserving form on the first /
+// last pass) and values go straight to the same positions of the
+// destination.  A full tile that TMA brought into shared memory (st, sv)
+// is written from there in 16-byte vectors; otherwise element by element
+// from global memory.  Out of line, so that the ranking path keeps its
+// register allocation.
+template <class K, bool FIRST, bool LAST>
+__device__ __forceinline__ K same_digit_key(K k, int desc) {
+  using KB = KeyBits<K>;
+  using U = typename KB::U;
+  if (FIRST) {
+    const U x = KB::to_ord(k, false);
+    return KB::cook(desc ? U(~x) : x);
+  }
+  if (LAST) {
+    const U uk = KB::raw(k);
+    return KB::from_ord(desc ? U(~uk) : uk, false);
+  }
+  return k;
+}
+template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST, int SRB, int TILE>
+__device__ __noinline__ void same_digit_copy(const K* __restrict__ kin, K* __restrict__ kout,
+                                             const V* __restrict__ vin, V* __restrict__ vout,
+                                             const K* st, const V* sv, bool staged, size_t tbase, int lim,
+                                             int desc, ST* status_row, bool downer) {
+  const int tid = threadIdx.x;
+  if (status_row && downer) status_row[tid] = ST(0);
+  const bool vec = staged && (reinterpret_cast<uintptr_t>(kout + tbase) % 16 == 0) &&
+                   (!HAS_V || reinterpret_cast<uintptr_t>(vout + tbase) % 16 == 0);
+  if (vec) {
+    constexpr int KN = Vec16<K>::N, KV = TILE / KN / SRB;
+    static_assert(TILE % (KN * SRB) == 0, "whole key vectors per thread");
+#pragma unroll
+    for (int j = 0; j < KV; ++j) {
+      const int g = j * SRB + tid;
+      Vec16<K> q = *reinterpret_cast<const Vec16<K>*>(st + size_t(g) * KN);
+#pragma unroll
+      for (int e = 0; e < KN; ++e) q.v[e] = same_digit_key<K, FIRST, LAST>(q.v[e], desc);
+      st_vec_stream(kout + tbase + size_t(g) * KN, q);
+    }
+    if (HAS_V) {
+      constexpr int VN = Vec16<V>::N, VV = TILE / VN / SRB;
+      static_assert(TILE % (VN * SRB) == 0, "whole value vectors per thread");
+#pragma unroll
+      for (int j = 0; j < VV; ++j) {
+        const int g = j * SRB + tid;
+        st_vec_stream(vout + tbase + size_t(g) * VN, *reinterpret_cast<const Vec16<V>*>(sv + size_t(g) * VN));
+      }
+    }
+    return;
+  }
+  for (int e = tid; e < lim; e += SRB) {
+    kout[tbase + e] = same_digit_key<K, FIRST, LAST>(kin[tbase + e], desc);
+    if (HAS_V) vout[tbase + e] = vin[tbase + e];
+  }
+}
+
 // HI: which 32-bit half of a 64-bit key holds this pass's digit (0 or 1,
 // known at compile time so the half is selected without a branch; 0 for
 // 32-bit keys).
@@ -302,7 +368,8 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
                 V* __restrict__ vout, size_t n, int shift, int desc,
                 const uint32_t* __restrict__ bins, ST* __restrict__ status,
                 ST* __restrict__ status_next, uint32_t* __restrict__ tile_counter,
-                uint32_t* __restrict__ err, uint32_t spin_limit, int tma_ok) {
+                uint32_t* __restrict__ err, uint32_t spin_limit, int tma_ok,
+                const int* __restrict__ same_digit) {
   using KB = KeyBits<K>;
   using U = typename KB::U;
   using S = Status<ST>;
@@ -315,21 +382,38 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
 #pragma unroll
   for (int i = tid; i < SW * RADIX; i += SRB) (&sm.wcnt[0][0])[i] = 0;
   if (tid == 0) {
-    sm.tile = atomicAdd(tile_counter, 1u);
+    const uint32_t t = atomicAdd(tile_counter, 1u);
+    sm.tile = t;
     mbar_init(&sm.bar, 1);
     fence_mbar_init();
-    const size_t b0 = size_t(sm.tile) * TILE;
+    const size_t b0 = size_t(t) * TILE;
     if (tma_ok && b0 + TILE <= n) {
       constexpr uint32_t kb = TILE * sizeof(K), vb = HAS_V ? TILE * sizeof(V) : 0;
       mbar_arrive_expect_tx(&sm.bar, kb + vb);
       tma_load_1d(sm.kin, kin + b0, kb, &sm.bar);
       if (HAS_V) tma_load_1d(sm.vin, vin + b0, vb, &sm.bar);
     }
+    // read after the copy is under way: it lands while the flag arrives
+    sm.same = same_digit[pass_of_shift(shift)];
   }
   __syncthreads();
   const size_t tile = sm.tile;
   const size_t tbase = tile * TILE;
   const int lim = (tbase + TILE <= n) ? TILE : int(n - tbase);  // valid keys in this tile
+  if (__builtin_expect(sm.same, 0)) {
+    // every key has this pass's digit: the order is unchanged, so the tile
+    // is copied to the same positions; no ranking, no look-back
+    const bool staged = tma_ok && lim == TILE;
+    if (staged && !mbar_wait(&sm.bar, 0, spin_limit)) {
+      if (tid == 0) atomicOr_system(err, kStatusTmaTimeout);
+      mbar_drain(&sm.bar, 0);  // let the copy land before the block goes on
+    }
+    same_digit_copy<K, V, HAS_V, ST, FIRST, LAST, SRB, TILE>(kin, kout, vin, vout, sm.kin, sm.vin, staged,
+                                                             tbase, lim, desc,
+                                                             LAST ? nullptr : status_next + tile * RADIX,
+                                                             downer);
+    return;
+  }
   if (tma_ok && lim == TILE) {
     if (!mbar_wait(&sm.bar, 0, spin_limit)) {
       if (tid == 0) atomicOr_system(err, kStatusTmaTimeout);
@@ -471,7 +555,8 @@ onesweep_kernel(const K* __restrict__ kin, K* __restrict__ kout, const V* __rest
 template <class K, class V, bool HAS_V, class ST, bool FIRST, bool LAST, int HI>
 int launch_sweep_t(const char* name, size_t tiles, cudaStream_t s, const K* src, K* dst,
                    const V* vsrc, V* vdst, size_t n, int shift, int desc, const uint32_t* bins,
-                   ST* status, ST* status_next, uint32_t* counter, uint32_t* err, uint32_t lim) {
+                   ST* status, ST* status_next, uint32_t* counter, uint32_t* err, uint32_t lim,
+                   const int* same) {
   const int tma_ok = (reinterpret_cast<uintptr_t>(src) % 16 == 0) &&
                      (!HAS_V || reinterpret_cast<uintptr_t>(vsrc) % 16 == 0);
   using SM = SweepSmem<K, V, HAS_V, ST>;
@@ -483,7 +568,7 @@ int launch_sweep_t(const char* name, size_t tiles, cudaStream_t s, const K* src,
   int bps = 0;
   B200_TRY(kernel_setup(ks, props, kern, threads, sizeof(SM), &bps));
   B200_LAUNCH(name, kern, (unsigned)tiles, threads, sizeof(SM), s, src, dst, vsrc, vdst, n, shift, desc,
-              bins, status, status_next, counter, err, lim, tma_ok);
+              bins, status, status_next, counter, err, lim, tma_ok, same);
   return B200_OK;
 }
 
@@ -491,26 +576,26 @@ template <class K, class V, bool HAS_V, class ST>
 int launch_sweep(const char* name, size_t tiles, cudaStream_t s, const K* src, K* dst,
                  const V* vsrc, V* vdst, size_t n, int shift, int first, int last, int desc,
                  const uint32_t* bins, ST* status, ST* status_next, uint32_t* counter,
-                 uint32_t* err, uint32_t lim) {
+                 uint32_t* err, uint32_t lim, const int* same) {
   // the first pass takes digit 0 (low half), the last the top digit
   constexpr int TOP = sizeof(K) == 8 ? 1 : 0;
   if (first)
     return launch_sweep_t<K, V, HAS_V, ST, true, false, 0>(name, tiles, s, src, dst, vsrc, vdst, n,
                                                            shift, desc, bins, status, status_next,
-                                                           counter, err, lim);
+                                                           counter, err, lim, same);
   if (last)
     return launch_sweep_t<K, V, HAS_V, ST, false, true, TOP>(name, tiles, s, src, dst, vsrc, vdst, n,
                                                              shift, desc, bins, status, status_next,
-                                                             counter, err, lim);
+                                                             counter, err, lim, same);
   if constexpr (sizeof(K) == 8) {
     if (shift >= 32)
       return launch_sweep_t<K, V, HAS_V, ST, false, false, 1>(name, tiles, s, src, dst, vsrc, vdst, n,
                                                               shift, desc, bins, status, status_next,
-                                                              counter, err, lim);
+                                                              counter, err, lim, same);
   }
   return launch_sweep_t<K, V, HAS_V, ST, false, false, 0>(name, tiles, s, src, dst, vsrc, vdst, n,
                                                           shift, desc, bins, status, status_next,
-                                                          counter, err, lim);
+                                                          counter, err, lim, same);
 }
 
 struct NoVal {};
@@ -540,6 +625,7 @@ int run_sort(const char* name, const K* kin, K* kout, const V* vin, V* vout, siz
   z.take<K>(n);                                    // alternate keys
   if (HAS_V) z.take<V>(n);                         // alternate values
   z.take<uint32_t>(P * RADIX);                     // bins
+  z.take<int>(P);                                  // passes whose digit is one value
   z.take<uint32_t>(P * RADIX + 64);                // hist + tile counters (memset)
   z.take<unsigned char>(2 * st_buf);               // ping-pong status words
   void* scr = nullptr;
@@ -548,6 +634,7 @@ int run_sort(const char* name, const K* kin, K* kout, const V* vin, V* vout, siz
   K* kalt = cv.take<K>(n);
   V* valt = HAS_V ? cv.take<V>(n) : nullptr;
   uint32_t* bins = cv.take<uint32_t>(P * RADIX);
+  int* same = cv.take<int>(P);
   uint32_t* hist = cv.take<uint32_t>(P * RADIX + 64);
   uint32_t* counters = hist + P * RADIX;
   unsigned char* stat = cv.take<unsigned char>(2 * st_buf);
@@ -568,7 +655,7 @@ int run_sort(const char* name, const K* kin, K* kout, const V* vin, V* vout, siz
     B200_LAUNCH("b200_sort_hist", (hist_kernel<K, P>), (unsigned)g, RB, smem, s, kin, n, desc, hist,
                 reinterpret_cast<uint4*>(stat), st_buf / 16);
   }
-  B200_LAUNCH("b200_sort_bins", bins_kernel<P>, 1, RADIX, 0, s, hist, bins);
+  B200_LAUNCH("b200_sort_bins", bins_kernel<P>, 1, RADIX, 0, s, hist, bins, uint32_t(n), same);
 
   using VV = typename std::conditional<HAS_V, V, uint32_t>::type;
   const uint32_t lim = spin_limit();
@@ -594,13 +681,13 @@ int run_sort(const char* name, const K* kin, K* kout, const V* vin, V* vout, siz
                                                      8 * p, first, last, desc, bins + p * RADIX,
                                                      static_cast<uint64_t*>(cur),
                                                      static_cast<uint64_t*>(nxt), counters + p,
-                                                     err, lim)));
+                                                     err, lim, same)));
     } else {
       B200_TRY((launch_sweep<K, VV, HAS_V, uint32_t>(sweep_name, tiles, s, src, dstk, vsrc, vdst, n,
                                                      8 * p, first, last, desc, bins + p * RADIX,
                                                      static_cast<uint32_t*>(cur),
                                                      static_cast<uint32_t*>(nxt), counters + p,
-                                                     err, lim)));
+                                                     err, lim, same)));
     }
   }
   static_assert(P % 2 == 0, "even number of digit passes ends in the home buffer");

@@ -246,3 +246,51 @@ def test_sort_large_sizes_exact(prims, n, kind):
             prims.sort_pairs(ko, vo, descending=desc)
             assert torch.equal(ko.view(sint), want), (kind, desc)
             assert torch.equal(vo, v[perm]), (kind, desc)        # stable: values in input order
+
+
+def _digits_varying(kt, n, seed, spec):
+    """Keys whose order-preserving form varies only in the digit positions
+    listed in spec (byte index -> True); the other digits are one value."""
+    rng = np.random.default_rng(seed)
+    ut = np.uint32 if np.dtype(kt).itemsize == 4 else np.uint64
+    nb = np.dtype(kt).itemsize
+    u = np.zeros(n, dtype=ut)
+    for b in range(nb):
+        byte = rng.integers(0, 256, n, dtype=np.uint64) if spec.get(b) else np.full(n, 0x5a, np.uint64)
+        u |= (byte.astype(ut) << ut(8 * b))
+    return u.view(kt) if kt in (np.uint32, np.uint64) else u.view(np.dtype(kt))
+
+
+# digit passes whose digit is the same for every key run as plain copies,
+# decided on the device: several such passes, first and last included, in
+# place and out of place, keys and pairs, ascending and descending
+@pytest.mark.parametrize("kt,spec", [
+    (np.uint64, {0: 1, 1: 1, 2: 1}),          # 5 of 8 passes copy
+    (np.uint64, {0: 1, 1: 1, 7: 1}),          # 5 copy
+    (np.uint64, {}),                          # all equal: every pass copies
+    (np.uint32, {0: 1, 1: 1}),                # 2 of 4 copy, the last included
+    (np.uint32, {1: 1, 3: 1}),                # the first pass copies
+    (np.int64, {0: 1, 4: 1}),                 # signed: 6 copy
+    (np.float64, {0: 1, 5: 1, 6: 1}),         # 5 copy (bit patterns of doubles)
+])
+def test_sort_constant_digits_exactly(prims, orc, kt, spec):
+    n = 300007
+    x = _digits_varying(kt, n, 11, spec)
+    if np.dtype(kt).kind == "f":
+        x = np.where(np.isnan(x), np.zeros_like(x), x)
+    for desc in (False, True):
+        d = to_dev(x)
+        prims.sort(d, descending=desc)  # in place
+        np.testing.assert_array_equal(to_host(d), orc.sort(x, descending=desc), err_msg=f"{spec} {desc}")
+        v = np.arange(n, dtype=np.int32)
+        dk, dv = to_dev(x), to_dev(v)
+        prims.sort_pairs(dk, dv, descending=desc)
+        ek, ev = orc.sort_pairs(x, v, descending=desc)
+        np.testing.assert_array_equal(to_host(dk), ek)
+        np.testing.assert_array_equal(to_host(dv), ev)
+    if kt in (np.uint32, np.uint64):
+        src = to_dev(x)
+        out = to_dev(np.zeros_like(x))
+        prims.sort_copy(src, out)  # out of place: the input stays
+        np.testing.assert_array_equal(to_host(out), orc.sort(x))
+        np.testing.assert_array_equal(to_host(src), x)
