@@ -16,10 +16,11 @@
 // memory.  A persistent grid (SM count x resident blocks) walks the tiles;
 // every tile has the same size (only each loop's last tile is short), so
 // the load is balanced whatever the length distribution.  Per-loop
-// reductions are fused: each tile writes a compensated partial, and the
-// last tile of a loop to finish (per-loop ticket) folds that loop's
-// partials in tile order, so the result is deterministic.  The tile size
-// and block size are autotuned per plan by timing the candidates.
+// reductions are fused: each warp keeps a compensated partial across the
+// tiles of one loop and stores it when its block moves to the next loop;
+// a second small launch adds each loop's warp partials in a fixed order,
+// so the result is deterministic.  The tile size and block size are
+// autotuned per plan by timing the candidates.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -41,11 +42,9 @@ struct b200_batch_plan_s {
   int64_t ntiles = 0;
   int32_t* d_tile_loop = nullptr;  // ntiles
   int64_t* d_loop_tile0 = nullptr; // nloops + 1
-  uint32_t* d_loop_cnt = nullptr;  // nloops, zero between launches
-  double* d_tile_part = nullptr;   // ntiles
+  double* d_tile_part = nullptr;   // ntiles x 16 warp partials of the runs
   int variant = -1;                // autotuned kernel variant (-1: default)
   // segmented sort classification
-  bool has_empty = false;          // some loop has no iterations (no tile)
   std::vector<int> big_segments;   // segments longer than the block sort
   int32_t* d_small = nullptr;      // ids of the small segments
   int nsmall = 0;
@@ -167,60 +166,37 @@ __device__ __forceinline__ double tile_axpy_sum(float a, const float* __restrict
   return double(s) + double(c);
 }
 
-// Fold one block's partial of a run of tiles [r0, r1) of `loop` into the
-// per-loop result.  The partial goes to the slot of the run's first tile and
-// zeros to the others, so that the loop's slots always hold one value per
-// tile; the block that completes the loop's tile count folds the slots in
-// tile order.  The runs are fixed by the grid, so the sum is deterministic.
-template <int BLOCK>
-__device__ __forceinline__ void flush_loop_run(double p, int loop, int64_t r0, int64_t r1,
-                                               const int64_t* __restrict__ loop_tile0,
-                                               double* __restrict__ sums, double* __restrict__ tile_part,
-                                               uint32_t* __restrict__ loop_cnt, double* sh, bool* last) {
-  p = block_sum<BLOCK>(p, sh);
-  const int64_t t0 = loop_tile0[loop];
-  const int64_t nt = loop_tile0[loop + 1] - t0;
-  for (int64_t k = r0 + threadIdx.x; k < r1; k += BLOCK) tile_part[k] = (k == r0) ? p : 0.0;
-  __threadfence();  // every writer publishes its slots before the ticket
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const uint32_t prev = atomicAdd(loop_cnt + loop, uint32_t(r1 - r0));
-    *last = (int64_t(prev) + (r1 - r0) == nt);
-  }
-  __syncthreads();
-  if (*last) {
-    __threadfence();
-    double q = 0.0;
-    for (int64_t k = threadIdx.x; k < nt; k += BLOCK) q += __ldcg(tile_part + t0 + k);
-    q = block_sum<BLOCK>(q, sh);
-    if (threadIdx.x == 0) {
-      sums[loop] = q;
-      loop_cnt[loop] = 0u;
-    }
-  }
-  __syncthreads();
-}
+// Warps per block of the largest batched variant: the run partials hold
+// one slot per (tile, warp) of it.
+constexpr int kMaxBatchWarps = 16;
 
 // All loops in one launch.  Each block takes a contiguous run of the tile
 // table (tiles are equal-sized, so the runs are balanced), prefetches the
 // next tile's descriptor, and keeps its partial sum in registers across the
-// tiles of one loop: the block reduction and the per-loop ticket run once
-// per loop the block touches instead of once per tile.
+// tiles of one loop.  When the loop changes, each warp reduces its lanes'
+// partials and stores them in the slot (first tile of the run, warp): no
+// fences, tickets or block barriers inside the loop.  batched_fold_kernel
+// then adds each loop's slots in run and warp order, so the sums are
+// deterministic for a given tiling.
 template <int BLOCK, int ITEMS>
 __global__ void __launch_bounds__(BLOCK)
 batched_axpy_sum_kernel(const int32_t* __restrict__ tile_loop,
                         const int64_t* __restrict__ loop_tile0,
                         const int64_t* __restrict__ loop_len, int64_t ntiles, float a,
                         const float* const* __restrict__ xs, float* const* __restrict__ ys,
-                        double* __restrict__ sums, double* __restrict__ tile_part,
-                        uint32_t* __restrict__ loop_cnt, int comp) {
+                        double* __restrict__ run_part, int comp) {
   constexpr int TILE = BLOCK * ITEMS;
-  __shared__ double sh[32];
-  __shared__ bool last;
+  static_assert(BLOCK / 32 <= kMaxBatchWarps, "one run slot per warp");
   const int64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
   const int64_t b0 = int64_t(blockIdx.x) * per;
   const int64_t b1 = b0 + per < ntiles ? b0 + per : ntiles;
   if (b0 >= b1) return;                            // block-uniform
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  auto flush = [&](double v, int64_t r0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) run_part[r0 * kMaxBatchWarps + warp] = v;
+  };
   int cur = -1;                                    // loop of the running partial
   int64_t run0 = b0, t0 = 0, len = 0;
   const float* x = nullptr;
@@ -231,7 +207,7 @@ batched_axpy_sum_kernel(const int32_t* __restrict__ tile_loop,
     const int loop = nxt;
     if (t + 1 < b1) nxt = tile_loop[t + 1];         // one tile ahead
     if (loop != cur) {                             // block-uniform
-      if (cur >= 0) flush_loop_run<BLOCK>(acc, cur, run0, t, loop_tile0, sums, tile_part, loop_cnt, sh, &last);
+      if (cur >= 0) flush(acc, run0);
       cur = loop;
       run0 = t;
       acc = 0.0;
@@ -244,7 +220,23 @@ batched_axpy_sum_kernel(const int32_t* __restrict__ tile_loop,
     const int64_t hi = min(lo + TILE, len);
     acc += tile_axpy_sum<BLOCK, ITEMS>(a, x, y, lo, hi, comp != 0);
   }
-  flush_loop_run<BLOCK>(acc, cur, run0, b1, loop_tile0, sums, tile_part, loop_cnt, sh, &last);
+  flush(acc, run0);
+}
+
+// Each loop's sum from its run partials.  The loop's runs start at its
+// first tile and at every block boundary (multiple of `per`, the tiles per
+// block of the main launch) inside it; a run's slots are added in warp
+// order.  A loop with no tile sums to 0.
+__global__ void __launch_bounds__(256)
+batched_fold_kernel(const int64_t* __restrict__ loop_tile0, int nloops, int64_t per, int warps,
+                    const double* __restrict__ run_part, double* __restrict__ sums) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nloops) return;
+  const int64_t T0 = loop_tile0[l], T1 = loop_tile0[l + 1];
+  double q = 0.0;
+  for (int64_t r0 = T0; r0 < T1; r0 = (r0 / per + 1) * per)
+    for (int w = 0; w < warps; ++w) q += run_part[r0 * kMaxBatchWarps + w];
+  sums[l] = q;
 }
 
 // One fused axpy + sum over a single loop (the per-loop launch that the
@@ -293,8 +285,11 @@ int launch_batched(b200_batch_plan_s* p, float a, const float* const* xs, float*
   if (grid > p->ntiles) grid = p->ntiles;
   if (grid < 1) grid = 1;
   B200_LAUNCH("b200_batched_axpy_sum", (batched_axpy_sum_kernel<BLOCK, ITEMS>), unsigned(grid),
-              BLOCK, 0, s, p->d_tile_loop, p->d_loop_tile0, p->d_lens, p->ntiles, a, xs, ys, sums,
-              p->d_tile_part, p->d_loop_cnt, comp);
+              BLOCK, 0, s, p->d_tile_loop, p->d_loop_tile0, p->d_lens, p->ntiles, a, xs, ys,
+              p->d_tile_part, comp);
+  const int64_t per = (p->ntiles + grid - 1) / grid;  // tiles per block, as the kernel splits them
+  B200_LAUNCH("b200_batched_fold", batched_fold_kernel, unsigned((p->nloops + 255) / 256), 256, 0, s,
+              p->d_loop_tile0, p->nloops, per, BLOCK / 32, p->d_tile_part, sums);
   return B200_OK;
 }
 
@@ -313,11 +308,9 @@ int dispatch_batched(int v, b200_batch_plan_s* p, float a, const float* const* x
 void free_tiling(b200_batch_plan_s* p) {
   cudaFree(p->d_tile_loop);
   cudaFree(p->d_loop_tile0);
-  cudaFree(p->d_loop_cnt);
   cudaFree(p->d_tile_part);
   p->d_tile_loop = nullptr;
   p->d_loop_tile0 = nullptr;
-  p->d_loop_cnt = nullptr;
   p->d_tile_part = nullptr;
   p->ntiles = 0;
 }
@@ -334,11 +327,9 @@ int build_tiling(b200_batch_plan_s* p, int tile) {
     for (int64_t k = t0[i]; k < t0[i + 1]; ++k) tl[k] = i;
   B200_CUDA(cudaMalloc(&p->d_tile_loop, tl.size() * sizeof(int32_t)));
   B200_CUDA(cudaMalloc(&p->d_loop_tile0, t0.size() * sizeof(int64_t)));
-  B200_CUDA(cudaMalloc(&p->d_loop_cnt, std::max(p->nloops, 1) * sizeof(uint32_t)));
-  B200_CUDA(cudaMalloc(&p->d_tile_part, tl.size() * sizeof(double)));
+  B200_CUDA(cudaMalloc(&p->d_tile_part, tl.size() * kMaxBatchWarps * sizeof(double)));
   B200_CUDA(cudaMemcpy(p->d_tile_loop, tl.data(), tl.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
   B200_CUDA(cudaMemcpy(p->d_loop_tile0, t0.data(), t0.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
-  B200_CUDA(cudaMemset(p->d_loop_cnt, 0, std::max(p->nloops, 1) * sizeof(uint32_t)));
   p->tile = tile;
   p->ntiles = nt;
   return B200_OK;
@@ -606,7 +597,6 @@ int b200_batch_plan_create(const int64_t* lens, int nloops, b200_batch_plan* out
                 cudaMemcpyHostToDevice), "plan offsets copy");
   std::vector<int32_t> small;
   for (int i = 0; i < nloops; ++i) {
-    if (lens[i] == 0) p->has_empty = true;
     if (lens[i] <= 1) continue;
     if (lens[i] <= SEG_CAP) small.push_back(i);
     else p->big_segments.push_back(i);
@@ -662,9 +652,7 @@ int b200_batched_axpy_sum_f32(b200_batch_plan p, float a, const float* const* xs
   }
   const Variant v = kVariants[p->variant];
   B200_TRY(build_tiling(p, v.block * v.items));
-  // loops of length zero have no tile: their sums are zero
-  if (p->has_empty)
-    B200_CUDA(cudaMemsetAsync(sums, 0, p->nloops * sizeof(double), static_cast<cudaStream_t>(stream)));
+  // loops of length zero have no tile: the fold writes their sums as zero
   B200_TRY(dispatch_batched(p->variant, p, a, xs, ys, sums, (mode & B200_MODE_COMPENSATED) ? 1 : 0,
                             static_cast<cudaStream_t>(stream)));
   clear_error();

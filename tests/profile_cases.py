@@ -15,6 +15,10 @@ Run from the repository root:
     python tests/profile_cases.py jacobi_mesh512
         three fused Jacobi sweeps of one 512^3 fp64 mesh (two 1.07 GB
         buffers).
+    python tests/profile_cases.py batched_4096_loops
+        the 4096-loop WorkGroup shape (lognormal lengths, median 2000,
+        sigma 1.5, 2.4e7 elements): one autotuned persistent fp32 axpy +
+        per-loop compensated sum, then two more launches of it.
 
 Each prints "ok" and nothing else.  The summaries under profiles/ quote the
 ncu commands that use them.
@@ -86,8 +90,25 @@ def jacobi_mesh512():
     plan.close()
 
 
+def batched_4096_loops():
+    import numpy as np
+    rng = np.random.default_rng(4)
+    lens = np.clip(np.round(np.exp(rng.normal(np.log(2000), 1.5, 4096))), 32, 1 << 20).astype(np.int64)
+    offs = np.concatenate([[0], np.cumsum(lens)])
+    x = torch.rand(int(offs[-1]), device="cuda", generator=_gen(2)) * 2 - 1
+    y = torch.rand(int(offs[-1]), device="cuda", generator=_gen(3)) * 2 - 1
+    px = torch.tensor([x.data_ptr() + 4 * int(o) for o in offs[:-1]], dtype=torch.int64, device="cuda")
+    py = torch.tensor([y.data_ptr() + 4 * int(o) for o in offs[:-1]], dtype=torch.int64, device="cuda")
+    sums = torch.zeros(len(lens), dtype=torch.float64, device="cuda")
+    plan = rg.BatchPlan(lens)
+    rg.batched_axpy_sum(plan, 1e-3, px, py, sums, autotune=True)
+    for _ in range(2):
+        rg.batched_axpy_sum(plan, 1e-3, px, py, sums)
+    plan.close()
+
+
 CASES = {f.__name__: f for f in (sort_pass, sort_k32_n2p27, sort_k64_n2p27, sort_pairs_n2p27,
-                                 scan_i64_n2p27, jacobi_mesh512)}
+                                 scan_i64_n2p27, jacobi_mesh512, batched_4096_loops)}
 
 if __name__ == "__main__":
     if len(sys.argv) != 2 or sys.argv[1] not in CASES:
