@@ -1020,7 +1020,9 @@ def bench_raja_api(lib):
     os.makedirs(out_dir, exist_ok=True)
     exe = os.path.join(out_dir, "bench_raja_api")
     src = os.path.join(ROOT, "tests", "cpp", "bench_raja_api.cu")
-    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(src), os.path.getmtime(lib_path)):
+    import glob
+    deps = [src, lib_path] + glob.glob(os.path.join(ROOT, "include", "raja_b200", "*.hpp"))
+    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(d) for d in deps):
         cmd = [b.nvcc(), "-std=c++17", "--extended-lambda", "--expt-relaxed-constexpr", "-O2", *b.ARCH,
                f"-I{ROOT}/include/raja_compat", f"-I{ROOT}/include", src, "-o", exe,
                f"-L{os.path.dirname(lib_path)}", "-lb200prims", "-Xlinker",

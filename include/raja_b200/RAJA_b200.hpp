@@ -211,16 +211,29 @@ inline LaunchCtx& ctx() {
 
 // WorkGroup capture (host): while a b200 WorkPool copies an enqueued loop
 // body, each captured b200 reducer gets a slot for that loop -- one
-// partial per tile of the loop and a ticket, in device memory -- and an
-// accumulator cell in mapped pinned memory, into which the last tile of
-// every run folds the loop's result (runs fold in stream order, so no host
-// work is needed per run).  The pool's registry owns both and records an
-// event behind the last run on each stream; a reducer's get() waits for
-// those events and reads its cell.
+// partial per (tile, warp) of the loop, in device memory -- an accumulator
+// cell in mapped pinned memory, and a fold entry.  After each run's loop
+// launches, one fold launch adds every entry's partials in (tile, warp)
+// order and folds the loop's result into the cell (runs fold in stream
+// order, so no host work is needed per run).  The pool's registry owns the
+// slots, cells and entries and records an event behind the last run on
+// each stream; a reducer's get() waits for those events and reads its cell.
 constexpr size_t kWgCellBytes = 32;  // value (at most 24 bytes), then a "has a value" word at byte 28
+// Device code that adds `count` partials in index order and folds the
+// result into a cell (one per reducer kind).  Its address sits in the
+// 16 bytes in front of a slot's partials, stored there on the device by the
+// warp that writes partial 0 of each run.
+using wg_fold_fn = void (*)(const void* parts, unsigned count, void* cell);
+constexpr size_t kWgSlotHeader = 16;
+struct WgFold {
+  const void* parts;  // the loop's partials: tile-major, one per warp of the block
+  void* cell;         // device address of the reducer's cell
+  long long loop;     // the loop's index in its group
+};
 struct WgRegistry {
   std::vector<void*> blocks;       // device memory of the slots
   std::vector<void*> host_blocks;  // mapped pinned memory of the cells
+  std::vector<WgFold> folds;       // one per (captured reducer, loop), in capture order
   unsigned char* cell_host = nullptr;
   unsigned char* cell_dev = nullptr;
   size_t cells_left = 0;
@@ -264,7 +277,7 @@ struct WgRegistry {
   }
   // Before a run's launches on stream s: when loops captured reducers, the
   // run follows every earlier run on other streams (runs of one group share
-  // the reducers' partials and tickets, and fold into the cells in order).
+  // the reducers' partials, and fold into the cells in order).
   // Runs issued while s is being captured into a graph are left out: the
   // graph's launches are ordered by the caller, and the reducers' cells are
   // read after the caller has synchronised the graph's stream.
@@ -305,7 +318,8 @@ struct WgRegistry {
 struct WgCaptureCtx {
   bool active = false;
   std::shared_ptr<WgRegistry> reg;
-  long long ntiles = 0;               // tiles of the loop being captured, at the smallest tile size
+  long long nslots = 0;               // partials the loop being captured needs (most over the tile shapes)
+  long long loop = 0;                 // its index in the group
   unsigned long long capture_id = 0;  // new for every enqueue
 };
 inline WgCaptureCtx& wg_capture() {
@@ -313,13 +327,6 @@ inline WgCaptureCtx& wg_capture() {
   return c;
 }
 
-// Device side of a WorkGroup run: the tile of the loop a block is running
-// and the loop's tile count at this run's tile size.  Set by the runner
-// kernels before each loop body runs.
-struct WgDevCtx {
-  long long tile;
-  long long ntiles;
-};
 
 // Grid for a kernel that always runs `block` threads: one block per
 // `block` x `items` elements, capped at the resident blocks of the whole
@@ -450,11 +457,13 @@ __device__ inline void grid_combine(const DevSlot<T>& s, T v, Merge merge) {
   }
 }
 
-// The device context of a WorkGroup run, one per block (set by the runner
-// kernels, read by the loop reducers' combine).
-__device__ __forceinline__ WgDevCtx& wg_dev_ctx() {
-  __shared__ WgDevCtx c;
-  return c;
+// The device context of a WorkGroup run: per warp of the block, the slot
+// its reducer partials go to for the tile being run (tile of the loop x
+// warps per block + warp).  Lane 0 of the warp writes it before the loop
+// body runs and reads it in the reducers' combine, so no barrier is needed.
+__device__ __forceinline__ long long* wg_warp_slots() {
+  __shared__ long long slots[32];
+  return slots;
 }
 
 // Fold count partials in index order with every thread of the block
@@ -485,6 +494,29 @@ __device__ inline T fold_partials(const T* parts, unsigned count, Merge merge) {
   return acc;
 }
 
+// A WorkGroup reducer's fold: add the loop's partials of this run in index
+// order (tile, then warp) and fold the result into the reducer's cell.  The
+// cell is mapped host memory; the runs of one group fold in stream order.
+template <class K>
+__device__ void wg_fold(const void* parts, unsigned count, void* cell_v) {
+  using V = typename K::V;
+  static_assert(sizeof(V) <= 24, "reducer value larger than a WorkGroup cell");
+  auto merge = [](V a, V b) { return K::merge(a, b); };
+  const V r = fold_partials(static_cast<const V*>(parts), count, merge);
+  if (lin_tid() == 0) {
+    unsigned char* cell = static_cast<unsigned char*>(cell_v);
+    volatile unsigned* has = reinterpret_cast<volatile unsigned*>(cell + 28);
+    V acc = r;
+    if (*has != 0u) {
+      V prev;
+      memcpy(&prev, cell, sizeof(V));
+      acc = merge(prev, r);
+    }
+    memcpy(cell, &acc, sizeof(V));
+    __threadfence_system();
+    *has = 1u;
+  }
+}
 // Stream-ordered pool of the current device for the C++ layer's per-launch
 // device memory (reducer partials, IndexSet tables).  Its release threshold
 // is unbounded: the device's default pool returns freed memory at every
@@ -674,14 +706,12 @@ class DevReducer {
   bool original_ = false;
   bool launch_copy_ = false;
   bool owner_ = false;
-  bool wg_ = false;  // a WorkGroup loop's copy: tile-ordered combine
+  bool wg_ = false;  // a WorkGroup loop's copy: per-warp partials, folded after the run
   DevSlot<V> slot_{nullptr, nullptr, nullptr};
   mutable V val_;
 
-  // The tile-ordered combine of a WorkGroup loop's reducer: every tile
-  // publishes its block's partial; the block that completes the loop's tile
-  // count folds the partials in tile order (deterministic) and folds the
-  // run's result into the reducer's accumulator cell.
+  // The combine of a WorkGroup loop's reducer: each warp of a tile stores
+  // its partial in its slot; the run's fold launch adds them (wg_fold).
   __device__ void wg_combine(V v) const;
 
  public:
@@ -697,25 +727,25 @@ class DevReducer {
     shared_ = o.shared_;
     LaunchCtx& c = ctx();
     WgCaptureCtx& w = wg_capture();
-    if (w.active && !o.launch_copy_ && w.ntiles == 0) {
+    if (w.active && !o.launch_copy_ && w.nslots == 0) {
       // an empty loop never runs: no slot, the reducer keeps its value
       slot_ = o.slot_;
       launch_copy_ = false;
     } else if (w.active && !o.launch_copy_) {
       if (shared_->slot_capture != w.capture_id) {
-        const size_t pbytes = ((size_t(w.ntiles > 0 ? w.ntiles : 1) * sizeof(V) + 255) / 256) * 256;
+        static_assert(alignof(V) <= kWgSlotHeader, "reducer values are aligned to at most 16 bytes");
+        const size_t pbytes = kWgSlotHeader + size_t(w.nslots) * sizeof(V);
         void* blk = nullptr;
-        check_cuda(cudaMalloc(&blk, pbytes + 256), "WorkGroup reducer slot");
-        check_cuda(cudaMemset(static_cast<char*>(blk) + pbytes, 0, sizeof(unsigned)), "WorkGroup reducer ticket");
+        check_cuda(cudaMalloc(&blk, pbytes), "WorkGroup reducer slot");
+        V* parts = reinterpret_cast<V*>(static_cast<char*>(blk) + kWgSlotHeader);
+        unsigned char *cell_host = nullptr, *cell_dev = nullptr;
+        w.reg->new_cell(&cell_host, &cell_dev);
         {
           std::lock_guard<std::mutex> g(w.reg->m);
           w.reg->blocks.push_back(blk);
+          w.reg->folds.push_back(WgFold{parts, cell_dev, w.loop});
         }
-        unsigned char *cell_host = nullptr, *cell_dev = nullptr;
-        w.reg->new_cell(&cell_host, &cell_dev);
-        shared_->wg_slot = DevSlot<V>{static_cast<V*>(blk),
-                                      reinterpret_cast<unsigned*>(static_cast<char*>(blk) + pbytes),
-                                      reinterpret_cast<V*>(cell_dev)};
+        shared_->wg_slot = DevSlot<V>{parts, nullptr, reinterpret_cast<V*>(cell_dev)};
         shared_->wg_cells.push_back(cell_host);
         if (std::find(shared_->wg_regs.begin(), shared_->wg_regs.end(), w.reg) == shared_->wg_regs.end())
           shared_->wg_regs.push_back(w.reg);
@@ -800,34 +830,14 @@ class DevReducer {
 
 template <class K>
 __device__ void DevReducer<K>::wg_combine(V v) const {
-  __shared__ bool last;
-  const WgDevCtx& c = wg_dev_ctx();
-  auto merge = [](V a, V b) { return K::merge(a, b); };
-  v = block_reduce(v, merge);
-  if (lin_tid() == 0) {
-    slot_.partials[c.tile] = v;
-    __threadfence();
-    last = ::atomicAdd(slot_.ticket, 1u) == unsigned(c.ntiles - 1);
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  const V r = fold_partials(slot_.partials, unsigned(c.ntiles), merge);
-  if (lin_tid() == 0) {
-    static_assert(sizeof(V) <= 24, "reducer value larger than a WorkGroup cell");
-    // the cell is mapped host memory; runs of one group fold in stream order
-    unsigned char* cell = reinterpret_cast<unsigned char*>(slot_.result);
-    volatile unsigned* has = reinterpret_cast<volatile unsigned*>(cell + 28);
-    V acc = r;
-    if (*has != 0u) {
-      V prev;
-      memcpy(&prev, cell, sizeof(V));
-      acc = merge(prev, r);
-    }
-    memcpy(cell, &acc, sizeof(V));
-    __threadfence_system();
-    *has = 1u;
-    *slot_.ticket = 0u;  // ready for the next run
+  // WorkGroup launches are 1-D with whole warps
+  const int lane = int(threadIdx.x & 31);
+  v = warp_fold(v, lane, 32, 32, [](V a, V b) { return K::merge(a, b); });
+  if (lane == 0) {
+    const long long slot = wg_warp_slots()[threadIdx.x >> 5];
+    slot_.partials[slot] = v;
+    if (slot == 0)  // once per run: the fold the run's fold launch calls
+      *reinterpret_cast<wg_fold_fn*>(reinterpret_cast<char*>(slot_.partials) - kWgSlotHeader) = wg_fold<K>;
   }
 }
 
@@ -2295,7 +2305,9 @@ constexpr int kWgItems = 8;  // elements per thread of a fixed-BLOCK WorkGroup t
 
 // All loops in one launch over tiles of `tile` elements: prefix[l] is the
 // first tile of loop l (prefix[nloops] the tile count), and block b runs
-// tiles b, b + grid, ...; a tile finds its loop by binary search.
+// tiles b, b + grid, ...; a tile finds its loop by binary search.  Nothing
+// is shared between the warps of a block (each warp's reducer partials go
+// to their own slot), so the kernel has no barrier.
 // The loop bodies are reached through device function pointers, which
 // makes the kernels take a full register budget unless it is capped: at
 // 32 registers a thread, 2048 threads fit on an SM and twice as many
@@ -2304,7 +2316,9 @@ template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK)
 wg_kernel(const long long* prefix, int nloops, long long tile, const WgLoop* loops,
           const unsigned char* bodies) {
-  WgDevCtx& c = wg_dev_ctx();
+  static_assert(BLOCK % 32 == 0 && BLOCK <= 1024, "b200_work blocks are whole warps");
+  long long* slots = wg_warp_slots();
+  const int warp = int(threadIdx.x >> 5);
   const long long ntiles = prefix[nloops];
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
     int lo = 0, hi = nloops;
@@ -2315,30 +2329,32 @@ wg_kernel(const long long* prefix, int nloops, long long tile, const WgLoop* loo
     }
     const WgLoop lp = loops[lo];
     const long long k = t - prefix[lo];
-    if (threadIdx.x == 0) {
-      c.tile = k;
-      c.ntiles = prefix[lo + 1] - prefix[lo];
-    }
-    __syncthreads();
+    if ((threadIdx.x & 31) == 0) slots[warp] = k * (BLOCK / 32) + warp;
     const long long a = k * tile;
     lp.fn(bodies + lp.body_off, lp.begin, a, a + tile < lp.len ? a + tile : lp.len);
-    __syncthreads();
   }
 }
 // One loop per launch (the ordered runners): block b runs tile b.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK)
 wg_one_kernel(const WgLoop* loops, int which, long long tile, const unsigned char* bodies) {
+  static_assert(BLOCK % 32 == 0 && BLOCK <= 1024, "b200_work blocks are whole warps");
   const WgLoop lp = loops[which];
-  WgDevCtx& c = wg_dev_ctx();
-  if (threadIdx.x == 0) {
-    c.tile = blockIdx.x;
-    c.ntiles = (lp.len + tile - 1) / tile;
-  }
-  __syncthreads();
+  const int warp = int(threadIdx.x >> 5);
+  if ((threadIdx.x & 31) == 0) wg_warp_slots()[warp] = (long long)blockIdx.x * (BLOCK / 32) + warp;
   const long long lo = (long long)blockIdx.x * tile;
   const long long hi = lo + tile < lp.len ? lo + tile : lp.len;
   lp.fn(bodies + lp.body_off, lp.begin, lo, hi);
+}
+// The reducers' folds of a run, one block per (reducer, loop): the loop has
+// prefix[l + 1] - prefix[l] tiles at the run's tile size, each with `warps`
+// partials.
+__global__ void __launch_bounds__(256)
+wg_fold_kernel(const WgFold* folds, const long long* prefix, int warps) {
+  const WgFold f = folds[blockIdx.x];
+  const long long count = (prefix[f.loop + 1] - prefix[f.loop]) * warps;
+  const wg_fold_fn fn = *reinterpret_cast<const wg_fold_fn*>(static_cast<const char*>(f.parts) - kWgSlotHeader);
+  fn(f.parts, unsigned(count), f.cell);
 }
 // The tile shapes a b200_work<BLOCK> group runs with: BLOCK x kWgItems, or
 // for BLOCK == 0 the tuner's candidates.
@@ -2350,12 +2366,15 @@ inline std::vector<tune::Shape> wg_shapes() {
     return std::vector<tune::Shape>(std::begin(tune::kWorkShapes), std::end(tune::kWorkShapes));
   }
 }
+// Reducer partials a loop of `len` elements needs: one per (tile, warp),
+// the most over the group's tile shapes.
 template <int BLOCK>
-inline long long wg_min_tile() {
+inline long long wg_slots(long long len) {
   long long m = 0;
   for (const tune::Shape& sh : wg_shapes<BLOCK>()) {
-    const long long t = (long long)sh.block * sh.items;
-    if (m == 0 || t < m) m = t;
+    const long long tile = (long long)sh.block * sh.items;
+    const long long n = (len + tile - 1) / tile * (sh.block / 32);
+    if (n > m) m = n;
   }
   return m;
 }
@@ -2388,12 +2407,11 @@ class WgCore {
   void enqueue(long long begin, long long len, const Body& body) {
     static_assert(std::is_copy_constructible<Body>::value, "b200_work loop bodies are copied");
     const wg_fn fp = wg_fn_of<Body>();
-    // reducer partials for the largest tile count any shape can run with
-    const long long tile = wg_min_tile<BLOCK>();
     WgCaptureCtx& w = wg_capture();
     w.active = true;
     w.reg = reg_;
-    w.ntiles = (len + tile - 1) / tile;
+    w.nslots = wg_slots<BLOCK>(len);
+    w.loop = (long long)loops_.size();
     ++w.capture_id;
     alignas(Body) unsigned char raw[sizeof(Body)];
     try {
@@ -2450,6 +2468,10 @@ class WgCore {
             if (nt > 0) k<<<unsigned(nt), NB(), 0, s>>>(loops, which, tile, bodies);
           }
         }
+        // the captured reducers' partials of this run, into their cells
+        if (nfolds_ > 0)
+          wg_fold_kernel<<<unsigned(nfolds_), 256, 0, s>>>(reinterpret_cast<const WgFold*>(d + folds_off_),
+                                                           prefix, NB() / 32);
       });
       check_cuda(cudaGetLastError(), "WorkGroup run");
     } catch (...) {
@@ -2475,6 +2497,10 @@ class WgCore {
     free_device();
     loops_.clear();
     bytes_.clear();
+    {
+      std::lock_guard<std::mutex> g(reg_->m);
+      reg_->folds.clear();
+    }
     uploaded_ = false;
     tuner_.reset();
   }
@@ -2488,6 +2514,8 @@ class WgCore {
     std::swap(uploaded_, o.uploaded_);
     std::swap(loops_off_, o.loops_off_);
     std::swap(bodies_off_, o.bodies_off_);
+    std::swap(folds_off_, o.folds_off_);
+    std::swap(nfolds_, o.nfolds_);
     std::swap(elements_, o.elements_);
     std::swap(shapes_, o.shapes_);
     std::swap(prefix_off_, o.prefix_off_);
@@ -2498,8 +2526,8 @@ class WgCore {
     if (dev_) cudaFree(dev_);
     dev_ = nullptr;
   }
-  // Loops, bodies and, per tile shape, the loops' first tiles, in one
-  // device allocation.
+  // Loops, bodies, the reducers' fold entries and, per tile shape, the
+  // loops' first tiles, in one device allocation.
   void upload() {
     free_device();
     shapes_ = wg_shapes<BLOCK>();
@@ -2522,9 +2550,16 @@ class WgCore {
       prefix_off_.push_back(off + first * sizeof(long long));
       ntiles_.push_back(acc);
     }
+    std::vector<WgFold> folds;
+    {
+      std::lock_guard<std::mutex> g(reg_->m);
+      folds = reg_->folds;
+    }
+    nfolds_ = folds.size();
     loops_off_ = 0;
     bodies_off_ = round(off + prefix.size() * sizeof(long long));
-    check_cuda(cudaMalloc(&dev_, bodies_off_ + bytes_.size() + 16), "WorkGroup storage");
+    folds_off_ = round(bodies_off_ + bytes_.size());
+    check_cuda(cudaMalloc(&dev_, folds_off_ + folds.size() * sizeof(WgFold) + 16), "WorkGroup storage");
     char* d = static_cast<char*>(dev_);
     check_cuda(cudaMemcpy(d + loops_off_, loops_.data(), loops_.size() * sizeof(WgLoop), cudaMemcpyHostToDevice),
                "WorkGroup loops");
@@ -2533,6 +2568,9 @@ class WgCore {
     if (!bytes_.empty())
       check_cuda(cudaMemcpy(d + bodies_off_, bytes_.data(), bytes_.size(), cudaMemcpyHostToDevice),
                  "WorkGroup bodies");
+    if (!folds.empty())
+      check_cuda(cudaMemcpy(d + folds_off_, folds.data(), folds.size() * sizeof(WgFold), cudaMemcpyHostToDevice),
+                 "WorkGroup reducer folds");
     tuner_.reset();
     if (shapes_.size() > 1)
       tuner_ = tune::make_tuner("WorkGroup", current_device_index(), -1, shapes_.data(), int(shapes_.size()));
@@ -2544,7 +2582,8 @@ class WgCore {
   std::shared_ptr<WgRegistry> reg_ = std::make_shared<WgRegistry>();
   void* dev_ = nullptr;
   bool uploaded_ = false;
-  size_t loops_off_ = 0, bodies_off_ = 0;
+  size_t loops_off_ = 0, bodies_off_ = 0, folds_off_ = 0;
+  size_t nfolds_ = 0;
   long long elements_ = 0;
   std::vector<tune::Shape> shapes_;
   std::vector<size_t> prefix_off_;  // per shape

@@ -13,7 +13,9 @@
 // and with the tuned shape b200_work<0>, against an ordered group (one
 // launch per loop, the reference's ordered CUDA runner,
 // policy/cuda/WorkGroup/WorkRunner.hpp:38-162).  Each run() returns after
-// its work is done (synchronous policy).
+// its work is done (synchronous policy); the tuned shape is also timed with
+// the asynchronous policy b200_work<0, true>, whose runs queue behind one
+// another, which gives the device time of a run.
 //
 // Prints one JSON object; bench.py builds and runs it.
 #include <chrono>
@@ -160,7 +162,7 @@ int main() {
     offs[l + 1] = offs[l] + Index_type(v);
   }
   const Index_type wtotal = offs[nloops];
-  float *wx = nullptr, *wy[3] = {nullptr, nullptr, nullptr};
+  float *wx = nullptr, *wy[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaMalloc(&wx, wtotal * sizeof(float));
   std::vector<float> hx(wtotal), hy(wtotal);
   for (Index_type i = 0; i < wtotal; ++i) {
@@ -173,22 +175,25 @@ int main() {
     cudaMemcpy(p, hy.data(), wtotal * sizeof(float), cudaMemcpyHostToDevice);
   }
   const int warm = 40, wreps = 20;
-  std::vector<double> s_ord, s_fix, s_tun;
-  RAJA::b200::tune::Report t_ord, t_fix, t_tun;
+  std::vector<double> s_ord, s_fix, s_tun, s_asy;
+  RAJA::b200::tune::Report t_ord, t_fix, t_tun, t_asy;
   const float w_ord = workgroup_ms<RAJA::b200_work<256>, RAJA::ordered>(offs, wx, wy[0], 3, 5, &s_ord, &t_ord);
   const float w_fix =
       workgroup_ms<RAJA::b200_work<256>, RAJA::unordered>(offs, wx, wy[1], warm, wreps, &s_fix, &t_fix);
   const float w_tun =
       workgroup_ms<RAJA::b200_work<0>, RAJA::unordered>(offs, wx, wy[2], warm, wreps, &s_tun, &t_tun);
+  const float w_asy =
+      workgroup_ms<RAJA::b200_work<0, true>, RAJA::unordered>(offs, wx, wy[3], warm, wreps, &s_asy, &t_asy);
   // the three groups ran different numbers of times: compare y and the sums
   // only between the two unordered groups (same runs), and check y of the
   // ordered group against a host restatement of its runs (3 warm-up, one
   // untimed and 5 timed)
-  std::vector<float> wy0(wtotal), wy1(wtotal), wy2(wtotal);
+  std::vector<float> wy0(wtotal), wy1(wtotal), wy2(wtotal), wy3(wtotal);
   cudaMemcpy(wy0.data(), wy[0], wtotal * sizeof(float), cudaMemcpyDeviceToHost);
   cudaMemcpy(wy1.data(), wy[1], wtotal * sizeof(float), cudaMemcpyDeviceToHost);
   cudaMemcpy(wy2.data(), wy[2], wtotal * sizeof(float), cudaMemcpyDeviceToHost);
-  bool wy_equal = wy1 == wy2;
+  cudaMemcpy(wy3.data(), wy[3], wtotal * sizeof(float), cudaMemcpyDeviceToHost);
+  bool wy_equal = wy1 == wy2 && wy1 == wy3;
   bool wy0_ok = true;
   for (Index_type i = 0; i < wtotal && wy0_ok; ++i) {
     float v = hy[i];
@@ -197,8 +202,10 @@ int main() {
   }
   double sum_rel = 0.0;
   for (int l = 0; l < nloops; ++l) {
-    const double d = std::fabs(s_fix[l] - s_tun[l]) / (std::fabs(s_fix[l]) + 1e-30);
-    sum_rel = d > sum_rel ? d : sum_rel;
+    for (const std::vector<double>* o : {&s_tun, &s_asy}) {
+      const double d = std::fabs(s_fix[l] - (*o)[l]) / (std::fabs(s_fix[l]) + 1e-30);
+      sum_rel = d > sum_rel ? d : sum_rel;
+    }
   }
   const double wbytes = 12.0 * double(wtotal);  // read x, read + write y per element
   std::printf("{\"segments\": %d, \"elements\": %lld, \"reps\": %d, "
@@ -210,11 +217,13 @@ int main() {
               "\"workgroup_ordered_per_loop_ms\": %.4f, \"workgroup_unordered_b200_work_256_ms\": %.4f, "
               "\"workgroup_unordered_tuned_ms\": %.4f, \"workgroup_tuned_shape\": [%d, %d], "
               "\"workgroup_tuner_settled\": %s, \"workgroup_tuned_gbs\": %.1f, "
+              "\"workgroup_unordered_tuned_async_ms\": %.4f, \"workgroup_async_shape\": [%d, %d], "
+              "\"workgroup_async_gbs\": %.1f, "
               "\"workgroup_speedup_tuned_vs_ordered\": %.1f, \"workgroup_y_equal\": %s, "
               "\"workgroup_ordered_y_exact\": %s, \"workgroup_sums_max_rel_diff_fixed_vs_tuned\": %.3g}\n",
               nseg, (long long)total, reps, r_one, r_per, r_per / r_one, bytes / r_one / 1e6, m_one, m_per,
               m_per / m_one, bytes / m_one / 1e6, same ? "true" : "false", nloops, (long long)wtotal, w_ord, w_fix,
               w_tun, t_tun.best.block, t_tun.best.items, t_tun.settled ? "true" : "false",
-              wbytes / w_tun / 1e6, w_ord / w_tun, wy_equal ? "true" : "false", wy0_ok ? "true" : "false", sum_rel);
+              wbytes / w_tun / 1e6, w_asy, t_asy.best.block, t_asy.best.items, wbytes / w_asy / 1e6, w_ord / w_tun, wy_equal ? "true" : "false", wy0_ok ? "true" : "false", sum_rel);
   return (same && wy_equal && wy0_ok) ? 0 : 1;
 }
