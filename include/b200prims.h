@@ -415,9 +415,8 @@ int b200_multi_reduce_bitand_u64(const int32_t* bins, const uint64_t* vals, size
  * indices [0, lens[i]); for the segmented primitives, segment i covers
  * [offsets[i], offsets[i+1]) of one flattened array, offsets being the
  * prefix sums of lens.  A plan belongs to the device current at creation.
- * A plan holds the per-loop tickets and tile partials of its runs, so calls
- * with one plan must not overlap on the GPU: issue them on one stream, or
- * order the streams.
+ * A plan holds the warp partials of its runs, so calls with one plan must
+ * not overlap on the GPU: issue them on one stream, or order the streams.
  * ====================================================================== */
 typedef struct b200_batch_plan_s* b200_batch_plan;
 
@@ -427,12 +426,18 @@ int b200_batch_plan_info(b200_batch_plan plan, int64_t* total, int64_t* ntiles, 
                          int* block);
 /* device array of the nloops+1 segment offsets */
 const int64_t* b200_batch_plan_offsets(b200_batch_plan plan);
+/* Pin the launch shape of the plan's batched loops: `block` threads with
+ * `items` elements per thread per tile, one of the shapes the autotuner
+ * times (256x8, 256x16, 512x8, 128x16, 256x4); B200_ERR_ARG for any other
+ * pair.  Like the fixed BLOCK of a b200_work<BLOCK> group. */
+int b200_batch_plan_set_shape(b200_batch_plan plan, int block, int items);
 
 /* Every loop i: y_i[j] += a * x_i[j]; sums[i] = sum_j y_i[j] (after the
  * update), for all loops in one persistent launch.  xs, ys: device arrays
  * of nloops device pointers; sums: device array of nloops doubles.
  * mode: B200_MODE_COMPENSATED for TwoSum partials (else naive FP32
- * partials); the per-loop fold is always in tile order (deterministic). */
+ * partials); each loop's partials are added in a fixed order (the sums are
+ * deterministic for a given plan shape). */
 int b200_batched_axpy_sum_f32(b200_batch_plan plan, float a, const float* const* xs,
                               float* const* ys, double* sums, int mode, b200_stream_t stream);
 /* Time the kernel variants (block size x items per thread) on this plan and

@@ -462,6 +462,11 @@ class BatchPlan:
         return {"total": total.value, "tiles": ntiles.value, "tile": tile.value,
                 "block": block.value}
 
+    def set_shape(self, block: int, items: int):
+        """Pin the batched loops' launch shape (block threads x items per
+        thread) to one of the autotuner's candidates."""
+        _lib.call("b200_batch_plan_set_shape", self.handle, int(block), int(items))
+
     def close(self):
         if getattr(self, "handle", None):
             _lib.load().b200_batch_plan_destroy(self.handle)

@@ -87,6 +87,7 @@ def _signatures() -> dict[str, tuple]:
         "b200_batch_plan_destroy": (_I, [_P]),
         "b200_batch_plan_info": (_I, [_P, _P, _P, _P, _P]),
         "b200_batch_plan_offsets": (_P, [_P]),
+        "b200_batch_plan_set_shape": (_I, [_P, _I, _I]),
         "b200_batched_axpy_sum_f32": (_I, [_P, C.c_float, _P, _P, _P, _I, _P]),
         "b200_batch_autotune_axpy_sum_f32": (_I, [_P, C.c_float, _P, _P, _P, _I, _P]),
         "b200_loop_axpy_sum_f32": (_I, [C.c_float, _P, _P, _SZ, _P, _I, _P]),

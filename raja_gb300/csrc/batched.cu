@@ -638,6 +638,18 @@ int b200_batch_plan_info(b200_batch_plan p, int64_t* total, int64_t* ntiles, int
 
 const int64_t* b200_batch_plan_offsets(b200_batch_plan p) { return p ? p->d_offsets : nullptr; }
 
+int b200_batch_plan_set_shape(b200_batch_plan p, int block, int items) {
+  B200_TRY(check_plan(p, "b200_batch_plan_set_shape"));
+  for (int v = 0; v < kNumVariants; ++v) {
+    if (kVariants[v].block != block || kVariants[v].items != items) continue;
+    B200_TRY(build_tiling(p, block * items));
+    p->variant = v;
+    clear_error();
+    return B200_OK;
+  }
+  return fail(B200_ERR_ARG, "b200_batch_plan_set_shape: %d x %d is not a batched shape", block, items);
+}
+
 int b200_batched_axpy_sum_f32(b200_batch_plan p, float a, const float* const* xs,
                               float* const* ys, double* sums, int mode, b200_stream_t stream) {
   B200_TRY(check_plan(p, "b200_batched_axpy_sum_f32"));

@@ -55,6 +55,46 @@ def test_batched_axpy_sum_matches_per_loop_oracle(prims, orc, autotune):
     assert info["total"] == int(lens.sum()) and info["tiles"] > 0
 
 
+@pytest.mark.parametrize("shape", [(256, 8), (256, 16), (512, 8), (128, 16), (256, 4)])
+def test_batched_every_launch_shape_loop_by_loop(prims, orc, shape):
+    """Each launch shape the autotuner picks from, pinned: loops carved from
+    one flat array at odd offsets, an empty loop between long ones (its sum
+    is 0), loops much longer than a block's run of tiles (their partials
+    come from several blocks), and a run of one-element loops."""
+    import torch
+    rng = np.random.default_rng(23)
+    lens = np.concatenate([lognormal_lengths(rng, 200, 3000, 1.2, 1, 1 << 17),
+                           [0, 1 << 19, 0, 1, 1, 1, 3 * (1 << 18) + 5, 0]]).astype(np.int64)
+    offs = np.concatenate([[0], np.cumsum(lens)]) + 3   # every loop starts off a 16-byte boundary
+    total = int(offs[-1]) + 3
+    x = rng.uniform(-1, 1, total).astype(np.float32)
+    y = rng.uniform(-1, 1, total).astype(np.float32)
+    dx, dy = to_dev(x), to_dev(y)
+    px = torch.tensor([dx.data_ptr() + 4 * int(o) for o in offs[:-1]], dtype=torch.int64, device="cuda")
+    py = torch.tensor([dy.data_ptr() + 4 * int(o) for o in offs[:-1]], dtype=torch.int64, device="cuda")
+    plan = prims.BatchPlan(lens)
+    plan.set_shape(*shape)
+    info = plan.info()
+    assert (info["block"], info["tile"]) == (shape[0], shape[0] * shape[1])
+    sums = torch.full((len(lens),), np.nan, dtype=torch.float64, device="cuda")
+    prims.batched_axpy_sum(plan, 0.25, px, py, sums)
+    got_sums, gy = to_host(sums), to_host(dy)
+    ref = y.copy()
+    orc.axpy(np.float32(0.25), x[3:-3], ref[3:-3])
+    np.testing.assert_allclose(gy, ref, rtol=4 * U32, atol=4 * U32)
+    assert np.array_equal(gy[:3], y[:3]) and np.array_equal(gy[-3:], y[-3:])  # nothing outside the loops
+    for i, n in enumerate(lens):
+        seg = gy[offs[i]:offs[i + 1]]
+        exact, lo = orc.exact_sum(seg)
+        bound = 1e-6 * float(np.abs(seg).sum())
+        assert abs((got_sums[i] - exact) - lo) <= bound, (shape, i, int(n), got_sums[i], exact)
+        if n == 0:
+            assert got_sums[i] == 0.0
+    with pytest.raises(Exception):
+        plan.set_shape(256, 3)
+    plan.close()
+
+
 def test_batched_full_workgroup_shape_loop_by_loop(prims, orc):
     """The batched-loops configuration at full size: 4096 loops with
     lognormal(median 2000, sigma 1.5) lengths clipped to [32, 2^20], carved
