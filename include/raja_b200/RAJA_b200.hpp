@@ -1248,34 +1248,67 @@ __global__ void __launch_bounds__(BLOCK) forall_list_kernel(Body body_in, const 
   for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < len; i += stride) body(idx[i]);
 }
 // Every segment of an IndexSet in one launch, whatever the mix of range,
-// strided and list segments: a table holds each segment's kind and
-// parameters, and a prefix of segment lengths maps the flat iteration k to
-// (segment, offset) by binary search.
-template <class T>
+// strided and list segments: a table holds each segment's parameters, and
+// a prefix of segment lengths maps the flat iteration k to (segment,
+// offset).  Index k of a segment is base + k * step (a range has step 1);
+// a list segment keeps the address of its indices in base and kListStep
+// (no stride a segment can have) in step.  An IndexSet of range segments
+// only keeps just the bases (8 bytes a segment instead of 16).
+constexpr long long kListStep = -9223372036854775807LL - 1;  // the most negative long long
 struct SegDesc {
-  int kind;       // 0 range, 1 strided range, 2 list
-  T begin;        // range / strided: first index
-  T step;         // strided: stride
-  const T* list;  // list: the indices (device-accessible)
+  long long base;
+  long long step;
 };
-template <int BLOCK, class Body, class T>
+// Largest s in [lo, nseg) with prefix[s] <= k, given prefix[lo] <= k < prefix[nseg].
+__device__ inline int seg_search(const long long* __restrict__ prefix, int lo, int nseg, long long k) {
+  int hi = nseg;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= k) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+// Block b runs a contiguous slice of the flat iterations; each thread
+// finds the segment of its first iteration by binary search and follows
+// its later ones (BLOCK apart) by walking forward a few segments, or by a
+// search of the rest of the table when the walk gets long.
+template <int BLOCK, bool RANGES, class Body, class T>
 __global__ void __launch_bounds__(BLOCK)
-forall_indexset_kernel(Body body_in, const SegDesc<T>* segs, const long long* prefix, int nseg,
+forall_indexset_kernel(Body body_in, const void* descs, const long long* __restrict__ prefix, int nseg,
                        long long total) {
+  // No early return: a captured reducer's combine (in the destructor of
+  // `body`) holds block barriers, which every thread of a warp must reach
+  // at the same point.
   Body body(body_in);
-  const long long stride = (long long)gridDim.x * BLOCK;
-  for (long long k = (long long)blockIdx.x * BLOCK + threadIdx.x; k < total; k += stride) {
-    int lo = 0, hi = nseg;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (prefix[mid] <= k) lo = mid;
-      else hi = mid;
+  const long long rows = (total + BLOCK - 1) / BLOCK;
+  const long long per = (rows + gridDim.x - 1) / gridDim.x * BLOCK;  // iterations per block
+  const long long b0 = (long long)blockIdx.x * per;
+  const long long b1 = b0 + per < total ? b0 + per : total;
+  long long k = b0 + threadIdx.x;
+  int s = k < b1 ? seg_search(prefix, 0, nseg, k) : 0;
+  long long lo = prefix[s], hi = prefix[s + 1];
+  for (; k < b1; k += BLOCK) {
+    if (k >= hi) {
+      int steps = 0;
+      do {
+        ++s;
+        lo = hi;
+        hi = prefix[s + 1];
+      } while (k >= hi && ++steps < 8);
+      if (k >= hi) {
+        s = seg_search(prefix, s, nseg, k);
+        lo = prefix[s];
+        hi = prefix[s + 1];
+      }
     }
-    const SegDesc<T> d = segs[lo];
-    const long long off = k - prefix[lo];
-    const T idx = d.kind == 0 ? T(d.begin + T(off))
-                              : (d.kind == 1 ? T(d.begin + T(off) * d.step) : d.list[off]);
-    body(idx);
+    const long long off = k - lo;
+    if constexpr (RANGES) {
+      body(T(static_cast<const long long*>(descs)[s] + off));
+    } else {
+      const SegDesc d = static_cast<const SegDesc*>(descs)[s];
+      body(d.step == kListStep ? reinterpret_cast<const T*>(d.base)[off] : T(d.base + off * d.step));
+    }
   }
 }
 
@@ -1384,12 +1417,13 @@ inline PinnedStage& pinned_stage() {
 }
 
 // Layout of an IndexSet's table, the same on the host and the device: the
-// segment descriptors (padded to 256 bytes), then the running lengths
-// (nseg + 1 entries).  Returns the total bytes; *desc_bytes is the padded
-// descriptor part.
-template <class T>
+// segment descriptors (SegDesc, or the bases alone for RANGES; padded to
+// 256 bytes), then the running lengths (nseg + 1 entries).  Returns the
+// total bytes; *desc_bytes is the padded descriptor part.
+template <bool RANGES>
 inline size_t seg_table_bytes(int nseg, size_t* desc_bytes) {
-  *desc_bytes = ((size_t(nseg) * sizeof(SegDesc<T>) + 255) / 256) * 256;
+  const size_t each = RANGES ? sizeof(long long) : sizeof(SegDesc);
+  *desc_bytes = ((size_t(nseg) * each + 255) / 256) * 256;
   return *desc_bytes + (size_t(nseg) + 1) * sizeof(long long);
 }
 
@@ -1397,7 +1431,7 @@ inline size_t seg_table_bytes(int nseg, size_t* desc_bytes) {
 // caller in the pinned stage buffer `host`) holds nseg descriptors and
 // their running lengths: one copy to launch-pool memory on the b200
 // stream, freed behind the launch.
-template <int BLOCK, bool Async, class T, class Body>
+template <int BLOCK, bool Async, bool RANGES, class T, class Body>
 void indexset_launch(const unsigned char* host, int nseg, size_t desc_bytes, size_t bytes, long long total,
                      Body&& body) {
   using B = std::decay_t<Body>;
@@ -1406,11 +1440,11 @@ void indexset_launch(const unsigned char* host, int nseg, size_t desc_bytes, siz
   void* tbl = launch_alloc(bytes, s, "indexset table");
   check_cuda(cudaMemcpyAsync(tbl, host, bytes, cudaMemcpyHostToDevice, s), "indexset table");
   pinned_stage().copied(s);
-  auto* d_desc = static_cast<SegDesc<T>*>(tbl);
+  const void* d_desc = tbl;
   long long* d_prefix = reinterpret_cast<long long*>(static_cast<char*>(tbl) + desc_bytes);
   tune::shaped_launch<BLOCK, tune::Tag<3, B, T>>("forall indexset", total, s, [&](auto NB, int items) {
-    auto k = forall_indexset_kernel<NB(), B, T>;
-    const unsigned g = grid_for<forall_indexset_kernel<NB(), B, T>>(NB(), total, items);
+    auto k = forall_indexset_kernel<NB(), RANGES, B, T>;
+    const unsigned g = grid_for<forall_indexset_kernel<NB(), RANGES, B, T>>(NB(), total, items);
     B lb = LaunchCopy<B>::make(body, g, s);
     k<<<g, NB(), 0, s>>>(lb, d_desc, d_prefix, nseg, total);
   });
@@ -1664,19 +1698,19 @@ void forall_impl(b200_exec<BLOCK, Async>, const TypedListSegment<T>& l, Body&& b
 namespace b200 {
 namespace detail {
 template <class T, class Seg>
-inline bool seg_desc(const Seg& g, SegDesc<T>* d, long long* len) {
+inline bool seg_desc(const Seg& g, SegDesc* d, long long* len) {
   using G = std::decay_t<Seg>;
   if constexpr (std::is_same<G, TypedRangeSegment<T>>::value) {
-    *d = SegDesc<T>{0, g.b, T(1), nullptr};
     *len = (long long)stripIndexType(g.size());
+    *d = SegDesc{(long long)g.b, 1};
     return true;
   } else if constexpr (std::is_same<G, TypedRangeStrideSegment<T>>::value) {
-    *d = SegDesc<T>{1, g.b, g.s, nullptr};
     *len = (long long)stripIndexType(g.size());
+    *d = SegDesc{(long long)g.b, *len > 1 ? (long long)g.s : 1};
     return true;
   } else if constexpr (std::is_same<G, TypedListSegment<T>>::value) {
-    *d = SegDesc<T>{2, T(0), T(0), g.data};
     *len = (long long)g.size();
+    *d = SegDesc{(long long)reinterpret_cast<intptr_t>(g.data), kListStep};
     return true;
   } else {
     return false;  // another segment type: run per segment
@@ -1691,23 +1725,37 @@ void forall_impl(b200_exec<BLOCK, Async> pol, const TypedIndexSet<Segs...>& is, 
   const auto& segs = is.segments();
   const int nseg = int(segs.size());
   if (nseg == 0) return;
+  constexpr bool kRanges = (std::is_same<Segs, TypedRangeSegment<T>>::value && ...);
   size_t db = 0;
-  const size_t bytes = b200::detail::seg_table_bytes<T>(nseg, &db);
+  const size_t bytes = b200::detail::seg_table_bytes<kRanges>(nseg, &db);
   unsigned char* h = b200::detail::pinned_stage().get(bytes);
-  auto* desc = reinterpret_cast<b200::detail::SegDesc<T>*>(h);
   long long* prefix = reinterpret_cast<long long*>(h + db);
+  long long acc = 0;
   prefix[0] = 0;
-  bool table_ok = true;
-  for (int i = 0; i < nseg && table_ok; ++i) {
-    long long len = 0;
-    table_ok = std::visit([&](const auto& g) { return b200::detail::seg_desc<T>(g, &desc[i], &len); }, segs[i]);
-    prefix[i + 1] = prefix[i] + len;
+  if constexpr (kRanges) {
+    auto* base = reinterpret_cast<long long*>(h);
+    for (int i = 0; i < nseg; ++i) {
+      std::visit([&](const auto& g) {
+        base[i] = (long long)g.b;
+        acc += (long long)stripIndexType(g.size());
+      }, segs[i]);
+      prefix[i + 1] = acc;
+    }
+  } else {
+    auto* desc = reinterpret_cast<b200::detail::SegDesc*>(h);
+    bool table_ok = true;
+    for (int i = 0; i < nseg && table_ok; ++i) {
+      long long len = 0;
+      table_ok = std::visit([&](const auto& g) { return b200::detail::seg_desc<T>(g, &desc[i], &len); }, segs[i]);
+      acc += len;
+      prefix[i + 1] = acc;
+    }
+    if (!table_ok) {
+      for (const auto& v : segs) std::visit([&](const auto& g) { forall_impl(pol, g, body); }, v);
+      return;
+    }
   }
-  if (!table_ok) {
-    for (const auto& v : segs) std::visit([&](const auto& g) { forall_impl(pol, g, body); }, v);
-    return;
-  }
-  b200::detail::indexset_launch<BLOCK, Async, T>(h, nseg, db, bytes, prefix[nseg], std::forward<Body>(body));
+  b200::detail::indexset_launch<BLOCK, Async, kRanges, T>(h, nseg, db, bytes, acc, std::forward<Body>(body));
 }
 
 // ------------------------------------------------------ forall with params

@@ -419,23 +419,28 @@ forall_impl(resources::Cuda cuda_res, b200_exec<BLOCK, Async> const& pol, Iterab
 namespace b200 {
 namespace detail {
 
-// Kind and parameters of one segment of RAJA's (range, strided, list);
-// false for another segment type.
-template <class T>
+// Parameters of one segment of RAJA's (range, strided, list) for the
+// one-launch table; *ok = false for another segment type.  RANGES: the
+// IndexSet holds range segments only, and the table keeps their bases.
+template <class T, bool RANGES>
 struct RefSegDesc {
   template <class Seg>
-  void operator()(const Seg& g, SegDesc<T>* d, long long* len, bool* ok) const {
+  void operator()(const Seg& g, unsigned char* descs, size_t i, long long* len, bool* ok) const {
     using G = std::decay_t<Seg>;
     *len = (long long)g.size();
-    if constexpr (std::is_same<G, TypedRangeSegment<T>>::value) {
-      *d = SegDesc<T>{0, *g.begin(), T(1), nullptr};
-    } else if constexpr (std::is_same<G, TypedRangeStrideSegment<T>>::value) {
-      const T step = *len > 1 ? T(*(g.begin() + 1) - *g.begin()) : T(1);
-      *d = SegDesc<T>{1, *g.begin(), step, nullptr};
-    } else if constexpr (std::is_same<G, TypedListSegment<T>>::value) {
-      *d = SegDesc<T>{2, T(0), T(0), g.begin()};
+    if constexpr (RANGES) {
+      reinterpret_cast<long long*>(descs)[i] = (long long)*g.begin();
     } else {
-      *ok = false;
+      SegDesc& d = reinterpret_cast<SegDesc*>(descs)[i];
+      if constexpr (std::is_same<G, TypedRangeSegment<T>>::value) {
+        d = SegDesc{(long long)*g.begin(), 1};
+      } else if constexpr (std::is_same<G, TypedRangeStrideSegment<T>>::value) {
+        d = SegDesc{(long long)*g.begin(), *len > 1 ? (long long)(*(g.begin() + 1) - *g.begin()) : 1};
+      } else if constexpr (std::is_same<G, TypedListSegment<T>>::value) {
+        d = SegDesc{(long long)reinterpret_cast<intptr_t>(g.begin()), kListStep};
+      } else {
+        *ok = false;
+      }
     }
   }
 };
@@ -467,19 +472,21 @@ void ref_indexset_forall(Res& r, const TypedIndexSet<SegmentTypes...>& iset, Loo
   ResourceStream bound(res_stream(r));
   bool ok = !has_reducer_params<ForallParams>();
   if (ok && nseg > 0) {
+    constexpr bool kRanges = (std::is_same<SegmentTypes, TypedRangeSegment<T>>::value && ...);
     size_t db = 0;
-    const size_t bytes = seg_table_bytes<T>(nseg, &db);
+    const size_t bytes = seg_table_bytes<kRanges>(nseg, &db);
     unsigned char* h = pinned_stage().get(bytes);
-    auto* desc = reinterpret_cast<SegDesc<T>*>(h);
     long long* prefix = reinterpret_cast<long long*>(h + db);
+    long long acc = 0;
     prefix[0] = 0;
     for (int i = 0; i < nseg && ok; ++i) {
       long long len = 0;
-      iset.segmentCall(size_t(i), RefSegDesc<T>{}, &desc[size_t(i)], &len, &ok);
-      prefix[size_t(i) + 1] = prefix[size_t(i)] + len;
+      iset.segmentCall(size_t(i), RefSegDesc<T, kRanges>{}, h, size_t(i), &len, &ok);
+      acc += len;
+      prefix[size_t(i) + 1] = acc;
     }
     if (ok) {
-      indexset_launch<BLOCK, Async, T>(h, nseg, db, bytes, prefix[nseg], std::forward<LoopBody>(loop_body));
+      indexset_launch<BLOCK, Async, kRanges, T>(h, nseg, db, bytes, acc, std::forward<LoopBody>(loop_body));
       return;
     }
   } else if (ok) {

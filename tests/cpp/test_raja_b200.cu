@@ -6,6 +6,7 @@
 //   N in {357, 32000}, plus/min/max, non-identity offsets), sort /
 //   stable_sort / sort_pairs, and test/functional/workgroup (a[i] += i + 5).
 // Prints one PASS/FAIL line per case; the exit status is the failure count.
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cmath>
@@ -1485,6 +1486,71 @@ void test_edge_cases() {
     cudaFree(ml);
     cudaFree(w);
     cudaFree(lst);
+  }
+  {
+    // One-launch IndexSets of 12,000 segments whose lengths mix long
+    // segments with runs of hundreds of empty and one-element segments, so
+    // that a thread's forward walk over segments outgrows its bound and
+    // falls back to a search; range-only and mixed (range, strided, list)
+    // tables, against seq_exec on disjoint indices.  The GPU writes device
+    // memory and the comparison reads a bulk copy of it.
+    std::mt19937 g(5);
+    const Index_type lens_pick[] = {0, 0, 1, 1, 2, 3, 40, 300, 2000};
+    std::vector<Index_type> lens;
+    for (int i = 0; i < 12000; ++i) {
+      const bool tiny_run = (i / 400) % 3 == 1;  // 400 segments of length 0 or 1
+      lens.push_back(tiny_run ? Index_type(g() % 2) : lens_pick[g() % 9]);
+    }
+    Index_type span = 0, nlist = 0;
+    for (size_t i = 0; i < lens.size(); ++i) {
+      span += 3 * lens[i] + 1;
+      if (i % 3 == 2) nlist += lens[i];
+    }
+    double* yd = nullptr;
+    cudaMalloc(&yd, span * sizeof(double));
+    std::vector<double> yg(span), yh2(span);
+    Index_type* lists = managed<Index_type>(nlist + 1);  // written here before any launch reads it
+    RAJA::TypedIndexSet<RAJA::RangeSegment> rset;
+    RAJA::IndexSet mset;
+    Index_type base = 0, lpos = 0;
+    for (size_t i = 0; i < lens.size(); ++i) {
+      const Index_type n = lens[i];
+      rset.push_back(RAJA::RangeSegment(base, base + n));
+      if (i % 3 == 0) {
+        mset.push_back(RAJA::RangeSegment(base, base + n));
+      } else if (i % 3 == 1) {
+        mset.push_back(RAJA::RangeStrideSegment(base, base + 3 * n, 3));
+      } else {
+        for (Index_type k = 0; k < n; ++k) lists[lpos + k] = base + 2 * n - 1 - k;
+        mset.push_back(RAJA::ListSegment(lists + lpos, n));
+        lpos += n;
+      }
+      base += 3 * n + 1;
+    }
+    long long want = 0;
+    for (Index_type n : lens) want += n;
+    bool oki = true;
+    double* yh = yh2.data();
+    for (int which = 0; which < 2; ++which) {
+      std::fill(yh2.begin(), yh2.end(), -1.0);
+      cudaMemcpy(yd, yh2.data(), span * sizeof(double), cudaMemcpyHostToDevice);
+      RAJA::ReduceSum<red, long long> icnt(0);
+      auto body = [=] RAJA_DEVICE(Index_type i) {
+        yd[i] += 2.0 * double(i) + 1.0;
+        icnt += 1;
+      };
+      if (which == 0) RAJA::forall<exec>(rset, body);
+      else RAJA::forall<exec>(mset, body);
+      auto hbody = [=](Index_type i) { yh[i] += 2.0 * double(i) + 1.0; };
+      if (which == 0) RAJA::forall<RAJA::seq_exec>(rset, hbody);
+      else RAJA::forall<RAJA::seq_exec>(mset, hbody);
+      oki = oki && icnt.get() == want;
+      cudaMemcpy(yg.data(), yd, span * sizeof(double), cudaMemcpyDeviceToHost);
+      oki = oki && yg == yh2;
+    }
+    CHECK("indexset_one_launch_tiny_segment_runs", oki);
+    cudaFree(yd);
+    cudaFree(lists);
   }
   {
     using wpol = RAJA::WorkGroupPolicy<RAJA::b200_work<256, false>, RAJA::unordered>;
