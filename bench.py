@@ -1011,7 +1011,8 @@ def bench_raja_api(lib):
     whole set against one launch per segment; all-range sets and sets mixing
     range, strided and list segments), and a WorkGroup of 4096 lognormal
     loops with per-loop ReduceSum<b200_reduce, float> (one unordered run,
-    fixed and tuned shape, against the ordered one-launch-per-loop run).
+    fixed and tuned shape, synchronous and queued, against the ordered
+    one-launch-per-loop run).
     The lambda bodies are C++ (tests/cpp/bench_raja_api.cu), built here
     with nvcc against the library."""
     import raja_gb300.build as b
