@@ -289,6 +289,11 @@ __device__ __forceinline__ void tma_load_1d(void* dst_smem, const void* src, uin
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+// Bring `bytes` (a multiple of 16, from a 16-byte aligned address) into
+// L2 without waiting for them.
+__device__ __forceinline__ void prefetch_l2_bulk(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void tma_store_1d(void* dst, const void* src_smem, uint32_t bytes) {
   asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
                "r"(smem_addr(src_smem)), "r"(bytes)

@@ -505,7 +505,7 @@ template <class Op, bool EXCL>
 __global__ void __launch_bounds__(SBLOCK, scan_min_blocks<Op>())
 scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op::T init,
             int tma_ok, int vec_out, uint64_t* words, uint32_t* tile_counter,
-            uint32_t* status, uint32_t spin_limit) {
+            uint32_t* status, uint32_t spin_limit, uint32_t pf_tiles) {
   using T = typename Op::T;
   constexpr int TS = Tile<Op>::SIZE;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -521,6 +521,10 @@ scan_kernel(const typename Op::T* in, typename Op::T* out, size_t n, typename Op
       mbar_arrive_expect_tx(&sm.bar, TS * sizeof(T));
       tma_load_1d(st, in + b0, TS * sizeof(T), &sm.bar);
     }
+    // the tile a block will claim about one generation of resident blocks
+    // later: into L2 now, so that its TMA load is an L2 read
+    const size_t pb = b0 + size_t(pf_tiles) * TS;
+    if (pf_tiles && tma_ok && pb + TS <= n) prefetch_l2_bulk(in + pb, TS * sizeof(T));
   }
   __syncthreads();
   const size_t tile = sm.tile;
@@ -547,8 +551,13 @@ int launch_scan(const char* name, unsigned grid, cudaStream_t s, const typename 
   B200_TRY(device_props(&props));
   int bps = 0;
   B200_TRY(kernel_setup(ks, props, kern, SBLOCK, sizeof(ScanSmem<Op>), &bps));
+  // L2 prefetch distance: one tile per SM.  Measured on GB300 for the
+  // int64 exclusive scan at 2^28 (64 KB tiles): none 0.815 ms; 152 tiles
+  // 0.689; 304 0.690; 456 0.75; 608 and more 0.91-0.97 (prefetched lines
+  // are evicted, or crowd out the demand loads, before their tile is claimed).
+  const uint32_t pf = uint32_t(props.sms);
   B200_LAUNCH(name, kern, grid, SBLOCK, sizeof(ScanSmem<Op>), s, in, out, n, init, tma_ok, vec_out,
-              words, counter, status, lim);
+              words, counter, status, lim, pf);
   return B200_OK;
 }
 
