@@ -15,7 +15,9 @@
 // spin_limit polls the tile gives up, ORs a code into the device status
 // word and finishes, so a broken invariant can never hang the GPU.
 // Global traffic is one TMA bulk read and one coalesced 16-byte write per
-// element group.  A tile's status (flag + carry) is published with plain
+// element group.  A block also prefetches into L2 the tile that will be
+// claimed one SM's worth of tiles later, so a block's own TMA load is
+// mostly an L2 read and less of its life goes to waiting for its tile.  A tile's status (flag + carry) is published with plain
 // relaxed stores and no fences: the carry is cut into 32-bit pieces, each
 // stored in a 64-bit word beside a copy of the flag, and a reader accepts a
 // status only when every word carries the same non-zero flag -- a torn read

@@ -14,7 +14,9 @@
 //      also zeroes the first pass's look-back status words;
 //   2. bins_kernel: exclusive scan of each histogram -> global digit bases;
 //   3. one onesweep_kernel per digit: a tile of 384 threads x 16-24 keys is
-//      loaded with coalesced warp-striped reads, ranked in registers with a
+//      loaded by one TMA bulk copy (the block also prefetches into L2 the
+//      tile claimed one SM's worth of tiles later, so most loads are L2
+//      reads), ranked in registers with a
 //      warp-level multisplit built from eight ballots per key (on this GPU
 //      __match_any_sync costs ~80 cycles per warp, the ballots a few), its
 //      per-digit counts are published before the ranking (early counts) and
