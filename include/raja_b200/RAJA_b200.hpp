@@ -737,12 +737,15 @@ class DevReducer {
         const size_t pbytes = kWgSlotHeader + size_t(w.nslots) * sizeof(V);
         void* blk = nullptr;
         check_cuda(cudaMalloc(&blk, pbytes), "WorkGroup reducer slot");
+        {
+          std::lock_guard<std::mutex> g(w.reg->m);
+          w.reg->blocks.push_back(blk);  // owned by the registry before anything else can throw
+        }
         V* parts = reinterpret_cast<V*>(static_cast<char*>(blk) + kWgSlotHeader);
         unsigned char *cell_host = nullptr, *cell_dev = nullptr;
         w.reg->new_cell(&cell_host, &cell_dev);
         {
           std::lock_guard<std::mutex> g(w.reg->m);
-          w.reg->blocks.push_back(blk);
           w.reg->folds.push_back(WgFold{parts, cell_dev, w.loop});
         }
         shared_->wg_slot = DevSlot<V>{parts, nullptr, reinterpret_cast<V*>(cell_dev)};
