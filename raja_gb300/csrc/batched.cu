@@ -166,6 +166,14 @@ __device__ __forceinline__ double tile_axpy_sum(float a, const float* __restrict
   return double(s) + double(c);
 }
 
+// L2 prefetch of the whole 16-byte granules inside [b, e): never a byte
+// outside the range.
+__device__ __forceinline__ void prefetch_l2_inside(const float* b, const float* e) {
+  const uintptr_t s = (reinterpret_cast<uintptr_t>(b) + 15) & ~uintptr_t(15);
+  const uintptr_t f = reinterpret_cast<uintptr_t>(e) & ~uintptr_t(15);
+  if (f > s) prefetch_l2_bulk(reinterpret_cast<const void*>(s), uint32_t(f - s));
+}
+
 // Warps per block of the largest batched variant: the run partials hold
 // one slot per (tile, warp) of it.
 constexpr int kMaxBatchWarps = 16;
@@ -218,6 +226,12 @@ batched_axpy_sum_kernel(const int32_t* __restrict__ tile_loop,
     }
     const int64_t lo = (t - t0) * TILE;
     const int64_t hi = min(lo + TILE, len);
+    if (threadIdx.x == 0 && t + 1 < b1 && nxt == loop) {
+      // the block's next tile, same loop: into L2 while this one runs
+      const int64_t hi2 = min(hi + TILE, len);
+      prefetch_l2_inside(x + hi, x + hi2);
+      prefetch_l2_inside(y + hi, y + hi2);
+    }
     acc += tile_axpy_sum<BLOCK, ITEMS>(a, x, y, lo, hi, comp != 0);
   }
   flush(acc, run0);
