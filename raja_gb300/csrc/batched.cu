@@ -48,6 +48,13 @@ struct b200_batch_plan_s {
   std::vector<int> big_segments;   // segments longer than the block sort
   int32_t* d_small = nullptr;      // ids of the small segments
   int nsmall = 0;
+  // long segments sorted together as (segment << 32 | key) in one 64-bit
+  // sort (set when there are several and they are short enough)
+  bool big_packed = false;
+  int64_t big_total = 0;           // keys in the long segments
+  int64_t* d_big_off = nullptr;    // nbig + 1 running lengths of the long segments
+  int64_t* d_big_src = nullptr;    // nbig offsets of the long segments in the keys
+  uint64_t* d_big_buf = nullptr;   // big_total packed keys
 };
 
 struct b200_graph_s {
@@ -536,9 +543,52 @@ segscan_kernel(const int32_t* in, int32_t* out, int64_t n, const int64_t* __rest
 // ------------------------------------------------------ segmented sort
 // Segments up to SEG_CAP keys are sorted by one block each with a bitonic
 // network in shared memory (padded to a power of two with the largest
-// key); longer segments go to the onesweep radix sort.
+// key); longer segments go to the onesweep radix sort.  Several long
+// segments of moderate length are sorted together: each key becomes
+// (segment << 32 | key) -- the key inverted for a descending sort -- and
+// one stable 64-bit sort leaves every segment's keys, in order, in that
+// segment's own range of the packed array (passes whose digit is zero for
+// every key, the top ones, run as plain copies).  That is about a dozen
+// launches instead of six per long segment.
 constexpr int SEG_CAP = 4096;
 constexpr int SEG_BLOCK = 256;
+constexpr int64_t SEG_PACK_MEAN = int64_t(1) << 18;  // long segments at most this long on average are packed
+
+__device__ __forceinline__ int big_seg_of(const int64_t* __restrict__ off, int nbig, int64_t e) {
+  int lo = 0, hi = nbig;  // off[0] = 0 <= e < off[nbig]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= e) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <bool DESC>
+__global__ void __launch_bounds__(256)
+segsort_pack_kernel(const uint32_t* __restrict__ keys, const int64_t* __restrict__ off,
+                    const int64_t* __restrict__ src, int nbig, int64_t total, uint64_t* __restrict__ packed) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += stride) {
+    const int sid = big_seg_of(off, nbig, e);
+    const uint32_t k = keys[src[sid] + (e - off[sid])];
+    packed[e] = (uint64_t(uint32_t(sid)) << 32) | uint64_t(DESC ? ~k : k);
+  }
+}
+
+// Back to the keys: the sort left segment sid's keys at [off[sid], off[sid+1]).
+template <bool DESC>
+__global__ void __launch_bounds__(256)
+segsort_unpack_kernel(uint32_t* __restrict__ keys, const int64_t* __restrict__ off,
+                      const int64_t* __restrict__ src, int64_t total, const uint64_t* __restrict__ packed) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += stride) {
+    const uint64_t v = packed[e];
+    const uint32_t sid = uint32_t(v >> 32);
+    const uint32_t k = uint32_t(v);
+    keys[src[sid] + (e - off[sid])] = DESC ? ~k : k;
+  }
+}
 
 template <bool DESC>
 __global__ void __launch_bounds__(SEG_BLOCK)
@@ -616,6 +666,25 @@ int b200_batch_plan_create(const int64_t* lens, int nloops, b200_batch_plan* out
     else p->big_segments.push_back(i);
   }
   p->nsmall = int(small.size());
+  for (int sid : p->big_segments) p->big_total += lens[sid];
+  const int nbig = int(p->big_segments.size());
+  p->big_packed = nbig >= 2 && p->big_total <= int64_t(nbig) * SEG_PACK_MEAN;
+  if (rc == B200_OK && p->big_packed) {
+    std::vector<int64_t> boff(static_cast<size_t>(nbig) + 1, 0), bsrc(static_cast<size_t>(nbig), 0);
+    for (int j = 0; j < nbig; ++j) {
+      boff[j + 1] = boff[j] + lens[p->big_segments[j]];
+      bsrc[j] = p->offsets[p->big_segments[j]];
+    }
+    ck(cudaMalloc(&p->d_big_off, boff.size() * sizeof(int64_t)), "plan long segments");
+    ck(cudaMalloc(&p->d_big_src, bsrc.size() * sizeof(int64_t)), "plan long segments");
+    ck(cudaMalloc(&p->d_big_buf, size_t(p->big_total) * sizeof(uint64_t)), "plan long segments");
+    if (rc == B200_OK) {
+      ck(cudaMemcpy(p->d_big_off, boff.data(), boff.size() * sizeof(int64_t), cudaMemcpyHostToDevice),
+         "plan long segments copy");
+      ck(cudaMemcpy(p->d_big_src, bsrc.data(), bsrc.size() * sizeof(int64_t), cudaMemcpyHostToDevice),
+         "plan long segments copy");
+    }
+  }
   ck(cudaMalloc(&p->d_small, std::max<size_t>(small.size(), 1) * sizeof(int32_t)), "plan small");
   if (rc == B200_OK && !small.empty())
     ck(cudaMemcpy(p->d_small, small.data(), small.size() * sizeof(int32_t), cudaMemcpyHostToDevice),
@@ -637,6 +706,9 @@ int b200_batch_plan_destroy(b200_batch_plan p) {
   cudaFree(p->d_lens);
   cudaFree(p->d_offsets);
   cudaFree(p->d_small);
+  cudaFree(p->d_big_off);
+  cudaFree(p->d_big_src);
+  cudaFree(p->d_big_buf);
   delete p;
   return B200_OK;
 }
@@ -817,8 +889,28 @@ int b200_segmented_sort_keys_u32(b200_batch_plan p, uint32_t* keys, int descendi
       B200_LAUNCH(name, segsort_small_kernel<false>, grid, SEG_BLOCK, 0, s, keys, p->d_offsets,
                   p->d_small, p->nsmall);
   }
-  for (int sid : p->big_segments) {
-    B200_TRY(b200_sort_keys_u32(keys + p->offsets[sid], size_t(p->lens[sid]), descending, stream));
+  if (p->big_packed) {
+    DeviceProps props;
+    B200_TRY(device_props(&props));
+    const int nbig = int(p->big_segments.size());
+    const unsigned grid = unsigned(std::min<int64_t>((p->big_total + 255) / 256, int64_t(props.sms) * 8));
+    if (descending)
+      B200_LAUNCH(name, segsort_pack_kernel<true>, grid, 256, 0, s, keys, p->d_big_off, p->d_big_src, nbig,
+                  p->big_total, p->d_big_buf);
+    else
+      B200_LAUNCH(name, segsort_pack_kernel<false>, grid, 256, 0, s, keys, p->d_big_off, p->d_big_src, nbig,
+                  p->big_total, p->d_big_buf);
+    B200_TRY(b200_sort_keys_u64(p->d_big_buf, size_t(p->big_total), 0, stream));
+    if (descending)
+      B200_LAUNCH(name, segsort_unpack_kernel<true>, grid, 256, 0, s, keys, p->d_big_off, p->d_big_src,
+                  p->big_total, p->d_big_buf);
+    else
+      B200_LAUNCH(name, segsort_unpack_kernel<false>, grid, 256, 0, s, keys, p->d_big_off, p->d_big_src,
+                  p->big_total, p->d_big_buf);
+  } else {
+    for (int sid : p->big_segments) {
+      B200_TRY(b200_sort_keys_u32(keys + p->offsets[sid], size_t(p->lens[sid]), descending, stream));
+    }
   }
   clear_error();
   return B200_OK;

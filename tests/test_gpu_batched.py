@@ -197,6 +197,35 @@ def test_segmented_sort_bit_exact(prims, orc):
                                           err_msg=f"seg {i} desc={desc}")
 
 
+@pytest.mark.parametrize("case", ["over_256_long_segments", "long_segments_sorted_one_by_one"])
+def test_segmented_sort_long_segment_paths(prims, orc, case):
+    """Long segments (more than 4096 keys) are sorted together as
+    (segment << 32 | key) in one 64-bit sort when there are several of
+    moderate length -- here more than 256 of them, so the segment bits reach
+    past the low byte of the high word -- and one sort call per segment when
+    they are long; keys with many duplicates, both directions, against the
+    oracle segment by segment."""
+    rng = np.random.default_rng(9)
+    if case == "over_256_long_segments":
+        lens = np.empty(600, dtype=np.int64)
+        lens[0::2] = 4097 + rng.integers(0, 700, 300)
+        lens[1::2] = rng.integers(0, 50, 300)
+    else:
+        lens = np.array([5, 600000, 3, 700000, 10, 0], dtype=np.int64)
+    plan = prims.BatchPlan(lens)
+    k = rng.integers(0, 1000, plan.total, dtype=np.uint64).astype(np.uint32)
+    k[::7] = rng.integers(0, 2 ** 32, k[::7].size, dtype=np.uint64).astype(np.uint32)
+    for desc in (False, True):
+        d = to_dev(k)
+        prims.segmented_sort(plan, d, descending=desc)
+        got = to_host(d)
+        for i in range(len(lens)):
+            a, b = plan.offsets[i], plan.offsets[i + 1]
+            np.testing.assert_array_equal(got[a:b], orc.sort(k[a:b], descending=desc),
+                                          err_msg=f"{case} seg {i} desc={desc}")
+    plan.close()
+
+
 def test_graph_capture_replays_batched_sweeps(prims):
     import torch
     rng = np.random.default_rng(5)
