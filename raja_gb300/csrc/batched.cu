@@ -46,8 +46,9 @@ struct b200_batch_plan_s {
   int variant = -1;                // autotuned kernel variant (-1: default)
   // segmented sort classification
   std::vector<int> big_segments;   // segments longer than the block sort
-  int32_t* d_small = nullptr;      // ids of the small segments
+  int32_t* d_small = nullptr;      // ids of the small segments: the warp-sized ones first
   int nsmall = 0;
+  int ntiny = 0;                   // small segments of at most SEG_WARP_CAP keys
   // long segments sorted together as (segment << 32 | key) in one 64-bit
   // sort (set when there are several and they are short enough)
   bool big_packed = false;
@@ -541,9 +542,10 @@ segscan_kernel(const int32_t* in, int32_t* out, int64_t n, const int64_t* __rest
 }
 
 // ------------------------------------------------------ segmented sort
-// Segments up to SEG_CAP keys are sorted by one block each with a bitonic
-// network in shared memory (padded to a power of two with the largest
-// key); longer segments go to the onesweep radix sort.  Several long
+// Segments up to SEG_CAP keys are sorted with a bitonic network in shared
+// memory (padded to a power of two with the largest key): one warp per
+// segment up to SEG_WARP_CAP keys, one block per longer one; longer
+// segments go to the onesweep radix sort.  Several long
 // segments of moderate length are sorted together: each key becomes
 // (segment << 32 | key) -- the key inverted for a descending sort -- and
 // one stable 64-bit sort leaves every segment's keys, in order, in that
@@ -552,6 +554,7 @@ segscan_kernel(const int32_t* in, int32_t* out, int64_t n, const int64_t* __rest
 // launches instead of six per long segment.
 constexpr int SEG_CAP = 4096;
 constexpr int SEG_BLOCK = 256;
+constexpr int SEG_WARP_CAP = 256;  // segments up to this long are sorted by one warp each
 constexpr int64_t SEG_PACK_MEAN = int64_t(1) << 18;  // long segments at most this long on average are packed
 
 __device__ __forceinline__ int big_seg_of(const int64_t* __restrict__ off, int nbig, int64_t e) {
@@ -625,6 +628,47 @@ segsort_small_kernel(uint32_t* keys, const int64_t* __restrict__ off,
   }
 }
 
+// Segments of at most SEG_WARP_CAP keys: one warp each, eight per block,
+// the same bitonic network in the warp's own slice of shared memory with
+// warp barriers between the stages.
+template <bool DESC>
+__global__ void __launch_bounds__(SEG_BLOCK)
+segsort_warp_kernel(uint32_t* keys, const int64_t* __restrict__ off,
+                    const int32_t* __restrict__ seg_ids, int ntiny) {
+  constexpr int WPB = SEG_BLOCK / 32;
+  __shared__ uint32_t sm[WPB][SEG_WARP_CAP];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t* w = sm[warp];
+  const int nw = int(gridDim.x) * WPB;
+  for (int b = int(blockIdx.x) * WPB + warp; b < ntiny; b += nw) {  // warp-uniform
+    const int sid = seg_ids[b];
+    const int64_t lo = off[sid];
+    const int len = int(off[sid + 1] - lo);
+    int p2 = 1;
+    while (p2 < len) p2 <<= 1;
+    const uint32_t pad = DESC ? 0u : 0xffffffffu;
+    for (int i = lane; i < p2; i += 32) w[i] = (i < len) ? keys[lo + i] : pad;
+    __syncwarp();
+    for (int k = 2; k <= p2; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int i = lane; i < p2 / 2; i += 32) {
+          const int lo_i = 2 * j * (i / j) + (i % j);
+          const int hi_i = lo_i + j;
+          const bool up = ((lo_i & k) == 0) != DESC;
+          const uint32_t x = w[lo_i], y = w[hi_i];
+          if ((x > y) == up) {
+            w[lo_i] = y;
+            w[hi_i] = x;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    for (int i = lane; i < len; i += 32) keys[lo + i] = w[i];
+    __syncwarp();
+  }
+}
+
 }  // namespace
 }  // namespace b200
 
@@ -659,12 +703,15 @@ int b200_batch_plan_create(const int64_t* lens, int nloops, b200_batch_plan* out
   }
   ck(cudaMemcpy(p->d_offsets, p->offsets.data(), (size_t(nloops) + 1) * sizeof(int64_t),
                 cudaMemcpyHostToDevice), "plan offsets copy");
-  std::vector<int32_t> small;
+  std::vector<int32_t> small, mid;
   for (int i = 0; i < nloops; ++i) {
     if (lens[i] <= 1) continue;
-    if (lens[i] <= SEG_CAP) small.push_back(i);
+    if (lens[i] <= SEG_WARP_CAP) small.push_back(i);
+    else if (lens[i] <= SEG_CAP) mid.push_back(i);
     else p->big_segments.push_back(i);
   }
+  p->ntiny = int(small.size());
+  small.insert(small.end(), mid.begin(), mid.end());
   p->nsmall = int(small.size());
   for (int sid : p->big_segments) p->big_total += lens[sid];
   const int nbig = int(p->big_segments.size());
@@ -878,16 +925,28 @@ int b200_segmented_sort_keys_u32(b200_batch_plan p, uint32_t* keys, int descendi
   if (p->total == 0) return B200_OK;
   if (!keys) return fail(B200_ERR_ARG, "%s: null keys", name);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (p->nsmall > 0) {
+  if (p->ntiny > 0) {
     DeviceProps props;
     B200_TRY(device_props(&props));
-    int grid = std::min(p->nsmall, props.sms * 8);
+    const int grid = std::min((p->ntiny + SEG_BLOCK / 32 - 1) / (SEG_BLOCK / 32), props.sms * 8);
+    if (descending)
+      B200_LAUNCH(name, segsort_warp_kernel<true>, grid, SEG_BLOCK, 0, s, keys, p->d_offsets, p->d_small,
+                  p->ntiny);
+    else
+      B200_LAUNCH(name, segsort_warp_kernel<false>, grid, SEG_BLOCK, 0, s, keys, p->d_offsets, p->d_small,
+                  p->ntiny);
+  }
+  if (p->nsmall > p->ntiny) {
+    DeviceProps props;
+    B200_TRY(device_props(&props));
+    const int nmid = p->nsmall - p->ntiny;
+    const int grid = std::min(nmid, props.sms * 8);
     if (descending)
       B200_LAUNCH(name, segsort_small_kernel<true>, grid, SEG_BLOCK, 0, s, keys, p->d_offsets,
-                  p->d_small, p->nsmall);
+                  p->d_small + p->ntiny, nmid);
     else
       B200_LAUNCH(name, segsort_small_kernel<false>, grid, SEG_BLOCK, 0, s, keys, p->d_offsets,
-                  p->d_small, p->nsmall);
+                  p->d_small + p->ntiny, nmid);
   }
   if (p->big_packed) {
     DeviceProps props;
