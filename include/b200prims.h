@@ -464,12 +464,15 @@ int b200_segmented_scan_inclusive_i32(b200_batch_plan plan, const int32_t* in, i
                                       b200_stream_t stream);
 int b200_segmented_scan_exclusive_i32(b200_batch_plan plan, const int32_t* in, int32_t* out,
                                       b200_stream_t stream);
-/* Sort the keys of every segment independently, in place. */
+/* Sort the keys of every segment independently, in place.  When the plan
+ * has several segments longer than 4096 keys, averaging at most 2^18, they
+ * are sorted together in one 64-bit sort, and the plan holds a buffer of
+ * 8 bytes per key of those segments for it. */
 int b200_segmented_sort_keys_u32(b200_batch_plan plan, uint32_t* keys, int descending,
                                  b200_stream_t stream);
 
 /* ======================================================================
- * Batched 3-D Jacobi sweeps -- the config-5 mesh sweeps that the reference
+ * Batched 3-D Jacobi sweeps over many meshes of different sizes, which the reference
  * writes with RAJA::launch + View/OffsetLayout and a ReduceMax residual
  * (pattern/launch/launch_core.hpp:150-460, util/OffsetLayout.hpp:166-244,
  * examples/jacobi.cpp:223-489), one launch per mesh per sweep.
